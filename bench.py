@@ -1,0 +1,406 @@
+"""Benchmark of the spatial-query hot path on GB300.
+
+Headline workload (one step = one pass of the path over one batch): first ray hit of 4,194,304 cosine-distributed rays
+against a 1024 x 1024-vertex fBm heightfield (2,093,058 triangles), the configuration the metric is quoted on. Inputs
+are seeded synthetic data with the benchmark's shapes and distributions (no dataset exists for this path).
+
+  value      Mqueries/s with rays and mesh resident in HBM (device pointers), CUDA events on the launching stream,
+             L2 flushed (256 MB write) before every timed step.
+  e2e        the same metric through the C ABI with host (pinned) buffers: host->device copies of the rays and
+             device->host copies of (time, index) inside the timed region.
+  roofline   algorithmic bytes per launch / mean ray-kernel duration (CUDA events recorded around each launch).
+  cpu_baseline  the oracle's restatement of the reference's CPU traversal (reference kd-tree, reference tie order) on a
+             bounded sample, all host threads.
+  extra      the other workloads (closest point, k-NN graph) measured the same way, device-resident.
+
+--impl reference times the reference's algorithm on the host cores instead (the CPU restatement, since the reference
+itself needs Eigen, which is absent).
+
+Multi-GPU: one process per GPU (torchrun); each rank runs an independent replica on its own batch (weak scaling);
+the only exchange is the max-over-ranks of the timed region.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from thea_gb300 import workloads as W  # noqa: E402
+
+RAYS = 4194304
+HF_GRID = 1024
+MESH_BYTES_CFG1 = 12 * (HF_GRID * HF_GRID) + 12 * 2093058        # vertices + faces
+ALGO_BYTES_CFG1 = 32 * RAYS + MESH_BYTES_CFG1                    # 24 B in + 8 B out per ray, mesh once
+CP_QUERIES = 262144
+ALGO_BYTES_CFG0 = 32 * CP_QUERIES + 12 * 40962 + 12 * 81920
+KNN_POINTS = 1048576
+ALGO_BYTES_CFG2 = 140 * KNN_POINTS
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary (profiles/ncu_traffic.txt), or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and not line.startswith("#") and parts[0] == kernel:
+            return float(parts[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# CPU baseline (oracle restatement of the reference path; test infrastructure used only as the baseline here)
+# ---------------------------------------------------------------------------------------------------------------------
+
+def cpu_ray_baseline(V, F, o, d, target_s=12.0, threads=None):
+    from oracle import oracle as O
+    O.build()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    m = O.MeshIndex(V, F)
+    build_s = time.perf_counter() - t0
+    n = 16384
+    t0 = time.perf_counter()
+    m.ray_ref(o[:n], d[:n], threads=threads)
+    dt = time.perf_counter() - t0
+    rate = n / max(dt, 1e-6)
+    n2 = int(min(len(o), max(n, rate * target_s)))
+    sel = np.linspace(0, len(o) - 1, n2).astype(np.int64)
+    t0 = time.perf_counter()
+    m.ray_ref(o[sel], d[sel], threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt / 1e6, "unit": "Mqueries/s", "cores": threads, "kind": "port",
+            "sample": "%d of the %d rays (evenly strided), reference kd-tree and traversal restated in C++ (oracle), "
+                      "%d threads; kd-tree build %.2f s not included" % (n2, len(o), threads, build_s)}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    V, F, o, d = W.config1()
+    threads = os.cpu_count() or 1
+    m = O.MeshIndex(V, F)
+    n = 16384
+    t0 = time.perf_counter()
+    m.ray_ref(o[:n], d[:n], threads=threads)
+    rate = n / max(time.perf_counter() - t0, 1e-6)
+    # each step: a bounded sample sized to ~8 s of host work
+    per_step = int(min(len(o), max(n, rate * 8.0 / max(1, args.steps + args.warmup) * 2)))
+    rng = np.random.default_rng(0)
+    times = []
+    for s in range(args.warmup + args.steps):
+        sel = rng.choice(len(o), per_step, replace=False)
+        t0 = time.perf_counter()
+        m.ray_ref(o[sel], d[sel], threads=threads)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    ms = 1000.0 * statistics.mean(times)
+    value = per_step / (ms / 1000.0) / 1e6
+    line = {"impl": "reference", "metric": "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)",
+            "value": value, "unit": "Mqueries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "ray_first_hit_heightfield_1024", "triangles": 2093058, "rays_per_step": per_step,
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "Mqueries/s", "cores": threads, "kind": "port",
+                             "sample": "%d random rays of the 4,194,304 per step; reference kd-tree and traversal "
+                                       "restated in C++ (the reference needs Eigen, absent here)" % per_step},
+            "e2e": {"value": value, "unit": "Mqueries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------------------------------
+
+def timed_steps(fn, steps, warmup, flush, stream):
+    """Runs warmup steps, then `steps` timed steps each preceded by an L2 flush; returns per-step ms (CUDA events)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import thea_gb300 as T
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    V, F, o, d = W.config1()
+    Vd, Fd = torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda()
+    od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bvh = T.MeshBvh(Vd, Fd, layouts=2)
+    torch.cuda.synchronize()
+    build_ms = 1000 * (time.perf_counter() - t0)
+    info = bvh.info()
+    out_t = torch.empty(RAYS, dtype=torch.float32, device="cuda")
+    out_i = torch.empty(RAYS, dtype=torch.int32, device="cuda")
+    from thea_gb300 import _native as N
+    L = N.lib()
+    import ctypes
+
+    def step():
+        N.check(L.thea_ray_intersection(bvh.handle, ctypes.c_void_p(od.data_ptr()), ctypes.c_void_p(dd.data_ptr()),
+                                        RAYS, -1.0, ctypes.c_void_p(out_t.data_ptr()),
+                                        ctypes.c_void_p(out_i.data_ptr()), None,
+                                        ctypes.c_void_p(stream.cuda_stream)))
+
+    # warm-up, then the timed region bracketed by barrier + synchronize, with clocks sampled during it
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    T.profiling_reset()
+    T.profiling(True)
+    launches0 = T.launch_count()
+    with ClockSampler(local_rank) as clk:
+        t_wall0 = time.perf_counter()
+        ms = timed_steps(step, args.steps, 0, flush, stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    launches = T.launch_count() - launches0
+    T.profiling(False)
+    k_ms, k_cnt = T.profiling_read("ray_kernel")
+    T.profiling_reset()
+    step_ms = sum(ms) / len(ms)
+    if dist:
+        tt = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    value = world * RAYS / (step_ms / 1000.0) / 1e6
+    kernel_ms = k_ms / max(1, k_cnt)
+    peak, peak_kind = peaks()
+    achieved = ALGO_BYTES_CFG1 / (kernel_ms / 1000.0) / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    ho = torch.from_numpy(o).pin_memory()
+    hd = torch.from_numpy(d).pin_memory()
+    ht = torch.empty(RAYS, dtype=torch.float32).pin_memory()
+    hi = torch.empty(RAYS, dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        N.check(L.thea_ray_intersection(bvh.handle, ctypes.c_void_p(ho.data_ptr()), ctypes.c_void_p(hd.data_ptr()),
+                                        RAYS, -1.0, ctypes.c_void_p(ht.data_ptr()), ctypes.c_void_p(hi.data_ptr()),
+                                        None, ctypes.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()  # synchronous: returns once results are in host memory
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    assert np.array_equal(hi.numpy(), out_i.cpu().numpy()), "host and device paths disagree"
+    hits = int((hi.numpy() >= 0).sum())
+
+    extra = {}
+    if not args.no_extra:
+        extra = extra_workloads(T, torch, stream, flush, args)
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu and world == 1:
+            cpu = cpu_ray_baseline(V, F, o, d)
+        traffic = ncu_traffic("ray_kernel")
+        line = {
+            "metric": "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)",
+            "value": value, "unit": "Mqueries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded fBm heightfield and cosine rays)",
+            "config": {"workload": "ray_first_hit_heightfield_1024", "triangles": 2093058, "vertices": 1048576,
+                       "rays": RAYS, "bvh_width": info["width"], "leaf_size": info["max_leaf_size"],
+                       "bvh_nodes": info["num_nodes"], "bvh_depth": info["depth"], "build_ms": build_ms,
+                       "hit_fraction": hits / RAYS, "l2": "flushed by a 256 MB write before every timed step",
+                       "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+            "e2e": {"value": world * RAYS / e2e_s / 1e6, "unit": "Mqueries/s", "h2d_bytes_per_step": RAYS * 24,
+                    "d2h_bytes_per_step": RAYS * 8},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "ray_kernel", "kernel_ms": kernel_ms,
+                         "algorithmic_bytes_per_launch": ALGO_BYTES_CFG1},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "wall_s_timed_region": t_wall,
+            "extra": extra,
+        }
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    bvh.close()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def extra_workloads(T, torch, stream, flush, args):
+    """Closest point (config 0) and the k-NN graph of area samples (config 2), device-resident."""
+    out = {}
+    steps = max(3, min(args.steps, 5))
+    # config 0: closest point on the noisy icosphere
+    V, F, Q = W.config0()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1)
+    Qd = torch.from_numpy(Q).cuda()
+    T.profiling_reset()
+    T.profiling(True)
+    ms = timed_steps(lambda: bvh.closest_element(Qd), steps, 2, flush, stream)
+    T.profiling(False)
+    k_ms, k_cnt = T.profiling_read("closest_kernel")
+    kms = k_ms / max(1, k_cnt)
+    out["closest_point_cfg0"] = {"value": CP_QUERIES / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
+                                 "ms_per_step": statistics.mean(ms), "kernel_ms": kms,
+                                 "roofline_frac": ALGO_BYTES_CFG0 / (kms / 1e3) / 1e9 / peaks()[0]}
+    bvh.close()
+    # config 2: 1,048,576 area samples of the config-0 mesh (reference Random stream), k = 16 graph excluding self
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pos, _, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), KNN_POINTS, 2)
+    torch.cuda.synchronize()
+    sample_ms = 1000 * (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    pb = T.PointBvh(pos)
+    torch.cuda.synchronize()
+    pbuild_ms = 1000 * (time.perf_counter() - t0)
+    T.profiling_reset()
+    T.profiling(True)
+    ms = timed_steps(lambda: pb.k_closest_self(16, device=True), steps, 2, flush, stream)
+    T.profiling(False)
+    k_ms, k_cnt = T.profiling_read("knn_kernel")
+    kms = k_ms / max(1, k_cnt)
+    out["knn_graph_cfg2"] = {"value": KNN_POINTS / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
+                             "ms_per_step": statistics.mean(ms), "kernel_ms": kms, "k": 16,
+                             "sampling_ms": sample_ms, "point_bvh_build_ms": pbuild_ms,
+                             "roofline_frac": ALGO_BYTES_CFG2 / (kms / 1e3) / 1e9 / peaks()[0]}
+    pb.close()
+    T.profiling_reset()
+    return out
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if "RANK" in os.environ else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    gpu_arm(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+// thea_gpu.hpp -- header-only C++ wrapper over the C ABI in thea_gpu.h, with the method names of the reference's
+// spatial-query classes (sidch/Thea: Code/Source/Algorithms/BvhN.hpp, MeshBvh.hpp, MeshSampler.hpp) in batched form.
+//
+// Arrays may live in host or device memory (see thea_gpu.h). Errors surface as thea_gpu::Exception carrying the status.
+#ifndef THEA_GPU_HPP
+#define THEA_GPU_HPP
+
+#include "thea_gpu.h"
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+namespace thea_gpu {
+
+class Exception : public std::runtime_error {
+ public:
+  Exception(thea_status s, std::string const & msg) : std::runtime_error(msg), status_(s) {}
+  thea_status status() const { return status_; }
+
+ private:
+  thea_status status_;
+};
+
+inline void check(thea_status s) {
+  if (s != THEA_OK) {
+    char const * m = thea_last_error_message();
+    throw Exception(s, std::string(thea_status_string(s)) + ": " + (m ? m : ""));
+  }
+}
+
+struct BuildOptions {
+  int32_t width = 4;          // 4 or 8 children per node
+  int32_t max_leaf_size = 0;  // 0: library default
+  uint32_t layouts = 0;       // THEA_LAYOUT_* mask for meshes, 0 = both
+  thea_build_config config() const {
+    thea_build_config c{};
+    c.width = width;
+    c.max_leaf_size = max_leaf_size;
+    c.layouts = layouts;
+    return c;
+  }
+};
+
+class BvhHandle {
+ public:
+  BvhHandle() = default;
+  BvhHandle(BvhHandle const &) = delete;
+  BvhHandle & operator=(BvhHandle const &) = delete;
+  BvhHandle(BvhHandle && o) noexcept : h_(o.h_) { o.h_ = nullptr; }
+  BvhHandle & operator=(BvhHandle && o) noexcept {
+    std::swap(h_, o.h_);
+    return *this;
+  }
+  ~BvhHandle() {
+    if (h_) thea_bvh_destroy(h_);
+  }
+  thea_bvh * get() const { return h_; }
+  thea_bvh_info info() const {
+    thea_bvh_info i;
+    check(thea_bvh_get_info(h_, &i));
+    return i;
+  }
+
+ protected:
+  thea_bvh * h_ = nullptr;
+};
+
+// MeshBvh: a BVH over the triangles of a mesh; element index = face index (MeshBvh::add + MeshBvh::init).
+class MeshBvh : public BvhHandle {
+ public:
+  MeshBvh(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t num_faces,
+          BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
+    thea_build_config c = opt.config();
+    check(thea_mesh_bvh_build(vertices, num_vertices, faces, num_faces, &c, stream, &h_));
+  }
+
+  // BvhN::closestElement<MetricL2>(query, dist_bound, compat, &dist, &closest_point), batched over n queries.
+  void closestElement(float const * queries, int64_t n, int32_t * indices, float * distances = nullptr,
+                      float * closest_points = nullptr, double dist_bound = -1, void * stream = nullptr) const {
+    check(thea_closest_element(h_, queries, n, (float)dist_bound, indices, distances, closest_points, stream));
+  }
+
+  // Single host query, as the reference's per-call form: returns the element index or -1.
+  int64_t closestElement(float const query[3], double dist_bound = -1, double * dist = nullptr,
+                         float * closest_point = nullptr) const {
+    int32_t idx = -1;
+    float d = -1, cp[3] = {0, 0, 0};
+    check(thea_closest_element(h_, query, 1, (float)dist_bound, &idx, &d, cp, nullptr));
+    if (idx >= 0) {
+      if (dist) *dist = d;
+      if (closest_point) { closest_point[0] = cp[0]; closest_point[1] = cp[1]; closest_point[2] = cp[2]; }
+    }
+    return idx;
+  }
+
+  // BvhN::rayStructureIntersection<RayIntersectionTester>(ray, max_time), batched: time (-1 = miss), element, normal.
+  void rayStructureIntersection(float const * origins, float const * directions, int64_t n, float * times,
+                                int32_t * indices, float * normals = nullptr, float max_time = -1,
+                                void * stream = nullptr) const {
+    check(thea_ray_intersection(h_, origins, directions, n, max_time, times, indices, normals, stream));
+  }
+
+  // BvhN::rayIntersectionTime<RayIntersectionTester>(ray, max_time), batched.
+  void rayIntersectionTime(float const * origins, float const * directions, int64_t n, float * times,
+                           float max_time = -1, void * stream = nullptr) const {
+    check(thea_ray_intersection(h_, origins, directions, n, max_time, times, nullptr, nullptr, stream));
+  }
+};
+
+// BvhN<Vector3, 3>: a BVH over points; element index = point index.
+class PointBvh : public BvhHandle {
+ public:
+  PointBvh(float const * points, int64_t num_points, BuildOptions const & opt = BuildOptions(),
+           void * stream = nullptr) {
+    thea_build_config c = opt.config();
+    c.layouts = 0;
+    check(thea_point_bvh_build(points, num_points, &c, stream, &h_));
+  }
+
+  // BvhN::kClosestPairs<MetricL2>(query, BoundedSortedArrayN<k, NeighborPair>&, dist_bound), batched: n x k indices
+  // and squared distances, sorted, unused slots -1. exclude (nullable): per-query element to skip.
+  void kClosestPairs(float const * queries, int64_t n, int32_t k, int32_t * indices, float * sq_distances,
+                     double dist_bound = -1, int32_t const * exclude = nullptr, void * stream = nullptr) const {
+    check(thea_k_closest(h_, queries, n, k, (float)dist_bound, exclude, indices, sq_distances, stream));
+  }
+
+  // k-nearest-neighbour graph of the indexed points (each point excluding itself), rows in point order.
+  void kClosestSelf(int32_t k, int32_t * indices, float * sq_distances, void * stream = nullptr) const {
+    check(thea_k_closest_self(h_, k, indices, sq_distances, stream));
+  }
+};
+
+// MeshSampler::sampleEvenlyByArea (EXACT count mode), drawing from Random(seed).
+class MeshSampler {
+ public:
+  MeshSampler(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t num_faces)
+      : v_(vertices), nv_(num_vertices), f_(faces), nf_(num_faces) {}
+
+  int64_t sampleEvenlyByArea(int64_t num_samples, float * positions, float * face_normals = nullptr,
+                             int32_t * face_indices = nullptr, uint32_t seed = 0, int32_t rng = THEA_RNG_THEA_MT,
+                             void * stream = nullptr) const {
+    int64_t got = 0;
+    check(thea_sample_by_area(v_, nv_, f_, nf_, num_samples, seed, rng, positions, face_normals, face_indices, &got,
+                              stream));
+    return got;
+  }
+
+ private:
+  float const * v_;
+  int64_t nv_;
+  int32_t const * f_;
+  int64_t nf_;
+};
+
+}  // namespace thea_gpu
+
+#endif  // THEA_GPU_HPP

@@ -1,0 +1,285 @@
+"""TEST INFRASTRUCTURE ONLY -- ctypes binding of the CPU oracle (``oracle/_build/liboracle.so``).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` may import this module. It restates
+Thea's CPU spatial-query path (reference mode: the reference's kd-tree and traversal order; contract mode: lowest index
+among ties) and is never used by the product path. Parity status: UNPINNED (no golden vector exists in the reference,
+whose Eigen dependency cannot be built here).
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+
+
+def build():
+    """Compile the oracle with its Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.oracle_mesh_create.restype = _vp
+        L.oracle_mesh_create.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_int]
+        L.oracle_mesh_destroy.argtypes = [_vp]
+        L.oracle_mesh_num_nodes.restype = _i64
+        L.oracle_mesh_num_nodes.argtypes = [_vp]
+        L.oracle_mesh_max_depth.restype = _i64
+        L.oracle_mesh_max_depth.argtypes = [_vp]
+        L.oracle_closest_ref.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f32p, ctypes.c_int]
+        L.oracle_closest_contract.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p, ctypes.c_int]
+        L.oracle_closest_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p,
+                                           ctypes.c_int, ctypes.c_int]
+        L.oracle_ray_ref.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, _f32p, _i32p, _f32p, ctypes.c_int]
+        L.oracle_ray_contract.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p, ctypes.c_int]
+        L.oracle_ray_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p,
+                                       ctypes.c_int, ctypes.c_int]
+        L.oracle_points_create.restype = _vp
+        L.oracle_points_create.argtypes = [_f32p, _i64, _i64, ctypes.c_int]
+        L.oracle_points_destroy.argtypes = [_vp]
+        for name in ("oracle_knn_ref", "oracle_knn_contract"):
+            getattr(L, name).argtypes = [_vp, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
+                                         ctypes.c_int]
+        L.oracle_knn_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
+                                       ctypes.c_int, ctypes.c_int]
+        L.oracle_sample_by_area.restype = _i64
+        L.oracle_sample_by_area.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_uint32, _f32p, _f32p, _i32p]
+        L.oracle_thea_random_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
+        L.oracle_std_mt19937_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
+        L.oracle_triangle_closest_points.argtypes = [_f32p, _f32p, _i64, _f32p, _f32p]
+        L.oracle_triangle_ray_times.argtypes = [_f32p, _f32p, _f32p, _i64, ctypes.c_float, _f32p]
+        L.oracle_triangle_props.argtypes = [_f32p, _i64, _f32p, _f32p, _i32p, _f32p]
+        L.oracle_box_ray_time.restype = ctypes.c_float
+        L.oracle_box_ray_time.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_float]
+        L.oracle_tree_depth.restype = _i64
+        L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def default_threads():
+    return os.cpu_count() or 1
+
+
+class MeshIndex:
+    """Reference kd-tree over mesh triangles (BvhN::init with Method::KDTREE, leaf size 5 by default)."""
+
+    def __init__(self, V, F, max_leaf=-1, fp64=False):
+        self.V = _f32(V).reshape(-1, 3)
+        self.F = _i32(F).reshape(-1, 3)
+        self.fp64 = bool(fp64)
+        self.h = lib().oracle_mesh_create(_p(self.V, _f32p), len(self.V), _p(self.F, _i32p), len(self.F), max_leaf,
+                                          int(fp64))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_mesh_destroy(self.h)
+            self.h = None
+
+    @property
+    def num_nodes(self):
+        return lib().oracle_mesh_num_nodes(self.h)
+
+    @property
+    def max_depth(self):
+        return lib().oracle_mesh_max_depth(self.h)
+
+    def closest_ref(self, q, dist_bound=-1.0, threads=None):
+        """Reference mode: returns (index, distance (double, sqrt of mad), closest point (float32))."""
+        q = _f32(q).reshape(-1, 3)
+        n = len(q)
+        idx = np.empty(n, np.int32)
+        dist = np.empty(n, np.float64)
+        cp = np.empty((n, 3), np.float32)
+        lib().oracle_closest_ref(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(dist, _f64p),
+                                 _p(cp, _f32p), threads or default_threads())
+        return idx, dist, cp
+
+    def closest_contract(self, q, dist_bound=-1.0, threads=None):
+        """Contract mode: returns (index, squared distance, closest point), lowest index among ties."""
+        q = _f32(q).reshape(-1, 3)
+        n = len(q)
+        idx = np.empty(n, np.int32)
+        d2 = np.empty(n, np.float64)
+        cp = np.empty((n, 3), np.float64)
+        lib().oracle_closest_contract(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(d2, _f64p),
+                                      _p(cp, _f64p), threads or default_threads())
+        return idx, d2, cp
+
+    def ray_ref(self, o, d, max_time=-1.0, threads=None):
+        """Reference mode rayStructureIntersection: returns (time, index, normal); time -1 on a miss."""
+        o = _f32(o).reshape(-1, 3)
+        d = _f32(d).reshape(-1, 3)
+        n = len(o)
+        t = np.empty(n, np.float32)
+        idx = np.empty(n, np.int32)
+        nrm = np.empty((n, 3), np.float32)
+        lib().oracle_ray_ref(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f32p), _p(idx, _i32p),
+                             _p(nrm, _f32p), threads or default_threads())
+        return t, idx, nrm
+
+    def ray_contract(self, o, d, max_time=-1.0, threads=None):
+        o = _f32(o).reshape(-1, 3)
+        d = _f32(d).reshape(-1, 3)
+        n = len(o)
+        t = np.empty(n, np.float64)
+        idx = np.empty(n, np.int32)
+        lib().oracle_ray_contract(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f64p),
+                                  _p(idx, _i32p), threads or default_threads())
+        return t, idx
+
+
+def closest_brute(V, F, q, dist_bound=-1.0, fp64=False, threads=None):
+    V = _f32(V).reshape(-1, 3)
+    F = _i32(F).reshape(-1, 3)
+    q = _f32(q).reshape(-1, 3)
+    n = len(q)
+    idx = np.empty(n, np.int32)
+    d2 = np.empty(n, np.float64)
+    cp = np.empty((n, 3), np.float64)
+    lib().oracle_closest_brute(_p(V, _f32p), len(V), _p(F, _i32p), len(F), _p(q, _f32p), n, float(dist_bound),
+                               _p(idx, _i32p), _p(d2, _f64p), _p(cp, _f64p), int(fp64), threads or default_threads())
+    return idx, d2, cp
+
+
+def ray_brute(V, F, o, d, max_time=-1.0, fp64=False, threads=None):
+    V = _f32(V).reshape(-1, 3)
+    F = _i32(F).reshape(-1, 3)
+    o = _f32(o).reshape(-1, 3)
+    d = _f32(d).reshape(-1, 3)
+    n = len(o)
+    t = np.empty(n, np.float64)
+    idx = np.empty(n, np.int32)
+    lib().oracle_ray_brute(_p(V, _f32p), len(V), _p(F, _i32p), len(F), _p(o, _f32p), _p(d, _f32p), n,
+                           float(max_time), _p(t, _f64p), _p(idx, _i32p), int(fp64), threads or default_threads())
+    return t, idx
+
+
+class PointIndex:
+    """Reference kd-tree over points (BvhN<Vector3, 3>)."""
+
+    def __init__(self, P, max_leaf=-1, fp64=False):
+        self.P = _f32(P).reshape(-1, 3)
+        self.h = lib().oracle_points_create(_p(self.P, _f32p), len(self.P), max_leaf, int(fp64))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_points_destroy(self.h)
+            self.h = None
+
+    def _knn(self, fn, q, k, dist_bound, exclude, threads):
+        q = _f32(q).reshape(-1, 3)
+        n = len(q)
+        idx = np.empty((n, k), np.int32)
+        d2 = np.empty((n, k), np.float64)
+        ex = None if exclude is None else _i32(exclude)
+        fn(self.h, _p(q, _f32p), n, int(k), float(dist_bound), _p(ex, _i32p), _p(idx, _i32p), _p(d2, _f64p),
+           threads or default_threads())
+        return idx, d2
+
+    def knn_ref(self, q, k, dist_bound=-1.0, exclude=None, threads=None):
+        return self._knn(lib().oracle_knn_ref, q, k, dist_bound, exclude, threads)
+
+    def knn_contract(self, q, k, dist_bound=-1.0, exclude=None, threads=None):
+        return self._knn(lib().oracle_knn_contract, q, k, dist_bound, exclude, threads)
+
+
+def knn_brute(P, q, k, dist_bound=-1.0, exclude=None, fp64=False, threads=None):
+    P = _f32(P).reshape(-1, 3)
+    q = _f32(q).reshape(-1, 3)
+    n = len(q)
+    idx = np.empty((n, k), np.int32)
+    d2 = np.empty((n, k), np.float64)
+    ex = None if exclude is None else _i32(exclude)
+    lib().oracle_knn_brute(_p(P, _f32p), len(P), _p(q, _f32p), n, int(k), float(dist_bound), _p(ex, _i32p),
+                           _p(idx, _i32p), _p(d2, _f64p), int(fp64), threads or default_threads())
+    return idx, d2
+
+
+def sample_by_area(V, F, n, seed):
+    """MeshSampler::sampleEvenlyByArea (EXACT) with Random(seed): returns (positions, face normals, face indices)."""
+    V = _f32(V).reshape(-1, 3)
+    F = _i32(F).reshape(-1, 3)
+    pos = np.empty((n, 3), np.float32)
+    nrm = np.empty((n, 3), np.float32)
+    face = np.empty(n, np.int32)
+    got = lib().oracle_sample_by_area(_p(V, _f32p), len(V), _p(F, _i32p), len(F), int(n), ctypes.c_uint32(seed),
+                                      _p(pos, _f32p), _p(nrm, _f32p), _p(face, _i32p))
+    return pos[:got], nrm[:got], face[:got]
+
+
+def thea_random_bits(seed, n):
+    out = np.empty(n, np.uint32)
+    lib().oracle_thea_random_bits(ctypes.c_uint32(seed), n, _p(out, _u32p))
+    return out
+
+
+def std_mt19937_bits(seed, n):
+    out = np.empty(n, np.uint32)
+    lib().oracle_std_mt19937_bits(ctypes.c_uint32(seed), n, _p(out, _u32p))
+    return out
+
+
+def triangle_closest_points(tris, p):
+    tris = _f32(tris).reshape(-1, 9)
+    p = _f32(p).reshape(-1, 3)
+    n = len(p)
+    cp = np.empty((n, 3), np.float32)
+    d2 = np.empty(n, np.float32)
+    lib().oracle_triangle_closest_points(_p(tris, _f32p), _p(p, _f32p), n, _p(cp, _f32p), _p(d2, _f32p))
+    return cp, d2
+
+
+def triangle_ray_times(tris, o, d, max_time=-1.0):
+    tris = _f32(tris).reshape(-1, 9)
+    o = _f32(o).reshape(-1, 3)
+    d = _f32(d).reshape(-1, 3)
+    n = len(o)
+    t = np.empty(n, np.float32)
+    lib().oracle_triangle_ray_times(_p(tris, _f32p), _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f32p))
+    return t
+
+
+def triangle_props(tris):
+    tris = _f32(tris).reshape(-1, 9)
+    n = len(tris)
+    nrm = np.empty((n, 3), np.float32)
+    dist = np.empty(n, np.float32)
+    axis = np.empty(n, np.int32)
+    area = np.empty(n, np.float32)
+    lib().oracle_triangle_props(_p(tris, _f32p), n, _p(nrm, _f32p), _p(dist, _f32p), _p(axis, _i32p), _p(area, _f32p))
+    return nrm, dist, axis, area
+
+
+def tree_depth(n, max_leaf=5):
+    return lib().oracle_tree_depth(int(n), int(max_leaf))

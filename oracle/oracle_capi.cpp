@@ -1,0 +1,354 @@
+// TEST INFRASTRUCTURE ONLY -- C entry points of the CPU oracle, loaded by the tests (ctypes) and by the CPU-baseline legs
+// of bench.py. Never linked into the product library. Parity status: UNPINNED (see thea_oracle.hpp).
+
+#include "thea_oracle.hpp"
+
+#include <random>
+
+using namespace oracle;
+
+namespace {
+
+struct MeshHandle {
+  int fp64 = 0;
+  MeshIndex<float> f;
+  MeshIndex<double> d;
+};
+
+struct PointHandle {
+  int fp64 = 0;
+  PointIndex<float> f;
+  PointIndex<double> d;
+};
+
+template <class S> V3<S> q3(float const * p, int64_t i) { return load3<S>(p + 3 * i); }
+
+}  // namespace
+
+extern "C" {
+
+int oracle_version() { return 1; }
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Mesh index (kd-tree over triangles, MeshBvh::init -> BvhN::init, MeshBvh.hpp:104-111)
+//---------------------------------------------------------------------------------------------------------------------------
+
+void * oracle_mesh_create(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t max_leaf, int fp64) {
+  MeshHandle * h = new MeshHandle;
+  h->fp64 = fp64;
+  if (fp64) h->d.init(V, nv, F, nf, max_leaf);
+  else h->f.init(V, nv, F, nf, max_leaf);
+  return h;
+}
+
+void oracle_mesh_destroy(void * h) { delete static_cast<MeshHandle *>(h); }
+
+int64_t oracle_mesh_num_nodes(void * hv) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  return h->fp64 ? (int64_t)h->d.tree.nodes.size() : (int64_t)h->f.tree.nodes.size();
+}
+
+int64_t oracle_mesh_max_depth(void * hv) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  return h->fp64 ? h->d.tree.max_depth : h->f.tree.max_depth;
+}
+
+// Reference-mode closest element (FP32 handle only). dist is sqrt(mad) in double, as BvhN::closestElement returns it.
+void oracle_closest_ref(void * hv, float const * q, int64_t n, double dist_bound, int32_t * idx, double * dist,
+                        float * cp, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      double mad = -1;
+      V3<float> c;
+      int64_t r = h->f.closestRef(q3<float>(q, i), dist_bound, mad, c);
+      idx[i] = (int32_t)r;
+      if (dist) dist[i] = r >= 0 ? std::sqrt(mad) : -1.0;
+      if (cp) {
+        cp[3 * i] = r >= 0 ? c.x : 0.f; cp[3 * i + 1] = r >= 0 ? c.y : 0.f; cp[3 * i + 2] = r >= 0 ? c.z : 0.f;
+      }
+    }
+  });
+}
+
+extern "C++" {
+template <class S>
+static void closestContractImpl(MeshIndex<S> const & m, float const * q, int64_t n, double dist_bound, int32_t * idx,
+                                double * d2, double * cp, int nthreads) {
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      S bd2 = 0;
+      V3<S> c;
+      int64_t r = m.closestContract(q3<S>(q, i), dist_bound, bd2, c);
+      idx[i] = (int32_t)r;
+      if (d2) d2[i] = r >= 0 ? (double)bd2 : -1.0;
+      if (cp) { cp[3 * i] = (double)c.x; cp[3 * i + 1] = (double)c.y; cp[3 * i + 2] = (double)c.z; }
+    }
+  });
+}
+}  // extern "C++"
+
+// Contract-mode closest element: lowest index among equal squared distances.
+void oracle_closest_contract(void * hv, float const * q, int64_t n, double dist_bound, int32_t * idx, double * d2,
+                             double * cp, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  if (h->fp64) closestContractImpl(h->d, q, n, dist_bound, idx, d2, cp, nthreads);
+  else closestContractImpl(h->f, q, n, dist_bound, idx, d2, cp, nthreads);
+}
+
+extern "C++" {
+template <class S>
+static void closestBruteImpl(float const * V, int64_t nv, int32_t const * F, int64_t nf, float const * q, int64_t n,
+                             double dist_bound, int32_t * idx, double * d2, double * cp, int nthreads) {
+  (void)nv;
+  std::vector<Tri<S>> tris((size_t)nf);
+  for (int64_t f = 0; f < nf; ++f)
+    tris[(size_t)f] = Tri<S>(q3<S>(V, F[3 * f]), q3<S>(V, F[3 * f + 1]), q3<S>(V, F[3 * f + 2]));
+  double mb = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      V3<S> p = q3<S>(q, i);
+      int64_t best = -1;
+      S bd = 0;
+      V3<S> bc;
+      for (int64_t f = 0; f < nf; ++f) {
+        V3<S> c;
+        S dd = triangleClosestPoints(tris[(size_t)f], p, c);
+        if (!(dd == dd)) continue;  // a NaN distance (coincident vertices) is never selected
+        if (mb >= 0 && !((double)dd < mb)) continue;
+        if (best < 0 || dd < bd) { best = f; bd = dd; bc = c; }
+      }
+      idx[i] = (int32_t)best;
+      if (d2) d2[i] = best >= 0 ? (double)bd : -1.0;
+      if (cp) { cp[3 * i] = (double)bc.x; cp[3 * i + 1] = (double)bc.y; cp[3 * i + 2] = (double)bc.z; }
+    }
+  });
+}
+}  // extern "C++"
+
+// Brute-force closest element over all triangles (contract mode by construction: scans in index order, strict less).
+void oracle_closest_brute(float const * V, int64_t nv, int32_t const * F, int64_t nf, float const * q, int64_t n,
+                          double dist_bound, int32_t * idx, double * d2, double * cp, int fp64, int nthreads) {
+  if (fp64) closestBruteImpl<double>(V, nv, F, nf, q, n, dist_bound, idx, d2, cp, nthreads);
+  else closestBruteImpl<float>(V, nv, F, nf, q, n, dist_bound, idx, d2, cp, nthreads);
+}
+
+// Reference-mode ray first hit (FP32 handle only): time (-1 = miss), element index, unit face normal.
+void oracle_ray_ref(void * hv, float const * o, float const * d, int64_t n, float max_time, float * t, int32_t * idx,
+                    float * normal, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      auto hit = h->f.rayRef(q3<float>(o, i), q3<float>(d, i), max_time);
+      t[i] = hit.idx >= 0 ? hit.t : -1.f;
+      idx[i] = (int32_t)hit.idx;
+      if (normal) {
+        V3<float> nn = hit.idx >= 0 ? h->f.tris[(size_t)hit.idx].normal : V3<float>(0, 0, 0);
+        normal[3 * i] = nn.x; normal[3 * i + 1] = nn.y; normal[3 * i + 2] = nn.z;
+      }
+    }
+  });
+}
+
+extern "C++" {
+template <class S>
+static void rayContractImpl(MeshIndex<S> const & m, float const * o, float const * d, int64_t n, double max_time,
+                            double * t, int32_t * idx, int nthreads) {
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      auto hit = rayContract(m, q3<S>(o, i), q3<S>(d, i), (S)max_time);
+      t[i] = hit.idx >= 0 ? (double)hit.t : -1.0;
+      idx[i] = (int32_t)hit.idx;
+    }
+  });
+}
+}  // extern "C++"
+
+void oracle_ray_contract(void * hv, float const * o, float const * d, int64_t n, double max_time, double * t,
+                         int32_t * idx, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  if (h->fp64) rayContractImpl(h->d, o, d, n, max_time, t, idx, nthreads);
+  else rayContractImpl(h->f, o, d, n, max_time, t, idx, nthreads);
+}
+
+extern "C++" {
+template <class S>
+static void rayBruteImpl(float const * V, int64_t nv, int32_t const * F, int64_t nf, float const * o, float const * d,
+                         int64_t n, double max_time, double * t, int32_t * idx, int nthreads) {
+  (void)nv;
+  std::vector<Tri<S>> tris((size_t)nf);
+  for (int64_t f = 0; f < nf; ++f)
+    tris[(size_t)f] = Tri<S>(q3<S>(V, F[3 * f]), q3<S>(V, F[3 * f + 1]), q3<S>(V, F[3 * f + 2]));
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      V3<S> oo = q3<S>(o, i), dd = q3<S>(d, i);
+      int64_t best = -1;
+      S bt = 0;
+      for (int64_t f = 0; f < nf; ++f) {
+        S tt = triangleRayTime(tris[(size_t)f], oo, dd, (S)max_time);
+        if (tt < S(0)) continue;
+        if (best < 0 || tt < bt) { best = f; bt = tt; }
+      }
+      t[i] = best >= 0 ? (double)bt : -1.0;
+      idx[i] = (int32_t)best;
+    }
+  });
+}
+}  // extern "C++"
+
+void oracle_ray_brute(float const * V, int64_t nv, int32_t const * F, int64_t nf, float const * o, float const * d,
+                      int64_t n, double max_time, double * t, int32_t * idx, int fp64, int nthreads) {
+  if (fp64) rayBruteImpl<double>(V, nv, F, nf, o, d, n, max_time, t, idx, nthreads);
+  else rayBruteImpl<float>(V, nv, F, nf, o, d, n, max_time, t, idx, nthreads);
+}
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Point index and k nearest neighbours
+//---------------------------------------------------------------------------------------------------------------------------
+
+void * oracle_points_create(float const * P, int64_t n, int64_t max_leaf, int fp64) {
+  PointHandle * h = new PointHandle;
+  h->fp64 = fp64;
+  if (fp64) h->d.init(P, n, max_leaf);
+  else h->f.init(P, n, max_leaf);
+  return h;
+}
+
+void oracle_points_destroy(void * h) { delete static_cast<PointHandle *>(h); }
+
+// Reference-mode k nearest neighbours (FP32 handle only). Unused slots: index -1, d2 -1.
+void oracle_knn_ref(void * hv, float const * q, int64_t n, int k, double dist_bound, int32_t const * exclude,
+                    int32_t * idx, double * d2, int nthreads) {
+  PointHandle * h = static_cast<PointHandle *>(hv);
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    std::vector<Neighbor> out;
+    for (int64_t i = b; i < e; ++i) {
+      h->f.knnRef(q3<float>(q, i), k, dist_bound, exclude ? (int64_t)exclude[i] : -1, out);
+      for (int j = 0; j < k; ++j) {
+        bool v = j < (int)out.size();
+        idx[i * k + j] = v ? (int32_t)out[(size_t)j].idx : -1;
+        d2[i * k + j] = v ? out[(size_t)j].mad : -1.0;
+      }
+    }
+  });
+}
+
+extern "C++" {
+template <class S>
+static void knnContractImpl(PointIndex<S> const & m, float const * q, int64_t n, int k, double dist_bound,
+                            int32_t const * exclude, int32_t * idx, double * d2, int nthreads) {
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    std::vector<std::pair<S, int64_t>> out;
+    for (int64_t i = b; i < e; ++i) {
+      m.knnContract(q3<S>(q, i), k, dist_bound, exclude ? (int64_t)exclude[i] : -1, out);
+      for (int j = 0; j < k; ++j) {
+        bool v = j < (int)out.size();
+        idx[i * k + j] = v ? (int32_t)out[(size_t)j].second : -1;
+        d2[i * k + j] = v ? (double)out[(size_t)j].first : -1.0;
+      }
+    }
+  });
+}
+}  // extern "C++"
+
+void oracle_knn_contract(void * hv, float const * q, int64_t n, int k, double dist_bound, int32_t const * exclude,
+                         int32_t * idx, double * d2, int nthreads) {
+  PointHandle * h = static_cast<PointHandle *>(hv);
+  if (h->fp64) knnContractImpl(h->d, q, n, k, dist_bound, exclude, idx, d2, nthreads);
+  else knnContractImpl(h->f, q, n, k, dist_bound, exclude, idx, d2, nthreads);
+}
+
+extern "C++" {
+template <class S>
+static void knnBruteImpl(float const * P, int64_t np, float const * q, int64_t n, int k, double dist_bound,
+                         int32_t const * exclude, int32_t * idx, double * d2, int nthreads) {
+  double mb = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    std::vector<std::pair<S, int64_t>> all;
+    for (int64_t i = b; i < e; ++i) {
+      V3<S> p = q3<S>(q, i);
+      all.clear();
+      for (int64_t j = 0; j < np; ++j) {
+        if (exclude && exclude[i] == j) continue;
+        S dd = squaredNorm(q3<S>(P, j) - p);
+        if (mb >= 0 && !((double)dd < mb)) continue;
+        all.emplace_back(dd, j);
+      }
+      size_t kk = std::min((size_t)k, all.size());
+      std::partial_sort(all.begin(), all.begin() + (long)kk, all.end());
+      for (int j = 0; j < k; ++j) {
+        bool v = j < (int)kk;
+        idx[i * k + j] = v ? (int32_t)all[(size_t)j].second : -1;
+        d2[i * k + j] = v ? (double)all[(size_t)j].first : -1.0;
+      }
+    }
+  });
+}
+}  // extern "C++"
+
+void oracle_knn_brute(float const * P, int64_t np, float const * q, int64_t n, int k, double dist_bound,
+                      int32_t const * exclude, int32_t * idx, double * d2, int fp64, int nthreads) {
+  if (fp64) knnBruteImpl<double>(P, np, q, n, k, dist_bound, exclude, idx, d2, nthreads);
+  else knnBruteImpl<float>(P, np, q, n, k, dist_bound, exclude, idx, d2, nthreads);
+}
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Sampler and random numbers
+//---------------------------------------------------------------------------------------------------------------------------
+
+int64_t oracle_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed,
+                              float * pos, float * nrm, int32_t * face) {
+  return sampleEvenlyByArea(V, nv, F, nf, n, seed, pos, nrm, face);
+}
+
+void oracle_thea_random_bits(uint32_t seed, int64_t n, uint32_t * out) {
+  TheaRandom r(seed);
+  for (int64_t i = 0; i < n; ++i) out[i] = r.bits();
+}
+
+// Independent known-answer source: the C++ standard library's MT19937 (same seeding and tempering as Thea's variant).
+void oracle_std_mt19937_bits(uint32_t seed, int64_t n, uint32_t * out) {
+  std::mt19937 g(seed);
+  for (int64_t i = 0; i < n; ++i) out[i] = (uint32_t)g();
+}
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Single-primitive entry points (FP32), for unit parity of the device functions
+//---------------------------------------------------------------------------------------------------------------------------
+
+// tris: 9 floats per triangle; per item i: closest point, squared distance, and the 'inside' flag of the projection.
+void oracle_triangle_closest_points(float const * tris, float const * p, int64_t n, float * cp, float * d2) {
+  for (int64_t i = 0; i < n; ++i) {
+    Tri<float> t(q3<float>(tris, 3 * i), q3<float>(tris, 3 * i + 1), q3<float>(tris, 3 * i + 2));
+    V3<float> c;
+    d2[i] = triangleClosestPoints(t, q3<float>(p, i), c);
+    cp[3 * i] = c.x; cp[3 * i + 1] = c.y; cp[3 * i + 2] = c.z;
+  }
+}
+
+void oracle_triangle_ray_times(float const * tris, float const * o, float const * d, int64_t n, float max_time,
+                               float * t) {
+  for (int64_t i = 0; i < n; ++i) {
+    Tri<float> tr(q3<float>(tris, 3 * i), q3<float>(tris, 3 * i + 1), q3<float>(tris, 3 * i + 2));
+    t[i] = triangleRayTime(tr, q3<float>(o, i), q3<float>(d, i), max_time);
+  }
+}
+
+// Per triangle: unit normal (3), plane offset, primary axis, area
+void oracle_triangle_props(float const * tris, int64_t n, float * normal, float * dist, int32_t * axis, float * area) {
+  for (int64_t i = 0; i < n; ++i) {
+    Tri<float> t(q3<float>(tris, 3 * i), q3<float>(tris, 3 * i + 1), q3<float>(tris, 3 * i + 2));
+    normal[3 * i] = t.normal.x; normal[3 * i + 1] = t.normal.y; normal[3 * i + 2] = t.normal.z;
+    dist[i] = t.dist; axis[i] = t.primary_axis; area[i] = t.area;
+  }
+}
+
+float oracle_box_ray_time(float const * lo, float const * hi, float const * o, float const * d, float max_time) {
+  Box<float> b;
+  b.lo = q3<float>(lo, 0); b.hi = q3<float>(hi, 0); b.is_null = false;
+  return boxRayIntersectionTime(b, q3<float>(o, 0), q3<float>(d, 0), max_time);
+}
+
+int64_t oracle_tree_depth(int64_t n, int max_leaf) { return treeDepth(n, max_leaf, 0.5f); }
+
+}  // extern "C"

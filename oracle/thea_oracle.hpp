@@ -1,0 +1,801 @@
+// TEST INFRASTRUCTURE ONLY -- the CPU oracle for the spatial-query hot path.
+//
+// This file restates, in plain C++17 without Eigen, the CPU algorithms of Thea's spatial-query path so that the CUDA
+// implementation can be checked against them. Only tests, the smoke check and the CPU-baseline legs of bench.py may
+// load it; the product library never links it, and nothing here is a fallback for the GPU path.
+//
+// Parity status: UNPINNED. The reference cannot be compiled in this environment (it needs Eigen >= 3.4, which is neither
+// vendored nor installed), and its own tests (Code/Source/Test/TestBvh.cpp) print results without asserting any value, so
+// no golden vector from the reference exists. The restatement follows the cited reference lines operation by operation;
+// the only partial known-answer pin is the Mersenne-Twister seeding and tempering, checked against std::mt19937 for the
+// outputs that Thea's variant shares with the standard generator.
+//
+// Arithmetic order. The reference computes in FP32 (Real = float, Code/Source/NumericType.hpp:40) through Eigen
+// fixed-size 3-vectors. Eigen reduces a 3-element sum (dot, squaredNorm) as e0 + (e1 + e2) when no SIMD packet fits the
+// size (the x86 SSE/AVX case: redux_novec_unroller splits the range in halves). Every reduction below uses that order, and
+// this file must be compiled with -ffp-contract=off so that no multiply-add is fused.
+//
+// Two result conventions are provided:
+//   * reference mode: the reference's own kd-tree build and traversal, whose ties go to the element found first in
+//     traversal order (strict-less replacement, Code/Source/Algorithms/BvhN.hpp:459-466);
+//   * contract mode: the same per-element arithmetic, with ties broken by the lowest element index. This is the
+//     structure-independent normalisation that the GPU path implements bit-exactly.
+// Each function is templated on the scalar type; instantiating it with double gives the FP64 twin used for error reports.
+
+#pragma once
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace oracle {
+
+//============================================================================================================================
+// Vectors (Eigen fixed-size 3-vector semantics, Code/Source/MatVec.hpp:56)
+//============================================================================================================================
+
+template <class S> struct V3 {
+  S x, y, z;
+  V3() : x(0), y(0), z(0) {}
+  V3(S a, S b, S c) : x(a), y(b), z(c) {}
+  S operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+  S & operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  bool operator==(V3 const & o) const { return x == o.x && y == o.y && z == o.z; }
+};
+
+template <class S> inline V3<S> operator+(V3<S> const & a, V3<S> const & b) { return V3<S>(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <class S> inline V3<S> operator-(V3<S> const & a, V3<S> const & b) { return V3<S>(a.x - b.x, a.y - b.y, a.z - b.z); }
+// scalar * vector and vector * scalar are both a per-component product
+template <class S> inline V3<S> operator*(S s, V3<S> const & a) { return V3<S>(s * a.x, s * a.y, s * a.z); }
+template <class S> inline V3<S> operator*(V3<S> const & a, S s) { return V3<S>(a.x * s, a.y * s, a.z * s); }
+template <class S> inline V3<S> operator/(V3<S> const & a, S s) { return V3<S>(a.x / s, a.y / s, a.z / s); }
+
+// Eigen redux order for 3 elements: e0 + (e1 + e2)
+template <class S> inline S dot(V3<S> const & a, V3<S> const & b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+template <class S> inline S squaredNorm(V3<S> const & a) { return a.x * a.x + (a.y * a.y + a.z * a.z); }
+template <class S> inline S norm(V3<S> const & a) { return std::sqrt(squaredNorm(a)); }
+template <class S> inline V3<S> cross(V3<S> const & a, V3<S> const & b) {
+  return V3<S>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// MatrixBase::normalized(): divide by the norm only if the squared norm is positive
+template <class S> inline V3<S> normalized(V3<S> const & a) {
+  S z = squaredNorm(a);
+  return z > S(0) ? a / std::sqrt(z) : a;
+}
+template <class S> inline V3<S> cwiseMin(V3<S> const & a, V3<S> const & b) {
+  return V3<S>(std::min(a.x, b.x), std::min(a.y, b.y), std::min(a.z, b.z));
+}
+template <class S> inline V3<S> cwiseMax(V3<S> const & a, V3<S> const & b) {
+  return V3<S>(std::max(a.x, b.x), std::max(a.y, b.y), std::max(a.z, b.z));
+}
+// Math::maxAbsAxis / maxAxis (Code/Source/MatrixUtil.hpp:84-115): first index of the maximum (Eigen visitor uses strict >)
+template <class S> inline int maxAbsAxis(V3<S> const & v) {
+  S a0 = std::fabs(v.x), a1 = std::fabs(v.y), a2 = std::fabs(v.z);
+  int m = 0; S best = a0;
+  if (a1 > best) { m = 1; best = a1; }
+  if (a2 > best) { m = 2; }
+  return m;
+}
+template <class S> inline int maxAxis(V3<S> const & v) {
+  int m = 0; S best = v.x;
+  if (v.y > best) { m = 1; best = v.y; }
+  if (v.z > best) { m = 2; }
+  return m;
+}
+
+template <class S> inline V3<S> load3(float const * p) { return V3<S>(S(p[0]), S(p[1]), S(p[2])); }
+
+//============================================================================================================================
+// Axis-aligned box (Code/Source/AxisAlignedBoxN.hpp)
+//============================================================================================================================
+
+template <class S> struct Box {
+  V3<S> lo, hi;
+  bool is_null = true;
+
+  // merge(point) / merge(box): AxisAlignedBoxN.hpp:237-271
+  void merge(V3<S> const & p) {
+    if (is_null) { lo = hi = p; is_null = false; }
+    else { lo = cwiseMin(lo, p); hi = cwiseMax(hi, p); }
+  }
+  void merge(Box const & b) {
+    if (!b.is_null) {
+      if (is_null) { lo = b.lo; hi = b.hi; is_null = false; }
+      else { lo = cwiseMin(lo, b.lo); hi = cwiseMax(hi, b.hi); }
+    }
+  }
+  // getCenter(): 0.5 * (hi + lo)
+  V3<S> center() const { return S(0.5) * (hi + lo); }
+  V3<S> extent() const { return hi - lo; }
+  // scaleCentered(scale): AxisAlignedBoxN.hpp:316-325
+  void scaleCentered(S s) {
+    if (!is_null) {
+      V3<S> c = center();
+      lo = s * (lo - c) + c;
+      hi = s * (hi - c) + c;
+    }
+  }
+  // squaredDistance(box): AxisAlignedBoxN.hpp:429-442
+  S squaredDistance(Box const & o) const {
+    if (is_null || o.is_null) return S(0);
+    V3<S> vmax = cwiseMin(hi, o.hi);
+    V3<S> vmin = cwiseMax(lo, o.lo);
+    V3<S> vdiff = vmin - vmax;
+    vdiff = cwiseMax(vdiff, V3<S>(0, 0, 0));
+    return squaredNorm(vdiff);
+  }
+  // squaredDistance(point): AxisAlignedBoxN.hpp:448-456
+  S squaredDistance(V3<S> const & p) const {
+    if (is_null) return S(0);
+    V3<S> vmax = cwiseMin(p, hi);
+    V3<S> vmin = cwiseMax(p, lo);
+    return squaredNorm(vmin - vmax);
+  }
+};
+
+// Math::eps(a, b) and fuzzyNe(a, 0) (Code/Source/Math.hpp:124-154)
+template <class S> inline bool fuzzyNeZero(S a) {
+  S const E = std::numeric_limits<S>::epsilon();
+  if (std::isinf(a)) return !(a == S(0) || std::fabs(a) <= E);
+  S larger = std::fabs(a);
+  S tol = larger > S(1) ? larger * E : E;
+  return !((a == S(0)) || std::fabs(a) <= tol);
+}
+
+// AxisAlignedBoxN::rayIntersection (...)::getTime (AxisAlignedBoxN.hpp:589-658): candidate-plane test; 0 if the origin is
+// inside, -1 on a miss.
+template <class S> S boxRayIntersectionTime(Box<S> const & b, V3<S> const & origin, V3<S> const & dir, S max_time) {
+  if (b.is_null) return S(-1);
+  if (max_time >= 0) {
+    S ray_sqlen = squaredNorm(dir);
+    S origin_sqdist = b.squaredDistance(origin);
+    if (origin_sqdist > max_time * max_time * ray_sqlen) return S(-1);
+  }
+  V3<S> max_t(-1, -1, -1), location;
+  bool inside = true;
+  for (int i = 0; i < 3; ++i) {
+    if (origin[i] < b.lo[i]) {
+      location[i] = b.lo[i];
+      inside = false;
+      if (fuzzyNeZero(dir[i])) max_t[i] = (b.lo[i] - origin[i]) / dir[i];
+    } else if (origin[i] > b.hi[i]) {
+      location[i] = b.hi[i];
+      inside = false;
+      if (fuzzyNeZero(dir[i])) max_t[i] = (b.hi[i] - origin[i]) / dir[i];
+    }
+  }
+  if (inside) return S(0);
+  int which = 0;
+  for (int i = 1; i < 3; ++i)
+    if (max_t[i] > max_t[which]) which = i;
+  if (max_t[which] < S(-0.5)) return S(-1);
+  for (int i = 0; i < 3; ++i) {
+    if (i != which) {
+      location[i] = origin[i] + max_t[which] * dir[i];
+      if (location[i] < b.lo[i] || location[i] > b.hi[i]) return S(-1);
+    }
+  }
+  return max_t[which];
+}
+
+//============================================================================================================================
+// Triangle (Code/Source/Triangle3.hpp, Code/Source/HyperplaneN.hpp, Code/Source/Hyperplane3.hpp)
+//============================================================================================================================
+
+template <class S> struct Tri {
+  V3<S> v0, v1, v2;
+  V3<S> normal;  // plane normal (unit), Hyperplane3.hpp:34-41
+  S dist;        // plane offset: normal . v0
+  int primary_axis;
+  V3<S> edge01, edge02;
+  S area;
+
+  Tri() {}
+  Tri(V3<S> a, V3<S> b, V3<S> c) : v0(a), v1(b), v2(c) { update(); }
+
+  // TriangleN<3>::update(): Triangle3.hpp:143-155
+  void update() {
+    normal = normalized(cross(v1 - v0, v2 - v0));
+    dist = dot(normal, v0);
+    primary_axis = maxAbsAxis(normal);
+    edge01 = v1 - v0;
+    edge02 = v2 - v0;
+    area = S(0.5) * std::fabs(dot(normal, cross(edge01, edge02)));
+  }
+
+  // getBounds(): Triangle3.hpp:215-219
+  Box<S> bounds() const {
+    Box<S> b;
+    b.lo = cwiseMin(v0, cwiseMin(v1, v2));
+    b.hi = cwiseMax(v0, cwiseMax(v1, v2));
+    b.is_null = false;
+    return b;
+  }
+};
+
+// Triangle3Internal::closestPointOnLineSegment: Triangle3.hpp:1311-1338
+template <class S>
+V3<S> closestPointOnLineSegment(V3<S> const & v0, V3<S> const & v1, V3<S> const & dir, S len, V3<S> const & p) {
+  V3<S> c = p - v0;
+  S t = dot(dir, c);
+  if (t <= S(0)) return v0;
+  else if (t >= len) return v1;
+  else return v0 + dir * t;
+}
+
+// Triangle3Internal::closestPointOnTrianglePerimeter: Triangle3.hpp:1342-1412
+template <class S> V3<S> closestPointOnTrianglePerimeter(V3<S> const & v0, V3<S> const & v1, V3<S> const & v2,
+                                                         V3<S> const & p) {
+  V3<S> v[3] = {v0, v1, v2};
+  V3<S> dir[3] = {v1 - v0, v2 - v1, v0 - v2};
+  S len[3];
+  for (int i = 0; i < 3; ++i) {
+    len[i] = norm(dir[i]);
+    dir[i] = dir[i] / len[i];
+  }
+  static int const next[3] = {1, 2, 0};
+  V3<S> r[3];
+  S d[3];
+  for (int i = 0; i < 3; ++i) {
+    r[i] = closestPointOnLineSegment(v[i], v[next[i]], dir[i], len[i], p);
+    d[i] = squaredNorm(r[i] - p);
+  }
+  int e;
+  if (d[0] < d[1]) e = (d[0] < d[2]) ? 0 : 2;
+  else e = (d[1] < d[2]) ? 1 : 2;
+  return r[e];
+}
+
+// Triangle3Internal::isPointInsideTriangle: Triangle3.hpp:1416-1462
+template <class S>
+bool isPointInsideTriangle(V3<S> const & v0, V3<S> const & v1, V3<S> const & v2, int primary_axis, V3<S> const & p) {
+  int i, j;
+  switch (primary_axis) {
+    case 1: i = 2; j = 0; break;
+    case 2: i = 0; j = 1; break;
+    default: i = 1; j = 2;
+  }
+  auto area2 = [i, j](V3<S> const & d, V3<S> const & e, V3<S> const & f) {
+    return (e[i] - d[i]) * (f[j] - d[j]) - (f[i] - d[i]) * (e[j] - d[j]);
+  };
+  S area = area2(v0, v1, v2);
+  if (area == S(0)) return v0 == p;
+  S inv_area = S(1) / area;
+  S b0 = area2(p, v1, v2) * inv_area;
+  if ((b0 < S(0)) || (b0 > S(1))) return false;
+  S b1 = area2(v0, p, v2) * inv_area;
+  if ((b1 < S(0)) || (b1 > S(1))) return false;
+  S b2 = S(1) - b0 - b1;
+  return (b2 >= S(0)) && (b2 <= S(1));
+}
+
+// TriangleN<3>::closestPoint: Triangle3.hpp:294-304 with HyperplaneN::closestPoint (HyperplaneN.hpp:145-160)
+template <class S> V3<S> triangleClosestPoint(Tri<S> const & t, V3<S> const & p) {
+  S sd = dot(p, t.normal) - t.dist;
+  V3<S> proj = p - sd * t.normal;
+  if (isPointInsideTriangle(t.v0, t.v1, t.v2, t.primary_axis, proj)) return proj;
+  return closestPointOnTrianglePerimeter(t.v0, t.v1, t.v2, p);
+}
+
+// MetricL2Impl<Triangle, Point>::closestPoints: MetricL2.hpp:209-215 -- squared distance, closest point on the triangle
+template <class S> S triangleClosestPoints(Tri<S> const & t, V3<S> const & p, V3<S> & cp) {
+  cp = triangleClosestPoint(t, p);
+  return squaredNorm(cp - p);
+}
+
+// Triangle3Internal::rayTriangleIntersectionTime: Triangle3.hpp:1466-1524 (Eberly). Returns -1 on a miss.
+template <class S>
+S rayTriangleIntersectionTime(V3<S> const & origin, V3<S> const & dir, V3<S> const & v0, V3<S> const & e01,
+                              V3<S> const & e02) {
+  S const EPS = std::numeric_limits<S>::epsilon();
+  V3<S> diff = origin - v0;
+  V3<S> n = cross(e01, e02);
+  S DdN = dot(dir, n);
+  int sign;
+  if (DdN > EPS) sign = 1;
+  else if (DdN < -EPS) { sign = -1; DdN = -DdN; }
+  else return S(-1);
+  S DdQxE2 = S(sign) * dot(dir, cross(diff, e02));
+  if (DdQxE2 >= S(0)) {
+    S DdE1xQ = S(sign) * dot(dir, cross(e01, diff));
+    if (DdE1xQ >= S(0)) {
+      if (DdQxE2 + DdE1xQ <= DdN) {
+        S QdN = S(-sign) * dot(diff, n);
+        if (QdN >= S(0)) return QdN / DdN;
+      }
+    }
+  }
+  return S(-1);
+}
+
+// TriangleN<3>::rayIntersection time: Triangle3.hpp:542-552 (hit if t >= 0 and (max_time < 0 or t <= max_time))
+template <class S> S triangleRayTime(Tri<S> const & t, V3<S> const & o, V3<S> const & d, S max_time) {
+  S time = rayTriangleIntersectionTime(o, d, t.v0, t.edge01, t.edge02);
+  if (time >= S(0) && (max_time < S(0) || time <= max_time)) return time;
+  return S(-1);
+}
+
+//============================================================================================================================
+// Median-split kd-tree (BvhN::initTree / createKdTree, BvhN.hpp:1366-1525)
+//============================================================================================================================
+
+// Math::treeDepth: Code/Source/Math.cpp:23-36
+inline int64_t treeDepth(int64_t n, int max_leaf, float max_child_fraction) {
+  if (n <= 0) return 0;
+  // the fraction is a Real (float), so the reference takes a float logarithm here
+  double log_inv_mcf = -(double)std::log(max_child_fraction);
+  int64_t d = (int64_t)std::ceil(std::log(n / (double)max_leaf) / log_inv_mcf);
+  return d < 0 ? 0 : d;
+}
+
+template <class S> struct KdNode {
+  int64_t depth = 0;
+  Box<S> bounds;
+  int64_t first = 0, count = 0;  // element index range in the tree's index array
+  int64_t child[2] = {-1, -1};
+  bool isLeaf() const { return child[0] < 0 && child[1] < 0; }
+};
+
+// A kd-tree over elements that expose bounds() (triangles) or are points. ElemBounds(i) gives the element's box.
+template <class S> struct KdTree {
+  std::vector<KdNode<S>> nodes;
+  std::vector<int64_t> index;  // element indices; each node owns a contiguous range
+  int64_t max_depth = 0;
+  int64_t max_leaf = 5;
+
+  // initTree + createKdTree. bounds_of(i) returns the element box, center_of(i) the split key (BoundedTraitsN::getCenter).
+  template <class BoundsF, class CenterF>
+  void build(int64_t n, BoundsF bounds_of, CenterF center_of, int64_t max_leaf_ = -1) {
+    nodes.clear();
+    index.resize((size_t)n);
+    if (n <= 0) return;
+    max_leaf = max_leaf_ <= 0 ? 5 : max_leaf_;
+    max_depth = treeDepth(n, (int)max_leaf, 0.5f);
+    for (int64_t i = 0; i < n; ++i) index[(size_t)i] = i;
+    nodes.reserve((size_t)(4 * n / max_leaf + 16));
+    KdNode<S> root;
+    root.depth = 0; root.first = 0; root.count = n;
+    for (int64_t i = 0; i < n; ++i) root.bounds.merge(bounds_of(i));
+    nodes.push_back(root);
+    recurse(0, bounds_of, center_of);
+    nodes[0].bounds.scaleCentered(S(1.05f));  // BOUNDS_EXPANSION_FACTOR, BvhN.hpp:1437, 2458
+  }
+
+  template <class BoundsF, class CenterF> void recurse(int64_t ni, BoundsF & bounds_of, CenterF & center_of) {
+    KdNode<S> start = nodes[(size_t)ni];
+    if (start.depth >= max_depth || start.count <= max_leaf) return;
+    int coord = maxAxis(start.bounds.extent());
+    int64_t mid = start.count / 2;
+    int64_t * base = index.data() + start.first;
+    std::nth_element(base, base + mid, base + start.count, [&](int64_t a, int64_t b) {
+      return center_of(a)[coord] < center_of(b)[coord];
+    });
+    for (int c = 0; c < 2; ++c) {
+      KdNode<S> child;
+      child.depth = start.depth + 1;
+      int64_t b = (c == 0) ? 0 : start.count - mid;
+      int64_t e = (c == 0) ? start.count - mid : start.count;
+      child.first = start.first + b;
+      child.count = e - b;
+      for (int64_t k = child.first; k < child.first + child.count; ++k) child.bounds.merge(bounds_of(index[(size_t)k]));
+      int64_t ci = (int64_t)nodes.size();
+      nodes.push_back(child);
+      nodes[(size_t)ni].child[c] = ci;
+      recurse(ci, bounds_of, center_of);
+      nodes[(size_t)ci].bounds.scaleCentered(S(1.05f));
+    }
+  }
+};
+
+// distanceLessThan: BvhN.hpp:178-181 (negative = "none", greater than any non-negative value)
+template <class U, class V> inline bool distanceLessThan(U lhs, V rhs) { return (lhs >= 0 && (rhs < 0 || lhs < rhs)); }
+
+// ChildDistanceArray ordering for two children (BoundedSortedArrayN<2, NodeDistance>::insert, stable on ties)
+template <class D> inline void orderTwo(D d0, D d1, int & first, int & second) {
+  if (distanceLessThan(d1, d0)) { first = 1; second = 0; }
+  else { first = 0; second = 1; }
+}
+
+//============================================================================================================================
+// Mesh index: triangles + kd-tree
+//============================================================================================================================
+
+template <class S> struct MeshIndex {
+  std::vector<Tri<S>> tris;
+  KdTree<S> tree;
+
+  void init(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t max_leaf = -1) {
+    (void)nv;
+    tris.resize((size_t)nf);
+    for (int64_t f = 0; f < nf; ++f)
+      tris[(size_t)f] = Tri<S>(load3<S>(V + 3 * (int64_t)F[3 * f]), load3<S>(V + 3 * (int64_t)F[3 * f + 1]),
+                               load3<S>(V + 3 * (int64_t)F[3 * f + 2]));
+    std::vector<Box<S>> boxes((size_t)nf);
+    std::vector<V3<S>> centers((size_t)nf);
+    for (size_t f = 0; f < (size_t)nf; ++f) { boxes[f] = tris[f].bounds(); centers[f] = boxes[f].center(); }
+    tree.build(nf, [&](int64_t i) -> Box<S> const & { return boxes[(size_t)i]; },
+               [&](int64_t i) -> V3<S> const & { return centers[(size_t)i]; }, max_leaf);
+  }
+
+  // ---- closest point, reference mode (closestElement -> closestPair -> processNeighbors, BvhN.hpp:1050-1114,1868-1893,
+  //      2038-2089). Returns the element index or -1; mad is the squared distance as stored by the reference (double).
+  int64_t closestRef(V3<S> const & q, double dist_bound, double & mad_out, V3<S> & cp_out) const {
+    if (tree.nodes.empty()) return -1;
+    Box<S> qb; qb.merge(q);
+    double mon_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    if (mon_bound >= 0) {
+      double lb = (double)qb.squaredDistance(tree.nodes[0].bounds);
+      if (lb >= 0 && lb > mon_bound) return -1;
+    }
+    int64_t best_idx = -1;
+    double best_mad = mon_bound >= 0 ? mon_bound : -1;
+    V3<S> best_cp;
+    closestRefRec(0, q, qb, best_idx, best_mad, best_cp);
+    if (best_idx >= 0) { mad_out = best_mad; cp_out = best_cp; }
+    return best_idx;
+  }
+
+  void closestRefRec(int64_t ni, V3<S> const & q, Box<S> const & qb, int64_t & best_idx, double & best_mad,
+                     V3<S> & best_cp) const {
+    KdNode<S> const & n = tree.nodes[(size_t)ni];
+    if (n.isLeaf()) {
+      for (int64_t k = n.first; k < n.first + n.count; ++k) {
+        int64_t idx = tree.index[(size_t)k];
+        V3<S> cp;
+        double mad = (double)triangleClosestPoints(tris[(size_t)idx], q, cp);
+        // allows(NeighborPair(-1, -1, mad)) then operator(): replace on strict less (BvhN.hpp:451-466)
+        if (mad < 0 || best_mad < 0 || mad < best_mad) {
+          if (best_mad < 0 || mad < best_mad) { best_mad = mad; best_idx = idx; best_cp = cp; }
+        }
+      }
+      return;
+    }
+    double d[2];
+    for (int c = 0; c < 2; ++c) d[c] = (double)qb.squaredDistance(tree.nodes[(size_t)n.child[c]].bounds);
+    int o[2];
+    orderTwo(d[0], d[1], o[0], o[1]);
+    for (int s = 0; s < 2; ++s) {
+      double cd = d[o[s]];
+      if (cd < 0 || best_mad < 0 || cd < best_mad) closestRefRec(n.child[o[s]], q, qb, best_idx, best_mad, best_cp);
+    }
+  }
+
+  // ---- closest point, contract mode: lowest index among equal squared distances; elements accepted only if
+  //      (double)d2 < dist_bound^2 when dist_bound >= 0 (the reference's strict bound test).
+  int64_t closestContract(V3<S> const & q, double dist_bound, S & best_d2, V3<S> & cp_out) const {
+    if (tree.nodes.empty()) return -1;
+    Box<S> qb; qb.merge(q);
+    double mon_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    int64_t best_idx = -1;
+    S bd2 = std::numeric_limits<S>::infinity();
+    V3<S> bcp;
+    std::vector<int64_t> stack;
+    stack.push_back(0);
+    while (!stack.empty()) {
+      int64_t ni = stack.back(); stack.pop_back();
+      KdNode<S> const & n = tree.nodes[(size_t)ni];
+      S bd = qb.squaredDistance(n.bounds);
+      if (best_idx >= 0 && bd > bd2) continue;
+      if (mon_bound >= 0 && (double)bd > mon_bound) continue;
+      if (n.isLeaf()) {
+        for (int64_t k = n.first; k < n.first + n.count; ++k) {
+          int64_t idx = tree.index[(size_t)k];
+          V3<S> cp;
+          S d2 = triangleClosestPoints(tris[(size_t)idx], q, cp);
+          if (!(d2 == d2)) continue;  // a NaN distance (coincident vertices) is never selected
+          if (mon_bound >= 0 && !((double)d2 < mon_bound)) continue;
+          if (best_idx < 0 || d2 < bd2 || (d2 == bd2 && idx < best_idx)) { bd2 = d2; best_idx = idx; bcp = cp; }
+        }
+      } else {
+        stack.push_back(n.child[1]);
+        stack.push_back(n.child[0]);
+      }
+    }
+    if (best_idx >= 0) { best_d2 = bd2; cp_out = bcp; }
+    return best_idx;
+  }
+
+  // ---- ray first hit, reference mode (rayStructureIntersection, BvhN.hpp:1292-1316, 2241-2291)
+  struct RayHit { S t; int64_t idx; };
+
+  RayHit rayRef(V3<S> const & o, V3<S> const & d, S max_time) const {
+    RayHit none{S(-1), -1};
+    if (tree.nodes.empty()) return none;
+    if (!(boxRayIntersectionTime(tree.nodes[0].bounds, o, d, max_time) > S(-0.5))) return none;
+    return rayRefRec(0, o, d, max_time);
+  }
+
+  RayHit rayRefRec(int64_t ni, V3<S> const & o, V3<S> const & d, S max_time) const {
+    KdNode<S> const & n = tree.nodes[(size_t)ni];
+    RayHit best{max_time, -1};
+    bool found = false;
+    if (n.isLeaf()) {
+      for (int64_t k = n.first; k < n.first + n.count; ++k) {
+        int64_t idx = tree.index[(size_t)k];
+        S t = triangleRayTime(tris[(size_t)idx], o, d, best.t);
+        if (distanceLessThan(t, best.t)) { best.t = t; best.idx = idx; found = true; }
+      }
+      return found ? best : RayHit{S(-1), -1};
+    }
+    S bt[2];
+    for (int c = 0; c < 2; ++c) bt[c] = boxRayIntersectionTime(tree.nodes[(size_t)n.child[c]].bounds, o, d, max_time);
+    int ord[2];
+    orderTwo(bt[0], bt[1], ord[0], ord[1]);
+    for (int s = 0; s < 2; ++s) {
+      if (distanceLessThan(bt[ord[s]], best.t)) {
+        RayHit h = rayRefRec(n.child[ord[s]], o, d, best.t);
+        if (distanceLessThan(h.t, best.t)) { best = h; found = true; }
+      }
+    }
+    return found ? best : RayHit{S(-1), -1};
+  }
+};
+
+// Conservative slab test used only by contract-mode traversal (returns entry time clamped at 0, or -1 on a miss). The
+// box is widened by a relative margin so that no triangle hit inside it can be rejected by rounding.
+template <class S> S slabEntry(Box<S> const & b, V3<S> const & o, V3<S> const & d) {
+  S tmin = S(0), tmax = std::numeric_limits<S>::infinity();
+  for (int i = 0; i < 3; ++i) {
+    S pad = (std::fabs(b.lo[i]) + std::fabs(b.hi[i]) + (b.hi[i] - b.lo[i])) * S(1e-5) + S(1e-30);
+    S lo = b.lo[i] - pad, hi = b.hi[i] + pad;
+    if (d[i] == S(0)) {
+      if (o[i] < lo || o[i] > hi) return S(-1);
+      continue;
+    }
+    S t0 = (lo - o[i]) / d[i], t1 = (hi - o[i]) / d[i];
+    if (t0 > t1) std::swap(t0, t1);
+    tmin = std::max(tmin, t0);
+    tmax = std::min(tmax, t1);
+    if (tmin > tmax) return S(-1);
+  }
+  return tmin;
+}
+
+// ---- ray first hit, contract mode: smallest valid t, lowest index among equal t
+template <class S> typename MeshIndex<S>::RayHit rayContract(MeshIndex<S> const & m, V3<S> const & o, V3<S> const & d,
+                                                             S max_time) {
+  typename MeshIndex<S>::RayHit best{S(-1), -1};
+  if (m.tree.nodes.empty()) return best;
+  std::vector<int64_t> stack;
+  stack.push_back(0);
+  while (!stack.empty()) {
+    int64_t ni = stack.back(); stack.pop_back();
+    KdNode<S> const & n = m.tree.nodes[(size_t)ni];
+    S te = slabEntry(n.bounds, o, d);
+    if (te < S(0)) continue;
+    if (best.idx >= 0 && te > best.t * (S(1) + S(1e-5))) continue;
+    if (max_time >= S(0) && te > max_time * (S(1) + S(1e-5))) continue;
+    if (n.isLeaf()) {
+      for (int64_t k = n.first; k < n.first + n.count; ++k) {
+        int64_t idx = m.tree.index[(size_t)k];
+        S t = triangleRayTime(m.tris[(size_t)idx], o, d, max_time);
+        if (t < S(0)) continue;
+        if (best.idx < 0 || t < best.t || (t == best.t && idx < best.idx)) { best.t = t; best.idx = idx; }
+      }
+    } else {
+      stack.push_back(n.child[1]);
+      stack.push_back(n.child[0]);
+    }
+  }
+  return best;
+}
+
+//============================================================================================================================
+// Point index + k nearest neighbours (kClosestPairs + KClosestPairsFunctor + BoundedSortedArrayN, BvhN.hpp:474-500,
+// 1139-1146; Code/Source/BoundedSortedArrayN.hpp:137-214; NeighborPair ordering ProximityQueryStructureN.hpp:117-123)
+//============================================================================================================================
+
+struct Neighbor { double mad; int64_t idx; };
+
+template <class S> struct PointIndex {
+  std::vector<V3<S>> pts;
+  std::vector<Box<S>> boxes;
+  KdTree<S> tree;
+
+  void init(float const * P, int64_t n, int64_t max_leaf = -1) {
+    pts.resize((size_t)n);
+    boxes.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i) { pts[(size_t)i] = load3<S>(P + 3 * i); boxes[(size_t)i].merge(pts[(size_t)i]); }
+    tree.build(n, [&](int64_t i) -> Box<S> const & { return boxes[(size_t)i]; },
+               [&](int64_t i) -> V3<S> const & { return pts[(size_t)i]; }, max_leaf);
+  }
+
+  static S pointSqDist(V3<S> const & a, V3<S> const & b) { return squaredNorm(a - b); }
+
+  // reference mode: results sorted by increasing distance; ties keep discovery order. exclude < 0: no filter.
+  void knnRef(V3<S> const & q, int k, double dist_bound, int64_t exclude, std::vector<Neighbor> & out) const {
+    out.clear();
+    if (tree.nodes.empty() || k <= 0) return;
+    double mad_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    Box<S> qb; qb.merge(q);
+    // root pruning: processNeighbors public (BvhN.hpp:1193-1206)
+    double rd = (double)qb.squaredDistance(tree.nodes[0].bounds);
+    if (!boxAllows(rd, out, k)) return;
+    knnRefRec(0, q, qb, k, mad_bound, exclude, out);
+  }
+
+  // KClosestPairsFunctor::allows for an incomplete pair (-1, -1, mad): insertable with query index -1 (<= semantics)
+  static bool boxAllows(double mad, std::vector<Neighbor> const & arr, int k) {
+    if (mad < 0) return true;
+    if ((int)arr.size() < k) return true;
+    return mad <= arr.back().mad;
+  }
+
+  void knnRefRec(int64_t ni, V3<S> const & q, Box<S> const & qb, int k, double mad_bound, int64_t exclude,
+                 std::vector<Neighbor> & arr) const {
+    KdNode<S> const & n = tree.nodes[(size_t)ni];
+    if (n.isLeaf()) {
+      for (int64_t kk = n.first; kk < n.first + n.count; ++kk) {
+        int64_t idx = tree.index[(size_t)kk];
+        if (idx == exclude) continue;  // FilterSelf (PointSet3.hpp:576-583) via elementPassesFilters
+        bool dup = false;
+        for (auto const & e : arr) if (e.idx == idx) { dup = true; break; }
+        if (dup) continue;
+        double mad = (double)pointSqDist(pts[(size_t)idx], q);
+        if (!boxAllows(mad, arr, k)) continue;
+        // operator(): (mad_bound < 0 || mad < mad_bound) && isInsertable(pair) -- strict for complete pairs
+        if ((mad_bound < 0 || mad < mad_bound) && ((int)arr.size() < k || mad < arr.back().mad)) {
+          // upperBound: first element strictly greater, i.e. after all equal distances (stable)
+          size_t ub = 0;
+          while (ub < arr.size() && !(mad < arr[ub].mad)) ++ub;
+          arr.insert(arr.begin() + (long)ub, Neighbor{mad, idx});
+          if ((int)arr.size() > k) arr.pop_back();
+        }
+      }
+      return;
+    }
+    double d[2];
+    for (int c = 0; c < 2; ++c) d[c] = (double)qb.squaredDistance(tree.nodes[(size_t)n.child[c]].bounds);
+    int o[2];
+    orderTwo(d[0], d[1], o[0], o[1]);
+    for (int s = 0; s < 2; ++s)
+      if (boxAllows(d[o[s]], arr, k)) knnRefRec(n.child[o[s]], q, qb, k, mad_bound, exclude, arr);
+  }
+
+  // contract mode: the k smallest (d2, index) pairs in lexicographic order
+  void knnContract(V3<S> const & q, int k, double dist_bound, int64_t exclude, std::vector<std::pair<S, int64_t>> & out)
+      const {
+    out.clear();
+    if (tree.nodes.empty() || k <= 0) return;
+    double mad_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    Box<S> qb; qb.merge(q);
+    std::vector<int64_t> stack;
+    stack.push_back(0);
+    while (!stack.empty()) {
+      int64_t ni = stack.back(); stack.pop_back();
+      KdNode<S> const & n = tree.nodes[(size_t)ni];
+      S bd = qb.squaredDistance(n.bounds);
+      if ((int)out.size() == k && bd > out.back().first) continue;
+      if (mad_bound >= 0 && (double)bd > mad_bound) continue;
+      if (n.isLeaf()) {
+        for (int64_t kk = n.first; kk < n.first + n.count; ++kk) {
+          int64_t idx = tree.index[(size_t)kk];
+          if (idx == exclude) continue;
+          S d2 = pointSqDist(pts[(size_t)idx], q);
+          if (mad_bound >= 0 && !((double)d2 < mad_bound)) continue;
+          std::pair<S, int64_t> cand(d2, idx);
+          if ((int)out.size() == k && !(cand < out.back())) continue;
+          auto it = std::upper_bound(out.begin(), out.end(), cand);
+          out.insert(it, cand);
+          if ((int)out.size() > k) out.pop_back();
+        }
+      } else {
+        stack.push_back(n.child[1]);
+        stack.push_back(n.child[0]);
+      }
+    }
+  }
+};
+
+//============================================================================================================================
+// Thea's Mersenne-Twister variant (Code/Source/Random.hpp:48-228, Code/Source/Random.cpp:49-157)
+//============================================================================================================================
+
+struct TheaRandom {
+  static constexpr int N = 624, M = 397, R = 31, U = 11, Sh = 7, T = 15, L = 18;
+  static constexpr uint32_t A = 0x9908B0DFu, B = 0x9D2C5680u, C = 0xEFC60000u;
+  uint32_t state[N];
+  int index;
+
+  // Random(uint32 seed): Random.cpp:49-60 (leaves index == N, so the first draw regenerates)
+  explicit TheaRandom(uint32_t seed) {
+    state[0] = seed;
+    for (index = 1; index < N; ++index)
+      state[index] = 1812433253u * (state[index - 1] ^ (state[index - 1] >> 30)) + (uint32_t)index;
+  }
+
+  // generate(): Random.cpp:99-132. The second loop starts at N - M + 1, so state[N - M] keeps its old value.
+  void generate() {
+    uint32_t const LOWER = (1u << R) - 1u, UPPER = 0xFFFFFFFFu << R;
+    uint32_t const mag01[2] = {0u, A};
+    for (int i = 0; i < N - M; ++i) {
+      uint32_t x = (state[i] & UPPER) | (state[i + 1] & LOWER);
+      state[i] = state[i + M] ^ (x >> 1) ^ mag01[x & 1u];
+    }
+    for (int i = N - M + 1; i < N - 1; ++i) {
+      uint32_t x = (state[i] & UPPER) | (state[i + 1] & LOWER);
+      state[i] = state[i + (M - N)] ^ (x >> 1) ^ mag01[x & 1u];
+    }
+    uint32_t y = (state[N - 1] & UPPER) | (state[0] & LOWER);
+    state[N - 1] = state[M - 1] ^ (y >> 1) ^ mag01[y & 1u];
+    index = 0;
+  }
+
+  // bits(): Random.cpp:68-97
+  uint32_t bits() {
+    if ((uint32_t)index >= (uint32_t)N) { generate(); index = 0; }
+    uint32_t r = state[index++];
+    r ^= r >> U;
+    r ^= (r << Sh) & B;
+    r ^= (r << T) & C;
+    r ^= r >> L;
+    return r;
+  }
+
+  // uniform01(): Random.hpp:126-131 -- (float)bits() * (1.0f / (float)0xFFFFFFFF)
+  float uniform01() {
+    static float const NORM = 1.0f / (float)0xFFFFFFFFul;
+    return (float)bits() * NORM;
+  }
+};
+
+//============================================================================================================================
+// MeshSampler::sampleEvenlyByArea, EXACT count mode (Code/Source/Algorithms/MeshSampler.hpp:100-204) with
+// TriangleN<3>::randomPoint (Triangle3.hpp:179-195), drawing from an explicit TheaRandom instead of Random::common().
+//============================================================================================================================
+
+inline int64_t sampleEvenlyByArea(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed,
+                                  float * pos, float * nrm, int32_t * face) {
+  (void)nv;
+  if (n <= 0 || nf <= 0) return 0;
+  std::vector<Tri<float>> tris((size_t)nf);
+  for (int64_t f = 0; f < nf; ++f)
+    tris[(size_t)f] = Tri<float>(load3<float>(V + 3 * (int64_t)F[3 * f]), load3<float>(V + 3 * (int64_t)F[3 * f + 1]),
+                                 load3<float>(V + 3 * (int64_t)F[3 * f + 2]));
+  double total_area = 0;
+  for (int64_t i = 0; i < nf; ++i) total_area += tris[(size_t)i].area;
+  if (total_area <= 0) return 0;
+  std::vector<double> cum((size_t)nf);
+  cum[0] = tris[0].area;
+  for (size_t i = 1; i < cum.size(); ++i) cum[i] = cum[i - 1] + tris[i].area;
+  TheaRandom rng(seed);
+  double const * first = cum.data();
+  double const * last = first + cum.size();
+  for (int64_t i = 0; i < n; ++i) {
+    double t = rng.uniform01() * total_area;
+    int64_t ti = std::min((int64_t)(std::lower_bound(first, last, t) - first), nf - 1);
+    Tri<float> const & tr = tris[(size_t)ti];
+    float s = rng.uniform01();
+    float u = rng.uniform01();
+    if (s + u > 1) { u = 1 - u; s = 1 - s; }
+    V3<float> p = s * tr.edge01 + u * tr.edge02 + tr.v0;
+    pos[3 * i] = p.x; pos[3 * i + 1] = p.y; pos[3 * i + 2] = p.z;
+    if (nrm) { nrm[3 * i] = tr.normal.x; nrm[3 * i + 1] = tr.normal.y; nrm[3 * i + 2] = tr.normal.z; }
+    if (face) face[i] = (int32_t)ti;
+  }
+  return n;
+}
+
+//============================================================================================================================
+// Thread pool helper for the CPU baseline: static partition of [0, n) over nthreads std::threads.
+//============================================================================================================================
+
+template <class F> void parallelFor(int64_t n, int nthreads, F f) {
+  if (nthreads <= 1 || n < 2) { f((int64_t)0, n); return; }
+  int64_t chunk = (n + nthreads - 1) / nthreads;
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t) {
+    int64_t b = t * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([=]() { f(b, e); });
+  }
+  for (auto & x : th) x.join();
+}
+
+}  // namespace oracle

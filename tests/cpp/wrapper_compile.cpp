@@ -1,0 +1,39 @@
+// Compiles the C++ wrapper against the library. With --no-device it only checks error reporting (no CUDA calls);
+// otherwise it runs one closest-point, ray and k-NN query on a tetrahedron and checks the answers.
+#include "thea_gpu.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+int main(int argc, char ** argv) {
+  bool no_device = argc > 1 && std::strcmp(argv[1], "--no-device") == 0;
+  if (thea_abi_version() != THEA_GPU_ABI_VERSION) return 1;
+  try {
+    thea_gpu::MeshBvh bad(nullptr, 0, nullptr, 0);
+    return 2;  // must have thrown
+  } catch (thea_gpu::Exception const & e) {
+    if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 3;
+  }
+  if (no_device) return 0;
+
+  float V[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+  int32_t F[] = {0, 1, 2, 0, 1, 3, 0, 2, 3, 1, 2, 3};
+  thea_gpu::MeshBvh mesh(V, 4, F, 4);
+  float q[3] = {0.25f, 0.25f, -1.0f};
+  double dist = -1;
+  float cp[3];
+  int64_t idx = mesh.closestElement(q, -1, &dist, cp);
+  if (idx != 0 || std::fabs(dist - 1.0) > 1e-6 || cp[2] != 0.0f) { std::printf("closest %lld %f\n", (long long)idx, dist); return 4; }
+  float o[3] = {0.2f, 0.2f, 2.0f}, d[3] = {0, 0, -1}, t = 0;
+  int32_t ti = -1;
+  mesh.rayStructureIntersection(o, d, 1, &t, &ti);
+  if (ti != 3) { std::printf("ray %d %f\n", ti, t); return 5; }
+  thea_gpu::PointBvh pts(V, 4);
+  int32_t ki[2];
+  float kd[2];
+  pts.kClosestPairs(q, 1, 2, ki, kd);
+  if (ki[0] != 0 || ki[1] != 1) { std::printf("knn %d %d\n", ki[0], ki[1]); return 6; }
+  std::printf("wrapper ok\n");
+  return 0;
+}

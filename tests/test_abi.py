@@ -1,0 +1,111 @@
+"""CPU tests of the C ABI: the library builds for sm_103a, loads, exports every symbol the header declares, and rejects
+bad arguments before touching the device."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "thea_gpu.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"THEA_API\s+[^;(]*?\b(thea_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from thea_gb300 import build as B
+    B.build()
+    from thea_gb300 import _native as N
+    return N.lib()
+
+
+def test_header_declares_the_query_api():
+    names = declared_symbols()
+    for required in ("thea_mesh_bvh_build", "thea_point_bvh_build", "thea_closest_element", "thea_ray_intersection",
+                     "thea_k_closest", "thea_k_closest_self", "thea_sample_by_area", "thea_bvh_destroy"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from thea_gb300 import _native as N
+    out = subprocess.run(["nm", "-D", "--defined-only", N.LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = set(line.split()[-1] for line in out.splitlines() if " T " in line)
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    # and nothing else of ours leaks
+    extra = sorted(s for s in exported if s.startswith("thea_") and s not in declared_symbols())
+    assert not extra, extra
+    # the ctypes signature table covers the header
+    assert sorted(N.SIGNATURES) == declared_symbols()
+
+
+def test_library_is_built_for_sm_103a(lib):
+    # ptxas -v reports the target of every compiled entry function in the build logs
+    from thea_gb300 import build as B
+    logs = [os.path.join(B.BUILD, f[:-3] + ".log") for f in B.sources()]
+    for log in logs:
+        text = open(log).read()
+        assert "arch=compute_103a,code=sm_103a" in text.splitlines()[0]
+        assert "for 'sm_103a'" in text
+
+
+def test_status_strings_and_version(lib):
+    assert lib.thea_abi_version() == 1
+    assert lib.thea_status_string(0) == b"ok"
+    assert lib.thea_status_string(1) == b"invalid argument"
+    assert lib.thea_status_string(99) == b"unknown status"
+
+
+def test_invalid_arguments_are_rejected_without_a_device(lib):
+    from thea_gb300 import _native as N
+    h = ctypes.c_void_p()
+    assert lib.thea_mesh_bvh_build(None, 3, None, 1, None, None, ctypes.byref(h)) == 1
+    assert b"null" in lib.thea_last_error_message()
+    V = np.zeros((3, 3), np.float32)
+    assert lib.thea_mesh_bvh_build(V.ctypes.data, 0, V.ctypes.data, 1, None, None, ctypes.byref(h)) == 1
+    cfg = N.BuildConfig()
+    cfg.reserved[0] = 7
+    assert lib.thea_point_bvh_build(V.ctypes.data, 3, ctypes.byref(cfg), None, ctypes.byref(h)) == 1
+    assert lib.thea_closest_element(None, None, 0, -1.0, None, None, None, None) == 1
+    assert lib.thea_ray_intersection(None, None, None, 0, -1.0, None, None, None, None) == 1
+    assert lib.thea_k_closest(None, None, 0, 4, -1.0, None, None, None, None) == 1
+    assert lib.thea_k_closest_self(None, 4, None, None, None) == 1
+    assert lib.thea_sample_by_area(None, 0, None, 0, 5, 1, 9, None, None, None, None, None) == 1
+    assert lib.thea_bvh_destroy(None) == 0
+    with pytest.raises(N.TheaError):
+        N.check(lib.thea_k_closest_self(None, 4, None, None, None))
+
+
+def test_profiling_and_launch_counter_without_device(lib):
+    before = lib.thea_launch_count()
+    assert lib.thea_profiling_enable(1) == 0
+    assert lib.thea_profiling_reset() == 0
+    ms = ctypes.c_double(-1)
+    cnt = ctypes.c_int64(-1)
+    assert lib.thea_profiling_read(b"nothing", ctypes.byref(ms), ctypes.byref(cnt)) == 0
+    assert ms.value == 0 and cnt.value == 0
+    assert lib.thea_profiling_enable(0) == 0
+    assert lib.thea_launch_count() == before
+
+
+def test_cpp_wrapper_compiles():
+    """The header-only C++ wrapper (reference method names over the C ABI) compiles and links against the library."""
+    from thea_gb300 import build as B
+    B.build()
+    src = os.path.join(ROOT, "tests", "cpp", "wrapper_compile.cpp")
+    out = os.path.join(ROOT, "tests", "cpp", "_build", "wrapper_compile")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), src, "-o", out,
+                        "-L", os.path.join(ROOT, "thea_gb300", "_lib"), "-lthea_gpu",
+                        "-Wl,-rpath," + os.path.join(ROOT, "thea_gb300", "_lib")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([out, "--no-device"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -1,0 +1,176 @@
+"""CPU tests of the oracle: known-answer checks, agreement between its reference and contract modes, agreement of its
+tree traversals with brute force, and the committed golden fixtures."""
+
+import os
+
+import numpy as np
+import pytest
+
+from thea_gb300 import workloads as W
+
+
+def test_random_matches_std_mt19937_where_the_variant_agrees(oracle):
+    # Thea's generate() skips re-twisting word N - M = 227 (Code/Source/Random.cpp:120); everything that does not
+    # depend on that word equals the standard MT19937, whose seeding and tempering Thea shares.
+    for seed in (5489, 0xFFFF, 1):
+        a = oracle.thea_random_bits(seed, 1248)
+        b = oracle.std_mt19937_bits(seed, 1248)
+        assert np.array_equal(a[:227], b[:227])
+        diff = np.nonzero(a[:624] != b[:624])[0]
+        assert set(diff.tolist()) <= {227, 454}
+        assert 227 in diff.tolist()
+
+
+def test_random_known_answer(oracle):
+    # std::mt19937 with the default seed gives 3499211612 as its first output; Thea's variant shares it.
+    assert oracle.thea_random_bits(5489, 1)[0] == 3499211612
+
+
+def test_tree_depth_formula(oracle):
+    # Math::treeDepth(n, 5, 0.5): ceil(log(n / 5) / -log(0.5f))
+    assert oracle.tree_depth(81920) == 14
+    assert oracle.tree_depth(5) == 0
+    assert oracle.tree_depth(1) == 0
+    assert oracle.tree_depth(11) == 2
+
+
+@pytest.mark.parametrize("sub,seed", [(1, 1), (2, 2), (3, 3)])
+def test_closest_contract_equals_brute_force(oracle, sub, seed):
+    V, F = W.noisy_icosphere(sub, seed)
+    Q = W.uniform_box_points(400, [-1.5] * 3, [1.5] * 3, seed + 100)
+    Q = np.concatenate([Q, V[:50], (V[:50] * 1.3).astype(np.float32)])
+    m = oracle.MeshIndex(V, F)
+    i1, d1, c1 = m.closest_contract(Q)
+    i2, d2, c2 = oracle.closest_brute(V, F, Q)
+    assert np.array_equal(i1, i2) and np.array_equal(d1, d2) and np.array_equal(c1, c2)
+    # reference mode picks an element at the same (bit-identical) distance
+    ri, rdist, rcp = m.closest_ref(Q)
+    Vt = V[F[ri]]
+    cp_ref, d2_ref = oracle.triangle_closest_points(Vt.reshape(-1, 9), Q)
+    assert np.array_equal(d2_ref.astype(np.float64), d1)
+    assert np.array_equal(np.sqrt(d2_ref.astype(np.float64)), rdist)
+
+
+def test_closest_dist_bound(oracle):
+    V, F = W.noisy_icosphere(2, 5)
+    Q = W.uniform_box_points(300, [-1.5] * 3, [1.5] * 3, 6)
+    m = oracle.MeshIndex(V, F)
+    for b in (0.05, 0.2, 0.6):
+        i1, d1, _ = m.closest_contract(Q, dist_bound=b)
+        i2, d2, _ = oracle.closest_brute(V, F, Q, dist_bound=b)
+        assert np.array_equal(i1, i2)
+        ri, _, _ = m.closest_ref(Q, dist_bound=b)
+        assert np.array_equal(ri >= 0, i1 >= 0)
+        assert np.all(d1[i1 >= 0] < b * b)
+
+
+def test_ray_contract_equals_brute_force(oracle):
+    V, F = W.heightfield(20, 7)
+    o, d = W.cosine_rays_down(500, 8)
+    m = oracle.MeshIndex(V, F)
+    t1, i1 = m.ray_contract(o, d)
+    t2, i2 = oracle.ray_brute(V, F, o, d)
+    assert np.array_equal(i1, i2) and np.array_equal(t1, t2)
+    rt, ri, rn = m.ray_ref(o, d)
+    assert np.array_equal(rt.astype(np.float64), t1)
+    for mt in (0.3, 0.55):
+        t3, i3 = m.ray_contract(o, d, max_time=mt)
+        t4, i4 = oracle.ray_brute(V, F, o, d, max_time=mt)
+        assert np.array_equal(i3, i4) and np.array_equal(t3, t4)
+
+
+def test_ray_random_directions_sphere(oracle):
+    V, F = W.noisy_icosphere(2, 9)
+    o, d = W.random_rays(500, [-2] * 3, [2] * 3, 10)
+    m = oracle.MeshIndex(V, F)
+    t1, i1 = m.ray_contract(o, d)
+    t2, i2 = oracle.ray_brute(V, F, o, d)
+    assert np.array_equal(i1, i2) and np.array_equal(t1, t2)
+
+
+def test_knn_contract_equals_brute_force(oracle):
+    P = W.uniform_box_points(3000, [0] * 3, [1] * 3, 11)
+    P[100:120] = P[0]  # exact duplicates: ties at distance 0 and equal distances elsewhere
+    Q = np.concatenate([P[:300], W.uniform_box_points(200, [-0.2] * 3, [1.2] * 3, 12)])
+    ex = np.concatenate([np.arange(300, dtype=np.int32), -np.ones(200, np.int32)])
+    pi = oracle.PointIndex(P)
+    for k in (1, 3, 8, 16):
+        i1, d1 = pi.knn_contract(Q, k, exclude=ex)
+        i2, d2 = oracle.knn_brute(P, Q, k, exclude=ex)
+        assert np.array_equal(i1, i2) and np.array_equal(d1, d2)
+        ri, rd = pi.knn_ref(Q, k, exclude=ex)
+        assert np.array_equal(rd, d1)  # same distances; indices may differ among ties
+    i1, d1 = pi.knn_contract(Q, 8, dist_bound=0.05)
+    i2, d2 = oracle.knn_brute(P, Q, 8, dist_bound=0.05)
+    assert np.array_equal(i1, i2)
+
+
+def test_sampler_is_deterministic_and_area_weighted(oracle):
+    V, F = W.noisy_icosphere(2, 13)
+    p1, n1, f1 = oracle.sample_by_area(V, F, 20000, 99)
+    p2, n2, f2 = oracle.sample_by_area(V, F, 20000, 99)
+    assert np.array_equal(p1, p2) and np.array_equal(f1, f2)
+    _, _, _, area = oracle.triangle_props(V[F].reshape(-1, 9))
+    counts = np.bincount(f1, minlength=len(F))
+    expected = 20000 * area / area.sum()
+    chi2 = np.sum((counts - expected) ** 2 / expected)
+    assert chi2 < 2.0 * len(F)  # loose goodness of fit
+    # each sample lies on its triangle's plane
+    nrm, dist, _, _ = oracle.triangle_props(V[F[f1]].reshape(-1, 9))
+    assert np.max(np.abs(np.sum(p1 * nrm, 1) - dist)) < 1e-5
+
+
+def test_sampler_zero_area_mesh(oracle):
+    V = np.zeros((3, 3), np.float32)
+    F = np.array([[0, 1, 2]], np.int32)
+    p, n, f = oracle.sample_by_area(V, F, 10, 1)
+    assert len(p) == 0
+
+
+def test_degenerate_triangles(oracle):
+    # zero-area triangles: coincident vertices and collinear vertices
+    V = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [0, 1, 0], [0, 0, 0]], np.float32)
+    F = np.array([[0, 1, 2], [0, 4, 3], [0, 1, 3]], np.int32)
+    Q = W.uniform_box_points(200, [-1] * 3, [2] * 3, 14)
+    m = oracle.MeshIndex(V, F)
+    i1, d1, _ = m.closest_contract(Q)
+    i2, d2, _ = oracle.closest_brute(V, F, Q)
+    assert np.array_equal(i1, i2) and np.array_equal(d1, d2)
+
+
+@pytest.mark.parametrize("name", ["closest", "ray", "sample_knn", "testbvh", "random"])
+def test_golden_fixtures_reproduce(oracle, golden_dir, name):
+    z = np.load(os.path.join(golden_dir, name + ".npz"))
+    if name == "closest":
+        m = oracle.MeshIndex(z["V"], z["F"])
+        i, d2, cp = m.closest_contract(z["Q"])
+        assert np.array_equal(i, z["index"]) and np.array_equal(d2.astype(np.float32), z["d2"])
+        assert np.array_equal(cp.astype(np.float32), z["cp"])
+        ri, rd, rcp = m.closest_ref(z["Q"])
+        assert np.array_equal(ri, z["ref_index"]) and np.array_equal(rd, z["ref_dist"])
+        bi, bd2, _ = m.closest_contract(z["Q"], dist_bound=float(z["bound"]))
+        assert np.array_equal(bi, z["bound_index"])
+    elif name == "ray":
+        m = oracle.MeshIndex(z["V"], z["F"])
+        t, i = m.ray_contract(z["O"], z["D"])
+        assert np.array_equal(i, z["index"]) and np.array_equal(t.astype(np.float32), z["time"])
+        rt, ri, rn = m.ray_ref(z["O"], z["D"])
+        assert np.array_equal(ri, z["ref_index"]) and np.array_equal(rn, z["ref_normal"])
+    elif name == "sample_knn":
+        p, n, f = oracle.sample_by_area(z["V"], z["F"], len(z["pos"]), int(z["seed"]))
+        assert np.array_equal(p, z["pos"]) and np.array_equal(n, z["nrm"]) and np.array_equal(f, z["face"])
+        pi = oracle.PointIndex(p)
+        ki, kd = pi.knn_contract(p, 8, exclude=np.arange(len(p), dtype=np.int32))
+        assert np.array_equal(ki, z["knn_index"])
+    elif name == "testbvh":
+        pi = oracle.PointIndex(z["points"])
+        i, d = pi.knn_contract(z["query"], 3, dist_bound=0.25)
+        assert np.array_equal(i, z["knn3_index"])
+        tm = oracle.MeshIndex(z["tri_vertices"], z["tri_faces"])
+        ti, td2, tcp = tm.closest_contract(z["query"], dist_bound=0.25)
+        assert np.array_equal(ti, z["tri_index"])
+        rt, ri = tm.ray_contract(np.zeros((1, 3), np.float32), z["ray_dir"][None])
+        assert np.array_equal(ri, z["ray_index"])
+    else:
+        assert np.array_equal(oracle.thea_random_bits(5489, 2000), z["seed_5489"])
+        assert np.array_equal(oracle.thea_random_bits(0xFFFF, 2000), z["seed_ffff"])

@@ -1,0 +1,91 @@
+"""ctypes binding of ``libthea_gpu.so`` (the C ABI declared in ``include/thea_gpu.h``).
+
+Loading fails loudly: there is no fallback implementation of any entry point.
+"""
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libthea_gpu.so")
+
+THEA_OK = 0
+STATUS_NAMES = {0: "THEA_OK", 1: "THEA_ERR_INVALID_ARGUMENT", 2: "THEA_ERR_OUT_OF_MEMORY",
+                3: "THEA_ERR_ADMISSION_REFUSED", 4: "THEA_ERR_DEVICE_TIMEOUT", 5: "THEA_ERR_CUDA",
+                6: "THEA_ERR_INTERNAL", 7: "THEA_ERR_NOT_SUPPORTED", 8: "THEA_ERR_CANCELLED"}
+
+LAYOUT_CLOSEST = 1
+LAYOUT_RAY = 2
+RNG_THEA_MT = 0
+RNG_COUNTER = 1
+
+# Every symbol the header declares, with (restype, argtypes)
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_u32 = ctypes.c_uint32
+_f32 = ctypes.c_float
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+class BuildConfig(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32), ("layouts", ctypes.c_uint32),
+                ("reserved", ctypes.c_int32 * 5)]
+
+
+class BvhInfo(ctypes.Structure):
+    _fields_ = [("num_elements", ctypes.c_int64), ("num_nodes", ctypes.c_int64), ("width", ctypes.c_int32),
+                ("max_leaf_size", ctypes.c_int32), ("is_mesh", ctypes.c_int32), ("depth", ctypes.c_int32),
+                ("device_bytes", ctypes.c_int64), ("bounds_lo", ctypes.c_float * 3), ("bounds_hi", ctypes.c_float * 3),
+                ("device_error_bits", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
+
+
+SIGNATURES = {
+    "thea_abi_version": (ctypes.c_int, []),
+    "thea_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "thea_last_error_message": (ctypes.c_char_p, []),
+    "thea_launch_count": (ctypes.c_int64, []),
+    "thea_profiling_enable": (ctypes.c_int, [ctypes.c_int]),
+    "thea_profiling_reset": (ctypes.c_int, []),
+    "thea_profiling_read": (ctypes.c_int, [ctypes.c_char_p, _f64p, _i64p]),
+    "thea_mesh_bvh_build": (ctypes.c_int, [_vp, _i64, _vp, _i64, ctypes.POINTER(BuildConfig), _vp,
+                                           ctypes.POINTER(_vp)]),
+    "thea_point_bvh_build": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(BuildConfig), _vp, ctypes.POINTER(_vp)]),
+    "thea_bvh_destroy": (ctypes.c_int, [_vp]),
+    "thea_bvh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(BvhInfo)]),
+    "thea_closest_element": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp]),
+    "thea_ray_intersection": (ctypes.c_int, [_vp, _vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp]),
+    "thea_k_closest": (ctypes.c_int, [_vp, _vp, _i64, _i32, _f32, _vp, _vp, _vp, _vp]),
+    "thea_k_closest_self": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp]),
+    "thea_sample_by_area": (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _u32, _i32, _vp, _vp, _vp, _i64p, _vp]),
+}
+
+_lib = None
+
+
+class TheaError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+def lib():
+    """Load the native library (built by thea_gb300.build); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("thea_gb300 native library not built (%s); run thea_gb300.build.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != THEA_OK:
+        msg = lib().thea_last_error_message()
+        raise TheaError(status, msg.decode() if msg else "")

@@ -1,0 +1,486 @@
+// The C ABI (include/thea_gpu.h): argument checks, status codes, host-pointer staging, launch accounting and event
+// timing. Nothing throws across the boundary.
+#include "bvh.hpp"
+#include "device_util.cuh"
+#include "query.hpp"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace thea {
+
+//============================================================================================================================
+// Launch accounting and optional per-kernel event timing
+//============================================================================================================================
+
+static std::atomic<int64_t> g_launches{0};
+static std::atomic<bool> g_profiling{false};
+
+struct TimedLaunch {
+  std::string name;
+  cudaEvent_t begin, end;
+};
+static std::mutex g_prof_mutex;
+static std::vector<TimedLaunch> g_prof;
+
+void note_launch(char const * kernel_name, cudaStream_t stream, cudaEvent_t * begin_event) {
+  (void)kernel_name;
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  *begin_event = nullptr;
+  if (g_profiling.load(std::memory_order_relaxed)) {
+    if (cudaEventCreate(begin_event) == cudaSuccess) cudaEventRecord(*begin_event, stream);
+    else *begin_event = nullptr;
+  }
+}
+
+void note_launch_end(char const * kernel_name, cudaStream_t stream, cudaEvent_t begin_event) {
+  if (!begin_event) return;
+  cudaEvent_t end = nullptr;
+  if (cudaEventCreate(&end) != cudaSuccess) {
+    cudaEventDestroy(begin_event);
+    return;
+  }
+  cudaEventRecord(end, stream);
+  std::lock_guard<std::mutex> lk(g_prof_mutex);
+  g_prof.push_back(TimedLaunch{kernel_name, begin_event, end});
+}
+
+//============================================================================================================================
+// Status plumbing
+//============================================================================================================================
+
+static thread_local std::string g_error;
+
+template <class F> static thea_status guarded(F && f) {
+  try {
+    f();
+    return THEA_OK;
+  } catch (Error const & e) {
+    g_error = e.what();
+    return e.status;
+  } catch (std::bad_alloc const &) {
+    g_error = "host allocation failed";
+    return THEA_ERR_OUT_OF_MEMORY;
+  } catch (std::exception const & e) {
+    g_error = e.what();
+    return THEA_ERR_INTERNAL;
+  } catch (...) {
+    g_error = "unknown error";
+    return THEA_ERR_INTERNAL;
+  }
+}
+
+//============================================================================================================================
+// Host-pointer staging
+//============================================================================================================================
+
+static bool is_host_pointer(void const * p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return !(a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged);
+}
+
+// Two non-blocking copy/compute streams per device, created once, used to overlap chunk transfers with kernels.
+static std::array<cudaStream_t, 2> staging_streams() {
+  static std::mutex m;
+  static std::map<int, std::array<cudaStream_t, 2>> streams;
+  int dev = 0;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(m);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  std::array<cudaStream_t, 2> s;
+  for (auto & x : s) THEA_CUDA_CHECK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  streams[dev] = s;
+  return s;
+}
+
+struct IoArray {
+  void * ptr;         // caller pointer (may be null for optional outputs)
+  size_t elem_bytes;  // bytes per query
+  bool output;
+  bool host;
+};
+
+// Runs fn(begin, count, device_pointers, stream) over [0, n). Device-resident calls run once, asynchronously, on the
+// caller's stream. If any array is host memory, the range is processed in chunks alternating between two staging
+// streams (copy in, kernel, copy out), ordered after prior work on `stream`; the call returns once the results are in
+// host memory.
+template <class Fn> static void run_staged(std::vector<IoArray> arrays, int64_t n, cudaStream_t stream, Fn && fn) {
+  bool any_host = false;
+  size_t host_bytes = 0;
+  for (auto & a : arrays) {
+    a.host = a.ptr && is_host_pointer(a.ptr);
+    if (a.host) {
+      any_host = true;
+      host_bytes += a.elem_bytes;
+    }
+  }
+  if (!any_host) {
+    std::vector<void *> ptrs;
+    for (auto & a : arrays) ptrs.push_back(a.ptr);
+    fn((int64_t)0, n, ptrs, stream);
+    return;
+  }
+  if (n <= 0) return;
+  int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)((64u << 20) / host_bytes)));
+  chunk = std::min<int64_t>(chunk, std::max<int64_t>(1 << 16, ceil_div(n, 8)));
+  auto ss = staging_streams();
+  Scratch buf0((size_t)chunk * host_bytes, stream), buf1((size_t)chunk * host_bytes, stream);
+  cudaEvent_t ready, done0, done1;
+  THEA_CUDA_CHECK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  THEA_CUDA_CHECK(cudaEventCreateWithFlags(&done0, cudaEventDisableTiming));
+  THEA_CUDA_CHECK(cudaEventCreateWithFlags(&done1, cudaEventDisableTiming));
+  THEA_CUDA_CHECK(cudaEventRecord(ready, stream));
+  THEA_CUDA_CHECK(cudaStreamWaitEvent(ss[0], ready, 0));
+  THEA_CUDA_CHECK(cudaStreamWaitEvent(ss[1], ready, 0));
+  std::exception_ptr failure;
+  try {
+    for (int64_t c = 0; c * chunk < n; ++c) {
+      int64_t begin = c * chunk, cnt = std::min(chunk, n - begin);
+      cudaStream_t s = ss[c & 1];
+      char * base = (c & 1) ? buf1.as<char>() : buf0.as<char>();
+      std::vector<void *> ptrs;
+      size_t off = 0;
+      for (auto & a : arrays) {
+        if (!a.ptr) { ptrs.push_back(nullptr); continue; }
+        if (a.host) {
+          void * dev = base + off;
+          off += (size_t)chunk * a.elem_bytes;
+          if (!a.output)
+            THEA_CUDA_CHECK(cudaMemcpyAsync(dev, (char const *)a.ptr + begin * a.elem_bytes, cnt * a.elem_bytes,
+                                            cudaMemcpyHostToDevice, s));
+          ptrs.push_back(dev);
+        } else {
+          ptrs.push_back((char *)a.ptr + begin * a.elem_bytes);
+        }
+      }
+      fn(begin, cnt, ptrs, s);
+      for (size_t i = 0; i < arrays.size(); ++i) {
+        auto & a = arrays[i];
+        if (a.ptr && a.host && a.output)
+          THEA_CUDA_CHECK(cudaMemcpyAsync((char *)a.ptr + begin * a.elem_bytes, ptrs[i], cnt * a.elem_bytes,
+                                          cudaMemcpyDeviceToHost, s));
+      }
+    }
+  } catch (...) {
+    failure = std::current_exception();
+  }
+  cudaEventRecord(done0, ss[0]);
+  cudaEventRecord(done1, ss[1]);
+  cudaStreamWaitEvent(stream, done0, 0);
+  cudaStreamWaitEvent(stream, done1, 0);
+  buf0.release();
+  buf1.release();
+  cudaError_t se = cudaStreamSynchronize(stream);
+  cudaEventDestroy(ready);
+  cudaEventDestroy(done0);
+  cudaEventDestroy(done1);
+  if (failure) std::rethrow_exception(failure);
+  THEA_CUDA_CHECK(se);
+}
+
+// Copies a whole host array to a new device buffer (or passes device memory through).
+struct DeviceView {
+  Scratch owned;
+  void const * ptr = nullptr;
+  DeviceView(void const * p, size_t bytes, cudaStream_t s) {
+    if (p && is_host_pointer(p)) {
+      owned = Scratch(bytes, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(owned.ptr, p, bytes, cudaMemcpyHostToDevice, s));
+      ptr = owned.ptr;
+    } else {
+      ptr = p;
+    }
+  }
+};
+
+// Largest float f with (double)f < bound^2: an element is accepted iff its FP32 squared distance d2 <= f, which is the
+// reference's test (double)d2 < dist_bound * dist_bound (BvhN.hpp:1094, 451-466, 490-494). +inf when unbounded.
+static float bound_threshold(float dist_bound) {
+  if (!(dist_bound >= 0.f)) return INFINITY;
+  double b2 = (double)dist_bound * (double)dist_bound;
+  float f = (float)b2;
+  if ((double)f >= b2) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+
+static unsigned * handle_error_word(thea_bvh const * b) { return b->err; }
+
+}  // namespace thea
+
+using namespace thea;
+
+//============================================================================================================================
+// C entry points
+//============================================================================================================================
+
+extern "C" {
+
+THEA_API int thea_abi_version(void) { return THEA_GPU_ABI_VERSION; }
+
+THEA_API const char * thea_status_string(thea_status s) {
+  switch (s) {
+    case THEA_OK: return "ok";
+    case THEA_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case THEA_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case THEA_ERR_ADMISSION_REFUSED: return "admission refused";
+    case THEA_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case THEA_ERR_CUDA: return "CUDA error";
+    case THEA_ERR_INTERNAL: return "internal error";
+    case THEA_ERR_NOT_SUPPORTED: return "not supported";
+    case THEA_ERR_CANCELLED: return "cancelled";
+  }
+  return "unknown status";
+}
+
+THEA_API const char * thea_last_error_message(void) { return g_error.c_str(); }
+
+THEA_API int64_t thea_launch_count(void) { return g_launches.load(); }
+
+THEA_API thea_status thea_profiling_enable(int enable) {
+  g_profiling.store(enable != 0);
+  return THEA_OK;
+}
+
+THEA_API thea_status thea_profiling_reset(void) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    for (auto & t : g_prof) {
+      cudaEventSynchronize(t.end);
+      cudaEventDestroy(t.begin);
+      cudaEventDestroy(t.end);
+    }
+    g_prof.clear();
+  });
+}
+
+THEA_API thea_status thea_profiling_read(const char * kernel_substring, double * total_ms, int64_t * launches) {
+  return guarded([&] {
+    THEA_REQUIRE(total_ms && launches, "profiling_read: null output");
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    double sum = 0;
+    int64_t cnt = 0;
+    for (auto & t : g_prof) {
+      if (kernel_substring && !strstr(t.name.c_str(), kernel_substring)) continue;
+      THEA_CUDA_CHECK(cudaEventSynchronize(t.end));
+      float ms = 0;
+      THEA_CUDA_CHECK(cudaEventElapsedTime(&ms, t.begin, t.end));
+      sum += ms;
+      ++cnt;
+    }
+    *total_ms = sum;
+    *launches = cnt;
+  });
+}
+
+static void check_config(thea_build_config const * cfg) {
+  if (!cfg) return;
+  for (int i = 0; i < 5; ++i) THEA_REQUIRE(cfg->reserved[i] == 0, "build config: reserved fields must be zero");
+}
+
+THEA_API thea_status thea_mesh_bvh_build(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                         int64_t num_faces, const thea_build_config * config, void * stream,
+                                         thea_bvh ** out_bvh) {
+  return guarded([&] {
+    THEA_REQUIRE(out_bvh, "mesh_bvh_build: out_bvh is null");
+    *out_bvh = nullptr;
+    THEA_REQUIRE(vertices && faces, "mesh_bvh_build: null vertices or faces");
+    THEA_REQUIRE(num_vertices > 0 && num_faces > 0, "mesh_bvh_build: empty mesh");
+    check_config(config);
+    thea_build_config cfg{};
+    if (config) cfg = *config;
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceView V(vertices, (size_t)num_vertices * 3 * sizeof(float), s);
+    DeviceView F(faces, (size_t)num_faces * 3 * sizeof(int32_t), s);
+    *out_bvh = build_bvh(true, (float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, num_faces, cfg, s);
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+THEA_API thea_status thea_point_bvh_build(const float * points, int64_t num_points, const thea_build_config * config,
+                                          void * stream, thea_bvh ** out_bvh) {
+  return guarded([&] {
+    THEA_REQUIRE(out_bvh, "point_bvh_build: out_bvh is null");
+    *out_bvh = nullptr;
+    THEA_REQUIRE(points, "point_bvh_build: null points");
+    THEA_REQUIRE(num_points > 0, "point_bvh_build: empty point set");
+    check_config(config);
+    thea_build_config cfg{};
+    if (config) cfg = *config;
+    THEA_REQUIRE(cfg.layouts == 0, "point_bvh_build: layouts apply to meshes only");
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceView P(points, (size_t)num_points * 3 * sizeof(float), s);
+    *out_bvh = build_bvh(false, (float const *)P.ptr, num_points, nullptr, 0, cfg, s);
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+THEA_API thea_status thea_bvh_destroy(thea_bvh * bvh) {
+  return guarded([&] {
+    if (!bvh) return;
+    destroy_bvh(bvh);
+  });
+}
+
+THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * info) {
+  return guarded([&] {
+    THEA_REQUIRE(bvh && info, "bvh_get_info: null argument");
+    memset(info, 0, sizeof(*info));
+    info->num_elements = bvh->n;
+    info->num_nodes = bvh->num_nodes;
+    info->width = bvh->width;
+    info->max_leaf_size = bvh->leaf_size;
+    info->is_mesh = bvh->is_mesh;
+    info->depth = bvh->depth;
+    info->device_bytes = bvh->device_bytes;
+    for (int i = 0; i < 3; ++i) {
+      info->bounds_lo[i] = bvh->lo[i];
+      info->bounds_hi[i] = bvh->hi[i];
+    }
+    unsigned * w = handle_error_word(bvh);
+    unsigned bits = 0;
+    THEA_CUDA_CHECK(cudaMemcpy(&bits, w, sizeof(bits), cudaMemcpyDeviceToHost));
+    info->device_error_bits = bits;
+  });
+}
+
+THEA_API thea_status thea_closest_element(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
+                                          float dist_bound, int32_t * out_index, float * out_distance,
+                                          float * out_closest_point, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "closest_element: a mesh BVH is required");
+    THEA_REQUIRE(mesh_bvh->cp_rec, "closest_element: the BVH was built without THEA_LAYOUT_CLOSEST");
+    THEA_REQUIRE(num_queries >= 0, "closest_element: negative query count");
+    if (num_queries == 0) return;
+    THEA_REQUIRE(queries && out_index, "closest_element: null queries or out_index");
+    float thresh = bound_threshold(dist_bound);
+    unsigned * err = handle_error_word(mesh_bvh);
+    run_staged({{(void *)queries, 12, false, false}, {out_index, 4, true, false}, {out_distance, 4, true, false},
+                {out_closest_point, 12, true, false}},
+               num_queries, (cudaStream_t)stream,
+               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+                 run_closest(mesh_bvh, (float const *)p[0], cnt, thresh, (int32_t *)p[1], (float *)p[2],
+                             (float *)p[3], err, s);
+               });
+  });
+}
+
+THEA_API thea_status thea_ray_intersection(const thea_bvh * mesh_bvh, const float * origins, const float * directions,
+                                           int64_t num_rays, float max_time, float * out_time, int32_t * out_index,
+                                           float * out_normal, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "ray_intersection: a mesh BVH is required");
+    THEA_REQUIRE(mesh_bvh->ray_rec, "ray_intersection: the BVH was built without THEA_LAYOUT_RAY");
+    THEA_REQUIRE(num_rays >= 0, "ray_intersection: negative ray count");
+    if (num_rays == 0) return;
+    THEA_REQUIRE(origins && directions && out_time, "ray_intersection: null origins, directions or out_time");
+    unsigned * err = handle_error_word(mesh_bvh);
+    float mt = max_time >= 0.f ? max_time : -1.f;
+    run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
+                {out_index, 4, true, false}, {out_normal, 12, true, false}},
+               num_rays, (cudaStream_t)stream,
+               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+                 run_ray(mesh_bvh, (float const *)p[0], (float const *)p[1], cnt, mt, (float *)p[2],
+                         (int32_t *)p[3], (float *)p[4], err, s);
+               });
+  });
+}
+
+THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * queries, int64_t num_queries, int32_t k,
+                                    float dist_bound, const int32_t * exclude_index, int32_t * out_index,
+                                    float * out_sq_distance, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "k_closest: a point BVH is required");
+    THEA_REQUIRE(k >= 1 && k <= 32, "k_closest: k must be in 1..32");
+    THEA_REQUIRE(num_queries >= 0, "k_closest: negative query count");
+    if (num_queries == 0) return;
+    THEA_REQUIRE(queries && out_index && out_sq_distance, "k_closest: null queries or outputs");
+    float thresh = bound_threshold(dist_bound);
+    unsigned * err = handle_error_word(point_bvh);
+    run_staged({{(void *)queries, 12, false, false}, {(void *)exclude_index, 4, false, false},
+                {out_index, (size_t)k * 4, true, false}, {out_sq_distance, (size_t)k * 4, true, false}},
+               num_queries, (cudaStream_t)stream,
+               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+                 run_knn(point_bvh, (float const *)p[0], cnt, k, thresh, (int32_t const *)p[1], (int32_t *)p[2],
+                         (float *)p[3], err, s);
+               });
+  });
+}
+
+THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,
+                                         float * out_sq_distance, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "k_closest_self: a point BVH is required");
+    THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_self: k must be in 1..32");
+    THEA_REQUIRE(out_index && out_sq_distance, "k_closest_self: null outputs");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned * err = handle_error_word(point_bvh);
+    int64_t n = point_bvh->n;
+    bool hi = is_host_pointer(out_index), hd = is_host_pointer(out_sq_distance);
+    // rows are written in element order, so host outputs are staged whole
+    Scratch di, dd;
+    int32_t * pi = out_index;
+    float * pd = out_sq_distance;
+    if (hi) { di = Scratch((size_t)n * k * 4, s); pi = di.as<int32_t>(); }
+    if (hd) { dd = Scratch((size_t)n * k * 4, s); pd = dd.as<float>(); }
+    run_knn(point_bvh, nullptr, n, k, INFINITY, nullptr, pi, pd, err, s);
+    if (hi) THEA_CUDA_CHECK(cudaMemcpyAsync(out_index, pi, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
+    if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, pd, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
+    if (hi || hd) THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                         int64_t num_faces, int64_t num_samples, uint32_t seed, int32_t rng,
+                                         float * out_positions, float * out_normals, int32_t * out_faces,
+                                         int64_t * out_num_written, void * stream) {
+  return guarded([&] {
+    if (out_num_written) *out_num_written = 0;
+    THEA_REQUIRE(rng == THEA_RNG_THEA_MT || rng == THEA_RNG_COUNTER, "sample_by_area: unknown rng");
+    THEA_REQUIRE(num_samples >= 0, "sample_by_area: negative sample count");
+    if (num_samples == 0) return;
+    THEA_REQUIRE(vertices && faces && num_vertices > 0 && num_faces > 0, "sample_by_area: empty mesh");
+    THEA_REQUIRE(out_positions, "sample_by_area: out_positions is null");
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceView V(vertices, (size_t)num_vertices * 3 * sizeof(float), s);
+    DeviceView F(faces, (size_t)num_faces * 3 * sizeof(int32_t), s);
+    struct Out {
+      void * user;
+      size_t bytes;
+      Scratch dev;
+      void * ptr;
+    };
+    Out o[3] = {{out_positions, (size_t)num_samples * 12, {}, nullptr},
+                {out_normals, (size_t)num_samples * 12, {}, nullptr},
+                {out_faces, (size_t)num_samples * 4, {}, nullptr}};
+    for (auto & x : o) {
+      x.ptr = x.user;
+      if (x.user && is_host_pointer(x.user)) {
+        x.dev = Scratch(x.bytes, s);
+        x.ptr = x.dev.ptr;
+      }
+    }
+    int64_t got = run_sample_by_area((float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, num_faces, num_samples,
+                                     seed, rng, (float *)o[0].ptr, (float *)o[1].ptr, (int32_t *)o[2].ptr, s);
+    for (auto & x : o)
+      if (x.dev.ptr && got > 0) THEA_CUDA_CHECK(cudaMemcpyAsync(x.user, x.ptr, x.bytes, cudaMemcpyDeviceToHost, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (out_num_written) *out_num_written = got;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,529 @@
+// LBVH build: element boxes -> 63-bit Morton codes -> stable radix sort -> Karras binary radix tree -> bottom-up box
+// refit -> top-down collapse into a W-wide tree whose leaves are contiguous runs of the sorted elements -> element records
+// in leaf order.
+//
+// Replaces BvhN::init / initTree / createKdTree (Code/Source/Algorithms/BvhN.hpp:705-794, 1366-1525). The reference
+// builds a median-split kd-tree with leaves of at most 5 elements and pads every node box by 5%; this build produces a
+// different tree over the same elements. Query results do not depend on the tree: every query returns the element with
+// the smallest distance or hit time, ties to the lowest index, and node boxes are padded so that no element at the best
+// distance can be pruned by rounding.
+#include "bvh.hpp"
+#include "device_util.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace thea {
+namespace {
+
+constexpr int BUILD_THREADS = 256;
+
+__device__ __forceinline__ int f2ord(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__host__ __device__ __forceinline__ float ord2f(int i) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff);
+#else
+  int j = i >= 0 ? i : i ^ 0x7fffffff;
+  float f;
+  memcpy(&f, &j, 4);
+  return f;
+#endif
+}
+
+// bounds[0..2] = min of element-box centres (ordered ints), [3..5] = max of centres, [6..8] = min of box lo,
+// [9..11] = max of box hi
+__global__ void elem_box_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t n, int is_mesh,
+                                float4 * __restrict__ elo, float4 * __restrict__ ehi, int * __restrict__ bounds) {
+  __shared__ int sb[12];
+  if (threadIdx.x < 12) sb[threadIdx.x] = ((threadIdx.x < 3) || (threadIdx.x >= 6 && threadIdx.x < 9)) ? INT_MAX : INT_MIN;
+  __syncthreads();
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    V3 lo, hi;
+    if (is_mesh) {
+      V3 a = load_v3(V + 3 * (int64_t)F[3 * i]);
+      V3 b = load_v3(V + 3 * (int64_t)F[3 * i + 1]);
+      V3 c = load_v3(V + 3 * (int64_t)F[3 * i + 2]);
+      lo = V3{fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z))};
+      hi = V3{fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z))};
+    } else {
+      lo = hi = load_v3(V + 3 * i);
+    }
+    elo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    ehi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+    V3 c = 0.5f * (hi + lo);
+    float cc[3] = {c.x, c.y, c.z}, ll[3] = {lo.x, lo.y, lo.z}, hh[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&sb[a], f2ord(cc[a]));
+      atomicMax(&sb[3 + a], f2ord(cc[a]));
+      atomicMin(&sb[6 + a], f2ord(ll[a]));
+      atomicMax(&sb[9 + a], f2ord(hh[a]));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    int t = threadIdx.x;
+    bool is_min = (t < 3) || (t >= 6 && t < 9);
+    if (is_min) atomicMin(&bounds[t], sb[t]);
+    else atomicMax(&bounds[t], sb[t]);
+  }
+}
+
+__device__ __forceinline__ uint64_t expand21(uint32_t v) {
+  uint64_t x = v & 0x1fffffull;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+
+__global__ void morton_kernel(float4 const * __restrict__ elo, float4 const * __restrict__ ehi, int64_t n,
+                              int const * __restrict__ bounds, uint64_t * __restrict__ keys,
+                              uint32_t * __restrict__ vals) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 l = elo[i], h = ehi[i];
+  float c[3] = {0.5f * (h.x + l.x), 0.5f * (h.y + l.y), 0.5f * (h.z + l.z)};
+  uint32_t q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float lo = ord2f(bounds[a]), hi = ord2f(bounds[3 + a]);
+    float ext = hi - lo;
+    float t = ext > 0.f ? (c[a] - lo) / ext : 0.f;
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    q[a] = min((uint32_t)(t * 2097152.0f), 2097151u);
+  }
+  keys[i] = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
+  vals[i] = (uint32_t)i;
+}
+
+// Common-prefix length of sorted keys i and j, extended by the indices when the keys are equal (Karras 2012)
+__device__ __forceinline__ int kdelta(uint64_t const * __restrict__ codes, int64_t n, int64_t i, int64_t j) {
+  if (j < 0 || j >= n) return -1;
+  uint64_t a = codes[i], b = codes[j];
+  if (a == b) return 64 + __clz((uint32_t)(i ^ j));
+  return __clzll((long long)(a ^ b));
+}
+
+// Binary radix tree. Child codes: >= 0 internal node, < 0 leaf at sorted position ~code.
+__global__ void karras_kernel(uint64_t const * __restrict__ codes, int64_t n, int * __restrict__ left,
+                              int * __restrict__ right, int * __restrict__ first, int * __restrict__ last,
+                              int * __restrict__ parent, int * __restrict__ leaf_parent) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int d = (kdelta(codes, n, i, i + 1) - kdelta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = kdelta(codes, n, i, i - d);
+  int64_t lmax = 2;
+  while (kdelta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int64_t l = 0;
+  for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+    if (kdelta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+  int64_t j = i + l * d;
+  int dnode = kdelta(codes, n, i, j);
+  int64_t s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (kdelta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+  int lc = (lo == gamma) ? ~(int)gamma : (int)gamma;
+  int rc = (hi == gamma + 1) ? ~(int)(gamma + 1) : (int)(gamma + 1);
+  left[i] = lc;
+  right[i] = rc;
+  first[i] = (int)lo;
+  last[i] = (int)hi;
+  if (lc < 0) leaf_parent[~lc] = (int)i; else parent[lc] = (int)i;
+  if (rc < 0) leaf_parent[~rc] = (int)i; else parent[rc] = (int)i;
+}
+
+__device__ __forceinline__ void child_box(int code, float4 const * __restrict__ elo, float4 const * __restrict__ ehi,
+                                          uint32_t const * __restrict__ sorted, float4 const * ilo, float4 const * ihi,
+                                          float4 & lo, float4 & hi) {
+  if (code < 0) {
+    uint32_t e = sorted[~code];
+    lo = elo[e];
+    hi = ehi[e];
+  } else {
+    lo = __ldcg(ilo + code);
+    hi = __ldcg(ihi + code);
+  }
+}
+
+// Bottom-up refit: the second thread to reach a node merges its two children and continues upwards.
+__global__ void refit_kernel(int64_t n, int const * __restrict__ left, int const * __restrict__ right,
+                             int const * __restrict__ parent, int const * __restrict__ leaf_parent,
+                             float4 const * __restrict__ elo, float4 const * __restrict__ ehi,
+                             uint32_t const * __restrict__ sorted, float4 * ilo, float4 * ihi,
+                             unsigned * __restrict__ visits) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int p = leaf_parent[s];
+  while (p >= 0) {
+    __threadfence();
+    unsigned old = atomicAdd(&visits[p], 1u);
+    if (old == 0) return;
+    float4 al, ah, bl, bh;
+    child_box(left[p], elo, ehi, sorted, ilo, ihi, al, ah);
+    child_box(right[p], elo, ehi, sorted, ilo, ihi, bl, bh);
+    __stcg(ilo + p, make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f));
+    __stcg(ihi + p, make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f));
+    p = parent[p];
+  }
+}
+
+struct CollapseArgs {
+  int const * left;
+  int const * right;
+  int const * first;
+  int const * last;
+  float4 const * elo;
+  float4 const * ehi;
+  uint32_t const * sorted;
+  float4 const * ilo;
+  float4 const * ihi;
+  int leaf_size;
+};
+
+__device__ __forceinline__ int code_count(CollapseArgs const & a, int code) {
+  return code < 0 ? 1 : a.last[code] - a.first[code] + 1;
+}
+__device__ __forceinline__ int code_first(CollapseArgs const & a, int code) { return code < 0 ? ~code : a.first[code]; }
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+  float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
+  return x * y + y * z + z * x;
+}
+
+// For each frontier binary node, choose the W binary subtrees that become the children of its wide node: starting from
+// the two children, repeatedly open the subtree with the largest surface area among those too big to be a leaf.
+template <int W>
+__global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
+                                       int * __restrict__ chosen, int * __restrict__ num_internal) {
+  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= fsize) return;
+  int b = frontier[f];
+  int codes[W];
+  int ne = 2;
+  codes[0] = a.left[b];
+  codes[1] = a.right[b];
+#pragma unroll
+  for (int e = 2; e < W; ++e) codes[e] = CHILD_EMPTY;
+  while (ne < W) {
+    int best = -1;
+    float best_sa = -1.f;
+    for (int e = 0; e < ne; ++e) {
+      int c = codes[e];
+      if (c >= 0 && code_count(a, c) > a.leaf_size) {
+        float sa = half_area(a.ilo[c], a.ihi[c]);
+        if (sa > best_sa) { best_sa = sa; best = e; }
+      }
+    }
+    if (best < 0) break;
+    int c = codes[best];
+    codes[best] = a.left[c];
+    codes[ne++] = a.right[c];
+  }
+  int nint = 0;
+  for (int e = 0; e < W; ++e) {
+    chosen[f * W + e] = codes[e];
+    if (codes[e] != CHILD_EMPTY && code_count(a, codes[e]) > a.leaf_size) ++nint;
+  }
+  num_internal[f] = nint;
+}
+
+// Pad a box outwards by a relative margin of its coordinates' magnitude, so that rounding in element distances and hit
+// times can never make an element that lies inside the box look closer than the box.
+__device__ __forceinline__ void pad_box(float4 & lo, float4 & hi) {
+  float const R = 1.0f / 1048576.0f;  // 2^-20
+  float px = (fabsf(lo.x) + fabsf(hi.x)) * R, py = (fabsf(lo.y) + fabsf(hi.y)) * R, pz = (fabsf(lo.z) + fabsf(hi.z)) * R;
+  lo.x -= px; lo.y -= py; lo.z -= pz;
+  hi.x += px; hi.y += py; hi.z += pz;
+}
+
+template <int W>
+__global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
+                                     int const * __restrict__ chosen, int const * __restrict__ offsets,
+                                     int64_t level_base, int64_t next_base, WideNode<W> * __restrict__ nodes,
+                                     int * __restrict__ next_frontier) {
+  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= fsize) return;
+  WideNode<W> node;
+  int k = 0;
+  int off = offsets[f];
+#pragma unroll
+  for (int e = 0; e < W; ++e) {
+    int code = chosen[f * W + e];
+    if (code == CHILD_EMPTY) {
+      node.lox[e] = node.loy[e] = node.loz[e] = INFINITY;
+      node.hix[e] = node.hiy[e] = node.hiz[e] = -INFINITY;
+      node.child[e] = CHILD_EMPTY;
+      continue;
+    }
+    float4 lo, hi;
+    child_box(code, a.elo, a.ehi, a.sorted, a.ilo, a.ihi, lo, hi);
+    pad_box(lo, hi);
+    node.lox[e] = lo.x; node.loy[e] = lo.y; node.loz[e] = lo.z;
+    node.hix[e] = hi.x; node.hiy[e] = hi.y; node.hiz[e] = hi.z;
+    int cnt = code_count(a, code);
+    if (cnt <= a.leaf_size) {
+      node.child[e] = encode_leaf(code_first(a, code), cnt);
+    } else {
+      node.child[e] = (int)(next_base + off + k);
+      next_frontier[off + k] = code;
+      ++k;
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
+  nodes[level_base + f] = node;
+}
+
+// A root that is a single leaf holding all n elements (n <= leaf size)
+template <int W> __global__ void single_leaf_root_kernel(WideNode<W> * nodes, int const * __restrict__ bounds, int n) {
+  WideNode<W> node;
+  for (int e = 0; e < W; ++e) {
+    node.lox[e] = node.loy[e] = node.loz[e] = INFINITY;
+    node.hix[e] = node.hiy[e] = node.hiz[e] = -INFINITY;
+    node.child[e] = CHILD_EMPTY;
+  }
+  float4 lo = make_float4(ord2f(bounds[6]), ord2f(bounds[7]), ord2f(bounds[8]), 0.f);
+  float4 hi = make_float4(ord2f(bounds[9]), ord2f(bounds[10]), ord2f(bounds[11]), 0.f);
+  pad_box(lo, hi);
+  node.lox[0] = lo.x; node.loy[0] = lo.y; node.loz[0] = lo.z;
+  node.hix[0] = hi.x; node.hiy[0] = hi.y; node.hiz[0] = hi.z;
+  node.child[0] = encode_leaf(0, n);
+  for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
+  nodes[0] = node;
+}
+
+__global__ void count_big_kernel(int const * __restrict__ first, int const * __restrict__ last, int64_t m, int leaf_size,
+                                 unsigned long long * __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool big = i < m && (last[i] - first[i] + 1) > leaf_size;
+  unsigned b = __ballot_sync(0xffffffffu, big);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
+}
+
+__global__ void mesh_records_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t n,
+                                    uint32_t const * __restrict__ sorted, float4 * __restrict__ cp_rec,
+                                    float4 * __restrict__ ray_rec, int32_t * __restrict__ leaf_to_elem) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int e = (int)sorted[s];
+  leaf_to_elem[s] = e;
+  V3 v0 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e]);
+  V3 v1 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e + 1]);
+  V3 v2 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e + 2]);
+  if (cp_rec) {
+    TriPlane pl = tri_plane(v0, v1, v2);
+    V3 d0, d1, d2;
+    float l0, l1, l2;
+    edge_dir(v0, v1, d0, l0);
+    edge_dir(v1, v2, d1, l1);
+    edge_dir(v2, v0, d2, l2);
+    float4 * r = cp_rec + s * CP_REC_F4;
+    r[0] = make_float4(v0.x, v0.y, v0.z, pl.dist);
+    r[1] = make_float4(v1.x, v1.y, v1.z, l0);
+    r[2] = make_float4(v2.x, v2.y, v2.z, l1);
+    r[3] = make_float4(pl.normal.x, pl.normal.y, pl.normal.z, __int_as_float(pl.axis));
+    r[4] = make_float4(d0.x, d0.y, d0.z, l2);
+    r[5] = make_float4(d1.x, d1.y, d1.z, __int_as_float(e));
+    r[6] = make_float4(d2.x, d2.y, d2.z, pl.area);
+    r[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (ray_rec) {
+    V3 e01 = v1 - v0, e02 = v2 - v0;
+    float4 * r = ray_rec + s * RAY_REC_F4;
+    r[0] = make_float4(v0.x, v0.y, v0.z, __int_as_float(e));
+    r[1] = make_float4(e01.x, e01.y, e01.z, 0.f);
+    r[2] = make_float4(e02.x, e02.y, e02.z, 0.f);
+  }
+}
+
+__global__ void point_records_kernel(float const * __restrict__ P, int64_t n, uint32_t const * __restrict__ sorted,
+                                     float4 * __restrict__ pt_rec, int32_t * __restrict__ leaf_to_elem) {
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int e = (int)sorted[s];
+  leaf_to_elem[s] = e;
+  V3 p = load_v3(P + 3 * (int64_t)e);
+  pt_rec[s] = make_float4(p.x, p.y, p.z, __int_as_float(e));
+}
+
+template <int W>
+void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, cudaStream_t stream) {
+  if (n <= a.leaf_size) {
+    THEA_CUDA_CHECK(cudaMallocAsync(&b->nodes, sizeof(WideNode<W>), stream));
+    THEA_LAUNCH(single_leaf_root_kernel<W>, 1, 1, 0, stream, (WideNode<W> *)b->nodes, d_bounds, (int)n);
+    b->num_nodes = 1;
+    b->depth = 1;
+    return;
+  }
+  // every wide node corresponds to a distinct binary node with more elements than a leaf holds
+  Scratch cnt(sizeof(unsigned long long), stream);
+  THEA_CUDA_CHECK(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes, stream));
+  THEA_LAUNCH(count_big_kernel, (unsigned)ceil_div(n - 1, BUILD_THREADS), BUILD_THREADS, 0, stream, a.first, a.last,
+              n - 1, a.leaf_size, cnt.as<unsigned long long>());
+  unsigned long long nbig = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&nbig, cnt.ptr, sizeof(nbig), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+  if (nbig < 1) nbig = 1;
+
+  WideNode<W> * nodes = nullptr;
+  THEA_CUDA_CHECK(cudaMallocAsync((void **)&nodes, (size_t)nbig * sizeof(WideNode<W>), stream));
+  Scratch fa((size_t)nbig * sizeof(int), stream), fb((size_t)nbig * sizeof(int), stream);
+  Scratch chosen((size_t)nbig * W * sizeof(int), stream);
+  Scratch nint((size_t)nbig * sizeof(int), stream), offs((size_t)nbig * sizeof(int), stream);
+  int root = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(fa.ptr, &root, sizeof(int), cudaMemcpyHostToDevice, stream));
+  int * cur = fa.as<int>();
+  int * nxt = fb.as<int>();
+  int64_t fsize = 1, base = 0;
+  int depth = 0;
+  while (fsize > 0) {
+    THEA_REQUIRE(base + fsize <= (int64_t)nbig, "BVH collapse exceeded its node bound");
+    unsigned grid = (unsigned)ceil_div(fsize, BUILD_THREADS);
+    THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
+                nint.as<int>());
+    exclusive_scan<int>(nint.as<int>(), offs.as<int>(), fsize, stream);
+    THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
+                offs.as<int>(), base, base + fsize, nodes, nxt);
+    int tail[2];
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[0], offs.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[1], nint.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+    base += fsize;
+    fsize = (int64_t)tail[0] + tail[1];
+    std::swap(cur, nxt);
+    ++depth;
+  }
+  b->nodes = nodes;
+  b->num_nodes = base;
+  b->depth = depth;
+}
+
+}  // namespace
+
+thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
+                     thea_build_config const & cfg, cudaStream_t stream) {
+  int64_t n = is_mesh ? nf : nv;
+  THEA_REQUIRE(n >= 1, "build: at least one element is required");
+  THEA_REQUIRE(n < (int64_t(1) << 27), "build: at most 2^27 - 1 elements per BVH");
+  int width = cfg.width == 0 ? 4 : cfg.width;
+  THEA_REQUIRE(width == 4 || width == 8, "build: width must be 4 or 8");
+  int leaf = cfg.max_leaf_size == 0 ? (is_mesh ? 4 : 8) : cfg.max_leaf_size;
+  THEA_REQUIRE(leaf >= 1 && leaf <= MAX_LEAF_SIZE, "build: max_leaf_size must be in 1..16");
+  uint32_t layouts = is_mesh ? (cfg.layouts == 0 ? (THEA_LAYOUT_CLOSEST | THEA_LAYOUT_RAY) : cfg.layouts) : 0u;
+  THEA_REQUIRE((layouts & ~3u) == 0, "build: unknown layout bits");
+
+  thea_bvh * b = new thea_bvh;
+  try {
+    THEA_CUDA_CHECK(cudaGetDevice(&b->device));
+    b->is_mesh = is_mesh ? 1 : 0;
+    b->width = width;
+    b->leaf_size = leaf;
+    b->layouts = layouts;
+    b->n = n;
+
+    Scratch elo((size_t)n * sizeof(float4), stream), ehi((size_t)n * sizeof(float4), stream);
+    Scratch bounds(12 * sizeof(int), stream);
+    int init[12];
+    for (int t = 0; t < 12; ++t) init[t] = ((t < 3) || (t >= 6 && t < 9)) ? INT_MAX : INT_MIN;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(bounds.ptr, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+    unsigned grid = (unsigned)ceil_div(n, BUILD_THREADS);
+    THEA_LAUNCH(elem_box_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, is_mesh ? 1 : 0, elo.as<float4>(),
+                ehi.as<float4>(), bounds.as<int>());
+
+    Scratch keys((size_t)n * sizeof(uint64_t), stream), vals((size_t)n * sizeof(uint32_t), stream);
+    THEA_LAUNCH(morton_kernel, grid, BUILD_THREADS, 0, stream, elo.as<float4>(), ehi.as<float4>(), n,
+                bounds.as<int>(), keys.as<uint64_t>(), vals.as<uint32_t>());
+    radix_sort_pairs(keys.as<uint64_t>(), vals.as<uint32_t>(), n, 63, stream);
+
+    int64_t m = n - 1;  // binary internal nodes
+    Scratch left((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), right((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream);
+    Scratch first((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), last((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream);
+    Scratch parent((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), leaf_parent((size_t)n * sizeof(int), stream);
+    Scratch ilo((size_t)std::max<int64_t>(m, 1) * sizeof(float4), stream), ihi((size_t)std::max<int64_t>(m, 1) * sizeof(float4), stream);
+    Scratch visits((size_t)std::max<int64_t>(m, 1) * sizeof(unsigned), stream);
+    if (m >= 1) {
+      THEA_CUDA_CHECK(cudaMemsetAsync(parent.ptr, 0xff, (size_t)m * sizeof(int), stream));
+      THEA_CUDA_CHECK(cudaMemsetAsync(leaf_parent.ptr, 0xff, (size_t)n * sizeof(int), stream));
+      THEA_CUDA_CHECK(cudaMemsetAsync(visits.ptr, 0, (size_t)m * sizeof(unsigned), stream));
+      THEA_LAUNCH(karras_kernel, (unsigned)ceil_div(m, BUILD_THREADS), BUILD_THREADS, 0, stream, keys.as<uint64_t>(),
+                  n, left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), parent.as<int>(),
+                  leaf_parent.as<int>());
+      THEA_LAUNCH(refit_kernel, grid, BUILD_THREADS, 0, stream, n, left.as<int>(), right.as<int>(), parent.as<int>(),
+                  leaf_parent.as<int>(), elo.as<float4>(), ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(),
+                  ihi.as<float4>(), visits.as<unsigned>());
+    }
+    CollapseArgs a{left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), elo.as<float4>(),
+                   ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(), ihi.as<float4>(), leaf};
+    if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), stream);
+    else collapse<8>(b, a, n, bounds.as<int>(), stream);
+    int64_t node_bytes = b->num_nodes * (width == 4 ? (int64_t)sizeof(WideNode<4>) : (int64_t)sizeof(WideNode<8>));
+
+    int need = b->depth * (width - 1) + 1;
+    if (need > (width == 4 ? 256 : 512))
+      throw Error(THEA_ERR_NOT_SUPPORTED, "build: tree too deep for the traversal stack (depth " +
+                                              std::to_string(b->depth) + ")");
+    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->err, sizeof(unsigned), stream));
+    THEA_CUDA_CHECK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), stream));
+    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->leaf_to_elem, (size_t)n * sizeof(int32_t), stream));
+    int64_t rec_bytes = n * (int64_t)sizeof(int32_t);
+    if (is_mesh) {
+      if (layouts & THEA_LAYOUT_CLOSEST) {
+        THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->cp_rec, (size_t)n * CP_REC_F4 * sizeof(float4), stream));
+        rec_bytes += n * CP_REC_F4 * (int64_t)sizeof(float4);
+      }
+      if (layouts & THEA_LAYOUT_RAY) {
+        THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->ray_rec, (size_t)n * RAY_REC_F4 * sizeof(float4), stream));
+        rec_bytes += n * RAY_REC_F4 * (int64_t)sizeof(float4);
+      }
+      THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, vals.as<uint32_t>(), b->cp_rec,
+                  b->ray_rec, b->leaf_to_elem);
+    } else {
+      THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
+      rec_bytes += n * (int64_t)sizeof(float4);
+      THEA_LAUNCH(point_records_kernel, grid, BUILD_THREADS, 0, stream, V, n, vals.as<uint32_t>(), b->pt_rec,
+                  b->leaf_to_elem);
+    }
+    int hb[12];
+    THEA_CUDA_CHECK(cudaMemcpyAsync(hb, bounds.ptr, sizeof(hb), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+    for (int t = 0; t < 3; ++t) {
+      b->lo[t] = ord2f(hb[6 + t]);
+      b->hi[t] = ord2f(hb[9 + t]);
+    }
+    b->device_bytes = node_bytes + rec_bytes;
+    return b;
+  } catch (...) {
+    cudaStreamSynchronize(stream);
+    destroy_bvh(b);
+    throw;
+  }
+}
+
+void destroy_bvh(thea_bvh * b) {
+  if (!b) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(b->device);
+  cudaDeviceSynchronize();
+  if (b->nodes) cudaFree(b->nodes);
+  if (b->cp_rec) cudaFree(b->cp_rec);
+  if (b->ray_rec) cudaFree(b->ray_rec);
+  if (b->pt_rec) cudaFree(b->pt_rec);
+  if (b->leaf_to_elem) cudaFree(b->leaf_to_elem);
+  if (b->err) cudaFree(b->err);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete b;
+}
+
+}  // namespace thea

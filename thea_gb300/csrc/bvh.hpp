@@ -1,0 +1,32 @@
+// The BVH handle shared by the build, the query kernels and the C ABI.
+#pragma once
+
+#include "common.cuh"
+
+// Opaque to C callers; immutable once built.
+struct thea_bvh {
+  int32_t is_mesh = 0;
+  int32_t width = 4;
+  int32_t leaf_size = 4;
+  int32_t depth = 0;
+  int32_t device = 0;
+  uint32_t layouts = 0;
+  int64_t n = 0;          // elements
+  int64_t num_nodes = 0;  // wide nodes; node 0 is the root
+  void * nodes = nullptr;          // WideNode<width>[num_nodes]
+  float4 * cp_rec = nullptr;       // mesh closest-point records, CP_REC_F4 per element, leaf order
+  float4 * ray_rec = nullptr;      // mesh ray records, RAY_REC_F4 per element, leaf order
+  float4 * pt_rec = nullptr;       // point records, 1 per element, leaf order
+  int32_t * leaf_to_elem = nullptr;  // leaf-order position -> element index
+  unsigned * err = nullptr;          // device word: error bits raised by query kernels
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  int64_t device_bytes = 0;
+};
+
+namespace thea {
+
+thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
+                     thea_build_config const & cfg, cudaStream_t stream);
+void destroy_bvh(thea_bvh * b);
+
+}  // namespace thea

@@ -1,0 +1,194 @@
+// Area-weighted mesh sampling: MeshSampler::sampleEvenlyByArea in EXACT count mode
+// (Code/Source/Algorithms/MeshSampler.hpp:100-204) with TriangleN<3>::randomPoint (Code/Source/Triangle3.hpp:179-195).
+//
+// Bit-identical to the reference when drawing from the reference's Random(seed) stream: the per-triangle FP32 areas, the
+// FP64 cumulative-area table built by a sequential sum in index order (so its rounding matches the reference's loop),
+// one lower_bound per sample, and the FP32 parallelogram point with reflection. Sample i consumes words 3i, 3i+1, 3i+2
+// of the stream (triangle choice, then s, then t).
+//
+// The Thea Mersenne-Twister stream (Code/Source/Random.cpp:49-132) is produced by one CTA: each 624-word twist runs as
+// three dependent phases of at most 227 independent updates (the second loop of Thea's generate() starts at N - M + 1,
+// so word N - M keeps its value), then all 624 words are tempered and written out. The counter mode draws the three
+// words of sample i from Philox-4x32-10 (Salmon et al., SC'11) keyed by the seed, which is fully parallel.
+#include "device_util.cuh"
+#include "query.hpp"
+
+namespace thea {
+namespace {
+
+constexpr int MT_N = 624, MT_M = 397;
+constexpr uint32_t MT_A = 0x9908B0DFu, MT_B = 0x9D2C5680u, MT_C = 0xEFC60000u;
+constexpr uint32_t MT_UPPER = 0x80000000u, MT_LOWER = 0x7fffffffu;
+constexpr int MT_THREADS = 256;
+
+__device__ __forceinline__ uint32_t mt_mix(uint32_t a, uint32_t b, uint32_t far) {
+  uint32_t x = (a & MT_UPPER) | (b & MT_LOWER);
+  return far ^ (x >> 1) ^ ((x & 1u) ? MT_A : 0u);
+}
+
+__device__ __forceinline__ uint32_t mt_temper(uint32_t r) {
+  r ^= r >> 11;
+  r ^= (r << 7) & MT_B;
+  r ^= (r << 15) & MT_C;
+  r ^= r >> 18;
+  return r;
+}
+
+// Writes `count` tempered words of Random(seed): Random::Random(seed) then bits() repeatedly.
+__global__ void __launch_bounds__(MT_THREADS) thea_mt_stream_kernel(uint32_t seed, int64_t count, uint32_t * __restrict__ out) {
+  __shared__ uint32_t s[MT_N];
+  int t = threadIdx.x;
+  if (t == 0) {
+    s[0] = seed;
+    for (int i = 1; i < MT_N; ++i) s[i] = 1812433253u * (s[i - 1] ^ (s[i - 1] >> 30)) + (uint32_t)i;
+  }
+  __syncthreads();
+  int64_t twists = ceil_div(count, MT_N);
+  for (int64_t k = 0; k < twists; ++k) {
+    uint32_t v;
+    // phase A: i in [0, N - M): uses old words i, i + 1, i + M
+    if (t < MT_N - MT_M) v = mt_mix(s[t], s[t + 1], s[t + MT_M]);
+    __syncthreads();
+    if (t < MT_N - MT_M) s[t] = v;
+    __syncthreads();
+    // phase B: i in [N - M + 1, 2 (N - M)): uses new word i - (N - M) and old words i, i + 1
+    int i = MT_N - MT_M + 1 + t;
+    if (i < 2 * (MT_N - MT_M)) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
+    __syncthreads();
+    if (i < 2 * (MT_N - MT_M)) s[i] = v;
+    __syncthreads();
+    // phase C: i in [2 (N - M), N - 1) and i = N - 1 (which pairs old word N - 1 with new word 0 and new word M - 1)
+    i = 2 * (MT_N - MT_M) + t;
+    if (i < MT_N - 1) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
+    else if (i == MT_N - 1) v = mt_mix(s[MT_N - 1], s[0], s[MT_M - 1]);
+    __syncthreads();
+    if (i < MT_N) s[i] = v;
+    __syncthreads();
+    int64_t base = k * MT_N;
+    for (int j = t; j < MT_N; j += MT_THREADS)
+      if (base + j < count) out[base + j] = mt_temper(s[j]);
+    // the next twist's phase A only reads s, and its first write follows a barrier
+  }
+}
+
+__global__ void tri_area_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t nf,
+                                float * __restrict__ area) {
+  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  V3 v0 = load_v3(V + 3 * (int64_t)F[3 * f]);
+  V3 v1 = load_v3(V + 3 * (int64_t)F[3 * f + 1]);
+  V3 v2 = load_v3(V + 3 * (int64_t)F[3 * f + 2]);
+  area[f] = tri_plane(v0, v1, v2).area;
+}
+
+// cum[i] = cum[i - 1] + area[i] in FP64, strictly in index order (MeshSampler.hpp:147-149, 166-169). One thread: the
+// sequence of roundings is what makes the triangle choice bit-identical. Areas are staged through shared memory by the
+// whole block so the serial chain only waits on shared-memory loads.
+__global__ void serial_cdf_kernel(float const * __restrict__ area, int64_t nf, double * __restrict__ cum) {
+  constexpr int CH = 2048;
+  __shared__ float a[CH];
+  __shared__ double c[CH];
+  double run = 0.0;
+  for (int64_t base = 0; base < nf; base += CH) {
+    int m = (nf - base) < CH ? (int)(nf - base) : CH;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) a[j] = area[base + j];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < m; ++j) {
+        run = (base + j == 0) ? (double)a[0] : run + (double)a[j];
+        c[j] = run;
+      }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) cum[base + j] = c[j];
+    __syncthreads();
+  }
+}
+
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3", SC'11)
+__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, ctr.x), lo0 = 0xD2511F53u * ctr.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, ctr.z), lo1 = 0xCD9E8D57u * ctr.z;
+    ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+    key.x += 0x9E3779B9u;
+    key.y += 0xBB67AE85u;
+  }
+  return ctr;
+}
+
+__global__ void sample_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t nf,
+                              double const * __restrict__ cum, uint32_t const * __restrict__ words, uint32_t seed,
+                              int64_t n, float * __restrict__ pos, float * __restrict__ nrm, int32_t * __restrict__ face) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t w0, w1, w2;
+  if (words) {
+    w0 = words[3 * i];
+    w1 = words[3 * i + 1];
+    w2 = words[3 * i + 2];
+  } else {
+    uint4 r = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), 0u, 0u), make_uint2(seed, 0x5EEDu));
+    w0 = r.x; w1 = r.y; w2 = r.z;
+  }
+  // Random::uniform01(): (float)bits() * (1.0f / (float)0xFFFFFFFF), the factor being 2^-32
+  float const NORM = 2.3283064365386963e-10f;
+  double total = cum[nf - 1];
+  double t = (double)(__uint2float_rn(w0) * NORM) * total;
+  // std::lower_bound: first position whose value is not less than t, clamped to the last triangle
+  int64_t lo = 0, len = nf;
+  while (len > 0) {
+    int64_t half = len >> 1;
+    if (cum[lo + half] < t) { lo = lo + half + 1; len = len - half - 1; }
+    else len = half;
+  }
+  int64_t tri = lo < nf - 1 ? lo : nf - 1;
+  V3 v0 = load_v3(V + 3 * (int64_t)F[3 * tri]);
+  V3 v1 = load_v3(V + 3 * (int64_t)F[3 * tri + 1]);
+  V3 v2 = load_v3(V + 3 * (int64_t)F[3 * tri + 2]);
+  V3 e01 = v1 - v0, e02 = v2 - v0;
+  float s = __uint2float_rn(w1) * NORM;
+  float u = __uint2float_rn(w2) * NORM;
+  if (s + u > 1.f) {
+    u = 1.f - u;
+    s = 1.f - s;
+  }
+  V3 p = (s * e01 + u * e02) + v0;
+  pos[3 * i] = p.x;
+  pos[3 * i + 1] = p.y;
+  pos[3 * i + 2] = p.z;
+  if (nrm) {
+    V3 nn = normalized(cross(e01, e02));
+    nrm[3 * i] = nn.x;
+    nrm[3 * i + 1] = nn.y;
+    nrm[3 * i + 2] = nn.z;
+  }
+  if (face) face[i] = (int32_t)tri;
+}
+
+}  // namespace
+
+int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
+                           float * pos, float * nrm, int32_t * face, cudaStream_t s) {
+  (void)nv;
+  if (n <= 0 || nf <= 0) return 0;
+  Scratch area((size_t)nf * sizeof(float), s);
+  Scratch cum((size_t)nf * sizeof(double), s);
+  THEA_LAUNCH(tri_area_kernel, (unsigned)ceil_div(nf, 256), 256, 0, s, V, F, nf, area.as<float>());
+  THEA_LAUNCH(serial_cdf_kernel, 1, 256, 0, s, area.as<float>(), nf, cum.as<double>());
+  double total = 0.0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&total, cum.as<double>() + nf - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (!(total > 0.0)) return 0;  // MeshSampler returns no samples for a zero-area mesh
+  Scratch words;
+  if (rng == THEA_RNG_THEA_MT) {
+    words = Scratch((size_t)n * 3 * sizeof(uint32_t), s);
+    THEA_LAUNCH(thea_mt_stream_kernel, 1, MT_THREADS, 0, s, seed, 3 * n, words.as<uint32_t>());
+  }
+  THEA_LAUNCH(sample_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, V, F, nf, cum.as<double>(), words.as<uint32_t>(),
+              seed, n, pos, nrm, face);
+  return n;
+}
+
+}  // namespace thea
