@@ -158,6 +158,30 @@ THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_ver
                                          float * out_positions, float * out_normals, int32_t * out_faces,
                                          int64_t * out_num_written, void * stream);
 
+/* ---- allocation-free sampling -------------------------------------------------------------------------------------- */
+
+/* Largest mesh (in triangles) that thea_sample_by_area_noalloc accepts. */
+#define THEA_NOALLOC_MAX_FACES 1048576
+
+/* Same results as thea_sample_by_area (bit-identical for both rng modes), for callers that cannot allocate device
+ * memory: a host application that hands this library a fixed device budget through its own pool allocator, a plugin that
+ * must not allocate behind its host's back, or a latency-critical loop that cannot afford cudaMalloc's implicit
+ * synchronization. This entry point has no counterpart in the reference (whose sampler runs on the CPU).
+ *
+ * It calls no cudaMalloc, cudaFree or other allocating routine. Its scratch (the cumulative-area table of up to
+ * THEA_NOALLOC_MAX_FACES triangles, the generator state and one chunk of random words: about 9 MiB) is a fixed device
+ * array inside the library, resident on every GPU that loads the library until the process exits. The caller passes
+ * device-resident inputs and outputs; host pointers and meshes with more than THEA_NOALLOC_MAX_FACES triangles are
+ * rejected with THEA_ERR_INVALID_ARGUMENT. The first call on each device looks up the array's device address (with that
+ * device current); make that first call before any stream capture. All calls on a device share the one array, and every
+ * call rewrites the parts it reads before reading them; calls whose work overlaps on the GPU (different streams or
+ * threads at the same time) race on it and must be serialized by the caller. The call synchronizes `stream` once, to
+ * read back the total area. */
+THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                                 int64_t num_faces, int64_t num_samples, uint32_t seed, int32_t rng,
+                                                 float * out_positions, float * out_normals, int32_t * out_faces,
+                                                 int64_t * out_num_written, void * stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -59,7 +59,11 @@ SIGNATURES = {
     "thea_k_closest": (ctypes.c_int, [_vp, _vp, _i64, _i32, _f32, _vp, _vp, _vp, _vp]),
     "thea_k_closest_self": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp]),
     "thea_sample_by_area": (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _u32, _i32, _vp, _vp, _vp, _i64p, _vp]),
+    "thea_sample_by_area_noalloc": (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _u32, _i32, _vp, _vp, _vp, _i64p,
+                                                   _vp]),
 }
+
+NOALLOC_MAX_FACES = 1048576
 
 _lib = None
 

@@ -483,4 +483,26 @@ THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_ver
   });
 }
 
+THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                                 int64_t num_faces, int64_t num_samples, uint32_t seed, int32_t rng,
+                                                 float * out_positions, float * out_normals, int32_t * out_faces,
+                                                 int64_t * out_num_written, void * stream) {
+  return guarded([&] {
+    if (out_num_written) *out_num_written = 0;
+    THEA_REQUIRE(rng == THEA_RNG_THEA_MT || rng == THEA_RNG_COUNTER, "sample_by_area_noalloc: unknown rng");
+    THEA_REQUIRE(num_samples >= 0, "sample_by_area_noalloc: negative sample count");
+    THEA_REQUIRE(num_faces <= THEA_NOALLOC_MAX_FACES,
+                 "sample_by_area_noalloc: the mesh has more than THEA_NOALLOC_MAX_FACES triangles");
+    if (num_samples == 0) return;
+    THEA_REQUIRE(vertices && faces && num_vertices > 0 && num_faces > 0, "sample_by_area_noalloc: empty mesh");
+    THEA_REQUIRE(out_positions, "sample_by_area_noalloc: out_positions is null");
+    void const * arrays[5] = {vertices, faces, out_positions, out_normals, out_faces};
+    for (void const * p : arrays)
+      THEA_REQUIRE(!p || !is_host_pointer(p), "sample_by_area_noalloc: every array must be device memory");
+    int64_t got = run_sample_by_area_noalloc(vertices, num_vertices, faces, num_faces, num_samples, seed, rng,
+                                             out_positions, out_normals, out_faces, (cudaStream_t)stream);
+    if (out_num_written) *out_num_written = got;
+  });
+}
+
 }  // extern "C"

@@ -18,4 +18,8 @@ void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
                            float * pos, float * nrm, int32_t * face, cudaStream_t s);
 
+// The same computation with all scratch in a fixed device array (no allocation); device pointers only.
+int64_t run_sample_by_area_noalloc(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n,
+                                   uint32_t seed, int rng, float * pos, float * nrm, int32_t * face, cudaStream_t s);
+
 }  // namespace thea

@@ -13,6 +13,9 @@
 #include "device_util.cuh"
 #include "query.hpp"
 
+#include <mutex>
+#include <string>
+
 namespace thea {
 namespace {
 
@@ -167,7 +170,149 @@ __global__ void sample_kernel(float const * __restrict__ V, int32_t const * __re
   if (face) face[i] = (int32_t)tri;
 }
 
+//============================================================================================================================
+// Allocation-free sampling. Its scratch lives in one file-scope device array instead of the stream-ordered pool:
+//   cum[]      FP64 cumulative areas, at most NOALLOC_MAX_FACES triangles (8 MiB)
+//   mt_state[] the Mersenne-Twister state carried from one chunk of samples to the next (2.4 KiB)
+//   words[]    the stream words of one chunk of NOALLOC_CHUNK samples (768 KiB)
+// Chunks hold 65,520 samples = 196,560 words = 315 whole twists, so each chunk ends on a twist boundary and the next
+// chunk resumes from the saved state with exactly the words the one-shot path would draw.
+//============================================================================================================================
+
+constexpr int64_t NOALLOC_CHUNK = 208 * 315;
+static_assert((3 * NOALLOC_CHUNK) % MT_N == 0, "a chunk must consume whole twists");
+
+struct NoAllocLayout {
+  double cum[THEA_NOALLOC_MAX_FACES];
+  uint32_t mt_state[MT_N];
+  uint32_t words[3 * NOALLOC_CHUNK];
+};
+
+// Per-face areas computed in place (the same tri_plane arithmetic as tri_area_kernel) and summed in index order by one
+// thread, exactly as serial_cdf_kernel does; no separate area array is needed.
+__global__ void noalloc_cdf_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t nf,
+                                   double * __restrict__ cum) {
+  constexpr int CH = 2048;
+  __shared__ float a[CH];
+  __shared__ double c[CH];
+  double run = 0.0;
+  for (int64_t base = 0; base < nf; base += CH) {
+    int m = (nf - base) < CH ? (int)(nf - base) : CH;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+      int64_t f = base + j;
+      V3 v0 = load_v3(V + 3 * (int64_t)F[3 * f]);
+      V3 v1 = load_v3(V + 3 * (int64_t)F[3 * f + 1]);
+      V3 v2 = load_v3(V + 3 * (int64_t)F[3 * f + 2]);
+      a[j] = tri_plane(v0, v1, v2).area;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < m; ++j) {
+        run = (base + j == 0) ? (double)a[0] : run + (double)a[j];
+        c[j] = run;
+      }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) cum[base + j] = c[j];
+    __syncthreads();
+  }
+}
+
+// Resumable form of thea_mt_stream_kernel: seeds the state when `first` is set, otherwise continues from `state`, and
+// stores the state back after the last twist.
+__global__ void __launch_bounds__(MT_THREADS) noalloc_mt_kernel(uint32_t seed, int first, uint32_t * __restrict__ state,
+                                                                int64_t count, uint32_t * __restrict__ out) {
+  __shared__ uint32_t s[MT_N];
+  int t = threadIdx.x;
+  if (first) {
+    if (t == 0) {
+      s[0] = seed;
+      for (int i = 1; i < MT_N; ++i) s[i] = 1812433253u * (s[i - 1] ^ (s[i - 1] >> 30)) + (uint32_t)i;
+    }
+  } else {
+    for (int j = t; j < MT_N; j += MT_THREADS) s[j] = state[j];
+  }
+  __syncthreads();
+  int64_t twists = ceil_div(count, MT_N);
+  for (int64_t k = 0; k < twists; ++k) {
+    uint32_t v;
+    if (t < MT_N - MT_M) v = mt_mix(s[t], s[t + 1], s[t + MT_M]);
+    __syncthreads();
+    if (t < MT_N - MT_M) s[t] = v;
+    __syncthreads();
+    int i = MT_N - MT_M + 1 + t;
+    if (i < 2 * (MT_N - MT_M)) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
+    __syncthreads();
+    if (i < 2 * (MT_N - MT_M)) s[i] = v;
+    __syncthreads();
+    i = 2 * (MT_N - MT_M) + t;
+    if (i < MT_N - 1) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
+    else if (i == MT_N - 1) v = mt_mix(s[MT_N - 1], s[0], s[MT_M - 1]);
+    __syncthreads();
+    if (i < MT_N) s[i] = v;
+    __syncthreads();
+    int64_t base = k * MT_N;
+    for (int j = t; j < MT_N; j += MT_THREADS)
+      if (base + j < count) out[base + j] = mt_temper(s[j]);
+  }
+  __syncthreads();
+  for (int j = t; j < MT_N; j += MT_THREADS) state[j] = s[j];
+}
+
 }  // namespace
+
+// The scratch of every allocation-free call on a device. In host code the name is only a stand-in: its device address
+// comes from cudaGetSymbolAddress (noalloc_scratch below).
+static __device__ __align__(256) unsigned char g_sample_scratch[sizeof(NoAllocLayout)];
+
+// Device address of g_sample_scratch on the current device, looked up once per device (with that device current) and
+// cached; the lookup loads the library's module on the device if needed.
+static NoAllocLayout * noalloc_scratch() {
+  static std::mutex m;
+  static NoAllocLayout * addr[256] = {};
+  int dev = 0;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  THEA_REQUIRE(dev >= 0 && dev < 256, "sample_by_area_noalloc: device ordinal out of range");
+  std::lock_guard<std::mutex> lk(m);
+  if (!addr[dev]) {
+    void * p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sample_scratch);
+    if (e != cudaSuccess || !p)
+      throw Error(THEA_ERR_CUDA, std::string("sample_by_area_noalloc: cudaGetSymbolAddress failed: ") +
+                                     cudaGetErrorString(e));
+    addr[dev] = static_cast<NoAllocLayout *>(p);
+  }
+  return addr[dev];
+}
+
+int64_t run_sample_by_area_noalloc(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n,
+                                   uint32_t seed, int rng, float * pos, float * nrm, int32_t * face, cudaStream_t s) {
+  (void)nv;
+  THEA_REQUIRE(nf <= THEA_NOALLOC_MAX_FACES,
+               "sample_by_area_noalloc: at most " + std::to_string((long long)THEA_NOALLOC_MAX_FACES) +
+                   " triangles (got " + std::to_string((long long)nf) + ")");
+  NoAllocLayout * scratch = noalloc_scratch();
+  if (n <= 0 || nf <= 0) return 0;
+  THEA_LAUNCH(noalloc_cdf_kernel, 1, 256, 0, s, V, F, nf, scratch->cum);
+  double total = 0.0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&total, scratch->cum + nf - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (!(total > 0.0)) return 0;
+  if (rng == THEA_RNG_COUNTER) {
+    THEA_LAUNCH(sample_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, V, F, nf, (double const *)scratch->cum,
+                (uint32_t const *)nullptr, seed, n, pos, nrm, face);
+    return n;
+  }
+  for (int64_t begin = 0; begin < n; begin += NOALLOC_CHUNK) {
+    int64_t cnt = n - begin < NOALLOC_CHUNK ? n - begin : NOALLOC_CHUNK;
+    THEA_LAUNCH(noalloc_mt_kernel, 1, MT_THREADS, 0, s, seed, begin == 0 ? 1 : 0, scratch->mt_state, 3 * cnt,
+                scratch->words);
+    THEA_LAUNCH(sample_kernel, (unsigned)ceil_div(cnt, 256), 256, 0, s, V, F, nf, (double const *)scratch->cum,
+                (uint32_t const *)scratch->words, seed, cnt, pos + 3 * begin, nrm ? nrm + 3 * begin : nullptr,
+                face ? face + begin : nullptr);
+  }
+  return n;
+}
 
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
                            float * pos, float * nrm, int32_t * face, cudaStream_t s) {
