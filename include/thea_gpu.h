@@ -60,7 +60,8 @@ typedef struct thea_build_config {
   int32_t width;          /* children per node: 4 or 8 (0 = default 4) */
   int32_t max_leaf_size;  /* elements per leaf, 1..16 (0 = default: 4 for meshes, 8 for points) */
   uint32_t layouts;       /* THEA_LAYOUT_* mask for meshes (0 = both) */
-  int32_t reserved[5];    /* must be zero */
+  int32_t query_order;    /* 1: traverse large query batches in Morton order of the query point; 0: caller order */
+  int32_t reserved[4];    /* must be zero */
 } thea_build_config;
 
 typedef struct thea_bvh_info {
@@ -129,6 +130,36 @@ THEA_API thea_status thea_ray_intersection(const thea_bvh * mesh_bvh, const floa
                                            int64_t num_rays, float max_time, float * out_time, int32_t * out_index,
                                            float * out_normal, void * stream);
 
+/* ---- precision modes ------------------------------------------------------------------------------------------------ */
+
+/* FP32_REFERENCE: the reference's FP32 arithmetic, bit for bit (the plain calls above use it).
+ * FP64_RECHECK: mixed precision. Closest element: FP32 traversal and element tests, and every element whose FP32
+ * distance lies within a band of the best (relative 2^-14 plus 2^-18 of the coordinate scale) is re-evaluated in FP64;
+ * the result is the FP64 nearest element (ties: lowest index) with its FP64 distance and closest point, rounded to FP32.
+ * Ray: the reference's FP32 verdict stays the primary result and, beside it, the watertight FP64 test (Woop, Benthin,
+ * Wald 2013) of every element the FP32 test accepted or rejected by a narrow margin gives an FP64 verdict. */
+#define THEA_PRECISION_FP32_REFERENCE 0
+#define THEA_PRECISION_FP64_RECHECK 1
+
+#define THEA_RAY_FLAG_HIT_DIFFERS 1     /* the FP32 and FP64 verdicts disagree on hit vs miss */
+#define THEA_RAY_FLAG_ELEMENT_DIFFERS 2 /* both hit, different elements */
+
+/* thea_closest_element with a precision mode and, if out_error is non-NULL, per query the absolute difference between
+ * the returned distance and the FP64 distance of the returned element (-1 when none). No reference counterpart beyond
+ * BvhN::closestElement (BvhN.hpp:1050-1063), whose arithmetic is FP32. */
+THEA_API thea_status thea_closest_element_ex(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
+                                             float dist_bound, int32_t precision, int32_t * out_index,
+                                             float * out_distance, float * out_closest_point, float * out_error,
+                                             void * stream);
+
+/* thea_ray_intersection with a precision mode. In FP64_RECHECK mode the optional outputs receive the watertight FP64
+ * verdict (time -1 / index -1 on a miss) and THEA_RAY_FLAG_* bits where it differs from the FP32 verdict. */
+THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const float * origins,
+                                              const float * directions, int64_t num_rays, float max_time,
+                                              int32_t precision, float * out_time, int32_t * out_index,
+                                              float * out_normal, float * out_time_fp64, int32_t * out_index_fp64,
+                                              int32_t * out_flags, void * stream);
+
 /* k nearest points of a point BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
  * index first). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
  * Code/Source/Algorithms/PointSet3.hpp:576-583). dist_bound < 0: unbounded; else only squared distances strictly below
@@ -141,6 +172,79 @@ THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * qu
 /* k-nearest-neighbour graph of the BVH's own points: query i is point i, excluding itself. Rows in point order. */
 THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,
                                          float * out_sq_distance, void * stream);
+
+/* ---- forests and batched queries ------------------------------------------------------------------------------------ */
+
+/* A forest holds one BVH per mesh (or point set), built together in one pass. Mesh m owns faces
+ * [mesh_face_offsets[m], mesh_face_offsets[m+1]) of `faces` (host array of num_meshes + 1 entries, each mesh non-empty);
+ * faces index the shared `vertices` array. Results report element indices within their own mesh. A forest is a
+ * thea_bvh: thea_bvh_destroy releases it. No reference counterpart: the reference builds one BvhN per mesh
+ * (BvhN.hpp:705); this replaces a loop of MeshBvh::init calls. */
+THEA_API thea_status thea_mesh_forest_build(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                            const int64_t * mesh_face_offsets, int32_t num_meshes,
+                                            const thea_build_config * config, void * stream, thea_bvh ** out_forest);
+
+/* One point BVH per point set: set m owns points [set_offsets[m], set_offsets[m+1]) (host array, sets non-empty). */
+THEA_API thea_status thea_point_forest_build(const float * points, const int64_t * set_offsets, int32_t num_sets,
+                                             const thea_build_config * config, void * stream,
+                                             thea_bvh ** out_forest);
+
+/* Batched queries in one persistent launch. Queries are grouped by mesh: queries of mesh m are
+ * [query_offsets[m], query_offsets[m+1]) (num_meshes + 1 entries). Every array must be device memory; the calls are
+ * asynchronous on `stream`, allocate only from the library's stream-ordered pool and never synchronize, so a sequence of
+ * them can be captured with thea_graph_capture_begin/end. queries_per_warp: queries a warp takes per work fetch
+ * (multiple of 32; 0 = 64). Per-query results as the single-BVH calls; the loop of closestElement calls over many meshes
+ * that this replaces is the reference's only form.
+ * hard_query_budget (closest element only): each query first runs on one thread for at most this many traversal steps;
+ * queries that need more (points deep inside a closed mesh, where thousands of nodes lie within the bound) are then
+ * finished by a whole warp each, 32 lanes expanding nodes together. 0 = default (32), negative = one thread per query
+ * throughout. Results do not depend on it. */
+THEA_API thea_status thea_batch_closest_element(const thea_bvh * mesh_forest, const float * queries,
+                                                const int64_t * query_offsets, int64_t num_queries, float dist_bound,
+                                                int32_t precision, int32_t queries_per_warp, int32_t hard_query_budget,
+                                                int32_t * out_index, float * out_distance, float * out_closest_point,
+                                                float * out_error, void * stream);
+THEA_API thea_status thea_batch_ray_intersection(const thea_bvh * mesh_forest, const float * origins,
+                                                 const float * directions, const int64_t * query_offsets,
+                                                 int64_t num_rays, float max_time, int32_t queries_per_warp,
+                                                 float * out_time, int32_t * out_index, void * stream);
+THEA_API thea_status thea_batch_k_closest(const thea_bvh * point_forest, const float * queries,
+                                          const int64_t * query_offsets, int64_t num_queries, int32_t k,
+                                          float dist_bound, int32_t queries_per_warp, int32_t * out_index,
+                                          float * out_sq_distance, void * stream);
+
+/* ---- CUDA graphs ------------------------------------------------------------------------------------------------------ */
+
+typedef struct thea_graph thea_graph;
+
+/* Captures the asynchronous calls issued on `stream` between begin and end (thread-local capture mode) into a CUDA
+ * graph, instantiated for replay with thea_graph_launch. Calls that synchronize (host arrays, builds, sampling) cannot
+ * be captured. */
+THEA_API thea_status thea_graph_capture_begin(void * stream);
+THEA_API thea_status thea_graph_capture_end(void * stream, thea_graph ** out_graph);
+THEA_API thea_status thea_graph_launch(thea_graph * graph, void * stream);
+THEA_API thea_status thea_graph_destroy(thea_graph * graph);
+
+/* ---- autotuning ------------------------------------------------------------------------------------------------------- */
+
+typedef struct thea_tuning {
+  int32_t width;              /* chosen BVH width */
+  int32_t max_leaf_size;      /* chosen leaf size */
+  int32_t queries_per_warp;   /* chosen work-fetch size */
+  float milliseconds;         /* time of the chosen configuration on the sample */
+  int32_t candidates;         /* configurations timed */
+  int32_t hard_query_budget;  /* chosen per-thread step budget (-1: one thread per query throughout) */
+  int32_t reserved[2];
+} thea_tuning;
+
+/* Times batched closest-point queries on a sample workload (a mesh forest's inputs plus device queries grouped by
+ * mesh) for every BVH width (4, 8) and leaf size (1, 2, 4): queries-per-warp (32, 64, 128) at the default step budget,
+ * then step budgets (12, 96, none) at the best queries-per-warp; returns the fastest. Synchronizes the stream. */
+THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                                 const int64_t * mesh_face_offsets, int32_t num_meshes,
+                                                 const float * queries, const int64_t * query_offsets,
+                                                 int64_t num_queries, int32_t precision, void * stream,
+                                                 thea_tuning * out_tuning);
 
 /* ---- sampling ------------------------------------------------------------------------------------------------------ */
 

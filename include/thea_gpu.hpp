@@ -34,11 +34,13 @@ struct BuildOptions {
   int32_t width = 4;          // 4 or 8 children per node
   int32_t max_leaf_size = 0;  // 0: library default
   uint32_t layouts = 0;       // THEA_LAYOUT_* mask for meshes, 0 = both
+  int32_t query_order = 0;    // 1: traverse large batches in Morton order of the query point
   thea_build_config config() const {
     thea_build_config c{};
     c.width = width;
     c.max_leaf_size = max_leaf_size;
     c.layouts = layouts;
+    c.query_order = query_order;
     return c;
   }
 };

@@ -31,7 +31,7 @@ _i64p = ctypes.POINTER(ctypes.c_int64)
 
 class BuildConfig(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32), ("layouts", ctypes.c_uint32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("query_order", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class BvhInfo(ctypes.Structure):
@@ -39,6 +39,12 @@ class BvhInfo(ctypes.Structure):
                 ("max_leaf_size", ctypes.c_int32), ("is_mesh", ctypes.c_int32), ("depth", ctypes.c_int32),
                 ("device_bytes", ctypes.c_int64), ("bounds_lo", ctypes.c_float * 3), ("bounds_hi", ctypes.c_float * 3),
                 ("device_error_bits", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32), ("queries_per_warp", ctypes.c_int32),
+                ("milliseconds", ctypes.c_float), ("candidates", ctypes.c_int32),
+                ("hard_query_budget", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 SIGNATURES = {
@@ -61,7 +67,28 @@ SIGNATURES = {
     "thea_sample_by_area": (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _u32, _i32, _vp, _vp, _vp, _i64p, _vp]),
     "thea_sample_by_area_noalloc": (ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _u32, _i32, _vp, _vp, _vp, _i64p,
                                                    _vp]),
+    "thea_closest_element_ex": (ctypes.c_int, [_vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "thea_ray_intersection_ex": (ctypes.c_int, [_vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "thea_mesh_forest_build": (ctypes.c_int, [_vp, _i64, _vp, _i64p, _i32, ctypes.POINTER(BuildConfig), _vp,
+                                              ctypes.POINTER(_vp)]),
+    "thea_point_forest_build": (ctypes.c_int, [_vp, _i64p, _i32, ctypes.POINTER(BuildConfig), _vp,
+                                               ctypes.POINTER(_vp)]),
+    "thea_batch_closest_element": (ctypes.c_int, [_vp, _vp, _vp, _i64, _f32, _i32, _i32, _i32, _vp, _vp, _vp, _vp,
+                                                  _vp]),
+    "thea_batch_ray_intersection": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp, _vp]),
+    "thea_batch_k_closest": (ctypes.c_int, [_vp, _vp, _vp, _i64, _i32, _f32, _i32, _vp, _vp, _vp]),
+    "thea_graph_capture_begin": (ctypes.c_int, [_vp]),
+    "thea_graph_capture_end": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "thea_graph_launch": (ctypes.c_int, [_vp, _vp]),
+    "thea_graph_destroy": (ctypes.c_int, [_vp]),
+    "thea_autotune_batch_closest": (ctypes.c_int, [_vp, _i64, _vp, _i64p, _i32, _vp, _vp, _i64, _i32, _vp,
+                                                   ctypes.POINTER(Tuning)]),
 }
+
+PRECISION_FP32_REFERENCE = 0
+PRECISION_FP64_RECHECK = 1
+RAY_FLAG_HIT_DIFFERS = 1
+RAY_FLAG_ELEMENT_DIFFERS = 2
 
 NOALLOC_MAX_FACES = 1048576
 

@@ -62,11 +62,12 @@ class _Arrays:
         return arr, ctypes.c_void_p(arr.ctypes.data if arr.size else 0)
 
 
-def _config(width, max_leaf_size, layouts):
+def _config(width, max_leaf_size, layouts, query_order=0):
     cfg = N.BuildConfig()
     cfg.width = int(width)
     cfg.max_leaf_size = int(max_leaf_size)
     cfg.layouts = int(layouts)
+    cfg.query_order = int(query_order)
     return cfg
 
 
@@ -101,12 +102,12 @@ class _Bvh:
 class MeshBvh(_Bvh):
     """BVH over the triangles of a mesh (MeshBvh::add + MeshBvh::init). Element index = face index."""
 
-    def __init__(self, vertices, faces, width=4, max_leaf_size=0, layouts=0):
+    def __init__(self, vertices, faces, width=4, max_leaf_size=0, layouts=0, query_order=0):
         super().__init__()
         io = _Arrays(vertices)
         pv, nv = io.input(vertices, np.float32, 3)
         pf, nf = io.input(faces, np.int32, 3)
-        cfg = _config(width, max_leaf_size, layouts)
+        cfg = _config(width, max_leaf_size, layouts, query_order)
         N.check(N.lib().thea_mesh_bvh_build(pv, nv, pf, nf, ctypes.byref(cfg), _stream_of(io.device),
                                             ctypes.byref(self._h)))
 
@@ -139,15 +140,170 @@ class MeshBvh(_Bvh):
         """BvhN::rayIntersectionTime: hit time per ray, -1 on a miss."""
         return self.ray_structure_intersection(origins, directions, max_time)[0]
 
+    def closest_element_ex(self, queries, dist_bound=-1.0, precision="fp32", closest_points=True, errors=True):
+        """closest_element with a precision mode ("fp32": the reference's arithmetic; "fp64": FP64 re-check band) and
+        per-query |returned distance - FP64 distance of the returned element|: (index, distance, cp, error)."""
+        io = _Arrays(queries)
+        pq, n = io.input(queries, np.float32, 3)
+        idx, pidx = io.output((n,), np.int32)
+        dist, pdist = io.output((n,), np.float32)
+        cp, pcp = io.output((n, 3), np.float32) if closest_points else (None, None)
+        err, perr = io.output((n,), np.float32) if errors else (None, None)
+        N.check(N.lib().thea_closest_element_ex(self._h, pq, n, float(dist_bound), _precision(precision), pidx, pdist,
+                                                pcp, perr, _stream_of(io.device)))
+        return idx, dist, cp, err
+
+    def ray_structure_intersection_ex(self, origins, directions, max_time=-1.0, precision="fp64"):
+        """Ray first hit with the FP64 watertight verdict beside the reference's FP32 one:
+        (time, index, time_fp64, index_fp64, flags)."""
+        io = _Arrays(origins)
+        po, n = io.input(origins, np.float32, 3)
+        pd, _ = io.input(directions, np.float32, 3)
+        t, pt = io.output((n,), np.float32)
+        idx, pidx = io.output((n,), np.int32)
+        t64, pt64 = io.output((n,), np.float32)
+        i64, pi64 = io.output((n,), np.int32)
+        fl, pfl = io.output((n,), np.int32)
+        N.check(N.lib().thea_ray_intersection_ex(self._h, po, pd, n, float(max_time), _precision(precision), pt, pidx,
+                                                 None, pt64, pi64, pfl, _stream_of(io.device)))
+        return t, idx, t64, i64, fl
+
+
+def _precision(p):
+    return {"fp32": N.PRECISION_FP32_REFERENCE, "fp64": N.PRECISION_FP64_RECHECK}[p]
+
+
+def _offsets_ptr(off):
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    return off, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+
+
+class MeshForest(_Bvh):
+    """One BVH per mesh, built in one pass (thea_mesh_forest_build). `faces` index the shared vertex array; mesh m owns
+    faces [face_offsets[m], face_offsets[m+1]). Queries are CUDA tensors grouped by mesh (query_offsets, int64 CUDA)."""
+
+    def __init__(self, vertices, faces, face_offsets, width=4, max_leaf_size=0, layouts=0):
+        super().__init__()
+        io = _Arrays(vertices)
+        pv, nv = io.input(vertices, np.float32, 3)
+        pf, _ = io.input(faces, np.int32, 3)
+        self._off, poff = _offsets_ptr(face_offsets)
+        self.num_meshes = len(self._off) - 1
+        cfg = _config(width, max_leaf_size, layouts)
+        N.check(N.lib().thea_mesh_forest_build(pv, nv, pf, poff, self.num_meshes, ctypes.byref(cfg),
+                                               _stream_of(io.device), ctypes.byref(self._h)))
+
+    def batch_closest_element(self, queries, query_offsets, dist_bound=-1.0, precision="fp32", queries_per_warp=0,
+                              hard_query_budget=0, closest_points=False, errors=False, out=None):
+        import torch
+        n = queries.shape[0]
+        if out is None:
+            out = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda"),
+                   torch.empty((n, 3), dtype=torch.float32, device="cuda") if closest_points else None,
+                   torch.empty(n, dtype=torch.float32, device="cuda") if errors else None)
+        idx, dist, cp, err = out
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        N.check(N.lib().thea_batch_closest_element(self._h, ptr(queries), ptr(query_offsets), n, float(dist_bound),
+                                                   _precision(precision), int(queries_per_warp),
+                                                   int(hard_query_budget), ptr(idx), ptr(dist), ptr(cp), ptr(err),
+                                                   _stream_of(True)))
+        return out
+
+    def batch_ray_intersection(self, origins, directions, query_offsets, max_time=-1.0, queries_per_warp=0):
+        import torch
+        n = origins.shape[0]
+        t = torch.empty(n, dtype=torch.float32, device="cuda")
+        idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        ptr = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+        N.check(N.lib().thea_batch_ray_intersection(self._h, ptr(origins), ptr(directions), ptr(query_offsets), n,
+                                                    float(max_time), int(queries_per_warp), ptr(t), ptr(idx),
+                                                    _stream_of(True)))
+        return t, idx
+
+
+class PointForest(_Bvh):
+    """One point BVH per point set (thea_point_forest_build); set m owns points [set_offsets[m], set_offsets[m+1])."""
+
+    def __init__(self, points, set_offsets, width=4, max_leaf_size=0):
+        super().__init__()
+        io = _Arrays(points)
+        pp, _ = io.input(points, np.float32, 3)
+        self._off, poff = _offsets_ptr(set_offsets)
+        cfg = _config(width, max_leaf_size, 0)
+        N.check(N.lib().thea_point_forest_build(pp, poff, len(self._off) - 1, ctypes.byref(cfg), _stream_of(io.device),
+                                                ctypes.byref(self._h)))
+
+    def batch_k_closest(self, queries, query_offsets, k, dist_bound=-1.0, queries_per_warp=0):
+        import torch
+        n = queries.shape[0]
+        idx = torch.empty((n, k), dtype=torch.int32, device="cuda")
+        d2 = torch.empty((n, k), dtype=torch.float32, device="cuda")
+        ptr = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+        N.check(N.lib().thea_batch_k_closest(self._h, ptr(queries), ptr(query_offsets), n, int(k), float(dist_bound),
+                                             int(queries_per_warp), ptr(idx), ptr(d2), _stream_of(True)))
+        return idx, d2
+
+
+class Graph:
+    """A CUDA graph captured from library calls issued on torch's current (non-default) stream:
+
+        with Graph() as g:
+            forest.batch_closest_element(...)
+        g.launch()
+    """
+
+    def __init__(self):
+        self._g = ctypes.c_void_p()
+
+    def __enter__(self):
+        import torch
+        self._stream = torch.cuda.current_stream()
+        N.check(N.lib().thea_graph_capture_begin(ctypes.c_void_p(self._stream.cuda_stream)))
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        st = N.lib().thea_graph_capture_end(ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self._g))
+        if exc_type is None:
+            N.check(st)
+
+    def launch(self):
+        import torch
+        N.check(N.lib().thea_graph_launch(self._g, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+    def close(self):
+        if self._g:
+            N.check(N.lib().thea_graph_destroy(self._g))
+            self._g = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_batch_closest(vertices, faces, face_offsets, queries, query_offsets, precision="fp32"):
+    """Times width x leaf size x queries-per-warp on a sample workload; returns the fastest as a dict."""
+    io = _Arrays(vertices)
+    pv, nv = io.input(vertices, np.float32, 3)
+    pf, _ = io.input(faces, np.int32, 3)
+    off, poff = _offsets_ptr(face_offsets)
+    t = N.Tuning()
+    N.check(N.lib().thea_autotune_batch_closest(pv, nv, pf, poff, len(off) - 1, ctypes.c_void_p(queries.data_ptr()),
+                                                ctypes.c_void_p(query_offsets.data_ptr()), queries.shape[0],
+                                                _precision(precision), _stream_of(True), ctypes.byref(t)))
+    return {"width": t.width, "max_leaf_size": t.max_leaf_size, "queries_per_warp": t.queries_per_warp,
+            "hard_query_budget": t.hard_query_budget, "milliseconds": t.milliseconds, "candidates": t.candidates}
+
 
 class PointBvh(_Bvh):
     """BVH over points (BvhN<Vector3, 3>). Element index = point index."""
 
-    def __init__(self, points, width=4, max_leaf_size=0):
+    def __init__(self, points, width=4, max_leaf_size=0, query_order=0):
         super().__init__()
         io = _Arrays(points)
         pp, n = io.input(points, np.float32, 3)
-        cfg = _config(width, max_leaf_size, 0)
+        cfg = _config(width, max_leaf_size, 0, query_order)
         N.check(N.lib().thea_point_bvh_build(pp, n, ctypes.byref(cfg), _stream_of(io.device), ctypes.byref(self._h)))
         self.n = n
 

@@ -3,7 +3,9 @@
 #include "bvh.hpp"
 #include "device_util.cuh"
 #include "query.hpp"
+#include "batch.hpp"
 
+#include <initializer_list>
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -51,6 +53,31 @@ void note_launch_end(char const * kernel_name, cudaStream_t stream, cudaEvent_t 
   cudaEventRecord(end, stream);
   std::lock_guard<std::mutex> lk(g_prof_mutex);
   g_prof.push_back(TimedLaunch{kernel_name, begin_event, end});
+}
+
+//============================================================================================================================
+// Scratch memory pool
+//============================================================================================================================
+
+cudaMemPool_t scratch_pool() {
+  static std::mutex m;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(m);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool;
+  THEA_CUDA_CHECK(cudaMemPoolCreate(&pool, &props));
+  uint64_t keep = ~uint64_t(0);
+  THEA_CUDA_CHECK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  pools[dev] = pool;
+  return pool;
 }
 
 //============================================================================================================================
@@ -289,7 +316,8 @@ THEA_API thea_status thea_profiling_read(const char * kernel_substring, double *
 
 static void check_config(thea_build_config const * cfg) {
   if (!cfg) return;
-  for (int i = 0; i < 5; ++i) THEA_REQUIRE(cfg->reserved[i] == 0, "build config: reserved fields must be zero");
+  for (int i = 0; i < 4; ++i) THEA_REQUIRE(cfg->reserved[i] == 0, "build config: reserved fields must be zero");
+  THEA_REQUIRE(cfg->query_order == 0 || cfg->query_order == 1, "build config: query_order must be 0 or 1");
 }
 
 THEA_API thea_status thea_mesh_bvh_build(const float * vertices, int64_t num_vertices, const int32_t * faces,
@@ -358,24 +386,72 @@ THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * inf
   });
 }
 
+static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries, float dist_bound,
+                         int32_t precision, int32_t * out_index, float * out_distance, float * out_closest_point,
+                         float * out_error, void * stream) {
+  THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "closest_element: a mesh BVH is required");
+  THEA_REQUIRE(mesh_bvh->cp_rec, "closest_element: the BVH was built without THEA_LAYOUT_CLOSEST");
+  THEA_REQUIRE(precision == THEA_PRECISION_FP32_REFERENCE || precision == THEA_PRECISION_FP64_RECHECK,
+               "closest_element: unknown precision mode");
+  THEA_REQUIRE(num_queries >= 0, "closest_element: negative query count");
+  if (num_queries == 0) return;
+  THEA_REQUIRE(queries && out_index, "closest_element: null queries or out_index");
+  ClosestParams cp;
+  cp.thresh = bound_threshold(dist_bound);
+  cp.bound2 = dist_bound >= 0.f ? (double)dist_bound * (double)dist_bound : -1.0;
+  cp.precision = precision;
+  cp.scene_scale = scene_scale_of(mesh_bvh);
+  unsigned * err = handle_error_word(mesh_bvh);
+  run_staged({{(void *)queries, 12, false, false}, {out_index, 4, true, false}, {out_distance, 4, true, false},
+              {out_closest_point, 12, true, false}, {out_error, 4, true, false}},
+             num_queries, (cudaStream_t)stream,
+             [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+               run_closest(mesh_bvh, (float const *)p[0], cnt, cp, (int32_t *)p[1], (float *)p[2], (float *)p[3],
+                           (float *)p[4], err, s);
+             });
+}
+
+static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const float * directions, int64_t num_rays,
+                     float max_time, int32_t precision, float * out_time, int32_t * out_index, float * out_normal,
+                     float * out_time64, int32_t * out_index64, int32_t * out_flags, void * stream) {
+  THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "ray_intersection: a mesh BVH is required");
+  THEA_REQUIRE(mesh_bvh->ray_rec, "ray_intersection: the BVH was built without THEA_LAYOUT_RAY");
+  THEA_REQUIRE(precision == THEA_PRECISION_FP32_REFERENCE || precision == THEA_PRECISION_FP64_RECHECK,
+               "ray_intersection: unknown precision mode");
+  THEA_REQUIRE(num_rays >= 0, "ray_intersection: negative ray count");
+  if (num_rays == 0) return;
+  THEA_REQUIRE(origins && directions && out_time, "ray_intersection: null origins, directions or out_time");
+  unsigned * err = handle_error_word(mesh_bvh);
+  RayParams rp;
+  rp.max_time = max_time >= 0.f ? max_time : -1.f;
+  rp.recheck = precision == THEA_PRECISION_FP64_RECHECK;
+  if (!rp.recheck) out_time64 = nullptr, out_index64 = nullptr, out_flags = nullptr;
+  run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
+              {out_index, 4, true, false}, {out_normal, 12, true, false}, {out_time64, 4, true, false},
+              {out_index64, 4, true, false}, {out_flags, 4, true, false}},
+             num_rays, (cudaStream_t)stream,
+             [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+               run_ray(mesh_bvh, (float const *)p[0], (float const *)p[1], cnt, rp, (float *)p[2], (int32_t *)p[3],
+                       (float *)p[4], (float *)p[5], (int32_t *)p[6], (int32_t *)p[7], err, s);
+             });
+}
+
 THEA_API thea_status thea_closest_element(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
                                           float dist_bound, int32_t * out_index, float * out_distance,
                                           float * out_closest_point, void * stream) {
   return guarded([&] {
-    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "closest_element: a mesh BVH is required");
-    THEA_REQUIRE(mesh_bvh->cp_rec, "closest_element: the BVH was built without THEA_LAYOUT_CLOSEST");
-    THEA_REQUIRE(num_queries >= 0, "closest_element: negative query count");
-    if (num_queries == 0) return;
-    THEA_REQUIRE(queries && out_index, "closest_element: null queries or out_index");
-    float thresh = bound_threshold(dist_bound);
-    unsigned * err = handle_error_word(mesh_bvh);
-    run_staged({{(void *)queries, 12, false, false}, {out_index, 4, true, false}, {out_distance, 4, true, false},
-                {out_closest_point, 12, true, false}},
-               num_queries, (cudaStream_t)stream,
-               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
-                 run_closest(mesh_bvh, (float const *)p[0], cnt, thresh, (int32_t *)p[1], (float *)p[2],
-                             (float *)p[3], err, s);
-               });
+    closest_impl(mesh_bvh, queries, num_queries, dist_bound, THEA_PRECISION_FP32_REFERENCE, out_index, out_distance,
+                 out_closest_point, nullptr, stream);
+  });
+}
+
+THEA_API thea_status thea_closest_element_ex(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
+                                             float dist_bound, int32_t precision, int32_t * out_index,
+                                             float * out_distance, float * out_closest_point, float * out_error,
+                                             void * stream) {
+  return guarded([&] {
+    closest_impl(mesh_bvh, queries, num_queries, dist_bound, precision, out_index, out_distance, out_closest_point,
+                 out_error, stream);
   });
 }
 
@@ -383,20 +459,19 @@ THEA_API thea_status thea_ray_intersection(const thea_bvh * mesh_bvh, const floa
                                            int64_t num_rays, float max_time, float * out_time, int32_t * out_index,
                                            float * out_normal, void * stream) {
   return guarded([&] {
-    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "ray_intersection: a mesh BVH is required");
-    THEA_REQUIRE(mesh_bvh->ray_rec, "ray_intersection: the BVH was built without THEA_LAYOUT_RAY");
-    THEA_REQUIRE(num_rays >= 0, "ray_intersection: negative ray count");
-    if (num_rays == 0) return;
-    THEA_REQUIRE(origins && directions && out_time, "ray_intersection: null origins, directions or out_time");
-    unsigned * err = handle_error_word(mesh_bvh);
-    float mt = max_time >= 0.f ? max_time : -1.f;
-    run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
-                {out_index, 4, true, false}, {out_normal, 12, true, false}},
-               num_rays, (cudaStream_t)stream,
-               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
-                 run_ray(mesh_bvh, (float const *)p[0], (float const *)p[1], cnt, mt, (float *)p[2],
-                         (int32_t *)p[3], (float *)p[4], err, s);
-               });
+    ray_impl(mesh_bvh, origins, directions, num_rays, max_time, THEA_PRECISION_FP32_REFERENCE, out_time, out_index,
+             out_normal, nullptr, nullptr, nullptr, stream);
+  });
+}
+
+THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const float * origins,
+                                              const float * directions, int64_t num_rays, float max_time,
+                                              int32_t precision, float * out_time, int32_t * out_index,
+                                              float * out_normal, float * out_time_fp64, int32_t * out_index_fp64,
+                                              int32_t * out_flags, void * stream) {
+  return guarded([&] {
+    ray_impl(mesh_bvh, origins, directions, num_rays, max_time, precision, out_time, out_index, out_normal,
+             out_time_fp64, out_index_fp64, out_flags, stream);
   });
 }
 
@@ -480,6 +555,251 @@ THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_ver
       if (x.dev.ptr && got > 0) THEA_CUDA_CHECK(cudaMemcpyAsync(x.user, x.ptr, x.bytes, cudaMemcpyDeviceToHost, s));
     THEA_CUDA_CHECK(cudaStreamSynchronize(s));
     if (out_num_written) *out_num_written = got;
+  });
+}
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Forests, batched queries, graphs, autotuning
+//---------------------------------------------------------------------------------------------------------------------------
+
+THEA_API thea_status thea_mesh_forest_build(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                            const int64_t * mesh_face_offsets, int32_t num_meshes,
+                                            const thea_build_config * config, void * stream, thea_bvh ** out_forest) {
+  return guarded([&] {
+    THEA_REQUIRE(out_forest, "mesh_forest_build: out_forest is null");
+    *out_forest = nullptr;
+    THEA_REQUIRE(vertices && faces && mesh_face_offsets, "mesh_forest_build: null argument");
+    THEA_REQUIRE(num_meshes >= 1 && num_vertices > 0, "mesh_forest_build: empty input");
+    check_config(config);
+    thea_build_config cfg{};
+    if (config) cfg = *config;
+    int64_t nf = mesh_face_offsets[num_meshes];
+    THEA_REQUIRE(nf > 0, "mesh_forest_build: no faces");
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceView V(vertices, (size_t)num_vertices * 3 * sizeof(float), s);
+    DeviceView F(faces, (size_t)nf * 3 * sizeof(int32_t), s);
+    *out_forest = build_forest(true, (float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, nf, mesh_face_offsets,
+                               num_meshes, cfg, s);
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+THEA_API thea_status thea_point_forest_build(const float * points, const int64_t * set_offsets, int32_t num_sets,
+                                             const thea_build_config * config, void * stream,
+                                             thea_bvh ** out_forest) {
+  return guarded([&] {
+    THEA_REQUIRE(out_forest, "point_forest_build: out_forest is null");
+    *out_forest = nullptr;
+    THEA_REQUIRE(points && set_offsets && num_sets >= 1, "point_forest_build: null or empty argument");
+    check_config(config);
+    thea_build_config cfg{};
+    if (config) cfg = *config;
+    THEA_REQUIRE(cfg.layouts == 0, "point_forest_build: layouts apply to meshes only");
+    int64_t n = set_offsets[num_sets];
+    THEA_REQUIRE(n > 0, "point_forest_build: no points");
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceView P(points, (size_t)n * 3 * sizeof(float), s);
+    *out_forest = build_forest(false, (float const *)P.ptr, n, nullptr, n, set_offsets, num_sets, cfg, s);
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+static int check_batch_common(const thea_bvh * f, const int64_t * qoff, int64_t nq, int32_t qpw,
+                              std::initializer_list<void const *> arrays, char const * what) {
+  THEA_REQUIRE(f, std::string(what) + ": null forest");
+  THEA_REQUIRE(qoff, std::string(what) + ": null query offsets");
+  THEA_REQUIRE(nq >= 0, std::string(what) + ": negative query count");
+  int chunk = qpw == 0 ? 64 : qpw;
+  THEA_REQUIRE(chunk >= 32 && chunk % 32 == 0 && chunk <= 4096,
+               std::string(what) + ": queries_per_warp must be a multiple of 32 in 32..4096");
+  THEA_REQUIRE(!is_host_pointer(qoff), std::string(what) + ": query offsets must be device memory");
+  for (void const * p : arrays)
+    THEA_REQUIRE(!p || !is_host_pointer(p), std::string(what) + ": every array must be device memory");
+  return chunk;
+}
+
+THEA_API thea_status thea_batch_closest_element(const thea_bvh * mesh_forest, const float * queries,
+                                                const int64_t * query_offsets, int64_t num_queries, float dist_bound,
+                                                int32_t precision, int32_t queries_per_warp, int32_t hard_query_budget,
+                                                int32_t * out_index, float * out_distance, float * out_closest_point,
+                                                float * out_error, void * stream) {
+  return guarded([&] {
+    int chunk = check_batch_common(mesh_forest, query_offsets, num_queries, queries_per_warp,
+                                   {queries, out_index, out_distance, out_closest_point, out_error},
+                                   "batch_closest_element");
+    THEA_REQUIRE(mesh_forest->is_mesh && mesh_forest->cp_rec,
+                 "batch_closest_element: a mesh forest with THEA_LAYOUT_CLOSEST is required");
+    THEA_REQUIRE(precision == THEA_PRECISION_FP32_REFERENCE || precision == THEA_PRECISION_FP64_RECHECK,
+                 "batch_closest_element: unknown precision mode");
+    if (num_queries == 0) return;
+    THEA_REQUIRE(queries && out_index, "batch_closest_element: null queries or out_index");
+    ClosestParams cp;
+    cp.thresh = bound_threshold(dist_bound);
+    cp.bound2 = dist_bound >= 0.f ? (double)dist_bound * (double)dist_bound : -1.0;
+    cp.precision = precision;
+    cp.scene_scale = scene_scale_of(mesh_forest);
+    cp.budget = hard_query_budget == 0 ? 32 : (hard_query_budget < 0 ? 0 : hard_query_budget);
+    run_batch_closest(mesh_forest, queries, query_offsets, num_queries, cp, chunk, out_index, out_distance,
+                      out_closest_point, out_error, (cudaStream_t)stream);
+  });
+}
+
+THEA_API thea_status thea_batch_ray_intersection(const thea_bvh * mesh_forest, const float * origins,
+                                                 const float * directions, const int64_t * query_offsets,
+                                                 int64_t num_rays, float max_time, int32_t queries_per_warp,
+                                                 float * out_time, int32_t * out_index, void * stream) {
+  return guarded([&] {
+    int chunk = check_batch_common(mesh_forest, query_offsets, num_rays, queries_per_warp,
+                                   {origins, directions, out_time, out_index}, "batch_ray_intersection");
+    THEA_REQUIRE(mesh_forest->is_mesh && mesh_forest->ray_rec,
+                 "batch_ray_intersection: a mesh forest with THEA_LAYOUT_RAY is required");
+    if (num_rays == 0) return;
+    THEA_REQUIRE(origins && directions && out_time, "batch_ray_intersection: null argument");
+    run_batch_ray(mesh_forest, origins, directions, query_offsets, num_rays, max_time >= 0.f ? max_time : -1.f, chunk,
+                  out_time, out_index, (cudaStream_t)stream);
+  });
+}
+
+THEA_API thea_status thea_batch_k_closest(const thea_bvh * point_forest, const float * queries,
+                                          const int64_t * query_offsets, int64_t num_queries, int32_t k,
+                                          float dist_bound, int32_t queries_per_warp, int32_t * out_index,
+                                          float * out_sq_distance, void * stream) {
+  return guarded([&] {
+    int chunk = check_batch_common(point_forest, query_offsets, num_queries, queries_per_warp,
+                                   {queries, out_index, out_sq_distance}, "batch_k_closest");
+    THEA_REQUIRE(!point_forest->is_mesh, "batch_k_closest: a point forest is required");
+    THEA_REQUIRE(k >= 1 && k <= 32, "batch_k_closest: k must be in 1..32");
+    if (num_queries == 0) return;
+    THEA_REQUIRE(queries && out_index && out_sq_distance, "batch_k_closest: null argument");
+    run_batch_knn(point_forest, queries, query_offsets, num_queries, k, bound_threshold(dist_bound), chunk, out_index,
+                  out_sq_distance, (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"
+
+struct thea_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+THEA_API thea_status thea_graph_capture_begin(void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(stream, "graph_capture_begin: the legacy default stream cannot be captured");
+    THEA_CUDA_CHECK(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+  });
+}
+
+THEA_API thea_status thea_graph_capture_end(void * stream, thea_graph ** out_graph) {
+  return guarded([&] {
+    THEA_REQUIRE(stream && out_graph, "graph_capture_end: null argument");
+    *out_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    THEA_CUDA_CHECK(cudaStreamEndCapture((cudaStream_t)stream, &g));
+    thea_graph * tg = new thea_graph;
+    tg->graph = g;
+    cudaError_t e = cudaGraphInstantiate(&tg->exec, g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      delete tg;
+      THEA_CUDA_CHECK(e);
+    }
+    *out_graph = tg;
+  });
+}
+
+THEA_API thea_status thea_graph_launch(thea_graph * graph, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(graph && graph->exec, "graph_launch: null graph");
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    THEA_CUDA_CHECK(cudaGraphLaunch(graph->exec, (cudaStream_t)stream));
+  });
+}
+
+THEA_API thea_status thea_graph_destroy(thea_graph * graph) {
+  return guarded([&] {
+    if (!graph) return;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    delete graph;
+  });
+}
+
+THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t num_vertices, const int32_t * faces,
+                                                 const int64_t * mesh_face_offsets, int32_t num_meshes,
+                                                 const float * queries, const int64_t * query_offsets,
+                                                 int64_t num_queries, int32_t precision, void * stream,
+                                                 thea_tuning * out_tuning) {
+  return guarded([&] {
+    THEA_REQUIRE(out_tuning, "autotune_batch_closest: null output");
+    THEA_REQUIRE(vertices && faces && mesh_face_offsets && queries && query_offsets && num_meshes >= 1 &&
+                     num_queries > 0,
+                 "autotune_batch_closest: null or empty argument");
+    THEA_REQUIRE(!is_host_pointer(queries) && !is_host_pointer(query_offsets),
+                 "autotune_batch_closest: queries and offsets must be device memory");
+    cudaStream_t s = (cudaStream_t)stream;
+    int64_t nf = mesh_face_offsets[num_meshes];
+    DeviceView V(vertices, (size_t)num_vertices * 3 * sizeof(float), s);
+    DeviceView F(faces, (size_t)nf * 3 * sizeof(int32_t), s);
+    Scratch idx((size_t)num_queries * 4, s), dist((size_t)num_queries * 4, s);
+    cudaEvent_t e0, e1;
+    THEA_CUDA_CHECK(cudaEventCreate(&e0));
+    THEA_CUDA_CHECK(cudaEventCreate(&e1));
+    thea_tuning best{};
+    best.milliseconds = INFINITY;
+    int tried = 0;
+    int const widths[2] = {4, 8}, leaves[3] = {1, 2, 4}, chunks[3] = {32, 64, 128}, budgets[3] = {12, 96, 0};
+    for (int w : widths)
+      for (int l : leaves) {
+        thea_build_config cfg{};
+        cfg.width = w;
+        cfg.max_leaf_size = l;
+        cfg.layouts = THEA_LAYOUT_CLOSEST;
+        thea_bvh * f = build_forest(true, (float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, nf,
+                                    mesh_face_offsets, num_meshes, cfg, s);
+        ClosestParams cp;
+        cp.precision = precision;
+        cp.scene_scale = scene_scale_of(f);
+        auto time_it = [&](int chunk, int budget) {
+          cp.budget = budget;
+          float times[3];
+          run_batch_closest(f, queries, query_offsets, num_queries, cp, chunk, idx.as<int32_t>(), dist.as<float>(),
+                            nullptr, nullptr, s);
+          for (float & t : times) {
+            THEA_CUDA_CHECK(cudaEventRecord(e0, s));
+            run_batch_closest(f, queries, query_offsets, num_queries, cp, chunk, idx.as<int32_t>(), dist.as<float>(),
+                              nullptr, nullptr, s);
+            THEA_CUDA_CHECK(cudaEventRecord(e1, s));
+            THEA_CUDA_CHECK(cudaEventSynchronize(e1));
+            THEA_CUDA_CHECK(cudaEventElapsedTime(&t, e0, e1));
+          }
+          std::sort(times, times + 3);
+          ++tried;
+          if (times[1] < best.milliseconds) {
+            best.width = w;
+            best.max_leaf_size = l;
+            best.queries_per_warp = chunk;
+            best.hard_query_budget = budget > 0 ? budget : -1;
+            best.milliseconds = times[1];
+          }
+          return times[1];
+        };
+        // queries per warp at the default budget, then the budget (including one thread throughout) at the best one
+        int best_chunk = chunks[0];
+        float best_t = INFINITY;
+        for (int c : chunks) {
+          float t = time_it(c, 32);
+          if (t < best_t) { best_t = t; best_chunk = c; }
+        }
+        for (int bud : budgets) time_it(best_chunk, bud);
+        destroy_bvh(f);
+      }
+    best.candidates = tried;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *out_tuning = best;
   });
 }
 

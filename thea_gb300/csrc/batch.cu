@@ -1,0 +1,421 @@
+// Batched queries over a forest (one BVH per mesh or point set, built together by build_forest).
+//
+// One persistent launch serves every mesh: the grid is sized to fill the GPU once (blocks per SM x SMs), and each warp
+// repeatedly takes the next chunk of queries from a global counter, so meshes with 1k or 100k queries and 320 or
+// 327,680 triangles share the SMs without a tail of idle blocks. Queries are grouped by mesh (query_offsets, M + 1
+// entries); a lane finds its query's mesh by binary search and starts from that mesh's root node. The whole call is
+// asynchronous and allocation-stable, so it can be captured once into a CUDA graph and replayed.
+#include "batch.hpp"
+#include "device_util.cuh"
+#include "traverse_ops.cuh"
+#include "warp_traverse.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+namespace thea {
+namespace {
+
+constexpr int BATCH_THREADS = 128;
+
+__device__ __forceinline__ int mesh_of_query(int64_t const * __restrict__ qoff, int M, int64_t q) {
+  int lo = 0, hi = M - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(qoff + mid) <= q) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Each warp takes `chunk` consecutive queries per fetch; lanes stride through them.
+__device__ __forceinline__ bool next_chunk(unsigned long long * counter, int chunk, int64_t nq, int64_t & base) {
+  unsigned long long b = 0;
+  if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, (unsigned long long)chunk);
+  b = __shfl_sync(0xffffffffu, b, 0);
+  base = (int64_t)b;
+  return base < nq;
+}
+
+template <int W, int STACK, int PREC>
+__global__ void __launch_bounds__(BATCH_THREADS)
+batch_closest_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff, int64_t nq,
+                     float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
+                     float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
+                     unsigned long long * counter, int chunk) {
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int64_t base;
+  while (next_chunk(counter, chunk, nq, base)) {
+    int64_t end = base + chunk < nq ? base + chunk : nq;
+    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
+      int m = mesh_of_query(qoff, f.M, q);
+      int root = __ldg(f.seg_root + m);
+      int64_t ebase = __ldg(f.seg_start + m);
+      V3 p = load_v3(queries + 3 * q);
+      ClosestOut r;
+      float dist;
+      if (PREC == THEA_PRECISION_FP64_RECHECK) {
+        float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+        r = closest_query_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, bound2, scale, f.err);
+        dist = (float)sqrt(r.d2_64);
+      } else {
+        r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, thresh, f.err);
+        dist = sqrtf(r.d2);
+      }
+      bool found = r.idx != INT_MAX;
+      out_index[q] = found ? r.idx : -1;
+      if (out_dist) out_dist[q] = found ? dist : -1.f;
+      if (out_cp) {
+        out_cp[3 * q] = found ? r.cp.x : 0.f;
+        out_cp[3 * q + 1] = found ? r.cp.y : 0.f;
+        out_cp[3 * q + 2] = found ? r.cp.z : 0.f;
+      }
+      if (out_err) {
+        float e = -1.f;
+        if (found) {
+          double d64 = r.d2_64;
+          if (PREC != THEA_PRECISION_FP64_RECHECK) {
+            D3 cp64;
+            cp_record_f64(f.cp_rec, r.slot, p, cp64, d64);
+          }
+          e = (float)fabs((double)dist - sqrt(d64));
+        }
+        out_err[q] = e;
+      }
+    }
+  }
+}
+
+//============================================================================================================================
+// Two-phase closest element: phase 1 runs one thread per query with a budget of stack pops; queries that run out are
+// queued with the best element found so far (a valid upper bound) and phase 2 finishes them with one warp per query.
+//============================================================================================================================
+
+struct HardQueue {
+  int64_t * q;
+  float * bound;  // FP32 squared distance of the best element found so far (+inf if none)
+  int32_t * idx;
+  int64_t * slot;
+  unsigned long long * count;
+};
+
+template <int PREC>
+__device__ __forceinline__ void write_closest(float4 const * __restrict__ rec, int64_t q, V3 p, bool found, float dist,
+                                              V3 cp, int idx, int64_t slot, double d2_64, int32_t * out_index,
+                                              float * out_dist, float * out_cp, float * out_err) {
+  out_index[q] = found ? idx : -1;
+  if (out_dist) out_dist[q] = found ? dist : -1.f;
+  if (out_cp) {
+    out_cp[3 * q] = found ? cp.x : 0.f;
+    out_cp[3 * q + 1] = found ? cp.y : 0.f;
+    out_cp[3 * q + 2] = found ? cp.z : 0.f;
+  }
+  if (out_err) {
+    float e = -1.f;
+    if (found) {
+      double d64 = d2_64;
+      if (PREC != THEA_PRECISION_FP64_RECHECK) {
+        D3 cp64;
+        cp_record_f64(rec, slot, p, cp64, d64);
+      }
+      e = (float)fabs((double)dist - sqrt(d64));
+    }
+    out_err[q] = e;
+  }
+}
+
+template <int W, int STACK, int PREC>
+__global__ void __launch_bounds__(BATCH_THREADS)
+batch_closest_phase1_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff,
+                            int64_t nq, float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
+                            float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
+                            unsigned long long * counter, int chunk, int budget, HardQueue hq) {
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int64_t base;
+  while (next_chunk(counter, chunk, nq, base)) {
+    int64_t end = base + chunk < nq ? base + chunk : nq;
+    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
+      int m = mesh_of_query(qoff, f.M, q);
+      int root = __ldg(f.seg_root + m);
+      int64_t ebase = __ldg(f.seg_start + m);
+      V3 p = load_v3(queries + 3 * q);
+      ClosestOut r;
+      float dist;
+      if (PREC == THEA_PRECISION_FP64_RECHECK) {
+        float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+        r = closest_query_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, bound2, scale, f.err, budget);
+        dist = (float)sqrt(r.d2_64);
+      } else {
+        r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, thresh, f.err, budget);
+        dist = sqrtf(r.d2);
+      }
+      if (!r.done) {
+        unsigned long long pos = atomicAdd(hq.count, 1ull);
+        hq.q[pos] = q;
+        hq.bound[pos] = r.best32;
+        hq.idx[pos] = PREC == THEA_PRECISION_FP64_RECHECK ? INT_MAX : r.idx;
+        hq.slot[pos] = r.slot;
+        continue;
+      }
+      write_closest<PREC>(f.cp_rec, q, p, r.idx != INT_MAX, dist, r.cp, r.idx, r.slot, r.d2_64, out_index, out_dist,
+                          out_cp, out_err);
+    }
+  }
+}
+
+constexpr int PHASE2_WARPS = BATCH_THREADS / 32;
+
+template <int W, int PREC>
+__global__ void __launch_bounds__(BATCH_THREADS)
+batch_closest_phase2_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff,
+                            float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
+                            float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
+                            HardQueue hq, unsigned long long * counter) {
+  __shared__ int s_code[PHASE2_WARPS][WARP_STACK];
+  __shared__ float s_lb[PHASE2_WARPS][WARP_STACK];
+  __shared__ float s_cd[PHASE2_WARPS][PREC == THEA_PRECISION_FP64_RECHECK ? WARP_CAND : 1];
+  __shared__ int64_t s_ck[PHASE2_WARPS][PREC == THEA_PRECISION_FP64_RECHECK ? WARP_CAND : 1];
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long total = *hq.count;
+  while (true) {
+    unsigned long long j = 0;
+    if (lane == 0) j = atomicAdd(counter, 1ull);
+    j = __shfl_sync(0xffffffffu, j, 0);
+    if (j >= total) break;
+    int64_t q = hq.q[j];
+    int m = mesh_of_query(qoff, f.M, q);
+    int root = __ldg(f.seg_root + m);
+    int64_t ebase = __ldg(f.seg_start + m);
+    V3 p = load_v3(queries + 3 * q);
+    if (PREC == THEA_PRECISION_FP64_RECHECK) {
+      float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+      WarpBest64 b = closest_warp_query_f64<W>(nodes, f.cp_rec, root, ebase, p, bound2, scale, hq.bound[j],
+                                               s_code[warp], s_lb[warp], s_cd[warp], s_ck[warp], f.err);
+      if (lane == 0) {
+        bool found = b.idx != INT_MAX;
+        V3 cp = V3{0.f, 0.f, 0.f};
+        if (found) {
+          D3 cp64;
+          double d64;
+          cp_record_f64(f.cp_rec, b.slot, p, cp64, d64);
+          cp = V3{(float)cp64.x, (float)cp64.y, (float)cp64.z};
+        }
+        write_closest<PREC>(f.cp_rec, q, p, found, (float)sqrt(b.d2), cp, b.idx, b.slot, b.d2, out_index, out_dist,
+                            out_cp, out_err);
+      }
+    } else {
+      WarpBest init;
+      init.idx = hq.idx[j];
+      init.d2 = init.idx != INT_MAX ? hq.bound[j] : thresh;
+      init.slot = hq.slot[j];
+      WarpBest b = closest_warp_query<W>(nodes, f.cp_rec, root, ebase, p, init, s_code[warp], s_lb[warp], f.err);
+      if (lane == 0) {
+        bool found = b.idx != INT_MAX;
+        V3 cp = V3{0.f, 0.f, 0.f};
+        if (found) cp_record_test(f.cp_rec, b.slot, p, cp);
+        write_closest<PREC>(f.cp_rec, q, p, found, sqrtf(b.d2), cp, b.idx, b.slot, 0.0, out_index, out_dist, out_cp,
+                            out_err);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <int W, int STACK>
+__global__ void __launch_bounds__(BATCH_THREADS)
+batch_ray_kernel(BatchForest f, float const * __restrict__ origins, float const * __restrict__ dirs,
+                 int64_t const * __restrict__ qoff, int64_t nq, float max_time, float * __restrict__ out_time,
+                 int32_t * __restrict__ out_index, unsigned long long * counter, int chunk) {
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int64_t base;
+  while (next_chunk(counter, chunk, nq, base)) {
+    int64_t end = base + chunk < nq ? base + chunk : nq;
+    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
+      int m = mesh_of_query(qoff, f.M, q);
+      RayOut r = ray_query<W, STACK, false>(nodes, f.ray_rec, __ldg(f.seg_root + m), __ldg(f.seg_start + m),
+                                            load_v3(origins + 3 * q), load_v3(dirs + 3 * q), max_time, f.err);
+      bool found = r.idx != INT_MAX;
+      out_time[q] = found ? r.t : -1.f;
+      if (out_index) out_index[q] = found ? r.idx : -1;
+    }
+  }
+}
+
+template <int W, int K, int STACK>
+__global__ void __launch_bounds__(BATCH_THREADS)
+batch_knn_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff, int64_t nq,
+                 int k_out, float thresh, int32_t * __restrict__ out_index, float * __restrict__ out_d2,
+                 unsigned long long * counter, int chunk) {
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int64_t base;
+  while (next_chunk(counter, chunk, nq, base)) {
+    int64_t end = base + chunk < nq ? base + chunk : nq;
+    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
+      int m = mesh_of_query(qoff, f.M, q);
+      float bd[K];
+      int bi[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
+      knn_query<W, K, STACK>(nodes, f.pt_rec, __ldg(f.seg_root + m), __ldg(f.seg_start + m), load_v3(queries + 3 * q),
+                             -1, bd, bi, f.err);
+      for (int j = 0; j < k_out; ++j) {
+        bool v = bi[j] != INT_MAX;
+        out_index[q * k_out + j] = v ? bi[j] : -1;
+        out_d2[q * k_out + j] = v ? bd[j] : -1.f;
+      }
+    }
+  }
+}
+
+int persistent_grid(void const * kernel) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    THEA_CUDA_CHECK(cudaGetDevice(&dev));
+    THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  int per_sm = 0;
+  THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BATCH_THREADS, 0));
+  return std::max(1, per_sm) * sms;
+}
+
+template <int W, int STACK>
+void launch_batch_closest(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq,
+                          ClosestParams const & cp, int32_t * idx, float * dist, float * cpt, float * err,
+                          unsigned long long * counter, int chunk, cudaStream_t s) {
+  if (cp.precision == THEA_PRECISION_FP64_RECHECK) {
+    auto k = batch_closest_kernel<W, STACK, THEA_PRECISION_FP64_RECHECK>;
+    THEA_LAUNCH_NAMED("batch_closest_kernel_fp64", k, persistent_grid((void const *)k), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
+                cp.scene_scale, idx, dist, cpt, err, counter, chunk);
+  } else {
+    auto k = batch_closest_kernel<W, STACK, THEA_PRECISION_FP32_REFERENCE>;
+    THEA_LAUNCH_NAMED("batch_closest_kernel_fp32", k, persistent_grid((void const *)k), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
+                cp.scene_scale, idx, dist, cpt, err, counter, chunk);
+  }
+}
+
+template <int W, int STACK, int PREC>
+void launch_two_phase(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq, ClosestParams const & cp,
+                      int32_t * idx, float * dist, float * cpt, float * err, unsigned long long * counters, int chunk,
+                      HardQueue hq, cudaStream_t s) {
+  auto k1 = batch_closest_phase1_kernel<W, STACK, PREC>;
+  THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
+              cp.scene_scale, idx, dist, cpt, err, counters, chunk, cp.budget, hq);
+  auto k2 = batch_closest_phase2_kernel<W, PREC>;
+  THEA_LAUNCH_NAMED("batch_closest_phase2_kernel", k2, persistent_grid((void const *)k2), BATCH_THREADS, 0, s, f, q, qoff, cp.thresh, cp.bound2,
+              cp.scene_scale, idx, dist, cpt, err, hq, counters + 1);
+}
+
+template <int W, int STACK>
+void launch_batch_two_phase(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq,
+                            ClosestParams const & cp, int32_t * idx, float * dist, float * cpt, float * err,
+                            unsigned long long * counters, int chunk, HardQueue hq, cudaStream_t s) {
+  if (cp.precision == THEA_PRECISION_FP64_RECHECK)
+    launch_two_phase<W, STACK, THEA_PRECISION_FP64_RECHECK>(f, q, qoff, nq, cp, idx, dist, cpt, err, counters, chunk,
+                                                            hq, s);
+  else
+    launch_two_phase<W, STACK, THEA_PRECISION_FP32_REFERENCE>(f, q, qoff, nq, cp, idx, dist, cpt, err, counters,
+                                                              chunk, hq, s);
+}
+
+template <int W, int STACK>
+void launch_batch_ray(BatchForest const & f, float const * o, float const * d, int64_t const * qoff, int64_t nq,
+                      float max_time, float * t, int32_t * idx, unsigned long long * counter, int chunk,
+                      cudaStream_t s) {
+  auto k = batch_ray_kernel<W, STACK>;
+  THEA_LAUNCH_NAMED("batch_ray_kernel", k, persistent_grid((void const *)k), BATCH_THREADS, 0, s, f, o, d, qoff, nq, max_time, t, idx, counter,
+              chunk);
+}
+
+template <int W, int K, int STACK>
+void launch_batch_knn_k(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq, int k, float thresh,
+                        int32_t * idx, float * d2, unsigned long long * counter, int chunk, cudaStream_t s) {
+  auto kern = batch_knn_kernel<W, K, STACK>;
+  THEA_LAUNCH_NAMED("batch_knn_kernel", kern, persistent_grid((void const *)kern), BATCH_THREADS, 0, s, f, q, qoff, nq, k, thresh, idx, d2,
+              counter, chunk);
+}
+
+template <int W, int STACK>
+void launch_batch_knn(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq, int k, float thresh,
+                      int32_t * idx, float * d2, unsigned long long * counter, int chunk, cudaStream_t s) {
+  if (k <= 1) launch_batch_knn_k<W, 1, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+  else if (k <= 2) launch_batch_knn_k<W, 2, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+  else if (k <= 4) launch_batch_knn_k<W, 4, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+  else if (k <= 8) launch_batch_knn_k<W, 8, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+  else if (k <= 16) launch_batch_knn_k<W, 16, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+  else launch_batch_knn_k<W, 32, STACK>(f, q, qoff, nq, k, thresh, idx, d2, counter, chunk, s);
+}
+
+}  // namespace
+
+BatchForest forest_view(thea_bvh const * b) {
+  BatchForest f;
+  f.nodes = b->nodes;
+  f.cp_rec = b->cp_rec;
+  f.ray_rec = b->ray_rec;
+  f.pt_rec = b->pt_rec;
+  f.seg_start = b->seg_start;
+  f.seg_root = b->seg_root;
+  f.M = b->num_segments;
+  f.err = b->err;
+  return f;
+}
+
+void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff, int64_t nq, ClosestParams const & cp,
+                       int chunk, int32_t * idx, float * dist, float * cpt, float * err, cudaStream_t s) {
+  if (nq <= 0) return;
+  BatchForest f = forest_view(b);
+  bool sm = small_stack_ok(b);
+  if (cp.budget > 0) {
+    Scratch counters(3 * sizeof(unsigned long long), s);
+    THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));
+    Scratch hq_q((size_t)nq * sizeof(int64_t), s), hq_b((size_t)nq * sizeof(float), s);
+    Scratch hq_i((size_t)nq * sizeof(int32_t), s), hq_s((size_t)nq * sizeof(int64_t), s);
+    auto * c = counters.as<unsigned long long>();
+    HardQueue hq{hq_q.as<int64_t>(), hq_b.as<float>(), hq_i.as<int32_t>(), hq_s.as<int64_t>(), c + 2};
+    if (b->width == 4) sm ? launch_batch_two_phase<4, 64>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s)
+                          : launch_batch_two_phase<4, 256>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s);
+    else sm ? launch_batch_two_phase<8, 128>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s)
+            : launch_batch_two_phase<8, 512>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s);
+    return;
+  }
+  Scratch counter(sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
+  auto * c = counter.as<unsigned long long>();
+  if (b->width == 4) sm ? launch_batch_closest<4, 64>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s)
+                        : launch_batch_closest<4, 256>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s);
+  else sm ? launch_batch_closest<8, 128>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s)
+          : launch_batch_closest<8, 512>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s);
+}
+
+void run_batch_ray(thea_bvh const * b, float const * o, float const * d, int64_t const * qoff, int64_t nq,
+                   float max_time, int chunk, float * t, int32_t * idx, cudaStream_t s) {
+  if (nq <= 0) return;
+  BatchForest f = forest_view(b);
+  Scratch counter(sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
+  auto * c = counter.as<unsigned long long>();
+  bool sm = small_stack_ok(b);
+  if (b->width == 4) sm ? launch_batch_ray<4, 64>(f, o, d, qoff, nq, max_time, t, idx, c, chunk, s)
+                        : launch_batch_ray<4, 256>(f, o, d, qoff, nq, max_time, t, idx, c, chunk, s);
+  else sm ? launch_batch_ray<8, 128>(f, o, d, qoff, nq, max_time, t, idx, c, chunk, s)
+          : launch_batch_ray<8, 512>(f, o, d, qoff, nq, max_time, t, idx, c, chunk, s);
+}
+
+void run_batch_knn(thea_bvh const * b, float const * q, int64_t const * qoff, int64_t nq, int k, float thresh,
+                   int chunk, int32_t * idx, float * d2, cudaStream_t s) {
+  if (nq <= 0) return;
+  BatchForest f = forest_view(b);
+  Scratch counter(sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
+  auto * c = counter.as<unsigned long long>();
+  bool sm = small_stack_ok(b);
+  if (b->width == 4) sm ? launch_batch_knn<4, 64>(f, q, qoff, nq, k, thresh, idx, d2, c, chunk, s)
+                        : launch_batch_knn<4, 256>(f, q, qoff, nq, k, thresh, idx, d2, c, chunk, s);
+  else sm ? launch_batch_knn<8, 128>(f, q, qoff, nq, k, thresh, idx, d2, c, chunk, s)
+          : launch_batch_knn<8, 512>(f, q, qoff, nq, k, thresh, idx, d2, c, chunk, s);
+}
+
+}  // namespace thea

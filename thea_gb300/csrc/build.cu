@@ -1,12 +1,18 @@
-// LBVH build: element boxes -> 63-bit Morton codes -> stable radix sort -> Karras binary radix tree -> bottom-up box
-// refit -> top-down collapse into a W-wide tree whose leaves are contiguous runs of the sorted elements -> element records
-// in leaf order.
+// LBVH build of a forest: one BVH per segment of elements (one segment for a single mesh or point set; one per mesh
+// for a batch), all built together in one pass: element boxes -> per-segment 3D Morton codes with the segment id in the
+// top bits -> one stable radix sort -> Karras binary radix trees that never cross a segment boundary -> bottom-up box
+// refit -> top-down collapse into W-wide trees whose leaves are contiguous runs of sorted elements -> element records in
+// leaf order.
 //
 // Replaces BvhN::init / initTree / createKdTree (Code/Source/Algorithms/BvhN.hpp:705-794, 1366-1525). The reference
 // builds a median-split kd-tree with leaves of at most 5 elements and pads every node box by 5%; this build produces a
 // different tree over the same elements. Query results do not depend on the tree: every query returns the element with
 // the smallest distance or hit time, ties to the lowest index, and node boxes are padded so that no element at the best
 // distance can be pruned by rounding.
+//
+// Index conventions: elements are addressed by their global sorted position; a leaf stores its first element relative to
+// its segment's first sorted position (so one segment may hold up to 2^27 - 1 elements while a forest may hold more),
+// and element records store the element's index within its segment (the face index within its mesh).
 #include "bvh.hpp"
 #include "device_util.cuh"
 
@@ -33,15 +39,27 @@ __host__ __device__ __forceinline__ float ord2f(int i) {
 #endif
 }
 
-// bounds[0..2] = min of element-box centres (ordered ints), [3..5] = max of centres, [6..8] = min of box lo,
-// [9..11] = max of box hi
+// Segment of element i: largest s with start[s] <= i (start has M + 1 entries, start[0] = 0)
+__device__ __forceinline__ int segment_of(int64_t const * __restrict__ start, int M, int64_t i) {
+  int lo = 0, hi = M - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Per-segment bounds, 12 ordered ints per segment: [0..2] min of box centres, [3..5] max of box centres,
+// [6..8] min of box lo, [9..11] max of box hi. A warp whose lanes share one segment reduces before its atomics.
 __global__ void elem_box_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t n, int is_mesh,
-                                float4 * __restrict__ elo, float4 * __restrict__ ehi, int * __restrict__ bounds) {
-  __shared__ int sb[12];
-  if (threadIdx.x < 12) sb[threadIdx.x] = ((threadIdx.x < 3) || (threadIdx.x >= 6 && threadIdx.x < 9)) ? INT_MAX : INT_MIN;
-  __syncthreads();
+                                int64_t const * __restrict__ seg_start, int M, float4 * __restrict__ elo,
+                                float4 * __restrict__ ehi, int * __restrict__ bounds) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
+  bool ok = i < n;
+  int v[12];
+  int seg = 0;
+  if (ok) {
     V3 lo, hi;
     if (is_mesh) {
       V3 a = load_v3(V + 3 * (int64_t)F[3 * i]);
@@ -55,22 +73,50 @@ __global__ void elem_box_kernel(float const * __restrict__ V, int32_t const * __
     elo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
     ehi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
     V3 c = 0.5f * (hi + lo);
-    float cc[3] = {c.x, c.y, c.z}, ll[3] = {lo.x, lo.y, lo.z}, hh[3] = {hi.x, hi.y, hi.z};
+    v[0] = v[3] = f2ord(c.x); v[1] = v[4] = f2ord(c.y); v[2] = v[5] = f2ord(c.z);
+    v[6] = f2ord(lo.x); v[7] = f2ord(lo.y); v[8] = f2ord(lo.z);
+    v[9] = f2ord(hi.x); v[10] = f2ord(hi.y); v[11] = f2ord(hi.z);
+    seg = M > 1 ? segment_of(seg_start, M, i) : 0;
+  } else {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      atomicMin(&sb[a], f2ord(cc[a]));
-      atomicMax(&sb[3 + a], f2ord(cc[a]));
-      atomicMin(&sb[6 + a], f2ord(ll[a]));
-      atomicMax(&sb[9 + a], f2ord(hh[a]));
+    for (int t = 0; t < 12; ++t) v[t] = ((t < 3) || (t >= 6 && t < 9)) ? INT_MAX : INT_MIN;
+    seg = -1;
+  }
+  int seg0 = __shfl_sync(0xffffffffu, seg, 0);
+  bool uniform = __all_sync(0xffffffffu, seg == seg0 || seg < 0) && seg0 >= 0;
+  if (uniform) {
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+      bool is_min = (t < 3) || (t >= 6 && t < 9);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        int u = __shfl_xor_sync(0xffffffffu, v[t], o);
+        v[t] = is_min ? min(v[t], u) : max(v[t], u);
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int t = 0; t < 12; ++t) {
+        bool is_min = (t < 3) || (t >= 6 && t < 9);
+        if (is_min) atomicMin(&bounds[12 * seg0 + t], v[t]);
+        else atomicMax(&bounds[12 * seg0 + t], v[t]);
+      }
+    }
+  } else if (ok) {
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+      bool is_min = (t < 3) || (t >= 6 && t < 9);
+      if (is_min) atomicMin(&bounds[12 * seg + t], v[t]);
+      else atomicMax(&bounds[12 * seg + t], v[t]);
     }
   }
-  __syncthreads();
-  if (threadIdx.x < 12) {
-    int t = threadIdx.x;
-    bool is_min = (t < 3) || (t >= 6 && t < 9);
-    if (is_min) atomicMin(&bounds[t], sb[t]);
-    else atomicMax(&bounds[t], sb[t]);
-  }
+}
+
+__global__ void init_bounds_kernel(int * __restrict__ bounds, int M) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 12 * (int64_t)M) return;
+  int t = (int)(i % 12);
+  bounds[i] = ((t < 3) || (t >= 6 && t < 9)) ? INT_MAX : INT_MIN;
 }
 
 __device__ __forceinline__ uint64_t expand21(uint32_t v) {
@@ -83,64 +129,75 @@ __device__ __forceinline__ uint64_t expand21(uint32_t v) {
   return x;
 }
 
+// key = (segment << 3 bpa) | Morton code with bpa bits per axis of the box centre within its segment's centre bounds
 __global__ void morton_kernel(float4 const * __restrict__ elo, float4 const * __restrict__ ehi, int64_t n,
-                              int const * __restrict__ bounds, uint64_t * __restrict__ keys,
-                              uint32_t * __restrict__ vals) {
+                              int64_t const * __restrict__ seg_start, int M, int const * __restrict__ bounds, int bpa,
+                              uint64_t * __restrict__ keys, uint32_t * __restrict__ vals) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int seg = M > 1 ? segment_of(seg_start, M, i) : 0;
   float4 l = elo[i], h = ehi[i];
   float c[3] = {0.5f * (h.x + l.x), 0.5f * (h.y + l.y), 0.5f * (h.z + l.z)};
+  float cells = (float)(1u << bpa);
   uint32_t q[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float lo = ord2f(bounds[a]), hi = ord2f(bounds[3 + a]);
+    float lo = ord2f(bounds[12 * seg + a]), hi = ord2f(bounds[12 * seg + 3 + a]);
     float ext = hi - lo;
     float t = ext > 0.f ? (c[a] - lo) / ext : 0.f;
     t = fminf(fmaxf(t, 0.f), 1.f);
-    q[a] = min((uint32_t)(t * 2097152.0f), 2097151u);
+    q[a] = min((uint32_t)(t * cells), (1u << bpa) - 1u);
   }
-  keys[i] = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
+  uint64_t code = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
+  keys[i] = ((uint64_t)seg << (3 * bpa)) | code;
   vals[i] = (uint32_t)i;
 }
 
-// Common-prefix length of sorted keys i and j, extended by the indices when the keys are equal (Karras 2012)
-__device__ __forceinline__ int kdelta(uint64_t const * __restrict__ codes, int64_t n, int64_t i, int64_t j) {
-  if (j < 0 || j >= n) return -1;
-  uint64_t a = codes[i], b = codes[j];
-  if (a == b) return 64 + __clz((uint32_t)(i ^ j));
-  return __clzll((long long)(a ^ b));
+// Common-prefix length of sorted keys i and j inside [a, b), extended by the positions when the keys are equal
+// (Karras 2012); -1 outside the segment.
+__device__ __forceinline__ int kdelta(uint64_t const * __restrict__ codes, int64_t a, int64_t b, int64_t i, int64_t j) {
+  if (j < a || j >= b) return -1;
+  uint64_t x = codes[i], y = codes[j];
+  if (x == y) return 64 + __clzll((long long)(i ^ j));
+  return __clzll((long long)(x ^ y));
 }
 
-// Binary radix tree. Child codes: >= 0 internal node, < 0 leaf at sorted position ~code.
-__global__ void karras_kernel(uint64_t const * __restrict__ codes, int64_t n, int * __restrict__ left,
-                              int * __restrict__ right, int * __restrict__ first, int * __restrict__ last,
-                              int * __restrict__ parent, int * __restrict__ leaf_parent) {
+// Binary radix trees, one per segment. The internal node at sorted position i of segment s lives in slot i - s.
+// Child codes: >= 0 an internal slot, < 0 a leaf at sorted position ~code.
+__global__ void karras_kernel(uint64_t const * __restrict__ codes, int64_t n, int64_t const * __restrict__ seg_start,
+                              int M, int mbits, int * __restrict__ left, int * __restrict__ right,
+                              int * __restrict__ first, int * __restrict__ last, int * __restrict__ parent,
+                              int * __restrict__ leaf_parent) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1) return;
-  int d = (kdelta(codes, n, i, i + 1) - kdelta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
-  int dmin = kdelta(codes, n, i, i - d);
+  if (i >= n) return;
+  int s = M > 1 ? (int)(codes[i] >> mbits) : 0;
+  int64_t a = M > 1 ? seg_start[s] : 0, b = M > 1 ? seg_start[s + 1] : n;
+  if (i >= b - 1) return;  // a segment of m elements has m - 1 internal nodes, at positions a .. b - 2
+  int d = (kdelta(codes, a, b, i, i + 1) - kdelta(codes, a, b, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = kdelta(codes, a, b, i, i - d);
   int64_t lmax = 2;
-  while (kdelta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  while (kdelta(codes, a, b, i, i + lmax * d) > dmin) lmax <<= 1;
   int64_t l = 0;
   for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
-    if (kdelta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    if (kdelta(codes, a, b, i, i + (l + t) * d) > dmin) l += t;
   int64_t j = i + l * d;
-  int dnode = kdelta(codes, n, i, j);
-  int64_t s = 0, t = l;
+  int dnode = kdelta(codes, a, b, i, j);
+  int64_t sp = 0, t = l;
   do {
     t = (t + 1) >> 1;
-    if (kdelta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+    if (kdelta(codes, a, b, i, i + (sp + t) * d) > dnode) sp += t;
   } while (t > 1);
-  int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  int64_t gamma = i + sp * d + (d < 0 ? -1 : 0);
   int64_t lo = i < j ? i : j, hi = i < j ? j : i;
-  int lc = (lo == gamma) ? ~(int)gamma : (int)gamma;
-  int rc = (hi == gamma + 1) ? ~(int)(gamma + 1) : (int)(gamma + 1);
-  left[i] = lc;
-  right[i] = rc;
-  first[i] = (int)lo;
-  last[i] = (int)hi;
-  if (lc < 0) leaf_parent[~lc] = (int)i; else parent[lc] = (int)i;
-  if (rc < 0) leaf_parent[~rc] = (int)i; else parent[rc] = (int)i;
+  int slot = (int)(i - s);
+  int lc = (lo == gamma) ? ~(int)gamma : (int)(gamma - s);
+  int rc = (hi == gamma + 1) ? ~(int)(gamma + 1) : (int)(gamma + 1 - s);
+  left[slot] = lc;
+  right[slot] = rc;
+  first[slot] = (int)lo;
+  last[slot] = (int)hi;
+  if (lc < 0) leaf_parent[~lc] = slot; else parent[lc] = slot;
+  if (rc < 0) leaf_parent[~rc] = slot; else parent[rc] = slot;
 }
 
 __device__ __forceinline__ void child_box(int code, float4 const * __restrict__ elo, float4 const * __restrict__ ehi,
@@ -188,6 +245,8 @@ struct CollapseArgs {
   uint32_t const * sorted;
   float4 const * ilo;
   float4 const * ihi;
+  int64_t const * seg_start;  // sorted position where each segment starts (nullptr: one segment)
+  int M;
   int leaf_size;
 };
 
@@ -247,6 +306,17 @@ __device__ __forceinline__ void pad_box(float4 & lo, float4 & hi) {
   hi.x += px; hi.y += py; hi.z += pz;
 }
 
+template <int W> __device__ __forceinline__ void clear_node(WideNode<W> & node) {
+#pragma unroll
+  for (int e = 0; e < W; ++e) {
+    node.lox[e] = node.loy[e] = node.loz[e] = INFINITY;
+    node.hix[e] = node.hiy[e] = node.hiz[e] = -INFINITY;
+    node.child[e] = CHILD_EMPTY;
+  }
+#pragma unroll
+  for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
+}
+
 template <int W>
 __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
                                      int const * __restrict__ chosen, int const * __restrict__ offsets,
@@ -255,17 +325,19 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
   int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= fsize) return;
   WideNode<W> node;
+  clear_node(node);
   int k = 0;
   int off = offsets[f];
+  // leaves store their first element relative to the segment's first sorted position
+  int64_t seg_base = 0;
+  if (a.M > 1) {
+    int64_t pos = a.first[frontier[f]];
+    seg_base = a.seg_start[segment_of(a.seg_start, a.M, pos)];
+  }
 #pragma unroll
   for (int e = 0; e < W; ++e) {
     int code = chosen[f * W + e];
-    if (code == CHILD_EMPTY) {
-      node.lox[e] = node.loy[e] = node.loz[e] = INFINITY;
-      node.hix[e] = node.hiy[e] = node.hiz[e] = -INFINITY;
-      node.child[e] = CHILD_EMPTY;
-      continue;
-    }
+    if (code == CHILD_EMPTY) continue;
     float4 lo, hi;
     child_box(code, a.elo, a.ehi, a.sorted, a.ilo, a.ihi, lo, hi);
     pad_box(lo, hi);
@@ -273,34 +345,55 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
     node.hix[e] = hi.x; node.hiy[e] = hi.y; node.hiz[e] = hi.z;
     int cnt = code_count(a, code);
     if (cnt <= a.leaf_size) {
-      node.child[e] = encode_leaf(code_first(a, code), cnt);
+      node.child[e] = encode_leaf((int)(code_first(a, code) - seg_base), cnt);
     } else {
       node.child[e] = (int)(next_base + off + k);
       next_frontier[off + k] = code;
       ++k;
     }
   }
-#pragma unroll
-  for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
   nodes[level_base + f] = node;
 }
 
-// A root that is a single leaf holding all n elements (n <= leaf size)
-template <int W> __global__ void single_leaf_root_kernel(WideNode<W> * nodes, int const * __restrict__ bounds, int n) {
-  WideNode<W> node;
-  for (int e = 0; e < W; ++e) {
-    node.lox[e] = node.loy[e] = node.loz[e] = INFINITY;
-    node.hix[e] = node.hiy[e] = node.hiz[e] = -INFINITY;
-    node.child[e] = CHILD_EMPTY;
+// Segment roots: big segments (more elements than a leaf) become level-0 frontier entries; small non-empty segments get
+// a single-leaf root node. Small roots take wide indices [0, num_small), big roots [num_small, num_small + num_big).
+__global__ void segment_flags_kernel(int64_t const * __restrict__ seg_start, int M, int64_t n, int leaf_size,
+                                     int * __restrict__ is_small, int * __restrict__ is_big) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= M) return;
+  int64_t a = seg_start ? seg_start[s] : 0, b = seg_start ? seg_start[s + 1] : n;
+  int64_t cnt = b - a;
+  is_small[s] = (cnt >= 1 && cnt <= leaf_size) ? 1 : 0;
+  is_big[s] = cnt > leaf_size ? 1 : 0;
+}
+
+template <int W>
+__global__ void segment_roots_kernel(CollapseArgs a, int64_t n, int const * __restrict__ is_small,
+                                     int const * __restrict__ small_rank, int const * __restrict__ is_big,
+                                     int const * __restrict__ big_rank, int num_small, int const * __restrict__ bounds,
+                                     WideNode<W> * __restrict__ nodes, int * __restrict__ frontier,
+                                     int * __restrict__ seg_root) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.M) return;
+  int64_t sa = a.seg_start ? a.seg_start[s] : 0, sb = a.seg_start ? a.seg_start[s + 1] : n;
+  if (is_big[s]) {
+    // the Karras root of the segment is the internal node at its first position, slot sa - s
+    frontier[big_rank[s]] = (int)(sa - s);
+    seg_root[s] = num_small + big_rank[s];
+  } else if (is_small[s]) {
+    WideNode<W> node;
+    clear_node(node);
+    float4 lo = make_float4(ord2f(bounds[12 * s + 6]), ord2f(bounds[12 * s + 7]), ord2f(bounds[12 * s + 8]), 0.f);
+    float4 hi = make_float4(ord2f(bounds[12 * s + 9]), ord2f(bounds[12 * s + 10]), ord2f(bounds[12 * s + 11]), 0.f);
+    pad_box(lo, hi);
+    node.lox[0] = lo.x; node.loy[0] = lo.y; node.loz[0] = lo.z;
+    node.hix[0] = hi.x; node.hiy[0] = hi.y; node.hiz[0] = hi.z;
+    node.child[0] = encode_leaf(0, (int)(sb - sa));
+    nodes[small_rank[s]] = node;
+    seg_root[s] = small_rank[s];
+  } else {
+    seg_root[s] = -1;  // empty segment
   }
-  float4 lo = make_float4(ord2f(bounds[6]), ord2f(bounds[7]), ord2f(bounds[8]), 0.f);
-  float4 hi = make_float4(ord2f(bounds[9]), ord2f(bounds[10]), ord2f(bounds[11]), 0.f);
-  pad_box(lo, hi);
-  node.lox[0] = lo.x; node.loy[0] = lo.y; node.loz[0] = lo.z;
-  node.hix[0] = hi.x; node.hiy[0] = hi.y; node.hiz[0] = hi.z;
-  node.child[0] = encode_leaf(0, n);
-  for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
-  nodes[0] = node;
 }
 
 __global__ void count_big_kernel(int const * __restrict__ first, int const * __restrict__ last, int64_t m, int leaf_size,
@@ -311,16 +404,19 @@ __global__ void count_big_kernel(int const * __restrict__ first, int const * __r
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
 }
 
+// Element records in sorted order; the stored index is the element's index within its segment.
 __global__ void mesh_records_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t n,
-                                    uint32_t const * __restrict__ sorted, float4 * __restrict__ cp_rec,
-                                    float4 * __restrict__ ray_rec, int32_t * __restrict__ leaf_to_elem) {
+                                    int64_t const * __restrict__ seg_start, int M, uint32_t const * __restrict__ sorted,
+                                    float4 * __restrict__ cp_rec, float4 * __restrict__ ray_rec,
+                                    int32_t * __restrict__ leaf_to_elem) {
   int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  int e = (int)sorted[s];
+  int64_t ge = (int64_t)sorted[s];
+  int e = (int)(M > 1 ? ge - seg_start[segment_of(seg_start, M, ge)] : ge);
   leaf_to_elem[s] = e;
-  V3 v0 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e]);
-  V3 v1 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e + 1]);
-  V3 v2 = load_v3(V + 3 * (int64_t)F[3 * (int64_t)e + 2]);
+  V3 v0 = load_v3(V + 3 * (int64_t)F[3 * ge]);
+  V3 v1 = load_v3(V + 3 * (int64_t)F[3 * ge + 1]);
+  V3 v2 = load_v3(V + 3 * (int64_t)F[3 * ge + 2]);
   if (cp_rec) {
     TriPlane pl = tri_plane(v0, v1, v2);
     V3 d0, d1, d2;
@@ -347,48 +443,63 @@ __global__ void mesh_records_kernel(float const * __restrict__ V, int32_t const 
   }
 }
 
-__global__ void point_records_kernel(float const * __restrict__ P, int64_t n, uint32_t const * __restrict__ sorted,
-                                     float4 * __restrict__ pt_rec, int32_t * __restrict__ leaf_to_elem) {
+__global__ void point_records_kernel(float const * __restrict__ P, int64_t n, int64_t const * __restrict__ seg_start,
+                                     int M, uint32_t const * __restrict__ sorted, float4 * __restrict__ pt_rec,
+                                     int32_t * __restrict__ leaf_to_elem) {
   int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  int e = (int)sorted[s];
+  int64_t ge = (int64_t)sorted[s];
+  int e = (int)(M > 1 ? ge - seg_start[segment_of(seg_start, M, ge)] : ge);
   leaf_to_elem[s] = e;
-  V3 p = load_v3(P + 3 * (int64_t)e);
+  V3 p = load_v3(P + 3 * ge);
   pt_rec[s] = make_float4(p.x, p.y, p.z, __int_as_float(e));
 }
 
 template <int W>
 void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, cudaStream_t stream) {
-  if (n <= a.leaf_size) {
-    THEA_CUDA_CHECK(cudaMallocAsync(&b->nodes, sizeof(WideNode<W>), stream));
-    THEA_LAUNCH(single_leaf_root_kernel<W>, 1, 1, 0, stream, (WideNode<W> *)b->nodes, d_bounds, (int)n);
-    b->num_nodes = 1;
-    b->depth = 1;
-    return;
-  }
-  // every wide node corresponds to a distinct binary node with more elements than a leaf holds
+  int M = a.M;
+  // segment roots
+  Scratch is_small((size_t)M * sizeof(int), stream), is_big((size_t)M * sizeof(int), stream);
+  Scratch small_rank((size_t)M * sizeof(int), stream), big_rank((size_t)M * sizeof(int), stream);
+  THEA_LAUNCH(segment_flags_kernel, (unsigned)ceil_div(M, BUILD_THREADS), BUILD_THREADS, 0, stream, a.seg_start, M, n,
+              a.leaf_size, is_small.as<int>(), is_big.as<int>());
+  exclusive_scan<int>(is_small.as<int>(), small_rank.as<int>(), M, stream);
+  exclusive_scan<int>(is_big.as<int>(), big_rank.as<int>(), M, stream);
+  int tails[4];
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&tails[0], small_rank.as<int>() + M - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&tails[1], is_small.as<int>() + M - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&tails[2], big_rank.as<int>() + M - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&tails[3], is_big.as<int>() + M - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  // every other wide node corresponds to a distinct binary node with more elements than a leaf holds
+  int64_t m = n - M;  // binary internal nodes in the forest (segments are non-empty)
   Scratch cnt(sizeof(unsigned long long), stream);
   THEA_CUDA_CHECK(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes, stream));
-  THEA_LAUNCH(count_big_kernel, (unsigned)ceil_div(n - 1, BUILD_THREADS), BUILD_THREADS, 0, stream, a.first, a.last,
-              n - 1, a.leaf_size, cnt.as<unsigned long long>());
+  if (m > 0)
+    THEA_LAUNCH(count_big_kernel, (unsigned)ceil_div(m, BUILD_THREADS), BUILD_THREADS, 0, stream, a.first, a.last, m,
+                a.leaf_size, cnt.as<unsigned long long>());
   unsigned long long nbig = 0;
   THEA_CUDA_CHECK(cudaMemcpyAsync(&nbig, cnt.ptr, sizeof(nbig), cudaMemcpyDeviceToHost, stream));
   THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
-  if (nbig < 1) nbig = 1;
+  int num_small = tails[0] + tails[1], num_big = tails[2] + tails[3];
+  int64_t cap = (int64_t)num_small + (int64_t)std::max<unsigned long long>(nbig, 1);
 
   WideNode<W> * nodes = nullptr;
-  THEA_CUDA_CHECK(cudaMallocAsync((void **)&nodes, (size_t)nbig * sizeof(WideNode<W>), stream));
-  Scratch fa((size_t)nbig * sizeof(int), stream), fb((size_t)nbig * sizeof(int), stream);
-  Scratch chosen((size_t)nbig * W * sizeof(int), stream);
-  Scratch nint((size_t)nbig * sizeof(int), stream), offs((size_t)nbig * sizeof(int), stream);
-  int root = 0;
-  THEA_CUDA_CHECK(cudaMemcpyAsync(fa.ptr, &root, sizeof(int), cudaMemcpyHostToDevice, stream));
+  THEA_CUDA_CHECK(cudaMallocAsync((void **)&nodes, (size_t)cap * sizeof(WideNode<W>), stream));
+  THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->seg_root, (size_t)M * sizeof(int32_t), stream));
+  Scratch fa((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream), fb((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
+  THEA_LAUNCH((segment_roots_kernel<W>), (unsigned)ceil_div(M, BUILD_THREADS), BUILD_THREADS, 0, stream, a, n,
+              is_small.as<int>(), small_rank.as<int>(), is_big.as<int>(), big_rank.as<int>(), num_small, d_bounds,
+              nodes, fa.as<int>(), b->seg_root);
+  Scratch chosen((size_t)std::max<int64_t>(cap, 1) * W * sizeof(int), stream);
+  Scratch nint((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
+  Scratch offs((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   int * cur = fa.as<int>();
   int * nxt = fb.as<int>();
-  int64_t fsize = 1, base = 0;
-  int depth = 0;
+  int64_t fsize = num_big, base = num_small;
+  int depth = num_small > 0 ? 1 : 0;
+  int levels = 0;
   while (fsize > 0) {
-    THEA_REQUIRE(base + fsize <= (int64_t)nbig, "BVH collapse exceeded its node bound");
+    THEA_REQUIRE(base + fsize <= cap, "BVH collapse exceeded its node bound");
     unsigned grid = (unsigned)ceil_div(fsize, BUILD_THREADS);
     THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
                 nint.as<int>());
@@ -402,26 +513,40 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
     base += fsize;
     fsize = (int64_t)tail[0] + tail[1];
     std::swap(cur, nxt);
-    ++depth;
+    ++levels;
   }
   b->nodes = nodes;
   b->num_nodes = base;
-  b->depth = depth;
+  b->depth = std::max(depth, levels);
 }
 
 }  // namespace
 
-thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
-                     thea_build_config const & cfg, cudaStream_t stream) {
-  int64_t n = is_mesh ? nf : nv;
+thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t n_elems,
+                        int64_t const * seg_start_host, int M, thea_build_config const & cfg, cudaStream_t stream) {
+  int64_t n = is_mesh ? n_elems : nv;
+  THEA_REQUIRE(M >= 1, "build: at least one segment is required");
   THEA_REQUIRE(n >= 1, "build: at least one element is required");
-  THEA_REQUIRE(n < (int64_t(1) << 27), "build: at most 2^27 - 1 elements per BVH");
+  THEA_REQUIRE(n < (int64_t(1) << 31) - 1, "build: at most 2^31 - 2 elements per forest");
   int width = cfg.width == 0 ? 4 : cfg.width;
   THEA_REQUIRE(width == 4 || width == 8, "build: width must be 4 or 8");
-  int leaf = cfg.max_leaf_size == 0 ? (is_mesh ? 4 : 8) : cfg.max_leaf_size;
+  int leaf = cfg.max_leaf_size == 0 ? (is_mesh ? 2 : 1) : cfg.max_leaf_size;
   THEA_REQUIRE(leaf >= 1 && leaf <= MAX_LEAF_SIZE, "build: max_leaf_size must be in 1..16");
   uint32_t layouts = is_mesh ? (cfg.layouts == 0 ? (THEA_LAYOUT_CLOSEST | THEA_LAYOUT_RAY) : cfg.layouts) : 0u;
   THEA_REQUIRE((layouts & ~3u) == 0, "build: unknown layout bits");
+  std::vector<int64_t> starts;
+  if (M > 1) {
+    THEA_REQUIRE(seg_start_host, "build: segment starts are required for more than one segment");
+    starts.assign(seg_start_host, seg_start_host + M + 1);
+    THEA_REQUIRE(starts[0] == 0 && starts[M] == n, "build: segment starts must run from 0 to the element count");
+    for (int s = 0; s < M; ++s) {
+      THEA_REQUIRE(starts[s + 1] > starts[s], "build: every segment must hold at least one element");
+      THEA_REQUIRE(starts[s + 1] - starts[s] < (int64_t(1) << 27), "build: at most 2^27 - 1 elements per segment");
+    }
+  } else {
+    THEA_REQUIRE(n < (int64_t(1) << 27), "build: at most 2^27 - 1 elements per BVH");
+    starts = {0, n};
+  }
 
   thea_bvh * b = new thea_bvh;
   try {
@@ -430,41 +555,54 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
     b->width = width;
     b->leaf_size = leaf;
     b->layouts = layouts;
+    b->query_order = cfg.query_order;
     b->n = n;
+    b->num_segments = M;
+    b->seg_start_host = starts;
+
+    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->seg_start, (size_t)(M + 1) * sizeof(int64_t), stream));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(b->seg_start, starts.data(), (size_t)(M + 1) * sizeof(int64_t),
+                                    cudaMemcpyHostToDevice, stream));
+    int64_t const * seg = b->seg_start;
 
     Scratch elo((size_t)n * sizeof(float4), stream), ehi((size_t)n * sizeof(float4), stream);
-    Scratch bounds(12 * sizeof(int), stream);
-    int init[12];
-    for (int t = 0; t < 12; ++t) init[t] = ((t < 3) || (t >= 6 && t < 9)) ? INT_MAX : INT_MIN;
-    THEA_CUDA_CHECK(cudaMemcpyAsync(bounds.ptr, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+    Scratch bounds((size_t)12 * M * sizeof(int), stream);
+    THEA_LAUNCH(init_bounds_kernel, (unsigned)ceil_div(12 * (int64_t)M, BUILD_THREADS), BUILD_THREADS, 0, stream,
+                bounds.as<int>(), M);
     unsigned grid = (unsigned)ceil_div(n, BUILD_THREADS);
-    THEA_LAUNCH(elem_box_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, is_mesh ? 1 : 0, elo.as<float4>(),
+    THEA_LAUNCH(elem_box_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, is_mesh ? 1 : 0, seg, M, elo.as<float4>(),
                 ehi.as<float4>(), bounds.as<int>());
 
+    int segbits = 0;
+    while ((int64_t(1) << segbits) < M) ++segbits;
+    int bpa = std::min(21, (63 - segbits) / 3);
+    int mbits = 3 * bpa;
     Scratch keys((size_t)n * sizeof(uint64_t), stream), vals((size_t)n * sizeof(uint32_t), stream);
-    THEA_LAUNCH(morton_kernel, grid, BUILD_THREADS, 0, stream, elo.as<float4>(), ehi.as<float4>(), n,
-                bounds.as<int>(), keys.as<uint64_t>(), vals.as<uint32_t>());
-    radix_sort_pairs(keys.as<uint64_t>(), vals.as<uint32_t>(), n, 63, stream);
+    THEA_LAUNCH(morton_kernel, grid, BUILD_THREADS, 0, stream, elo.as<float4>(), ehi.as<float4>(), n, seg, M,
+                bounds.as<int>(), bpa, keys.as<uint64_t>(), vals.as<uint32_t>());
+    radix_sort_pairs(keys.as<uint64_t>(), vals.as<uint32_t>(), n, mbits + segbits, stream);
 
-    int64_t m = n - 1;  // binary internal nodes
-    Scratch left((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), right((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream);
-    Scratch first((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), last((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream);
-    Scratch parent((size_t)std::max<int64_t>(m, 1) * sizeof(int), stream), leaf_parent((size_t)n * sizeof(int), stream);
-    Scratch ilo((size_t)std::max<int64_t>(m, 1) * sizeof(float4), stream), ihi((size_t)std::max<int64_t>(m, 1) * sizeof(float4), stream);
-    Scratch visits((size_t)std::max<int64_t>(m, 1) * sizeof(unsigned), stream);
+    int64_t m = n - M;  // binary internal nodes
+    size_t mm = (size_t)std::max<int64_t>(m, 1);
+    Scratch left(mm * sizeof(int), stream), right(mm * sizeof(int), stream);
+    Scratch first(mm * sizeof(int), stream), last(mm * sizeof(int), stream);
+    Scratch parent(mm * sizeof(int), stream), leaf_parent((size_t)n * sizeof(int), stream);
+    Scratch ilo(mm * sizeof(float4), stream), ihi(mm * sizeof(float4), stream);
+    Scratch visits(mm * sizeof(unsigned), stream);
     if (m >= 1) {
       THEA_CUDA_CHECK(cudaMemsetAsync(parent.ptr, 0xff, (size_t)m * sizeof(int), stream));
       THEA_CUDA_CHECK(cudaMemsetAsync(leaf_parent.ptr, 0xff, (size_t)n * sizeof(int), stream));
       THEA_CUDA_CHECK(cudaMemsetAsync(visits.ptr, 0, (size_t)m * sizeof(unsigned), stream));
-      THEA_LAUNCH(karras_kernel, (unsigned)ceil_div(m, BUILD_THREADS), BUILD_THREADS, 0, stream, keys.as<uint64_t>(),
-                  n, left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), parent.as<int>(),
+      THEA_LAUNCH(karras_kernel, grid, BUILD_THREADS, 0, stream, keys.as<uint64_t>(), n, seg, M, mbits,
+                  left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), parent.as<int>(),
                   leaf_parent.as<int>());
       THEA_LAUNCH(refit_kernel, grid, BUILD_THREADS, 0, stream, n, left.as<int>(), right.as<int>(), parent.as<int>(),
                   leaf_parent.as<int>(), elo.as<float4>(), ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(),
                   ihi.as<float4>(), visits.as<unsigned>());
     }
     CollapseArgs a{left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), elo.as<float4>(),
-                   ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(), ihi.as<float4>(), leaf};
+                   ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(), ihi.as<float4>(),
+                   M > 1 ? seg : nullptr, M, leaf};
     if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), stream);
     else collapse<8>(b, a, n, bounds.as<int>(), stream);
     int64_t node_bytes = b->num_nodes * (width == 4 ? (int64_t)sizeof(WideNode<4>) : (int64_t)sizeof(WideNode<8>));
@@ -486,20 +624,31 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
         THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->ray_rec, (size_t)n * RAY_REC_F4 * sizeof(float4), stream));
         rec_bytes += n * RAY_REC_F4 * (int64_t)sizeof(float4);
       }
-      THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, vals.as<uint32_t>(), b->cp_rec,
-                  b->ray_rec, b->leaf_to_elem);
+      THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, seg, M, vals.as<uint32_t>(),
+                  b->cp_rec, b->ray_rec, b->leaf_to_elem);
     } else {
       THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
       rec_bytes += n * (int64_t)sizeof(float4);
-      THEA_LAUNCH(point_records_kernel, grid, BUILD_THREADS, 0, stream, V, n, vals.as<uint32_t>(), b->pt_rec,
+      THEA_LAUNCH(point_records_kernel, grid, BUILD_THREADS, 0, stream, V, n, seg, M, vals.as<uint32_t>(), b->pt_rec,
                   b->leaf_to_elem);
     }
-    int hb[12];
-    THEA_CUDA_CHECK(cudaMemcpyAsync(hb, bounds.ptr, sizeof(hb), cudaMemcpyDeviceToHost, stream));
+    std::vector<int> hb((size_t)12 * M);
+    THEA_CUDA_CHECK(cudaMemcpyAsync(hb.data(), bounds.ptr, hb.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+    b->seg_lo.resize((size_t)3 * M);
+    b->seg_hi.resize((size_t)3 * M);
+    for (int s = 0; s < M; ++s)
+      for (int t = 0; t < 3; ++t) {
+        b->seg_lo[3 * s + t] = ord2f(hb[12 * s + 6 + t]);
+        b->seg_hi[3 * s + t] = ord2f(hb[12 * s + 9 + t]);
+      }
     for (int t = 0; t < 3; ++t) {
-      b->lo[t] = ord2f(hb[6 + t]);
-      b->hi[t] = ord2f(hb[9 + t]);
+      b->lo[t] = b->seg_lo[t];
+      b->hi[t] = b->seg_hi[t];
+      for (int s = 1; s < M; ++s) {
+        b->lo[t] = std::min(b->lo[t], b->seg_lo[3 * s + t]);
+        b->hi[t] = std::max(b->hi[t], b->seg_hi[3 * s + t]);
+      }
     }
     b->device_bytes = node_bytes + rec_bytes;
     return b;
@@ -508,6 +657,11 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
     destroy_bvh(b);
     throw;
   }
+}
+
+thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
+                     thea_build_config const & cfg, cudaStream_t stream) {
+  return build_forest(is_mesh, V, nv, F, nf, nullptr, 1, cfg, stream);
 }
 
 void destroy_bvh(thea_bvh * b) {
@@ -522,6 +676,8 @@ void destroy_bvh(thea_bvh * b) {
   if (b->pt_rec) cudaFree(b->pt_rec);
   if (b->leaf_to_elem) cudaFree(b->leaf_to_elem);
   if (b->err) cudaFree(b->err);
+  if (b->seg_start) cudaFree(b->seg_start);
+  if (b->seg_root) cudaFree(b->seg_root);
   if (prev >= 0) cudaSetDevice(prev);
   delete b;
 }

@@ -3,6 +3,8 @@
 
 #include "common.cuh"
 
+#include <vector>
+
 // Opaque to C callers; immutable once built.
 struct thea_bvh {
   int32_t is_mesh = 0;
@@ -11,6 +13,7 @@ struct thea_bvh {
   int32_t depth = 0;
   int32_t device = 0;
   uint32_t layouts = 0;
+  int32_t query_order = 0;  // traverse large batches in Morton order of the query point
   int64_t n = 0;          // elements
   int64_t num_nodes = 0;  // wide nodes; node 0 is the root
   void * nodes = nullptr;          // WideNode<width>[num_nodes]
@@ -21,12 +24,23 @@ struct thea_bvh {
   unsigned * err = nullptr;          // device word: error bits raised by query kernels
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   int64_t device_bytes = 0;
+  // forest of one BVH per segment (one segment for a single mesh / point set)
+  int32_t num_segments = 1;
+  int64_t * seg_start = nullptr;     // device, num_segments + 1: first sorted position (= first element) of each segment
+  int32_t * seg_root = nullptr;      // device, num_segments: root wide node of each segment
+  std::vector<int64_t> seg_start_host;
+  std::vector<float> seg_lo, seg_hi;  // per-segment element bounds (3 floats each)
 };
 
 namespace thea {
 
 thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
                      thea_build_config const & cfg, cudaStream_t stream);
+
+// One BVH per segment of elements [seg_start[s], seg_start[s+1]) (host array of M + 1 entries; segments non-empty).
+// Mesh faces index the shared vertex array; element records store indices within their segment.
+thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t n_elems,
+                        int64_t const * seg_start_host, int M, thea_build_config const & cfg, cudaStream_t stream);
 void destroy_bvh(thea_bvh * b);
 
 }  // namespace thea

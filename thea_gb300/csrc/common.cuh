@@ -57,8 +57,12 @@ struct LaunchScope {
 
 // Launch a kernel with bookkeeping, then check the launch itself for errors.
 #define THEA_LAUNCH(kernel, grid, block, smem, stream, ...)                                                        \
+  THEA_LAUNCH_NAMED(#kernel, kernel, grid, block, smem, stream, __VA_ARGS__)
+
+// The same, with an explicit name for the timing records (for kernels held in a variable).
+#define THEA_LAUNCH_NAMED(name, kernel, grid, block, smem, stream, ...)                                            \
   do {                                                                                                            \
-    ::thea::LaunchScope _scope(#kernel, stream);                                                                  \
+    ::thea::LaunchScope _scope(name, stream);                                                                     \
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                                                   \
     THEA_CUDA_CHECK(cudaGetLastError());                                                                          \
   } while (0)

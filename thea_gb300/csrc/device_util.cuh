@@ -8,16 +8,23 @@
 
 #include "common.cuh"
 
+#include <algorithm>
+#include <cstring>
+
 namespace thea {
 
-// A device buffer taken from the stream-ordered pool and returned to it when the owner goes out of scope.
+// The library's own stream-ordered memory pool on the current device (created once per device, with a release
+// threshold high enough that freed scratch stays mapped for the next call instead of going back to the driver).
+cudaMemPool_t scratch_pool();
+
+// A device buffer taken from the library's stream-ordered pool and returned to it when the owner goes out of scope.
 struct Scratch {
   void * ptr = nullptr;
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   Scratch() {}
   Scratch(size_t n, cudaStream_t s) : bytes(n), stream(s) {
-    if (n) THEA_CUDA_CHECK(cudaMallocAsync(&ptr, n, s));
+    if (n) THEA_CUDA_CHECK(cudaMallocFromPoolAsync(&ptr, n, scratch_pool(), s));
   }
   Scratch(Scratch const &) = delete;
   Scratch & operator=(Scratch const &) = delete;
@@ -241,18 +248,23 @@ static __global__ void rs_global_hist_kernel(uint64_t const * __restrict__ keys,
 }
 
 // Sorts (keys, vals) by key, stably, considering bits [0, key_bits). Results end in keys/vals. n < 2^32.
-inline void radix_sort_pairs(uint64_t * keys, uint32_t * vals, int64_t n, int key_bits, cudaStream_t stream) {
+// probe_passes: read a digit histogram back to the host first and skip passes in which every key has the same digit
+// (synchronizes the stream); without it every pass runs and the call stays asynchronous.
+inline void radix_sort_pairs(uint64_t * keys, uint32_t * vals, int64_t n, int key_bits, cudaStream_t stream,
+                             bool probe_passes = true) {
   if (n <= 1) return;
   THEA_REQUIRE(n < (int64_t(1) << 32), "radix sort: too many elements");
   int passes = (key_bits + 7) / 8;
-  // which passes are needed
-  Scratch ghist(8 * RS_BINS * sizeof(uint32_t), stream);
-  THEA_CUDA_CHECK(cudaMemsetAsync(ghist.ptr, 0, ghist.bytes, stream));
-  int hb = (int)std::min<int64_t>(ceil_div(n, 256), 1024);
-  THEA_LAUNCH(rs_global_hist_kernel, hb, 256, 0, stream, keys, n, ghist.as<uint32_t>());
   uint32_t h_hist[8 * RS_BINS];
-  THEA_CUDA_CHECK(cudaMemcpyAsync(h_hist, ghist.ptr, sizeof(h_hist), cudaMemcpyDeviceToHost, stream));
-  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+  memset(h_hist, 0, sizeof(h_hist));
+  if (probe_passes) {
+    Scratch ghist(8 * RS_BINS * sizeof(uint32_t), stream);
+    THEA_CUDA_CHECK(cudaMemsetAsync(ghist.ptr, 0, ghist.bytes, stream));
+    int hb = (int)std::min<int64_t>(ceil_div(n, 256), 1024);
+    THEA_LAUNCH(rs_global_hist_kernel, hb, 256, 0, stream, keys, n, ghist.as<uint32_t>());
+    THEA_CUDA_CHECK(cudaMemcpyAsync(h_hist, ghist.ptr, sizeof(h_hist), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+  }
 
   int64_t num_tiles = ceil_div(n, RS_TILE);
   Scratch keys_alt((size_t)n * sizeof(uint64_t), stream);

@@ -1,0 +1,559 @@
+// Per-query traversal routines shared by the single-BVH kernels and the batched persistent kernels, plus the FP64
+// re-check arithmetic.
+//
+// Each routine walks one BVH of a forest from its root node with a per-thread stack of (node or leaf code, lower bound),
+// nearest child first. Leaves hold element positions relative to their segment's first sorted position (elem_base).
+#pragma once
+
+#include "traverse.cuh"
+
+namespace thea {
+
+//============================================================================================================================
+// FP64 twin of the triangle arithmetic: the same algorithm as the FP32 path (Triangle3.hpp:143-155, 294-304,
+// 1311-1462; HyperplaneN.hpp:145-160), evaluated in double from the FP32 vertices, with the same operation order.
+//============================================================================================================================
+
+struct D3 {
+  double x, y, z;
+};
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 operator*(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ D3 operator*(D3 a, double s) { return D3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ D3 operator/(D3 a, double s) { return D3{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double dotd(D3 a, D3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+__device__ __forceinline__ double sqnormd(D3 a) { return a.x * a.x + (a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ D3 crossd(D3 a, D3 b) {
+  return D3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ D3 todd(V3 v) { return D3{(double)v.x, (double)v.y, (double)v.z}; }
+
+__device__ __forceinline__ bool inside_d(D3 v0, D3 v1, D3 v2, int axis, D3 p) {
+  double v0i, v0j, v1i, v1j, v2i, v2j, pi, pj;
+  if (axis == 1) {
+    v0i = v0.z; v0j = v0.x; v1i = v1.z; v1j = v1.x; v2i = v2.z; v2j = v2.x; pi = p.z; pj = p.x;
+  } else if (axis == 2) {
+    v0i = v0.x; v0j = v0.y; v1i = v1.x; v1j = v1.y; v2i = v2.x; v2j = v2.y; pi = p.x; pj = p.y;
+  } else {
+    v0i = v0.y; v0j = v0.z; v1i = v1.y; v1j = v1.z; v2i = v2.y; v2j = v2.z; pi = p.y; pj = p.z;
+  }
+  double area = (v1i - v0i) * (v2j - v0j) - (v2i - v0i) * (v1j - v0j);
+  if (area == 0.0) return v0.x == p.x && v0.y == p.y && v0.z == p.z;
+  double inv_area = 1.0 / area;
+  double b0 = ((v1i - pi) * (v2j - pj) - (v2i - pi) * (v1j - pj)) * inv_area;
+  if ((b0 < 0.0) || (b0 > 1.0)) return false;
+  double b1 = ((pi - v0i) * (v2j - v0j) - (v2i - v0i) * (pj - v0j)) * inv_area;
+  if ((b1 < 0.0) || (b1 > 1.0)) return false;
+  double b2 = 1.0 - b0 - b1;
+  return (b2 >= 0.0) && (b2 <= 1.0);
+}
+
+__device__ __forceinline__ D3 seg_d(D3 a, D3 b, D3 dir, double len, D3 p) {
+  D3 c = p - a;
+  double t = dotd(dir, c);
+  if (t <= 0.0) return a;
+  if (t >= len) return b;
+  return a + dir * t;
+}
+
+// Squared distance (and closest point) from p to the triangle, in FP64
+__device__ __forceinline__ double closest_point_f64(V3 fv0, V3 fv1, V3 fv2, V3 fp, D3 & cp) {
+  D3 v0 = todd(fv0), v1 = todd(fv1), v2 = todd(fv2), p = todd(fp);
+  D3 n = crossd(v1 - v0, v2 - v0);
+  double z = sqnormd(n);
+  if (z > 0.0) n = n / sqrt(z);
+  double dist = dotd(n, v0);
+  double a0 = fabs(n.x), a1 = fabs(n.y), a2 = fabs(n.z);
+  int axis = 0;
+  double best = a0;
+  if (a1 > best) { axis = 1; best = a1; }
+  if (a2 > best) axis = 2;
+  double sd = dotd(p, n) - dist;
+  D3 proj = p - sd * n;
+  if (inside_d(v0, v1, v2, axis, proj)) {
+    cp = proj;
+  } else {
+    D3 e[3] = {v1 - v0, v2 - v1, v0 - v2};
+    double len[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      len[i] = sqrt(sqnormd(e[i]));
+      e[i] = e[i] / len[i];
+    }
+    D3 r0 = seg_d(v0, v1, e[0], len[0], p), r1 = seg_d(v1, v2, e[1], len[1], p), r2 = seg_d(v2, v0, e[2], len[2], p);
+    double q0 = sqnormd(r0 - p), q1 = sqnormd(r1 - p), q2 = sqnormd(r2 - p);
+    if (q0 < q1) cp = (q0 < q2) ? r0 : r2;
+    else cp = (q1 < q2) ? r1 : r2;
+  }
+  return sqnormd(cp - p);
+}
+
+// Watertight ray/triangle test in FP64 (Woop, Benthin, Wald, "Watertight Ray/Triangle Intersection", JCGT 2013):
+// shear the triangle into the ray's frame, evaluate the three edge functions, accept points on edges. Returns the hit
+// time (>= 0) or -1.
+__device__ __forceinline__ double ray_triangle_watertight_f64(V3 fo, V3 fd, V3 fv0, V3 fe01, V3 fe02) {
+  D3 o = todd(fo), d = todd(fd);
+  D3 v0 = todd(fv0);
+  D3 v1 = v0 + todd(fe01), v2 = v0 + todd(fe02);
+  double ad[3] = {fabs(d.x), fabs(d.y), fabs(d.z)};
+  int kz = (ad[0] > ad[1]) ? ((ad[0] > ad[2]) ? 0 : 2) : ((ad[1] > ad[2]) ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  double dd[3] = {d.x, d.y, d.z};
+  if (dd[kz] < 0.0) { int t = kx; kx = ky; ky = t; }
+  if (dd[kz] == 0.0) return -1.0;
+  double Sx = dd[kx] / dd[kz], Sy = dd[ky] / dd[kz], Sz = 1.0 / dd[kz];
+  D3 A = v0 - o, B = v1 - o, C = v2 - o;
+  double a[3] = {A.x, A.y, A.z}, b[3] = {B.x, B.y, B.z}, c[3] = {C.x, C.y, C.z};
+  double Ax = a[kx] - Sx * a[kz], Ay = a[ky] - Sy * a[kz];
+  double Bx = b[kx] - Sx * b[kz], By = b[ky] - Sy * b[kz];
+  double Cx = c[kx] - Sx * c[kz], Cy = c[ky] - Sy * c[kz];
+  double U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if ((U < 0.0 || V < 0.0 || W < 0.0) && (U > 0.0 || V > 0.0 || W > 0.0)) return -1.0;
+  double det = U + V + W;
+  if (det == 0.0) return -1.0;
+  double T = U * (Sz * a[kz]) + V * (Sz * b[kz]) + W * (Sz * c[kz]);
+  double t = T / det;
+  return t >= 0.0 ? t : -1.0;
+}
+
+//============================================================================================================================
+// Closest element
+//============================================================================================================================
+
+// Squared distance and closest point of the record at sorted position k (FP32, reference arithmetic)
+__device__ __forceinline__ float cp_record_test(float4 const * __restrict__ rec, int64_t k, V3 p, V3 & cp) {
+  float4 const * r = rec + k * CP_REC_F4;
+  float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), nn = __ldg(r + 3);
+  V3 v0 = xyz(a), v1 = xyz(b), v2 = xyz(c), nrm = xyz(nn);
+  // HyperplaneN::closestPoint: p - signedDistance(p) * normal, signedDistance = p . normal - dist
+  float sd = dot(p, nrm) - a.w;
+  V3 proj = p - sd * nrm;
+  if (point_inside_triangle(v0, v1, v2, __float_as_int(nn.w), proj)) {
+    cp = proj;
+  } else {
+    float4 e0 = __ldg(r + 4), e1 = __ldg(r + 5), e2 = __ldg(r + 6);
+    cp = closest_on_perimeter(v0, v1, v2, xyz(e0), b.w, xyz(e1), c.w, xyz(e2), e0.w, p);
+  }
+  return squared_norm(cp - p);
+}
+
+__device__ __forceinline__ int cp_record_index(float4 const * __restrict__ rec, int64_t k) {
+  return __float_as_int(__ldg(rec + k * CP_REC_F4 + 5).w);
+}
+
+// FP64 squared distance and closest point of record k. Kept out of line: every caller shares one copy of the long FP64
+// sequence, which matters on a GPU whose FP64 pipe is narrow.
+static __device__ __noinline__ double cp_record_f64_call(float4 const * __restrict__ rec, int64_t k, V3 p, D3 * cp) {
+  float4 const * r = rec + k * CP_REC_F4;
+  return closest_point_f64(xyz(__ldg(r)), xyz(__ldg(r + 1)), xyz(__ldg(r + 2)), p, *cp);
+}
+
+__device__ __forceinline__ float cp_record_f64(float4 const * __restrict__ rec, int64_t k, V3 p, D3 & cp, double & d2) {
+  d2 = cp_record_f64_call(rec, k, p, &cp);
+  return (float)d2;
+}
+
+struct ClosestOut {
+  int idx;      // element index within its mesh, INT_MAX if none
+  float d2;     // FP32 squared distance (reference mode) or the FP64 squared distance rounded (re-check mode)
+  V3 cp;
+  double d2_64;  // FP64 squared distance of the chosen element (re-check mode, or when an error estimate is wanted)
+  int64_t slot;  // sorted position of the chosen element
+  float best32;  // re-check mode: smallest FP32 squared distance of an accepted element (an upper bound), +inf if none
+  bool done;     // false when the pop budget ran out before the search finished
+};
+
+// Pushes the children of an expanded node whose lower bound passes `lim` (misses carry a NaN bound and never pass),
+// nearest on top. Leaves go on the stack too, so every child is visited in order of its bound.
+template <int W, int STACK>
+__device__ __forceinline__ void push_children(NodeRegs<W> const & nd, float const (&lb)[W], float lim,
+                                              int (&stk)[STACK], float (&stkd)[STACK], int & sp, unsigned * err) {
+  uint32_t key[W];
+  int cc[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    bool keep = nd.child[c] != CHILD_EMPTY && lb[c] <= lim;
+    key[c] = keep ? __float_as_uint(lb[c]) : 0xffffffffu;
+    cc[c] = nd.child[c];
+  }
+  sort_children<W>(key, cc);
+#pragma unroll
+  for (int c = W - 1; c >= 0; --c) {
+    if (key[c] != 0xffffffffu) {
+      if (sp < STACK) {
+        stk[sp] = cc[c];
+        stkd[sp] = __uint_as_float(key[c]);
+        ++sp;
+      } else {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+      }
+    }
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void point_child_bounds(NodeRegs<W> const & nd, V3 p, float (&lb)[W]) {
+#pragma unroll
+  for (int c = 0; c < W; ++c)
+    lb[c] = point_box_d2(p.x, p.y, p.z, nd.lox[c], nd.loy[c], nd.loz[c], nd.hix[c], nd.hiy[c], nd.hiz[c]);
+}
+
+// FP32 reference-arithmetic search: smallest (d2, index), accepting d2 <= thresh. With budget > 0 the search stops
+// after that many stack pops (done = false), leaving the best found so far.
+template <int W, int STACK>
+__device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restrict__ nodes,
+                                                    float4 const * __restrict__ rec, int root, int64_t elem_base, V3 p,
+                                                    float thresh, unsigned * err, int budget = 0) {
+  bool done = true;
+  float best = thresh;
+  int best_idx = INT_MAX;
+  int64_t best_slot = -1;
+  V3 best_cp = V3{0.f, 0.f, 0.f};
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = root;
+  stkd[sp] = 0.f;
+  ++sp;
+  int pops = 0;
+  while (sp > 0) {
+    if (budget > 0 && ++pops > budget) {
+      done = false;
+      break;
+    }
+    --sp;
+    int code = stk[sp];
+    if (stkd[sp] > best * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        V3 cp;
+        float d2 = cp_record_test(rec, k, p, cp);
+        if (d2 <= best) {
+          int idx = cp_record_index(rec, k);
+          if (d2 < best || idx < best_idx) {
+            best = d2;
+            best_idx = idx;
+            best_cp = cp;
+            best_slot = k;
+          }
+        }
+      }
+    }
+  }
+  ClosestOut o;
+  o.idx = best_idx;
+  o.d2 = best;
+  o.cp = best_cp;
+  o.d2_64 = 0.0;
+  o.slot = best_slot;
+  o.best32 = best;
+  o.done = done;
+  return o;
+}
+
+// Mixed-precision search: FP32 traversal and element tests; every element whose FP32 distance lies within a band of
+// the current FP32 best is re-evaluated in FP64, and the result is the FP64 minimum (ties: lowest index) with its FP64
+// distance and closest point. The band is relative 2^-14 of the distance plus 2^-18 of the coordinate scale `scale`
+// (the largest coordinate magnitude of the query and the mesh): FP32 closest-point arithmetic is accurate to about
+// 8 ulps of that scale, so the element that is nearest in FP64 always falls inside the band of the FP32 best.
+// Candidates are collected during the traversal and evaluated together at the end, when the band is final; an entry
+// pushed out of the full list while still inside the band is evaluated then. Accepts elements with FP64 d2 < bound2
+// (bound2 < 0: unbounded).
+template <int W, int STACK>
+__device__ __forceinline__ ClosestOut closest_query_f64(WideNode<W> const * __restrict__ nodes,
+                                                        float4 const * __restrict__ rec, int root, int64_t elem_base,
+                                                        V3 p, double bound2, float scale, unsigned * err,
+                                                        int budget = 0) {
+  bool done = true;
+  int pops = 0;
+  float const REL = 1.0f + 1.0f / 16384.0f;
+  float abs_tol = scale * (1.0f / 262144.0f);
+  float best32 = INFINITY;  // smallest FP32 squared distance seen among accepted elements
+  float lim = bound2 >= 0.0 ? __double2float_ru(bound2) : INFINITY;  // band limit on FP32 squared distances
+  if (bound2 >= 0.0) {
+    float lb0 = sqrtf(lim) * REL + abs_tol;
+    lim = lb0 * lb0;
+  }
+  double best64 = INFINITY;
+  int best_idx = INT_MAX;
+  int64_t best_slot = -1;
+  D3 best_cp = D3{0.0, 0.0, 0.0};
+  constexpr int NCAND = 8;
+  float cand_d[NCAND];
+  int64_t cand_k[NCAND];
+#pragma unroll
+  for (int j = 0; j < NCAND; ++j) { cand_d[j] = INFINITY; cand_k[j] = -1; }
+  int64_t pending = -1;  // an entry pushed out of the full list while inside the band
+  auto eval64 = [&](int64_t k) {
+    D3 cp64;
+    double d64 = cp_record_f64_call(rec, k, p, &cp64);
+    if (bound2 >= 0.0 && !(d64 < bound2)) return;
+    int idx = cp_record_index(rec, k);
+    if (d64 < best64 || (d64 == best64 && idx < best_idx)) {
+      best64 = d64;
+      best_idx = idx;
+      best_cp = cp64;
+      best_slot = k;
+    }
+  };
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = root;
+  stkd[sp] = 0.f;
+  ++sp;
+  while (sp > 0) {
+    if (budget > 0 && ++pops > budget) {
+      done = false;
+      break;
+    }
+    --sp;
+    int code = stk[sp];
+    if (stkd[sp] > lim * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children<W, STACK>(nd, lb, lim * PRUNE_SLACK, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        V3 cp;
+        float d2 = cp_record_test(rec, k, p, cp);
+        if (!(d2 <= lim)) continue;
+        if (d2 < best32) {
+          best32 = d2;
+          float lb1 = sqrtf(best32) * REL + abs_tol;
+          lim = fminf(lim, lb1 * lb1);
+        }
+        // the candidate takes a slot that has left the band, else the farthest slot if that is farther than it
+        int slot_j = -1;
+        float worst = d2;
+#pragma unroll
+        for (int j = 0; j < NCAND; ++j)
+          if (slot_j < 0 && !(cand_d[j] <= lim)) slot_j = j;  // empty slots hold +inf
+        if (slot_j < 0) {
+#pragma unroll
+          for (int j = 0; j < NCAND; ++j)
+            if (cand_d[j] > worst) { worst = cand_d[j]; slot_j = j; }
+        }
+        int64_t evict = slot_j < 0 ? k : -1;
+#pragma unroll
+        for (int j = 0; j < NCAND; ++j) {
+          if (j == slot_j) {
+            if (cand_d[j] <= lim) evict = cand_k[j];
+            cand_d[j] = d2;
+            cand_k[j] = k;
+          }
+        }
+        if (evict >= 0) {
+          if (pending >= 0) eval64(pending);
+          pending = evict;
+        }
+      }
+    }
+  }
+  // evaluate the candidates still inside the final band, one slot at a time with the warp's lanes together
+  if (pending >= 0) eval64(pending);
+#pragma unroll 1
+  for (int j = 0; j < NCAND; ++j) {
+    float dj = 0.f;
+    int64_t kj = -1;
+#pragma unroll
+    for (int t = 0; t < NCAND; ++t)
+      if (t == j) { dj = cand_d[t]; kj = cand_k[t]; }
+    if (dj <= lim) eval64(kj);
+  }
+  ClosestOut o;
+  o.idx = best_idx;
+  o.d2_64 = best64;
+  o.d2 = (float)best64;
+  o.cp = V3{(float)best_cp.x, (float)best_cp.y, (float)best_cp.z};
+  o.slot = best_slot;
+  o.best32 = best32;
+  o.done = done;
+  return o;
+}
+
+//============================================================================================================================
+// First ray hit
+//============================================================================================================================
+
+struct RayOut {
+  float t;       // FP32 reference verdict: hit time, or the initial bound when nothing was hit
+  int idx;       // INT_MAX if none
+  int64_t slot;
+  double t64;    // watertight FP64 verdict (re-check mode): hit time or +inf
+  int idx64;
+  int64_t slot64;
+};
+
+static __device__ __noinline__ double watertight_f64_call(V3 o, V3 d, float4 a, float4 b, float4 c) {
+  return ray_triangle_watertight_f64(o, d, xyz(a), xyz(b), xyz(c));
+}
+
+// Reference verdict (FP32 Eberly test with the parallel threshold) and, when `recheck` is set, the watertight FP64
+// verdict over every element the FP32 test accepted or rejected by a narrow margin (within 2^-12 of the determinant on
+// an edge test, or near the parallel threshold).
+template <int W, int STACK, bool RECHECK>
+__device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                                            int root, int64_t elem_base, V3 o, V3 d, float max_time, unsigned * err) {
+  float ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
+  float iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
+  float iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
+  float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+  float best = max_time >= 0.f ? max_time : INFINITY;
+  int best_idx = INT_MAX;
+  int64_t best_slot = -1;
+  double best64 = max_time >= 0.f ? (double)max_time : INFINITY;
+  int idx64 = INT_MAX;
+  int64_t slot64 = -1;
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = root;
+  stkd[sp] = 0.f;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int code = stk[sp];
+    float bound = RECHECK ? fmaxf(best, (float)best64) : best;
+    if (stkd[sp] > bound * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        float tx0 = __fmaf_rn(nd.lox[c], ix, ox), tx1 = __fmaf_rn(nd.hix[c], ix, ox);
+        float ty0 = __fmaf_rn(nd.loy[c], iy, oy), ty1 = __fmaf_rn(nd.hiy[c], iy, oy);
+        float tz0 = __fmaf_rn(nd.loz[c], iz, oz), tz1 = __fmaf_rn(nd.hiz[c], iz, oz);
+        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
+        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
+      }
+      push_children<W, STACK>(nd, lb, bound * PRUNE_SLACK, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        float4 const * r = rec + k * RAY_REC_F4;
+        float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+        float t = ray_triangle_time(o, d, xyz(a), xyz(b), xyz(c));
+        int idx = __float_as_int(a.w);
+        // TriangleN<3>::rayIntersection accepts t >= 0 and, with a bound, t <= max_time
+        if (t >= 0.f && t <= best) {
+          if (t < best || idx < best_idx) {
+            best = t;
+            best_idx = idx;
+            best_slot = k;
+          }
+        }
+        if (RECHECK) {
+          bool candidate = t >= 0.f;
+          if (!candidate) {
+            // narrow FP32 rejections: recompute the edge tests' margins
+            V3 diff = o - xyz(a);
+            V3 nrm = cross(xyz(b), xyz(c));
+            float DdN = dot(d, nrm);
+            float s = DdN < 0.f ? -1.f : 1.f;
+            float adn = fabsf(DdN);
+            float e1 = s * dot(d, cross(diff, xyz(c)));
+            float e2 = s * dot(d, cross(xyz(b), diff));
+            float eta = adn * (1.0f / 4096.0f);
+            candidate = adn <= 4.f * 1.1920928955078125e-07f ||
+                        (fminf(fminf(e1, e2), adn - e1 - e2) >= -eta && fmaxf(fabsf(e1), fabsf(e2)) <= 2.f * adn);
+          }
+          if (candidate) {
+            double t64 = watertight_f64_call(o, d, a, b, c);
+            if (t64 >= 0.0 && (max_time < 0.f || t64 <= (double)max_time) &&
+                (t64 < best64 || (t64 == best64 && idx < idx64))) {
+              best64 = t64;
+              idx64 = idx;
+              slot64 = k;
+            }
+          }
+        }
+      }
+    }
+  }
+  RayOut out;
+  out.t = best;
+  out.idx = best_idx;
+  out.slot = best_slot;
+  out.t64 = best64;
+  out.idx64 = idx64;
+  out.slot64 = slot64;
+  return out;
+}
+
+//============================================================================================================================
+// k nearest points
+//============================================================================================================================
+
+// Insert (d, i) into sorted register arrays, lexicographic (distance, index); the last entry falls off.
+template <int K> __device__ __forceinline__ void knn_insert(float (&bd)[K], int (&bi)[K], float d, int i) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    bool lt = (d < bd[j]) || (d == bd[j] && i < bi[j]);
+    float td = bd[j];
+    int ti = bi[j];
+    bd[j] = lt ? d : td;
+    bi[j] = lt ? i : ti;
+    d = lt ? td : d;
+    i = lt ? ti : i;
+  }
+}
+
+template <int W, int K, int STACK>
+__device__ __forceinline__ void knn_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts,
+                                          int root, int64_t elem_base, V3 p, int excl, float (&bd)[K], int (&bi)[K],
+                                          unsigned * err) {
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = root;
+  stkd[sp] = 0.f;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int code = stk[sp];
+    if (stkd[sp] > bd[K - 1] * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children<W, STACK>(nd, lb, bd[K - 1] * PRUNE_SLACK, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        float4 a = __ldg(pts + k);
+        int idx = __float_as_int(a.w);
+        if (idx == excl) continue;
+        // MetricL2Impl<point, point>::closestPoints: (element - query).squaredNorm()
+        float d2 = squared_norm(xyz(a) - p);
+        if (d2 < bd[K - 1] || (d2 == bd[K - 1] && idx < bi[K - 1])) knn_insert<K>(bd, bi, d2, idx);
+      }
+    }
+  }
+}
+
+}  // namespace thea

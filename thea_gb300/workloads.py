@@ -163,6 +163,83 @@ def config0(scale=1.0):
     return V, F, Q
 
 
+def config3_spec(num_meshes=4096, seed=CONFIG_SEEDS[3], min_level=2, max_level=7, min_q=1000, max_q=100000):
+    """Per-mesh parameters of the batched workload: subdivision level (uniform over min..max, so triangle counts are
+    log-uniform from 20 * 4^min to 20 * 4^max), per-axis stretch U[0.5, 2], log-uniform query count, noise seed."""
+    rng = np.random.default_rng(seed)
+    levels = rng.integers(min_level, max_level + 1, size=num_meshes)
+    scales = rng.uniform(0.5, 2.0, size=(num_meshes, 3))
+    nq = np.exp(rng.uniform(np.log(min_q), np.log(max_q), size=num_meshes)).astype(np.int64)
+    mesh_seeds = rng.integers(0, 2 ** 31 - 1, size=num_meshes)
+    return levels, scales, nq, mesh_seeds
+
+
+def config3_numpy(num_meshes, seed=CONFIG_SEEDS[3], **kw):
+    """Concatenated batch (host arrays): V, F (indices into V), face_offsets, queries, query_offsets, levels.
+    Each mesh is a seeded noisy icosphere with an affine stretch; its queries are uniform in its box grown by 50%."""
+    levels, scales, nq, seeds = config3_spec(num_meshes, seed, **kw)
+    Vs, Fs, Qs = [], [], []
+    vbase = 0
+    for m in range(num_meshes):
+        V, F = noisy_icosphere(int(levels[m]), int(seeds[m]), scale=scales[m])
+        lo, hi = V.min(0).astype(np.float64), V.max(0).astype(np.float64)
+        c, e = 0.5 * (lo + hi), 1.5 * (hi - lo)
+        Q = uniform_box_points(int(nq[m]), c - 0.5 * e, c + 0.5 * e, int(seeds[m]) + 1)
+        Vs.append(V)
+        Fs.append(F + vbase)
+        Qs.append(Q)
+        vbase += len(V)
+    face_off = np.concatenate([[0], np.cumsum([len(f) for f in Fs])]).astype(np.int64)
+    q_off = np.concatenate([[0], np.cumsum([len(q) for q in Qs])]).astype(np.int64)
+    return (np.concatenate(Vs), np.concatenate(Fs).astype(np.int32), face_off, np.concatenate(Qs), q_off, levels)
+
+
+def config3_torch(num_meshes=4096, seed=CONFIG_SEEDS[3], device="cuda", **kw):
+    """The batched workload generated on the GPU (same per-mesh parameters as config3_numpy; noise and queries drawn
+    with torch's generator, so values differ from the NumPy version). Returns CUDA tensors V, F, query positions and
+    query offsets, plus host face offsets (int64) and per-mesh levels."""
+    import torch
+    levels, scales, nq, seeds = config3_spec(num_meshes, seed, **kw)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    nv_l = {L: len(icosphere(L)[0]) for L in range(int(levels.min()), int(levels.max()) + 1)}
+    nf_l = {L: len(icosphere(L)[1]) for L in nv_l}
+    nv = np.array([nv_l[int(L)] for L in levels], np.int64)
+    nf = np.array([nf_l[int(L)] for L in levels], np.int64)
+    voff = np.concatenate([[0], np.cumsum(nv)])
+    foff = np.concatenate([[0], np.cumsum(nf)]).astype(np.int64)
+    qoff = np.concatenate([[0], np.cumsum(nq)]).astype(np.int64)
+    V = torch.empty((int(voff[-1]), 3), dtype=torch.float32, device=device)
+    F = torch.empty((int(foff[-1]), 3), dtype=torch.int32, device=device)
+    sc = torch.as_tensor(scales, dtype=torch.float32, device=device)
+    for L in nv_l:
+        ms = np.nonzero(levels == L)[0]
+        if len(ms) == 0:
+            continue
+        tv, tf = icosphere(L)
+        tv = torch.as_tensor(tv, dtype=torch.float32, device=device)
+        tf = torch.as_tensor(tf, dtype=torch.int64, device=device)
+        msd = torch.as_tensor(ms, device=device)
+        r = 1.0 + 0.01 * torch.randn((len(ms), len(tv), 1), generator=g, device=device)
+        vals = tv[None] * r * sc[msd][:, None, :]
+        vb = torch.as_tensor(voff[ms], device=device)
+        V[(vb[:, None] + torch.arange(len(tv), device=device)[None]).reshape(-1)] = vals.reshape(-1, 3)
+        fb = torch.as_tensor(foff[ms], device=device)
+        F[(fb[:, None] + torch.arange(len(tf), device=device)[None]).reshape(-1)] = \
+            (tf[None] + vb[:, None, None]).reshape(-1, 3).to(torch.int32)
+    mesh_of_v = torch.repeat_interleave(torch.arange(num_meshes, device=device), torch.as_tensor(nv, device=device))
+    lo = torch.full((num_meshes, 3), float("inf"), device=device).scatter_reduce(
+        0, mesh_of_v[:, None].expand(-1, 3), V, reduce="amin")
+    hi = torch.full((num_meshes, 3), float("-inf"), device=device).scatter_reduce(
+        0, mesh_of_v[:, None].expand(-1, 3), V, reduce="amax")
+    c, e = 0.5 * (lo + hi), 1.5 * (hi - lo)
+    mesh_of_q = torch.repeat_interleave(torch.arange(num_meshes, device=device), torch.as_tensor(nq, device=device))
+    u = torch.rand((int(qoff[-1]), 3), generator=g, device=device)
+    Q = (c[mesh_of_q] + (u - 0.5) * e[mesh_of_q]).contiguous()
+    qoff_d = torch.as_tensor(qoff, device=device)
+    return V, F, foff, Q, qoff_d, levels
+
+
 def config1(grid=1024, nrays=4194304):
     """Ray first hit: 1024^2 heightfield (2,093,058 tris), 4,194,304 cosine rays from z = 0.5."""
     s = CONFIG_SEEDS[1]
