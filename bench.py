@@ -420,8 +420,9 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
         sfo.append(sfo[-1] + Fm.shape[0])
         sqo.append(sqo[-1] + sq[-1].shape[0])
     t0 = time.perf_counter()
+    # tuned for the mixed-precision mode (FP32 traversal, FP64 re-check), the configuration the target is quoted on
     tune = T.autotune_batch_closest(torch.cat(sv), torch.cat(sf), np.array(sfo, np.int64), torch.cat(sq),
-                                    torch.as_tensor(np.array(sqo, np.int64), device="cuda"))
+                                    torch.as_tensor(np.array(sqo, np.int64), device="cuda"), precision="fp64")
     res["autotune"] = dict(tune, seconds=time.perf_counter() - t0)
     t0 = time.perf_counter()
     forest = T.MeshForest(V, F, foff, width=tune["width"], max_leaf_size=tune["max_leaf_size"], layouts=1)
@@ -429,18 +430,20 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
     res["forest_build_s"] = time.perf_counter() - t0
     for prec in ("fp32", "fp64"):
         out = (torch.empty(nq, dtype=torch.int32, device="cuda"), torch.empty(nq, dtype=torch.float32, device="cuda"),
-               None, torch.empty(nq, dtype=torch.float32, device="cuda"))
+               torch.empty((nq, 3), dtype=torch.float32, device="cuda"), None)
         s = torch.cuda.Stream()
         torch.cuda.synchronize()
+        kw = dict(precision=prec, queries_per_warp=tune["queries_per_warp"],
+                  hard_query_budget=tune["hard_query_budget"])
         with torch.cuda.stream(s):
             with T.Graph() as g:
-                forest.batch_closest_element(Q, qoff, precision=prec, queries_per_warp=tune["queries_per_warp"],
-                                             hard_query_budget=tune["hard_query_budget"], errors=True, out=out)
+                forest.batch_closest_element(Q, qoff, closest_points=True, out=out, **kw)
             ms = timed_steps(g.launch, max(3, min(args.steps, 5)), 2, flush, s)
         g.close()
-        # error vs FP64 relative to the distance, floored at 1e-6 of the scene scale (distances near zero)
-        d = out[1]
-        rel = (out[3] / torch.clamp(d, min=1e-6 * float(Q.abs().max()))).max().item()
+        # accuracy, untimed: |distance - FP64 distance of the returned element| relative to the distance, floored at
+        # 1e-6 of the scene scale (distances near zero)
+        _, d, _, e = forest.batch_closest_element(Q, qoff, errors=True, **kw)
+        rel = (e / torch.clamp(d, min=1e-6 * float(Q.abs().max()))).max().item()
         res["batched_" + prec] = {"value": nq / (statistics.median(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
                                   "ms": statistics.median(ms), "max_rel_error_vs_fp64": rel}
     forest.close()

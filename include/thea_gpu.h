@@ -238,8 +238,9 @@ typedef struct thea_tuning {
 } thea_tuning;
 
 /* Times batched closest-point queries on a sample workload (a mesh forest's inputs plus device queries grouped by
- * mesh) for every BVH width (4, 8) and leaf size (1, 2, 4): queries-per-warp (32, 64, 128) at the default step budget,
- * then step budgets (12, 96, none) at the best queries-per-warp; returns the fastest. Synchronizes the stream. */
+ * mesh) for every BVH width (4, 8) and leaf size (1, 2, 4): queries-per-warp (32, 64, 128) with one thread per query
+ * throughout, then step budgets (12, 32, 128) at the best queries-per-warp; returns the fastest (36 candidates).
+ * Synchronizes the stream. */
 THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t num_vertices, const int32_t * faces,
                                                  const int64_t * mesh_face_offsets, int32_t num_meshes,
                                                  const float * queries, const int64_t * query_offsets,

@@ -140,5 +140,5 @@ def test_autotune_returns_a_valid_fast_config(T, batch):
     tune = T.autotune_batch_closest(dev(V), dev(F), foff, dev(Q), dev(qoff))
     assert tune["candidates"] == 36
     assert tune["width"] in (4, 8) and tune["max_leaf_size"] in (1, 2, 4) and tune["queries_per_warp"] in (32, 64, 128)
-    assert tune["hard_query_budget"] in (12, 32, 96, -1)
+    assert tune["hard_query_budget"] in (12, 32, 128, -1)
     assert 0 < tune["milliseconds"] < 1000

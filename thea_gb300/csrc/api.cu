@@ -750,7 +750,7 @@ THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t
     thea_tuning best{};
     best.milliseconds = INFINITY;
     int tried = 0;
-    int const widths[2] = {4, 8}, leaves[3] = {1, 2, 4}, chunks[3] = {32, 64, 128}, budgets[3] = {12, 96, 0};
+    int const widths[2] = {4, 8}, leaves[3] = {1, 2, 4}, chunks[3] = {32, 64, 128}, budgets[3] = {12, 32, 128};
     for (int w : widths)
       for (int l : leaves) {
         thea_build_config cfg{};
@@ -786,11 +786,11 @@ THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t
           }
           return times[1];
         };
-        // queries per warp at the default budget, then the budget (including one thread throughout) at the best one
+        // queries per warp with one thread per query throughout, then the two-phase budgets at the best one
         int best_chunk = chunks[0];
         float best_t = INFINITY;
         for (int c : chunks) {
-          float t = time_it(c, 32);
+          float t = time_it(c, 0);
           if (t < best_t) { best_t = t; best_chunk = c; }
         }
         for (int bud : budgets) time_it(best_chunk, bud);

@@ -38,58 +38,13 @@ __device__ __forceinline__ bool next_chunk(unsigned long long * counter, int chu
   return base < nq;
 }
 
-template <int W, int STACK, int PREC>
-__global__ void __launch_bounds__(BATCH_THREADS)
-batch_closest_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff, int64_t nq,
-                     float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
-                     float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
-                     unsigned long long * counter, int chunk) {
-  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
-  int64_t base;
-  while (next_chunk(counter, chunk, nq, base)) {
-    int64_t end = base + chunk < nq ? base + chunk : nq;
-    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
-      int m = mesh_of_query(qoff, f.M, q);
-      int root = __ldg(f.seg_root + m);
-      int64_t ebase = __ldg(f.seg_start + m);
-      V3 p = load_v3(queries + 3 * q);
-      ClosestOut r;
-      float dist;
-      if (PREC == THEA_PRECISION_FP64_RECHECK) {
-        float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-        r = closest_query_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, bound2, scale, f.err);
-        dist = (float)sqrt(r.d2_64);
-      } else {
-        r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, thresh, f.err);
-        dist = sqrtf(r.d2);
-      }
-      bool found = r.idx != INT_MAX;
-      out_index[q] = found ? r.idx : -1;
-      if (out_dist) out_dist[q] = found ? dist : -1.f;
-      if (out_cp) {
-        out_cp[3 * q] = found ? r.cp.x : 0.f;
-        out_cp[3 * q + 1] = found ? r.cp.y : 0.f;
-        out_cp[3 * q + 2] = found ? r.cp.z : 0.f;
-      }
-      if (out_err) {
-        float e = -1.f;
-        if (found) {
-          double d64 = r.d2_64;
-          if (PREC != THEA_PRECISION_FP64_RECHECK) {
-            D3 cp64;
-            cp_record_f64(f.cp_rec, r.slot, p, cp64, d64);
-          }
-          e = (float)fabs((double)dist - sqrt(d64));
-        }
-        out_err[q] = e;
-      }
-    }
-  }
-}
-
 //============================================================================================================================
-// Two-phase closest element: phase 1 runs one thread per query with a budget of stack pops; queries that run out are
-// queued with the best element found so far (a valid upper bound) and phase 2 finishes them with one warp per query.
+// Closest element. Each warp works in rounds of 32 queries, one per lane; every lane of the warp takes part in every
+// round (lanes past the end of the chunk carry no query), so the warp-wide FP64 step of the mixed-precision search and
+// the FP64 error estimate run with all lanes together.
+//
+// Two-phase form: with budget > 0, phase 1 stops a query after that many stack pops and queues it with the best
+// element found so far (a valid upper bound); phase 2 finishes the queued queries with one warp per query.
 //============================================================================================================================
 
 struct HardQueue {
@@ -100,10 +55,9 @@ struct HardQueue {
   unsigned long long * count;
 };
 
-template <int PREC>
-__device__ __forceinline__ void write_closest(float4 const * __restrict__ rec, int64_t q, V3 p, bool found, float dist,
-                                              V3 cp, int idx, int64_t slot, double d2_64, int32_t * out_index,
-                                              float * out_dist, float * out_cp, float * out_err) {
+// d64: FP64 squared distance of the returned element (for the error estimate)
+__device__ __forceinline__ void write_closest(int64_t q, bool found, float dist, V3 cp, int idx, double d64,
+                                              int32_t * out_index, float * out_dist, float * out_cp, float * out_err) {
   out_index[q] = found ? idx : -1;
   if (out_dist) out_dist[q] = found ? dist : -1.f;
   if (out_cp) {
@@ -111,56 +65,90 @@ __device__ __forceinline__ void write_closest(float4 const * __restrict__ rec, i
     out_cp[3 * q + 1] = found ? cp.y : 0.f;
     out_cp[3 * q + 2] = found ? cp.z : 0.f;
   }
-  if (out_err) {
-    float e = -1.f;
-    if (found) {
-      double d64 = d2_64;
-      if (PREC != THEA_PRECISION_FP64_RECHECK) {
-        D3 cp64;
-        cp_record_f64(rec, slot, p, cp64, d64);
-      }
-      e = (float)fabs((double)dist - sqrt(d64));
-    }
-    out_err[q] = e;
+  if (out_err) out_err[q] = found ? (float)fabs((double)dist - sqrt(d64)) : -1.f;
+}
+
+struct ClosestArgs {
+  float const * queries;
+  int64_t const * qoff;
+  float thresh;
+  double bound2;
+  float scene_scale;
+  int32_t * out_index;
+  float * out_dist;
+  float * out_cp;
+  float * out_err;
+};
+
+// One round: lane query q when active. Called by all 32 lanes of the warp together.
+template <int W, int STACK, int PREC>
+__device__ __forceinline__ void closest_round(BatchForest const & f, ClosestArgs const & a, int64_t q, bool active,
+                                              int budget, HardQueue const & hq, F64WarpBuf * buf) {
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int root = 0;
+  int64_t ebase = 0;
+  V3 p = V3{0.f, 0.f, 0.f};
+  if (active) {
+    int m = mesh_of_query(a.qoff, f.M, q);
+    root = __ldg(f.seg_root + m);
+    ebase = __ldg(f.seg_start + m);
+    p = load_v3(a.queries + 3 * q);
   }
+  ClosestOut r;
+  r.idx = INT_MAX;
+  r.d2 = 0.f;
+  r.d2_64 = 0.0;
+  r.slot = -1;
+  r.best32 = INFINITY;
+  r.done = true;
+  float dist = 0.f;
+  if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
+    float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+    F64Search s;
+    if (active) closest_search_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, a.bound2, scale, f.err, s, budget);
+    else f64_search_init(s);
+    f64_resolve_warp(s, active && s.done, f.cp_rec, ebase, p, a.bound2, *buf);
+    r = f64_result(s);
+    dist = (float)sqrt(r.d2_64);
+  } else {
+    if (active) r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, a.thresh, f.err, budget);
+    dist = sqrtf(r.d2);
+  }
+  if (active && !r.done) {
+    unsigned long long pos = atomicAdd(hq.count, 1ull);
+    hq.q[pos] = q;
+    hq.bound[pos] = r.best32;
+    hq.idx[pos] = PREC == THEA_PRECISION_FP64_RECHECK ? INT_MAX : r.idx;
+    hq.slot[pos] = r.slot;
+  }
+  bool fin = active && r.done;
+  bool found = r.idx != INT_MAX;
+  double d64 = r.d2_64;
+  if (PREC != THEA_PRECISION_FP64_RECHECK && a.out_err) {
+    __syncwarp();
+    if (fin && found) {
+      D3 cp64;
+      cp_record_f64(f.cp_rec, r.slot, p, cp64, d64);
+    }
+  }
+  if (fin) write_closest(q, found, dist, r.cp, r.idx, d64, a.out_index, a.out_dist, a.out_cp, a.out_err);
 }
 
 template <int W, int STACK, int PREC>
 __global__ void __launch_bounds__(BATCH_THREADS)
-batch_closest_phase1_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff,
-                            int64_t nq, float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
-                            float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
-                            unsigned long long * counter, int chunk, int budget, HardQueue hq) {
-  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+batch_closest_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned long long * counter, int chunk, int budget,
+                     HardQueue hq) {
+  F64WarpBuf * buf = nullptr;
+  if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
+    __shared__ F64WarpBuf s_buf[BATCH_THREADS / 32];
+    buf = &s_buf[threadIdx.x >> 5];
+  }
+  int lane = threadIdx.x & 31;
   int64_t base;
   while (next_chunk(counter, chunk, nq, base)) {
     int64_t end = base + chunk < nq ? base + chunk : nq;
-    for (int64_t q = base + (threadIdx.x & 31); q < end; q += 32) {
-      int m = mesh_of_query(qoff, f.M, q);
-      int root = __ldg(f.seg_root + m);
-      int64_t ebase = __ldg(f.seg_start + m);
-      V3 p = load_v3(queries + 3 * q);
-      ClosestOut r;
-      float dist;
-      if (PREC == THEA_PRECISION_FP64_RECHECK) {
-        float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-        r = closest_query_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, bound2, scale, f.err, budget);
-        dist = (float)sqrt(r.d2_64);
-      } else {
-        r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, thresh, f.err, budget);
-        dist = sqrtf(r.d2);
-      }
-      if (!r.done) {
-        unsigned long long pos = atomicAdd(hq.count, 1ull);
-        hq.q[pos] = q;
-        hq.bound[pos] = r.best32;
-        hq.idx[pos] = PREC == THEA_PRECISION_FP64_RECHECK ? INT_MAX : r.idx;
-        hq.slot[pos] = r.slot;
-        continue;
-      }
-      write_closest<PREC>(f.cp_rec, q, p, r.idx != INT_MAX, dist, r.cp, r.idx, r.slot, r.d2_64, out_index, out_dist,
-                          out_cp, out_err);
-    }
+    for (int64_t r0 = base; r0 < end; r0 += 32)
+      closest_round<W, STACK, PREC>(f, a, r0 + lane, r0 + lane < end, budget, hq, buf);
   }
 }
 
@@ -168,10 +156,7 @@ constexpr int PHASE2_WARPS = BATCH_THREADS / 32;
 
 template <int W, int PREC>
 __global__ void __launch_bounds__(BATCH_THREADS)
-batch_closest_phase2_kernel(BatchForest f, float const * __restrict__ queries, int64_t const * __restrict__ qoff,
-                            float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
-                            float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
-                            HardQueue hq, unsigned long long * counter) {
+batch_closest_phase2_kernel(BatchForest f, ClosestArgs a, HardQueue hq, unsigned long long * counter) {
   __shared__ int s_code[PHASE2_WARPS][WARP_STACK];
   __shared__ float s_lb[PHASE2_WARPS][WARP_STACK];
   __shared__ float s_cd[PHASE2_WARPS][PREC == THEA_PRECISION_FP64_RECHECK ? WARP_CAND : 1];
@@ -185,13 +170,13 @@ batch_closest_phase2_kernel(BatchForest f, float const * __restrict__ queries, i
     j = __shfl_sync(0xffffffffu, j, 0);
     if (j >= total) break;
     int64_t q = hq.q[j];
-    int m = mesh_of_query(qoff, f.M, q);
+    int m = mesh_of_query(a.qoff, f.M, q);
     int root = __ldg(f.seg_root + m);
     int64_t ebase = __ldg(f.seg_start + m);
-    V3 p = load_v3(queries + 3 * q);
+    V3 p = load_v3(a.queries + 3 * q);
     if (PREC == THEA_PRECISION_FP64_RECHECK) {
-      float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-      WarpBest64 b = closest_warp_query_f64<W>(nodes, f.cp_rec, root, ebase, p, bound2, scale, hq.bound[j],
+      float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+      WarpBest64 b = closest_warp_query_f64<W>(nodes, f.cp_rec, root, ebase, p, a.bound2, scale, hq.bound[j],
                                                s_code[warp], s_lb[warp], s_cd[warp], s_ck[warp], f.err);
       if (lane == 0) {
         bool found = b.idx != INT_MAX;
@@ -202,21 +187,26 @@ batch_closest_phase2_kernel(BatchForest f, float const * __restrict__ queries, i
           cp_record_f64(f.cp_rec, b.slot, p, cp64, d64);
           cp = V3{(float)cp64.x, (float)cp64.y, (float)cp64.z};
         }
-        write_closest<PREC>(f.cp_rec, q, p, found, (float)sqrt(b.d2), cp, b.idx, b.slot, b.d2, out_index, out_dist,
-                            out_cp, out_err);
+        write_closest(q, found, (float)sqrt(b.d2), cp, b.idx, b.d2, a.out_index, a.out_dist, a.out_cp, a.out_err);
       }
     } else {
       WarpBest init;
       init.idx = hq.idx[j];
-      init.d2 = init.idx != INT_MAX ? hq.bound[j] : thresh;
+      init.d2 = init.idx != INT_MAX ? hq.bound[j] : a.thresh;
       init.slot = hq.slot[j];
       WarpBest b = closest_warp_query<W>(nodes, f.cp_rec, root, ebase, p, init, s_code[warp], s_lb[warp], f.err);
       if (lane == 0) {
         bool found = b.idx != INT_MAX;
         V3 cp = V3{0.f, 0.f, 0.f};
-        if (found) cp_record_test(f.cp_rec, b.slot, p, cp);
-        write_closest<PREC>(f.cp_rec, q, p, found, sqrtf(b.d2), cp, b.idx, b.slot, 0.0, out_index, out_dist, out_cp,
-                            out_err);
+        double d64 = 0.0;
+        if (found) {
+          cp_record_test(f.cp_rec, b.slot, p, cp);
+          if (a.out_err) {
+            D3 cp64;
+            cp_record_f64(f.cp_rec, b.slot, p, cp64, d64);
+          }
+        }
+        write_closest(q, found, sqrtf(b.d2), cp, b.idx, d64, a.out_index, a.out_dist, a.out_cp, a.out_err);
       }
     }
     __syncwarp();
@@ -281,43 +271,29 @@ int persistent_grid(void const * kernel) {
   return std::max(1, per_sm) * sms;
 }
 
-template <int W, int STACK>
-void launch_batch_closest(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq,
-                          ClosestParams const & cp, int32_t * idx, float * dist, float * cpt, float * err,
-                          unsigned long long * counter, int chunk, cudaStream_t s) {
-  if (cp.precision == THEA_PRECISION_FP64_RECHECK) {
-    auto k = batch_closest_kernel<W, STACK, THEA_PRECISION_FP64_RECHECK>;
-    THEA_LAUNCH_NAMED("batch_closest_kernel_fp64", k, persistent_grid((void const *)k), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
-                cp.scene_scale, idx, dist, cpt, err, counter, chunk);
-  } else {
-    auto k = batch_closest_kernel<W, STACK, THEA_PRECISION_FP32_REFERENCE>;
-    THEA_LAUNCH_NAMED("batch_closest_kernel_fp32", k, persistent_grid((void const *)k), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
-                cp.scene_scale, idx, dist, cpt, err, counter, chunk);
-  }
-}
-
 template <int W, int STACK, int PREC>
-void launch_two_phase(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq, ClosestParams const & cp,
-                      int32_t * idx, float * dist, float * cpt, float * err, unsigned long long * counters, int chunk,
-                      HardQueue hq, cudaStream_t s) {
-  auto k1 = batch_closest_phase1_kernel<W, STACK, PREC>;
-  THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, q, qoff, nq, cp.thresh, cp.bound2,
-              cp.scene_scale, idx, dist, cpt, err, counters, chunk, cp.budget, hq);
+void launch_closest_prec(BatchForest const & f, ClosestArgs const & a, int64_t nq, int budget,
+                         unsigned long long * counters, int chunk, HardQueue const & hq, cudaStream_t s) {
+  auto k1 = batch_closest_kernel<W, STACK, PREC>;
+  if (budget <= 0) {
+    THEA_LAUNCH_NAMED(PREC == THEA_PRECISION_FP64_RECHECK ? "batch_closest_kernel_fp64" : "batch_closest_kernel_fp32",
+                      k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a, nq, counters, chunk, 0, hq);
+    return;
+  }
+  THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a, nq,
+                    counters, chunk, budget, hq);
   auto k2 = batch_closest_phase2_kernel<W, PREC>;
-  THEA_LAUNCH_NAMED("batch_closest_phase2_kernel", k2, persistent_grid((void const *)k2), BATCH_THREADS, 0, s, f, q, qoff, cp.thresh, cp.bound2,
-              cp.scene_scale, idx, dist, cpt, err, hq, counters + 1);
+  THEA_LAUNCH_NAMED("batch_closest_phase2_kernel", k2, persistent_grid((void const *)k2), BATCH_THREADS, 0, s, f, a, hq,
+                    counters + 1);
 }
 
 template <int W, int STACK>
-void launch_batch_two_phase(BatchForest const & f, float const * q, int64_t const * qoff, int64_t nq,
-                            ClosestParams const & cp, int32_t * idx, float * dist, float * cpt, float * err,
-                            unsigned long long * counters, int chunk, HardQueue hq, cudaStream_t s) {
-  if (cp.precision == THEA_PRECISION_FP64_RECHECK)
-    launch_two_phase<W, STACK, THEA_PRECISION_FP64_RECHECK>(f, q, qoff, nq, cp, idx, dist, cpt, err, counters, chunk,
-                                                            hq, s);
+void launch_batch_closest(BatchForest const & f, ClosestArgs const & a, int64_t nq, int prec, int budget,
+                          unsigned long long * counters, int chunk, HardQueue const & hq, cudaStream_t s) {
+  if (prec == THEA_PRECISION_FP64_RECHECK)
+    launch_closest_prec<W, STACK, THEA_PRECISION_FP64_RECHECK>(f, a, nq, budget, counters, chunk, hq, s);
   else
-    launch_two_phase<W, STACK, THEA_PRECISION_FP32_REFERENCE>(f, q, qoff, nq, cp, idx, dist, cpt, err, counters,
-                                                              chunk, hq, s);
+    launch_closest_prec<W, STACK, THEA_PRECISION_FP32_REFERENCE>(f, a, nq, budget, counters, chunk, hq, s);
 }
 
 template <int W, int STACK>
@@ -368,26 +344,19 @@ void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff
   if (nq <= 0) return;
   BatchForest f = forest_view(b);
   bool sm = small_stack_ok(b);
-  if (cp.budget > 0) {
-    Scratch counters(3 * sizeof(unsigned long long), s);
-    THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));
-    Scratch hq_q((size_t)nq * sizeof(int64_t), s), hq_b((size_t)nq * sizeof(float), s);
-    Scratch hq_i((size_t)nq * sizeof(int32_t), s), hq_s((size_t)nq * sizeof(int64_t), s);
-    auto * c = counters.as<unsigned long long>();
-    HardQueue hq{hq_q.as<int64_t>(), hq_b.as<float>(), hq_i.as<int32_t>(), hq_s.as<int64_t>(), c + 2};
-    if (b->width == 4) sm ? launch_batch_two_phase<4, 64>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s)
-                          : launch_batch_two_phase<4, 256>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s);
-    else sm ? launch_batch_two_phase<8, 128>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s)
-            : launch_batch_two_phase<8, 512>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, hq, s);
-    return;
-  }
-  Scratch counter(sizeof(unsigned long long), s);
-  THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
-  auto * c = counter.as<unsigned long long>();
-  if (b->width == 4) sm ? launch_batch_closest<4, 64>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s)
-                        : launch_batch_closest<4, 256>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s);
-  else sm ? launch_batch_closest<8, 128>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s)
-          : launch_batch_closest<8, 512>(f, q, qoff, nq, cp, idx, dist, cpt, err, c, chunk, s);
+  ClosestArgs a{q, qoff, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, err};
+  int budget = cp.budget > 0 ? cp.budget : 0;
+  Scratch counters(3 * sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));
+  auto * c = counters.as<unsigned long long>();
+  size_t hq_n = budget > 0 ? (size_t)nq : 0;
+  Scratch hq_q(hq_n * sizeof(int64_t), s), hq_b(hq_n * sizeof(float), s);
+  Scratch hq_i(hq_n * sizeof(int32_t), s), hq_s(hq_n * sizeof(int64_t), s);
+  HardQueue hq{hq_q.as<int64_t>(), hq_b.as<float>(), hq_i.as<int32_t>(), hq_s.as<int64_t>(), c + 2};
+  if (b->width == 4) sm ? launch_batch_closest<4, 64>(f, a, nq, cp.precision, budget, c, chunk, hq, s)
+                        : launch_batch_closest<4, 256>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
+  else sm ? launch_batch_closest<8, 128>(f, a, nq, cp.precision, budget, c, chunk, hq, s)
+          : launch_batch_closest<8, 512>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
 }
 
 void run_batch_ray(thea_bvh const * b, float const * o, float const * d, int64_t const * qoff, int64_t nq,

@@ -21,21 +21,41 @@ closest_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict
                int64_t n, float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
                float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
                unsigned * __restrict__ err, uint32_t const * __restrict__ order) {
+  // no early exit: the FP64 step and the error estimate run with the warp's lanes together
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  if (order) q = order[q];
-  V3 p = load_v3(queries + 3 * q);
+  bool active = q < n;
+  if (active && order) q = order[q];
+  V3 p = active ? load_v3(queries + 3 * q) : V3{0.f, 0.f, 0.f};
   ClosestOut r;
-  float dist;
-  if (PREC == THEA_PRECISION_FP64_RECHECK) {
+  r.idx = INT_MAX;
+  r.d2 = 0.f;
+  r.d2_64 = 0.0;
+  r.slot = -1;
+  float dist = 0.f;
+  if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
+    __shared__ F64WarpBuf buf[QUERY_THREADS / 32];
     float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-    r = closest_query_f64<W, STACK>(nodes, rec, 0, 0, p, bound2, scale, err);
+    F64Search s;
+    if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, bound2, scale, err, s);
+    else f64_search_init(s);
+    f64_resolve_warp(s, active, rec, 0, p, bound2, buf[threadIdx.x >> 5]);
+    r = f64_result(s);
     dist = (float)sqrt(r.d2_64);
   } else {
-    r = closest_query<W, STACK>(nodes, rec, 0, 0, p, thresh, err);
+    if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, thresh, err);
     dist = sqrtf(r.d2);
   }
   bool found = r.idx != INT_MAX;
+  double d64 = r.d2_64;
+  if (PREC != THEA_PRECISION_FP64_RECHECK && out_err) {
+    // FP64 distance of the returned element, evaluated with the warp's lanes together
+    __syncwarp();
+    if (active && found) {
+      D3 cp64;
+      cp_record_f64(rec, r.slot, p, cp64, d64);
+    }
+  }
+  if (!active) return;
   out_index[q] = found ? r.idx : -1;
   if (out_dist) out_dist[q] = found ? dist : -1.f;
   if (out_cp) {
@@ -43,19 +63,8 @@ closest_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict
     out_cp[3 * q + 1] = found ? r.cp.y : 0.f;
     out_cp[3 * q + 2] = found ? r.cp.z : 0.f;
   }
-  if (out_err) {
-    // |returned distance - FP64 distance of the returned element|
-    float e = -1.f;
-    if (found) {
-      double d64 = r.d2_64;
-      if (PREC != THEA_PRECISION_FP64_RECHECK) {
-        D3 cp64;
-        cp_record_f64(rec, r.slot, p, cp64, d64);
-      }
-      e = (float)fabs((double)dist - sqrt(d64));
-    }
-    out_err[q] = e;
-  }
+  // |returned distance - FP64 distance of the returned element|
+  if (out_err) out_err[q] = found ? (float)fabs((double)dist - sqrt(d64)) : -1.f;
 }
 
 //============================================================================================================================

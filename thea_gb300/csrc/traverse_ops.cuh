@@ -262,51 +262,78 @@ __device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restri
   return o;
 }
 
-// Mixed-precision search: FP32 traversal and element tests; every element whose FP32 distance lies within a band of
-// the current FP32 best is re-evaluated in FP64, and the result is the FP64 minimum (ties: lowest index) with its FP64
-// distance and closest point. The band is relative 2^-14 of the distance plus 2^-18 of the coordinate scale `scale`
-// (the largest coordinate magnitude of the query and the mesh): FP32 closest-point arithmetic is accurate to about
-// 8 ulps of that scale, so the element that is nearest in FP64 always falls inside the band of the FP32 best.
-// Candidates are collected during the traversal and evaluated together at the end, when the band is final; an entry
-// pushed out of the full list while still inside the band is evaluated then. Accepts elements with FP64 d2 < bound2
+// Mixed-precision search, in two steps. closest_search_f64 runs the FP32 traversal and element tests of one query and
+// collects every element whose FP32 distance lies within a band of the FP32 best; f64_resolve_warp then evaluates the
+// collected elements of all 32 lanes of a warp in FP64 together and picks, per query, the FP64 minimum (ties: lowest
+// index) with its FP64 distance and closest point. FP64 arithmetic is a narrow pipe on this GPU and a warp instruction
+// costs the same whether one lane or 32 take part, so the evaluations are gathered into full-warp rounds instead of
+// running inside each lane's divergent traversal.
+//
+// The band is relative 2^-14 of the distance plus 2^-18 of the coordinate scale `scale` (the largest coordinate
+// magnitude of the query and the mesh): FP32 closest-point arithmetic is accurate to about 8 ulps of that scale, so the
+// element that is nearest in FP64 always falls inside the band of the FP32 best. A relative band alone would not do:
+// near the surface the FP32 error is absolute, not relative to the distance. Accepts elements with FP64 d2 < bound2
 // (bound2 < 0: unbounded).
+constexpr int F64_CAND = 8;  // band entries a lane keeps for the warp-wide FP64 step
+
+struct F64Search {
+  float cand_d[F64_CAND];  // FP32 squared distances of the kept entries (+inf: empty slot)
+  int cand_k[F64_CAND];    // their sorted positions relative to the segment start (-1: empty slot)
+  float lim;               // final band limit on FP32 squared distances
+  float best32;            // smallest FP32 squared distance of an accepted element (+inf if none)
+  // best of the entries already evaluated in FP64 by the lane itself (entries pushed out of a full list)
+  double best64;
+  int best_idx;
+  int64_t best_slot;
+  float cpx, cpy, cpz;
+  bool done;               // false when the pop budget ran out before the traversal finished
+};
+
+__device__ __forceinline__ void f64_search_init(F64Search & s) {
+#pragma unroll
+  for (int j = 0; j < F64_CAND; ++j) {
+    s.cand_d[j] = INFINITY;
+    s.cand_k[j] = -1;
+  }
+  s.lim = INFINITY;
+  s.best32 = INFINITY;
+  s.best64 = INFINITY;
+  s.best_idx = INT_MAX;
+  s.best_slot = -1;
+  s.cpx = s.cpy = s.cpz = 0.f;
+  s.done = true;
+}
+
+// Folds one FP64 evaluation into the lane's best (FP64 squared distance d64, closest point cp, sorted position k)
+__device__ __forceinline__ void f64_take(F64Search & s, float4 const * __restrict__ rec, int64_t k, double d64, float cx,
+                                         float cy, float cz, double bound2) {
+  if (bound2 >= 0.0 && !(d64 < bound2)) return;
+  int idx = cp_record_index(rec, k);
+  if (d64 < s.best64 || (d64 == s.best64 && idx < s.best_idx)) {
+    s.best64 = d64;
+    s.best_idx = idx;
+    s.best_slot = k;
+    s.cpx = cx;
+    s.cpy = cy;
+    s.cpz = cz;
+  }
+}
+
 template <int W, int STACK>
-__device__ __forceinline__ ClosestOut closest_query_f64(WideNode<W> const * __restrict__ nodes,
-                                                        float4 const * __restrict__ rec, int root, int64_t elem_base,
-                                                        V3 p, double bound2, float scale, unsigned * err,
-                                                        int budget = 0) {
-  bool done = true;
+__device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restrict__ nodes,
+                                                   float4 const * __restrict__ rec, int root, int64_t elem_base, V3 p,
+                                                   double bound2, float scale, unsigned * err, F64Search & s,
+                                                   int budget = 0) {
+  f64_search_init(s);
   int pops = 0;
   float const REL = 1.0f + 1.0f / 16384.0f;
   float abs_tol = scale * (1.0f / 262144.0f);
-  float best32 = INFINITY;  // smallest FP32 squared distance seen among accepted elements
-  float lim = bound2 >= 0.0 ? __double2float_ru(bound2) : INFINITY;  // band limit on FP32 squared distances
+  float lim = bound2 >= 0.0 ? __double2float_ru(bound2) : INFINITY;
   if (bound2 >= 0.0) {
     float lb0 = sqrtf(lim) * REL + abs_tol;
     lim = lb0 * lb0;
   }
-  double best64 = INFINITY;
-  int best_idx = INT_MAX;
-  int64_t best_slot = -1;
-  D3 best_cp = D3{0.0, 0.0, 0.0};
-  constexpr int NCAND = 8;
-  float cand_d[NCAND];
-  int64_t cand_k[NCAND];
-#pragma unroll
-  for (int j = 0; j < NCAND; ++j) { cand_d[j] = INFINITY; cand_k[j] = -1; }
-  int64_t pending = -1;  // an entry pushed out of the full list while inside the band
-  auto eval64 = [&](int64_t k) {
-    D3 cp64;
-    double d64 = cp_record_f64_call(rec, k, p, &cp64);
-    if (bound2 >= 0.0 && !(d64 < bound2)) return;
-    int idx = cp_record_index(rec, k);
-    if (d64 < best64 || (d64 == best64 && idx < best_idx)) {
-      best64 = d64;
-      best_idx = idx;
-      best_cp = cp64;
-      best_slot = k;
-    }
-  };
+  float best32 = INFINITY;
   int stk[STACK];
   float stkd[STACK];
   int sp = 0;
@@ -315,7 +342,7 @@ __device__ __forceinline__ ClosestOut closest_query_f64(WideNode<W> const * __re
   ++sp;
   while (sp > 0) {
     if (budget > 0 && ++pops > budget) {
-      done = false;
+      s.done = false;
       break;
     }
     --sp;
@@ -330,62 +357,115 @@ __device__ __forceinline__ ClosestOut closest_query_f64(WideNode<W> const * __re
     } else {
       int first, count;
       decode_leaf(code, first, count);
-      int64_t k0 = elem_base + first;
-      for (int64_t k = k0; k < k0 + count; ++k) {
+      for (int kr = first; kr < first + count; ++kr) {
         V3 cp;
-        float d2 = cp_record_test(rec, k, p, cp);
+        float d2 = cp_record_test(rec, elem_base + kr, p, cp);
         if (!(d2 <= lim)) continue;
         if (d2 < best32) {
           best32 = d2;
           float lb1 = sqrtf(best32) * REL + abs_tol;
           lim = fminf(lim, lb1 * lb1);
         }
-        // the candidate takes a slot that has left the band, else the farthest slot if that is farther than it
+        // the entry takes a slot that has left the band, else the farthest slot if that is farther than it
         int slot_j = -1;
         float worst = d2;
 #pragma unroll
-        for (int j = 0; j < NCAND; ++j)
-          if (slot_j < 0 && !(cand_d[j] <= lim)) slot_j = j;  // empty slots hold +inf
+        for (int j = 0; j < F64_CAND; ++j)
+          if (slot_j < 0 && !(s.cand_k[j] >= 0 && s.cand_d[j] <= lim)) slot_j = j;
         if (slot_j < 0) {
 #pragma unroll
-          for (int j = 0; j < NCAND; ++j)
-            if (cand_d[j] > worst) { worst = cand_d[j]; slot_j = j; }
+          for (int j = 0; j < F64_CAND; ++j)
+            if (s.cand_d[j] > worst) { worst = s.cand_d[j]; slot_j = j; }
         }
-        int64_t evict = slot_j < 0 ? k : -1;
+        int evict = slot_j < 0 ? kr : -1;
 #pragma unroll
-        for (int j = 0; j < NCAND; ++j) {
+        for (int j = 0; j < F64_CAND; ++j) {
           if (j == slot_j) {
-            if (cand_d[j] <= lim) evict = cand_k[j];
-            cand_d[j] = d2;
-            cand_k[j] = k;
+            if (s.cand_k[j] >= 0 && s.cand_d[j] <= lim) evict = s.cand_k[j];
+            s.cand_d[j] = d2;
+            s.cand_k[j] = kr;
           }
         }
         if (evict >= 0) {
-          if (pending >= 0) eval64(pending);
-          pending = evict;
+          // more band entries than slots (rare): this one is evaluated by the lane alone
+          D3 c64;
+          double d64 = cp_record_f64_call(rec, elem_base + evict, p, &c64);
+          f64_take(s, rec, elem_base + evict, d64, (float)c64.x, (float)c64.y, (float)c64.z, bound2);
         }
       }
     }
   }
-  // evaluate the candidates still inside the final band, one slot at a time with the warp's lanes together
-  if (pending >= 0) eval64(pending);
-#pragma unroll 1
-  for (int j = 0; j < NCAND; ++j) {
-    float dj = 0.f;
-    int64_t kj = -1;
+  s.lim = lim;
+  s.best32 = best32;
+}
+
+// Shared-memory work list of one warp for f64_resolve_warp
+struct F64WarpBuf {
+  int64_t k[32 * F64_CAND];
+  double d[32 * F64_CAND];
+  float cp[32 * F64_CAND][3];
+  float p[32][3];
+  unsigned char owner[32 * F64_CAND];
+};
+
+// Evaluates in FP64 the band entries of every lane of the warp, in full-warp rounds, and folds each lane's results
+// into its own F64Search. All 32 lanes call it together; `active` is false for a lane without a query (or with a
+// query that is not finished), whose entries are ignored.
+__device__ __forceinline__ void f64_resolve_warp(F64Search & s, bool active, float4 const * __restrict__ rec,
+                                                 int64_t elem_base, V3 p, double bound2, F64WarpBuf & b) {
+  unsigned const FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  bool keep[F64_CAND];
+  int c = 0;
 #pragma unroll
-    for (int t = 0; t < NCAND; ++t)
-      if (t == j) { dj = cand_d[t]; kj = cand_k[t]; }
-    if (dj <= lim) eval64(kj);
+  for (int j = 0; j < F64_CAND; ++j) {
+    keep[j] = active && s.cand_k[j] >= 0 && s.cand_d[j] <= s.lim;
+    c += keep[j] ? 1 : 0;
   }
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  int total = __shfl_sync(FULL, incl, 31);
+  int off = incl - c;
+  b.p[lane][0] = p.x;
+  b.p[lane][1] = p.y;
+  b.p[lane][2] = p.z;
+  int w = off;
+#pragma unroll
+  for (int j = 0; j < F64_CAND; ++j) {
+    if (keep[j]) {
+      b.k[w] = elem_base + s.cand_k[j];
+      b.owner[w] = (unsigned char)lane;
+      ++w;
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < total; i += 32) {
+    int o = b.owner[i];
+    V3 q = V3{b.p[o][0], b.p[o][1], b.p[o][2]};
+    D3 c64;
+    b.d[i] = cp_record_f64_call(rec, b.k[i], q, &c64);
+    b.cp[i][0] = (float)c64.x;
+    b.cp[i][1] = (float)c64.y;
+    b.cp[i][2] = (float)c64.z;
+  }
+  __syncwarp();
+  for (int i = off; i < off + c; ++i) f64_take(s, rec, b.k[i], b.d[i], b.cp[i][0], b.cp[i][1], b.cp[i][2], bound2);
+  __syncwarp();
+}
+
+__device__ __forceinline__ ClosestOut f64_result(F64Search const & s) {
   ClosestOut o;
-  o.idx = best_idx;
-  o.d2_64 = best64;
-  o.d2 = (float)best64;
-  o.cp = V3{(float)best_cp.x, (float)best_cp.y, (float)best_cp.z};
-  o.slot = best_slot;
-  o.best32 = best32;
-  o.done = done;
+  o.idx = s.best_idx;
+  o.d2_64 = s.best64;
+  o.d2 = (float)s.best64;
+  o.cp = V3{s.cpx, s.cpy, s.cpz};
+  o.slot = s.best_slot;
+  o.best32 = s.best32;
+  o.done = s.done;
   return o;
 }
 
