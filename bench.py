@@ -389,7 +389,99 @@ def extra_workloads(T, torch, stream, flush, args):
     pb.close()
     T.profiling_reset()
     out["batched_closest_cfg3"] = batched_config3(T, torch, stream, flush, args)
+    out["serving_cfg4"] = serving_config4(T, torch, args)
     return out
+
+
+def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, seed=W.CONFIG_SEEDS[4]):
+    """Config 4: a server with 256 resident meshes drawn as in config 3 and an 8 GB admission budget. Requests arrive
+    Poisson at 2,000/s for `seconds`: 60% closest point, 25% first ray hit, 15% k-NN (k = 8) over the mesh's vertices,
+    each with a log-uniform 1..1,048,576 queries uniform in its mesh's box grown by 50% (rays: origins there, uniform
+    directions). Query and result arrays are pinned host memory; latency runs from submit to results written back."""
+    res = {}
+    V, F, foff, _, _, levels = W.config3_torch(num_meshes, seed=seed, min_q=1, max_q=2)
+    srv = T.Server(memory_budget_bytes=8 << 30)
+    t0 = time.perf_counter()
+    ids, boxes = [], []
+    for m in range(num_meshes):
+        Fm = F[foff[m]:foff[m + 1]]
+        lo, hi = int(Fm.min()), int(Fm.max()) + 1
+        Vm = V[lo:hi]
+        ids.append(srv.add_mesh(Vm, Fm - lo))
+        boxes.append((Vm.min(0).values.cpu().numpy(), Vm.max(0).values.cpu().numpy()))
+    st = srv.stats()
+    res["meshes"] = num_meshes
+    res["resident_bytes"] = st["resident_bytes"]
+    res["build_s"] = time.perf_counter() - t0
+    del V, F
+    # the request stream
+    rng = np.random.default_rng(seed)
+    n_req = int(rate * seconds)
+    arrive = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    kind = rng.choice(3, size=n_req, p=[0.60, 0.25, 0.15])
+    mesh = rng.integers(0, num_meshes, n_req)
+    nq = np.exp(rng.uniform(0.0, np.log(1 << 20), n_req)).astype(np.int64).clip(1, 1 << 20)
+    # per mesh, one pinned array of points uniform in its grown box, as long as its largest request; shared directions
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    pts = {}
+    for m in np.unique(mesh):
+        n = int(nq[mesh == m].max())
+        lo, hi = boxes[m]
+        c, e = 0.5 * (lo + hi), 1.5 * (hi - lo)
+        u = torch.rand((n, 3), generator=g, device="cuda")
+        pts[m] = (u * torch.as_tensor(e, device="cuda") + torch.as_tensor(c - 0.5 * e, device="cuda")).cpu().pin_memory()
+    dirs = torch.nn.functional.normalize(torch.randn((1 << 20, 3), generator=g, device="cuda"), dim=1).cpu().pin_memory()
+    # results: a pinned ring far larger than what can be in flight
+    ring_idx = torch.empty(64 << 20, dtype=torch.int32).pin_memory()
+    ring_val = torch.empty(64 << 20, dtype=torch.float32).pin_memory()
+    pos = [0]
+
+    def outputs(rows):
+        if pos[0] + rows > ring_idx.numel():
+            pos[0] = 0
+        a, b = ring_idx[pos[0]:pos[0] + rows], ring_val[pos[0]:pos[0] + rows]
+        pos[0] += rows
+        return a, b
+
+    names = ("closest", "ray", "knn")
+    tickets = [None] * n_req
+    srv.reset_stats()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        start = time.perf_counter()
+        for r in range(n_req):
+            now = time.perf_counter() - start
+            if arrive[r] > now:
+                time.sleep(arrive[r] - now)
+            n, m, kd = int(nq[r]), int(mesh[r]), names[kind[r]]
+            k = 8 if kd == "knn" else 1
+            oi, ov = outputs(n * k)
+            q = pts[m][:n]
+            d = dirs[:n] if kd == "ray" else None
+            tickets[r] = srv.submit(kd, ids[m], q, directions=d, k=k, out=(oi, ov))
+        submit_s = time.perf_counter() - start
+        lat = np.zeros(n_req)
+        for r, t in enumerate(tickets):
+            t.wait()
+            lat[r] = t.latency_ms
+            assert t.status == 0
+        total_s = time.perf_counter() - start
+    st = srv.stats()
+    srv.close()
+    small = nq <= 65536
+    res.update({
+        "requests": n_req, "offered_rate_per_s": n_req / arrive[-1], "submit_span_s": submit_s, "drain_s": total_s,
+        "queries": int(nq.sum()), "mix": {"closest": int((kind == 0).sum()), "ray": int((kind == 1).sum()),
+                                           "knn": int((kind == 2).sum())},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+        "small_requests": int(small.sum()), "small_p50_ms": float(np.percentile(lat[small], 50)),
+        "small_p99_ms": float(np.percentile(lat[small], 99)),
+        "sustained_queries_per_s": float(nq.sum() / total_s), "server_queries_per_s": st["queries_per_second"],
+        "batches": st["batches"], "clocks": clk.summary(),
+        "io": "pinned host arrays, staged by the server", "precision": "fp32 reference arithmetic",
+    })
+    return res
 
 
 def batched_config3(T, torch, stream, flush, args, num_meshes=4096):

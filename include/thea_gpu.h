@@ -47,7 +47,8 @@ typedef enum thea_status {
   THEA_ERR_CUDA = 5,               /* a CUDA runtime call failed */
   THEA_ERR_INTERNAL = 6,
   THEA_ERR_NOT_SUPPORTED = 7,
-  THEA_ERR_CANCELLED = 8           /* serving: request was cancelled before it ran */
+  THEA_ERR_CANCELLED = 8,          /* serving: request was cancelled before it ran */
+  THEA_ERR_WAIT_TIMEOUT = 9        /* serving: a host-side wait ended before the request finished */
 } thea_status;
 
 typedef struct thea_bvh thea_bvh; /* opaque, immutable after build; owns device copies of the elements and nodes */
@@ -286,6 +287,107 @@ THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t
                                                  int64_t num_faces, int64_t num_samples, uint32_t seed, int32_t rng,
                                                  float * out_positions, float * out_normals, int32_t * out_faces,
                                                  int64_t * out_num_written, void * stream);
+
+/* ---- serving ------------------------------------------------------------------------------------------------------- */
+
+/* A request loop over meshes kept resident in device memory. The reference has no serving layer (its queries are
+ * synchronous C++ calls on a BvhN); these entry points are new. Each request is one of the three query kinds against one
+ * resident mesh, with the same per-query results as the single-BVH calls (thea_closest_element, thea_ray_intersection,
+ * thea_k_closest over the mesh's vertices): bit-identical, whatever else is in flight.
+ *
+ * Continuous batching: a dispatcher thread cuts requests into pieces of at most max_piece_queries queries and packs
+ * pending pieces (smallest remaining request first; a request pending longer than max_wait_ms goes first) into batches
+ * of at most max_batch_queries queries, one persistent launch per query kind. Up to `slots` batches are in flight at
+ * once, each on its own stream, so requests that arrive while others run are admitted as soon as a slot and memory
+ * free up, and their copies and kernels overlap with the batches already on the device.
+ *
+ * Admission: resident BVHs (mesh BVH with both layouts plus a point BVH over the mesh's vertices) and the device staging
+ * buffers of in-flight pieces count against memory_budget_bytes. A mesh that does not fit is refused at
+ * thea_server_add_mesh, a request whose smallest piece can never fit is refused at submit (both
+ * THEA_ERR_ADMISSION_REFUSED), and other requests wait until earlier pieces finish. Request arrays may be host memory
+ * (staged through device buffers; pinned memory makes the copies asynchronous) or device memory (used in place, no
+ * staging bytes). They must stay valid, and outputs untouched, until thea_server_wait has returned the request. */
+
+typedef struct thea_server thea_server;
+
+typedef struct thea_server_config {
+  int64_t memory_budget_bytes;   /* resident BVHs + staging of in-flight pieces (0: 8 GiB) */
+  int32_t slots;                 /* batches in flight at once, one stream each (0: 3) */
+  int32_t max_batch_queries;     /* queries per batch (0: 262144) */
+  int32_t max_piece_queries;     /* largest piece of one request (0: 65536) */
+  int32_t precision;             /* closest-element requests: THEA_PRECISION_* */
+  int32_t width;                 /* BVH width of resident meshes, 4 or 8 (0: 4) */
+  int32_t max_leaf_size;         /* leaf size of resident mesh BVHs (0: default) */
+  int32_t small_request_queries; /* requests of at most this many queries get their own latency figures (0: 65536) */
+  int32_t max_wait_ms;           /* pending longer than this: served before smaller requests (0: 20) */
+  int32_t test_executor;         /* 1: test executor for the host-side scheduling logic. No CUDA call at all: meshes are
+                                    not built (their size is estimated), no results are written, and a batch finishes
+                                    test_ns_per_query x its queries after it starts. 0: the GPU. */
+  int32_t test_ns_per_query;
+  int32_t reserved[6];           /* must be zero */
+} thea_server_config;
+
+#define THEA_REQUEST_CLOSEST 0  /* closest element: thea_closest_element */
+#define THEA_REQUEST_RAY 1      /* first ray hit: thea_ray_intersection */
+#define THEA_REQUEST_KNN 2      /* k nearest mesh vertices: thea_k_closest */
+
+typedef struct thea_request {
+  int32_t type;              /* THEA_REQUEST_* */
+  int32_t mesh;              /* id from thea_server_add_mesh */
+  int64_t num_queries;       /* >= 1 */
+  const float * queries;     /* closest and k-NN: query points; ray: origins (3 floats each) */
+  const float * directions;  /* ray only (3 floats each) */
+  float bound;               /* closest: dist_bound; ray: max_time; k-NN: dist_bound (negative: none) */
+  int32_t k;                 /* k-NN: 1..32 */
+  int32_t * out_index;       /* closest and ray: num_queries; k-NN: num_queries x k (-1: none) */
+  float * out_value;         /* closest: distance; ray: hit time; k-NN: squared distance (-1: none); may be NULL */
+  float * out_point;         /* closest only: closest points (3 floats each); may be NULL */
+} thea_request;
+
+typedef struct thea_server_stats {
+  int64_t submitted;
+  int64_t completed;
+  int64_t failed;
+  int64_t cancelled;
+  int64_t refused;           /* requests refused at submit */
+  int64_t queries_completed;
+  int64_t batches;
+  int64_t resident_meshes;
+  int64_t resident_bytes;
+  int64_t inflight_bytes;    /* staging bytes of pieces admitted and not finished */
+  int64_t pending_requests;
+  double p50_ms;             /* latency from submit to results written, completed requests */
+  double p99_ms;
+  double max_ms;
+  double small_p50_ms;       /* the same over requests of at most small_request_queries queries */
+  double small_p99_ms;
+  double busy_seconds;       /* first submit to last completion since the last reset */
+  double queries_per_second; /* queries_completed / busy_seconds */
+} thea_server_stats;
+
+/* Starts the dispatcher thread on the current device. */
+THEA_API thea_status thea_server_create(const thea_server_config * config, thea_server ** out_server);
+/* Pending requests end THEA_ERR_CANCELLED; batches on the device are waited for; all memory is released. */
+THEA_API thea_status thea_server_destroy(thea_server * server);
+/* Builds and keeps resident the BVHs of one mesh (vertices and faces as for thea_mesh_bvh_build, host or device).
+ * Synchronous. THEA_ERR_ADMISSION_REFUSED if it does not fit the budget. */
+THEA_API thea_status thea_server_add_mesh(thea_server * server, const float * vertices, int64_t num_vertices,
+                                          const int32_t * faces, int64_t num_faces, int32_t * out_mesh);
+/* The mesh takes no new requests; its memory is released when the requests already submitted for it have finished. */
+THEA_API thea_status thea_server_remove_mesh(thea_server * server, int32_t mesh);
+/* Queues a request and returns at once with its ticket. */
+THEA_API thea_status thea_server_submit(thea_server * server, const thea_request * request, uint64_t * out_ticket);
+/* Waits up to timeout_us microseconds (negative: no limit) for a request. THEA_OK: the request ended and its ticket is
+ * retired; *out_request_status is its outcome (THEA_OK, THEA_ERR_CANCELLED, THEA_ERR_CUDA, ...) and *out_latency_ms the
+ * time from submit to results written. THEA_ERR_WAIT_TIMEOUT: not finished yet (wait again). Either output may be NULL. */
+THEA_API thea_status thea_server_wait(thea_server * server, uint64_t ticket, int64_t timeout_us,
+                                      thea_status * out_request_status, double * out_latency_ms);
+/* Cancels the pieces of a request that have not started; a request with pieces on the device finishes those and ends
+ * THEA_ERR_CANCELLED with its outputs partly written. */
+THEA_API thea_status thea_server_cancel(thea_server * server, uint64_t ticket);
+THEA_API thea_status thea_server_get_stats(thea_server * server, thea_server_stats * out_stats);
+/* Clears the latency records and counters (not the resident meshes). */
+THEA_API thea_status thea_server_reset_stats(thea_server * server);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -12,7 +12,12 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libthea_gpu.so")
 THEA_OK = 0
 STATUS_NAMES = {0: "THEA_OK", 1: "THEA_ERR_INVALID_ARGUMENT", 2: "THEA_ERR_OUT_OF_MEMORY",
                 3: "THEA_ERR_ADMISSION_REFUSED", 4: "THEA_ERR_DEVICE_TIMEOUT", 5: "THEA_ERR_CUDA",
-                6: "THEA_ERR_INTERNAL", 7: "THEA_ERR_NOT_SUPPORTED", 8: "THEA_ERR_CANCELLED"}
+                6: "THEA_ERR_INTERNAL", 7: "THEA_ERR_NOT_SUPPORTED", 8: "THEA_ERR_CANCELLED",
+                9: "THEA_ERR_WAIT_TIMEOUT"}
+THEA_ERR_INVALID_ARGUMENT = 1
+THEA_ERR_ADMISSION_REFUSED = 3
+THEA_ERR_CANCELLED = 8
+THEA_ERR_WAIT_TIMEOUT = 9
 
 LAYOUT_CLOSEST = 1
 LAYOUT_RAY = 2
@@ -46,6 +51,34 @@ class Tuning(ctypes.Structure):
                 ("milliseconds", ctypes.c_float), ("candidates", ctypes.c_int32),
                 ("hard_query_budget", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_int64), ("slots", ctypes.c_int32),
+                ("max_batch_queries", ctypes.c_int32), ("max_piece_queries", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32),
+                ("small_request_queries", ctypes.c_int32), ("max_wait_ms", ctypes.c_int32),
+                ("test_executor", ctypes.c_int32), ("test_ns_per_query", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("mesh", ctypes.c_int32), ("num_queries", ctypes.c_int64),
+                ("queries", ctypes.c_void_p), ("directions", ctypes.c_void_p), ("bound", ctypes.c_float),
+                ("k", ctypes.c_int32), ("out_index", ctypes.c_void_p), ("out_value", ctypes.c_void_p),
+                ("out_point", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "refused",
+                                              "queries_completed", "batches", "resident_meshes", "resident_bytes",
+                                              "inflight_bytes", "pending_requests")] + \
+               [(n, ctypes.c_double) for n in ("p50_ms", "p99_ms", "max_ms", "small_p50_ms", "small_p99_ms",
+                                               "busy_seconds", "queries_per_second")]
+
+
+REQUEST_CLOSEST = 0
+REQUEST_RAY = 1
+REQUEST_KNN = 2
 
 SIGNATURES = {
     "thea_abi_version": (ctypes.c_int, []),
@@ -83,6 +116,15 @@ SIGNATURES = {
     "thea_graph_destroy": (ctypes.c_int, [_vp]),
     "thea_autotune_batch_closest": (ctypes.c_int, [_vp, _i64, _vp, _i64p, _i32, _vp, _vp, _i64, _i32, _vp,
                                                    ctypes.POINTER(Tuning)]),
+    "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
+    "thea_server_destroy": (ctypes.c_int, [_vp]),
+    "thea_server_add_mesh": (ctypes.c_int, [_vp, _vp, _i64, _vp, _i64, ctypes.POINTER(_i32)]),
+    "thea_server_remove_mesh": (ctypes.c_int, [_vp, _i32]),
+    "thea_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "thea_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, _i64, ctypes.POINTER(ctypes.c_int), _f64p]),
+    "thea_server_cancel": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+    "thea_server_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "thea_server_reset_stats": (ctypes.c_int, [_vp]),
 }
 
 PRECISION_FP32_REFERENCE = 0

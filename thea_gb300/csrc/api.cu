@@ -4,6 +4,7 @@
 #include "device_util.cuh"
 #include "query.hpp"
 #include "batch.hpp"
+#include "serve.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -270,6 +271,7 @@ THEA_API const char * thea_status_string(thea_status s) {
     case THEA_ERR_INTERNAL: return "internal error";
     case THEA_ERR_NOT_SUPPORTED: return "not supported";
     case THEA_ERR_CANCELLED: return "cancelled";
+    case THEA_ERR_WAIT_TIMEOUT: return "wait timed out";
   }
   return "unknown status";
 }
@@ -822,6 +824,81 @@ THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t
     int64_t got = run_sample_by_area_noalloc(vertices, num_vertices, faces, num_faces, num_samples, seed, rng,
                                              out_positions, out_normals, out_faces, (cudaStream_t)stream);
     if (out_num_written) *out_num_written = got;
+  });
+}
+
+//============================================================================================================================
+// Serving loop
+//============================================================================================================================
+
+THEA_API thea_status thea_server_create(const thea_server_config * config, thea_server ** out_server) {
+  return guarded([&] {
+    THEA_REQUIRE(config && out_server, "server_create: null argument");
+    *out_server = nullptr;
+    *out_server = server_create(*config);
+  });
+}
+
+THEA_API thea_status thea_server_destroy(thea_server * server) {
+  return guarded([&] {
+    if (server) server_destroy(server);
+  });
+}
+
+THEA_API thea_status thea_server_add_mesh(thea_server * server, const float * vertices, int64_t num_vertices,
+                                          const int32_t * faces, int64_t num_faces, int32_t * out_mesh) {
+  return guarded([&] {
+    THEA_REQUIRE(server && out_mesh, "server_add_mesh: null argument");
+    *out_mesh = -1;
+    *out_mesh = server_add_mesh(server, vertices, num_vertices, faces, num_faces);
+  });
+}
+
+THEA_API thea_status thea_server_remove_mesh(thea_server * server, int32_t mesh) {
+  return guarded([&] {
+    THEA_REQUIRE(server, "server_remove_mesh: null server");
+    server_remove_mesh(server, mesh);
+  });
+}
+
+THEA_API thea_status thea_server_submit(thea_server * server, const thea_request * request, uint64_t * out_ticket) {
+  return guarded([&] {
+    THEA_REQUIRE(server && request && out_ticket, "server_submit: null argument");
+    *out_ticket = 0;
+    *out_ticket = server_submit(server, *request);
+  });
+}
+
+THEA_API thea_status thea_server_wait(thea_server * server, uint64_t ticket, int64_t timeout_us,
+                                      thea_status * out_request_status, double * out_latency_ms) {
+  thea_status w = THEA_OK;
+  thea_status g = guarded([&] {
+    THEA_REQUIRE(server, "server_wait: null server");
+    w = server_wait(server, ticket, timeout_us, out_request_status, out_latency_ms);
+  });
+  if (g != THEA_OK) return g;
+  if (w == THEA_ERR_WAIT_TIMEOUT) g_error = "server_wait: the request has not finished";
+  return w;
+}
+
+THEA_API thea_status thea_server_cancel(thea_server * server, uint64_t ticket) {
+  return guarded([&] {
+    THEA_REQUIRE(server, "server_cancel: null server");
+    server_cancel(server, ticket);
+  });
+}
+
+THEA_API thea_status thea_server_get_stats(thea_server * server, thea_server_stats * out_stats) {
+  return guarded([&] {
+    THEA_REQUIRE(server && out_stats, "server_get_stats: null argument");
+    server_stats(server, out_stats);
+  });
+}
+
+THEA_API thea_status thea_server_reset_stats(thea_server * server) {
+  return guarded([&] {
+    THEA_REQUIRE(server, "server_reset_stats: null server");
+    server_reset_stats(server);
   });
 }
 

@@ -401,7 +401,7 @@ __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restric
 
 // Shared-memory work list of one warp for f64_resolve_warp
 struct F64WarpBuf {
-  int64_t k[32 * F64_CAND];
+  float4 const * r[32 * F64_CAND];  // record of each entry (lanes may query different meshes)
   double d[32 * F64_CAND];
   float cp[32 * F64_CAND][3];
   float p[32][3];
@@ -410,7 +410,8 @@ struct F64WarpBuf {
 
 // Evaluates in FP64 the band entries of every lane of the warp, in full-warp rounds, and folds each lane's results
 // into its own F64Search. All 32 lanes call it together; `active` is false for a lane without a query (or with a
-// query that is not finished), whose entries are ignored.
+// query that is not finished), whose entries are ignored. `rec` and `elem_base` are the lane's own (lanes of one warp
+// may query different meshes).
 __device__ __forceinline__ void f64_resolve_warp(F64Search & s, bool active, float4 const * __restrict__ rec,
                                                  int64_t elem_base, V3 p, double bound2, F64WarpBuf & b) {
   unsigned const FULL = 0xffffffffu;
@@ -437,7 +438,7 @@ __device__ __forceinline__ void f64_resolve_warp(F64Search & s, bool active, flo
 #pragma unroll
   for (int j = 0; j < F64_CAND; ++j) {
     if (keep[j]) {
-      b.k[w] = elem_base + s.cand_k[j];
+      b.r[w] = rec + (elem_base + s.cand_k[j]) * CP_REC_F4;
       b.owner[w] = (unsigned char)lane;
       ++w;
     }
@@ -447,13 +448,14 @@ __device__ __forceinline__ void f64_resolve_warp(F64Search & s, bool active, flo
     int o = b.owner[i];
     V3 q = V3{b.p[o][0], b.p[o][1], b.p[o][2]};
     D3 c64;
-    b.d[i] = cp_record_f64_call(rec, b.k[i], q, &c64);
+    b.d[i] = cp_record_f64_call(b.r[i], 0, q, &c64);
     b.cp[i][0] = (float)c64.x;
     b.cp[i][1] = (float)c64.y;
     b.cp[i][2] = (float)c64.z;
   }
   __syncwarp();
-  for (int i = off; i < off + c; ++i) f64_take(s, rec, b.k[i], b.d[i], b.cp[i][0], b.cp[i][1], b.cp[i][2], bound2);
+  for (int i = off; i < off + c; ++i)
+    f64_take(s, rec, (b.r[i] - rec) / CP_REC_F4, b.d[i], b.cp[i][0], b.cp[i][1], b.cp[i][2], bound2);
   __syncwarp();
 }
 
