@@ -248,6 +248,26 @@ THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t
                                                  int64_t num_queries, int32_t precision, void * stream,
                                                  thea_tuning * out_tuning);
 
+/* ---- tensor-core k-NN candidates ----------------------------------------------------------------------------------- */
+
+#define THEA_KNN_CANDIDATES_TRAVERSAL 0  /* best-first BVH traversal from an unbounded start (thea_k_closest_self) */
+#define THEA_KNN_CANDIDATES_GRAM 1       /* tensor-core Gram tiles seed the traversal with an exact bound */
+
+/* thea_k_closest_self with a choice of candidate generation; results are identical for both modes. GRAM: the points,
+ * in the BVH's leaf (Morton) order, are scored in tiles of 128 queries x 512 neighbouring candidates by tcgen05 MMAs
+ * (FP16 operands, FP32 accumulation in tensor memory) on keys |b|^2 - 2 a.b; each query's best-scoring candidates are
+ * re-ranked with the reference's FP32 squared distance, and the k-th of those (an upper bound on the k-th neighbour
+ * distance, from actual points) seeds the exact BVH search. Sets with fewer than 512 points use the traversal alone. */
+THEA_API thea_status thea_k_closest_self_ex(const thea_bvh * point_bvh, int32_t k, int32_t candidates,
+                                            int32_t * out_index, float * out_sq_distance, void * stream);
+
+/* The Gram tile alone (device arrays; a: num_a <= 128 points, b: num_b <= 512 points, 3 floats each; out_keys: 128 x 512
+ * floats): out_keys[r * 512 + j] = |b_j|^2 - 2 a_r . b_j with coordinates relative to a[0], divided by the largest
+ * coordinate magnitude of the tile, rounded to FP16, accumulated in FP32 by the tensor cores. Rows r >= num_a and
+ * columns j >= num_b are padding. */
+THEA_API thea_status thea_point_gram_tile(const float * a, int32_t num_a, const float * b, int32_t num_b,
+                                          float * out_keys, void * stream);
+
 /* ---- sampling ------------------------------------------------------------------------------------------------------ */
 
 #define THEA_RNG_THEA_MT 0   /* the reference's Random(seed) stream: bit-identical samples */

@@ -76,6 +76,9 @@ class ServerStats(ctypes.Structure):
                                                "busy_seconds", "queries_per_second")]
 
 
+KNN_CANDIDATES_TRAVERSAL = 0
+KNN_CANDIDATES_GRAM = 1
+
 REQUEST_CLOSEST = 0
 REQUEST_RAY = 1
 REQUEST_KNN = 2
@@ -116,6 +119,8 @@ SIGNATURES = {
     "thea_graph_destroy": (ctypes.c_int, [_vp]),
     "thea_autotune_batch_closest": (ctypes.c_int, [_vp, _i64, _vp, _i64p, _i32, _vp, _vp, _i64, _i32, _vp,
                                                    ctypes.POINTER(Tuning)]),
+    "thea_k_closest_self_ex": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
+    "thea_point_gram_tile": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp]),
     "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "thea_server_destroy": (ctypes.c_int, [_vp]),
     "thea_server_add_mesh": (ctypes.c_int, [_vp, _vp, _i64, _vp, _i64, ctypes.POINTER(_i32)]),

@@ -318,8 +318,9 @@ class PointBvh(_Bvh):
                                        _stream_of(io.device)))
         return idx, d2
 
-    def k_closest_self(self, k, device=False):
-        """k-nearest-neighbour graph of the indexed points, each excluding itself; rows in point order."""
+    def k_closest_self(self, k, device=False, candidates="traversal"):
+        """k-nearest-neighbour graph of the indexed points, each excluding itself; rows in point order.
+        candidates="gram": tensor-core Gram tiles seed the search with an exact bound (same results)."""
         if device:
             import torch
             io = _Arrays(torch.empty(0, device="cuda"))
@@ -327,8 +328,21 @@ class PointBvh(_Bvh):
             io = _Arrays(np.empty(0))
         idx, pidx = io.output((self.n, k), np.int32)
         d2, pd2 = io.output((self.n, k), np.float32)
-        N.check(N.lib().thea_k_closest_self(self._h, int(k), pidx, pd2, _stream_of(io.device)))
+        mode = {"traversal": N.KNN_CANDIDATES_TRAVERSAL, "gram": N.KNN_CANDIDATES_GRAM}[candidates]
+        N.check(N.lib().thea_k_closest_self_ex(self._h, int(k), mode, pidx, pd2, _stream_of(io.device)))
         return idx, d2
+
+
+def point_gram_tile(a, b):
+    """Tensor-core Gram tile of two CUDA point sets (a: <= 128 points, b: <= 512): keys [128, 512] with
+    keys[r, j] = |b_j|^2 - 2 a_r . b_j in the tile's normalised FP16 frame (thea_point_gram_tile)."""
+    import torch
+    a = a.to(torch.float32).contiguous()
+    b = b.to(torch.float32).contiguous()
+    keys = torch.empty((128, 512), dtype=torch.float32, device=a.device)
+    N.check(N.lib().thea_point_gram_tile(ctypes.c_void_p(a.data_ptr()), a.shape[0], ctypes.c_void_p(b.data_ptr()),
+                                         b.shape[0], ctypes.c_void_p(keys.data_ptr()), _stream_of(True)))
+    return keys
 
 
 def sample_evenly_by_area(vertices, faces, num_samples, seed, rng="thea"):

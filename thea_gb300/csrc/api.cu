@@ -5,6 +5,7 @@
 #include "query.hpp"
 #include "batch.hpp"
 #include "serve.hpp"
+#include "gram.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -498,26 +499,56 @@ THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * qu
   });
 }
 
+static void knn_self_impl(const thea_bvh * point_bvh, int32_t k, int32_t candidates, int32_t * out_index,
+                          float * out_sq_distance, void * stream) {
+  THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "k_closest_self: a point BVH is required");
+  THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_self: k must be in 1..32");
+  THEA_REQUIRE(candidates == THEA_KNN_CANDIDATES_TRAVERSAL || candidates == THEA_KNN_CANDIDATES_GRAM,
+               "k_closest_self: unknown candidate mode");
+  THEA_REQUIRE(out_index && out_sq_distance, "k_closest_self: null outputs");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned * err = handle_error_word(point_bvh);
+  int64_t n = point_bvh->n;
+  bool hi = is_host_pointer(out_index), hd = is_host_pointer(out_sq_distance);
+  // rows are written in element order, so host outputs are staged whole
+  Scratch di, dd, bound;
+  int32_t * pi = out_index;
+  float * pd = out_sq_distance;
+  if (hi) { di = Scratch((size_t)n * k * 4, s); pi = di.as<int32_t>(); }
+  if (hd) { dd = Scratch((size_t)n * k * 4, s); pd = dd.as<float>(); }
+  float const * ib = nullptr;
+  if (candidates == THEA_KNN_CANDIDATES_GRAM && gram_supported(n)) {
+    bound = Scratch((size_t)n * 4, s);
+    run_gram_bounds(point_bvh, k, bound.as<float>(), s);
+    ib = bound.as<float>();
+  }
+  run_knn(point_bvh, nullptr, n, k, INFINITY, nullptr, pi, pd, err, s, ib);
+  if (hi) THEA_CUDA_CHECK(cudaMemcpyAsync(out_index, pi, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
+  if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, pd, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
+  if (hi || hd) THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+}
+
 THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,
                                          float * out_sq_distance, void * stream) {
   return guarded([&] {
-    THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "k_closest_self: a point BVH is required");
-    THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_self: k must be in 1..32");
-    THEA_REQUIRE(out_index && out_sq_distance, "k_closest_self: null outputs");
-    cudaStream_t s = (cudaStream_t)stream;
-    unsigned * err = handle_error_word(point_bvh);
-    int64_t n = point_bvh->n;
-    bool hi = is_host_pointer(out_index), hd = is_host_pointer(out_sq_distance);
-    // rows are written in element order, so host outputs are staged whole
-    Scratch di, dd;
-    int32_t * pi = out_index;
-    float * pd = out_sq_distance;
-    if (hi) { di = Scratch((size_t)n * k * 4, s); pi = di.as<int32_t>(); }
-    if (hd) { dd = Scratch((size_t)n * k * 4, s); pd = dd.as<float>(); }
-    run_knn(point_bvh, nullptr, n, k, INFINITY, nullptr, pi, pd, err, s);
-    if (hi) THEA_CUDA_CHECK(cudaMemcpyAsync(out_index, pi, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
-    if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, pd, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
-    if (hi || hd) THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    knn_self_impl(point_bvh, k, THEA_KNN_CANDIDATES_TRAVERSAL, out_index, out_sq_distance, stream);
+  });
+}
+
+THEA_API thea_status thea_k_closest_self_ex(const thea_bvh * point_bvh, int32_t k, int32_t candidates,
+                                            int32_t * out_index, float * out_sq_distance, void * stream) {
+  return guarded([&] { knn_self_impl(point_bvh, k, candidates, out_index, out_sq_distance, stream); });
+}
+
+THEA_API thea_status thea_point_gram_tile(const float * a, int32_t num_a, const float * b, int32_t num_b,
+                                          float * out_keys, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(a && b && out_keys, "point_gram_tile: null argument");
+    THEA_REQUIRE(num_a >= 1 && num_a <= gram_tile_rows() && num_b >= 1 && num_b <= gram_tile_cols(),
+                 "point_gram_tile: at most 128 rows and 512 columns");
+    THEA_REQUIRE(!is_host_pointer(a) && !is_host_pointer(b) && !is_host_pointer(out_keys),
+                 "point_gram_tile: arrays must be device memory");
+    run_gram_tile(a, num_a, b, num_b, out_keys, nullptr, (cudaStream_t)stream);
   });
 }
 

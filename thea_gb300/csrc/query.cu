@@ -116,7 +116,8 @@ template <int W, int K, int STACK>
 __global__ void __launch_bounds__(QUERY_THREADS)
 knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
            int64_t n, int k_out, float thresh, int32_t const * __restrict__ exclude, int32_t * __restrict__ out_index,
-           float * __restrict__ out_d2, unsigned * __restrict__ err, uint32_t const * __restrict__ order) {
+           float * __restrict__ out_d2, unsigned * __restrict__ err, uint32_t const * __restrict__ order,
+           float const * __restrict__ init_bound) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   if (order) q = order[q];
@@ -134,10 +135,13 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
     excl = __float_as_int(a.w);
     row = excl;
   }
+  // init_bound (self mode, per leaf position): an upper bound on the k-th neighbour's squared distance, inclusive, from
+  // actual points; the search keeps every point within it, so the result is the same as without it
+  float start = init_bound ? fminf(thresh, init_bound[q]) : thresh;
   float bd[K];
   int bi[K];
 #pragma unroll
-  for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
+  for (int j = 0; j < K; ++j) { bd[j] = start; bi[j] = INT_MAX; }
   knn_query<W, K, STACK>(nodes, pts, 0, 0, p, excl, bd, bi, err);
   for (int j = 0; j < k_out; ++j) {
     bool v = bi[j] != INT_MAX;
@@ -233,20 +237,20 @@ void launch_ray(thea_bvh const * b, float const * o, float const * d, int64_t n,
 
 template <int W, int K, int STACK>
 void launch_knn_k(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex,
-                  int32_t * idx, float * d2, unsigned * err, uint32_t const * order, cudaStream_t s) {
+                  int32_t * idx, float * d2, unsigned * err, uint32_t const * order, float const * ib, cudaStream_t s) {
   THEA_LAUNCH((knn_kernel<W, K, STACK>), (unsigned)ceil_div(n, QUERY_THREADS), QUERY_THREADS, 0, s,
-              (WideNode<W> const *)b->nodes, b->pt_rec, q, n, k, thresh, ex, idx, d2, err, order);
+              (WideNode<W> const *)b->nodes, b->pt_rec, q, n, k, thresh, ex, idx, d2, err, order, ib);
 }
 
 template <int W, int STACK>
 void launch_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
-                float * d2, unsigned * err, uint32_t const * order, cudaStream_t s) {
-  if (k <= 1) launch_knn_k<W, 1, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
-  else if (k <= 2) launch_knn_k<W, 2, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
-  else if (k <= 4) launch_knn_k<W, 4, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
-  else if (k <= 8) launch_knn_k<W, 8, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
-  else if (k <= 16) launch_knn_k<W, 16, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
-  else launch_knn_k<W, 32, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+                float * d2, unsigned * err, uint32_t const * order, float const * ib, cudaStream_t s) {
+  if (k <= 1) launch_knn_k<W, 1, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
+  else if (k <= 2) launch_knn_k<W, 2, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
+  else if (k <= 4) launch_knn_k<W, 4, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
+  else if (k <= 8) launch_knn_k<W, 8, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
+  else if (k <= 16) launch_knn_k<W, 16, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
+  else launch_knn_k<W, 32, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
 }
 
 }  // namespace
@@ -281,16 +285,17 @@ void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, Ra
 }
 
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
-             float * d2, unsigned * err, cudaStream_t s) {
+             float * d2, unsigned * err, cudaStream_t s, float const * init_bound) {
   if (n <= 0) return;
   // self mode already runs in leaf order
   QueryOrder ord(b, q, nullptr, q ? n : 0, s);
   uint32_t const * o = ord.order;
+  float const * ib = q ? nullptr : init_bound;
   bool sm = small_stack_ok(b);
-  if (b->width == 4) sm ? launch_knn<4, 64>(b, q, n, k, thresh, ex, idx, d2, err, o, s)
-                        : launch_knn<4, 256>(b, q, n, k, thresh, ex, idx, d2, err, o, s);
-  else sm ? launch_knn<8, 128>(b, q, n, k, thresh, ex, idx, d2, err, o, s)
-          : launch_knn<8, 512>(b, q, n, k, thresh, ex, idx, d2, err, o, s);
+  if (b->width == 4) sm ? launch_knn<4, 64>(b, q, n, k, thresh, ex, idx, d2, err, o, ib, s)
+                        : launch_knn<4, 256>(b, q, n, k, thresh, ex, idx, d2, err, o, ib, s);
+  else sm ? launch_knn<8, 128>(b, q, n, k, thresh, ex, idx, d2, err, o, ib, s)
+          : launch_knn<8, 512>(b, q, n, k, thresh, ex, idx, d2, err, o, ib, s);
 }
 
 }  // namespace thea

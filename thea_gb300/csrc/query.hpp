@@ -25,8 +25,9 @@ void run_closest(thea_bvh const * b, float const * q, int64_t n, ClosestParams c
 void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, RayParams const & rp, float * t,
              int32_t * idx, float * nrm, float * t64, int32_t * idx64, int32_t * flags, unsigned * err, cudaStream_t s);
 // q == nullptr: self mode over the BVH's own points (n = number of points, rows in element order)
+// init_bound (self mode only): per leaf position, an inclusive upper bound on the k-th neighbour's squared distance
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
-             float * d2, unsigned * err, cudaStream_t s);
+             float * d2, unsigned * err, cudaStream_t s, float const * init_bound = nullptr);
 
 // Returns the number of samples written (0 when the total area is not positive); synchronizes the stream.
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,

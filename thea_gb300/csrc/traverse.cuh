@@ -60,5 +60,7 @@ template <int W> struct StackSize { static constexpr int value = W == 4 ? 64 : 1
 
 // Device-side error bits reported through the handle's error word
 constexpr unsigned ERR_STACK_OVERFLOW = 1u;
+// a bounded wait of the tensor-core k-NN candidate kernel gave up (its queries fell back to the plain search)
+constexpr unsigned ERR_GRAM_TIMEOUT = 2u;
 
 }  // namespace thea
