@@ -386,6 +386,20 @@ def extra_workloads(T, torch, stream, flush, args):
                              "ms_per_step": statistics.mean(ms), "kernel_ms": kms, "k": 16,
                              "sampling_ms": sample_ms, "point_bvh_build_ms": pbuild_ms,
                              "roofline_frac": ALGO_BYTES_CFG2 / (kms / 1e3) / 1e9 / peaks()[0]}
+    # the same graph with tensor-core Gram candidates seeding the exact search (identical results)
+    T.profiling_reset()
+    T.profiling(True)
+    ms = timed_steps(lambda: pb.k_closest_self(16, device=True, candidates="gram"), steps, 2, flush, stream)
+    T.profiling(False)
+    g_ms, g_cnt = T.profiling_read("gram_bound_kernel")
+    k_ms, k_cnt = T.profiling_read("knn_kernel")
+    i0, d0 = pb.k_closest_self(16, device=True)
+    i1, d1 = pb.k_closest_self(16, device=True, candidates="gram")
+    out["knn_graph_cfg2"]["gram_candidates"] = {
+        "value": KNN_POINTS / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
+        "ms_per_step": statistics.mean(ms), "gram_kernel_ms": g_ms / max(1, g_cnt),
+        "bounded_search_ms": k_ms / max(1, k_cnt), "tensor_flop_per_step": 2 * 16 * 512 * KNN_POINTS,
+        "identical_to_traversal": bool(torch.equal(i0, i1) and torch.equal(d0, d1))}
     pb.close()
     T.profiling_reset()
     out["batched_closest_cfg3"] = batched_config3(T, torch, stream, flush, args)
