@@ -332,8 +332,8 @@ typedef struct thea_server thea_server;
 
 typedef struct thea_server_config {
   int64_t memory_budget_bytes;   /* resident BVHs + staging of in-flight pieces (0: 8 GiB) */
-  int32_t slots;                 /* batches in flight at once, one stream each (0: 3) */
-  int32_t max_batch_queries;     /* queries per batch (0: 262144) */
+  int32_t slots;                 /* batches in flight at once, one stream each (0: 4) */
+  int32_t max_batch_queries;     /* queries per batch (0: 131072) */
   int32_t max_piece_queries;     /* largest piece of one request (0: 65536) */
   int32_t precision;             /* closest-element requests: THEA_PRECISION_* */
   int32_t width;                 /* BVH width of resident meshes, 4 or 8 (0: 4) */
@@ -344,7 +344,10 @@ typedef struct thea_server_config {
                                     not built (their size is estimated), no results are written, and a batch finishes
                                     test_ns_per_query x its queries after it starts. 0: the GPU. */
   int32_t test_ns_per_query;
-  int32_t reserved[6];           /* must be zero */
+  int32_t hard_query_budget;     /* > 0: closest-element stack pops on one thread before a query is finished by a warp
+                                    of its own in a second launch; <= 0: one thread per query throughout (default:
+                                    measured lower p99 latency on the config-4 mix) */
+  int32_t reserved[5];           /* must be zero */
 } thea_server_config;
 
 #define THEA_REQUEST_CLOSEST 0  /* closest element: thea_closest_element */

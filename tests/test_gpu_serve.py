@@ -75,10 +75,13 @@ REQUESTS = [("closest", 0, 1, -1.0), ("closest", 1, 777, -1.0), ("closest", 2, 5
             ("ray", 1, 65537, -1.0), ("knn", 0, 20000, -1.0)]
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_requests_alone_and_in_a_mix_equal_the_single_bvh_calls(T, meshes, precision):
+# hard_query_budget: 0 = one thread per query throughout (default), 256 = two-phase, 3 = nearly every closest-point
+# query finishes on a warp of its own
+@pytest.mark.parametrize("precision,budget", [("fp32", 0), ("fp64", 0), ("fp32", 3), ("fp64", 3), ("fp32", 256)])
+def test_requests_alone_and_in_a_mix_equal_the_single_bvh_calls(T, meshes, precision, budget):
     ref = Reference(T, meshes, precision)
-    with T.Server(precision=precision, max_piece_queries=4096, max_batch_queries=16384, slots=3) as s:
+    with T.Server(precision=precision, max_piece_queries=4096, max_batch_queries=16384, slots=3,
+                  hard_query_budget=budget) as s:
         ids = [s.add_mesh(V, F) for V, F in meshes]
         cases = []
         for j, (kind, m, n, bound) in enumerate(REQUESTS):

@@ -58,7 +58,7 @@ class ServerConfig(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32),
                 ("small_request_queries", ctypes.c_int32), ("max_wait_ms", ctypes.c_int32),
                 ("test_executor", ctypes.c_int32), ("test_ns_per_query", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("hard_query_budget", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 class Request(ctypes.Structure):

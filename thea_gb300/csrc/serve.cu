@@ -12,6 +12,7 @@
 #include "device_util.cuh"
 #include "query.hpp"
 #include "traverse_ops.cuh"
+#include "warp_traverse.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -67,10 +68,20 @@ __device__ __forceinline__ bool next_round(unsigned long long * counter, int64_t
   return base < nq;
 }
 
+// Closest-element queries that ran out of their stack-pop budget in the first kernel, finished one warp per query by
+// the second (a deep query inside a large mesh would otherwise hold its whole batch for milliseconds).
+struct ServeHardQueue {
+  int64_t * q;
+  float * bound;  // FP32 squared distance of the best element found so far (+inf if none)
+  int32_t * idx;
+  int64_t * slot;
+  unsigned long long * count;
+};
+
 template <int W, int STACK, int PREC>
 __global__ void __launch_bounds__(SERVE_THREADS)
 serve_closest_kernel(ServeTask const * __restrict__ tasks, int64_t const * __restrict__ off, int T, int64_t nq,
-                     unsigned long long * counter) {
+                     unsigned long long * counter, int budget, ServeHardQueue hq) {
   F64WarpBuf * buf = nullptr;
   if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
     __shared__ F64WarpBuf s_buf[SERVE_THREADS / 32];
@@ -96,18 +107,29 @@ serve_closest_kernel(ServeTask const * __restrict__ tasks, int64_t const * __res
     r.idx = INT_MAX;
     r.d2 = 0.f;
     r.d2_64 = 0.0;
+    r.slot = -1;
+    r.best32 = INFINITY;
+    r.done = true;
     float dist = 0.f;
     if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
       float scale = active ? fmaxf(t->scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)))) : 0.f;
       F64Search s;
-      if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, t->bound2, scale, t->err, s);
+      if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, t->bound2, scale, t->err, s, budget);
       else f64_search_init(s);
-      f64_resolve_warp(s, active, rec, 0, p, active ? t->bound2 : -1.0, *buf);
+      f64_resolve_warp(s, active && s.done, rec, 0, p, active ? t->bound2 : -1.0, *buf);
       r = f64_result(s);
       dist = (float)sqrt(r.d2_64);
     } else {
-      if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, t->thresh, t->err);
+      if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, t->thresh, t->err, budget);
       dist = sqrtf(r.d2);
+    }
+    if (active && !r.done) {
+      unsigned long long pos = atomicAdd(hq.count, 1ull);
+      hq.q[pos] = q;
+      hq.bound[pos] = r.best32;
+      hq.idx[pos] = PREC == THEA_PRECISION_FP64_RECHECK ? INT_MAX : r.idx;
+      hq.slot[pos] = r.slot;
+      active = false;
     }
     if (active) {
       bool found = r.idx != INT_MAX;
@@ -119,6 +141,69 @@ serve_closest_kernel(ServeTask const * __restrict__ tasks, int64_t const * __res
         t->out_point[3 * i + 2] = found ? r.cp.z : 0.f;
       }
     }
+  }
+}
+
+template <int W, int PREC>
+__global__ void __launch_bounds__(SERVE_THREADS)
+serve_closest_phase2_kernel(ServeTask const * __restrict__ tasks, int64_t const * __restrict__ off, int T,
+                            ServeHardQueue hq, unsigned long long * counter) {
+  constexpr int WARPS = SERVE_THREADS / 32;
+  __shared__ int s_code[WARPS][WARP_STACK];
+  __shared__ float s_lb[WARPS][WARP_STACK];
+  __shared__ float s_cd[WARPS][PREC == THEA_PRECISION_FP64_RECHECK ? WARP_CAND : 1];
+  __shared__ int64_t s_ck[WARPS][PREC == THEA_PRECISION_FP64_RECHECK ? WARP_CAND : 1];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long total = *hq.count;
+  while (true) {
+    unsigned long long j = 0;
+    if (lane == 0) j = atomicAdd(counter, 1ull);
+    j = __shfl_sync(0xffffffffu, j, 0);
+    if (j >= total) break;
+    int64_t q = hq.q[j];
+    int ti = task_of(off, T, q);
+    ServeTask const * t = tasks + ti;
+    int64_t i = q - __ldg(off + ti);
+    V3 p = load_v3(t->in0 + 3 * i);
+    WideNode<W> const * nodes = (WideNode<W> const *)t->nodes;
+    bool found;
+    float dist;
+    V3 cp = V3{0.f, 0.f, 0.f};
+    int idx;
+    if (PREC == THEA_PRECISION_FP64_RECHECK) {
+      float scale = fmaxf(t->scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+      WarpBest64 b = closest_warp_query_f64<W>(nodes, t->rec, 0, 0, p, t->bound2, scale, hq.bound[j], s_code[warp],
+                                               s_lb[warp], s_cd[warp], s_ck[warp], t->err);
+      found = b.idx != INT_MAX;
+      idx = b.idx;
+      dist = (float)sqrt(b.d2);
+      if (found && lane == 0 && t->out_point) {
+        D3 cp64;
+        double d64;
+        cp_record_f64(t->rec, b.slot, p, cp64, d64);
+        cp = V3{(float)cp64.x, (float)cp64.y, (float)cp64.z};
+      }
+    } else {
+      WarpBest init;
+      init.idx = hq.idx[j];
+      init.d2 = init.idx != INT_MAX ? hq.bound[j] : t->thresh;
+      init.slot = hq.slot[j];
+      WarpBest b = closest_warp_query<W>(nodes, t->rec, 0, 0, p, init, s_code[warp], s_lb[warp], t->err);
+      found = b.idx != INT_MAX;
+      idx = b.idx;
+      dist = sqrtf(b.d2);
+      if (found && lane == 0 && t->out_point) cp_record_test(t->rec, b.slot, p, cp);
+    }
+    if (lane == 0) {
+      t->out_index[i] = found ? idx : -1;
+      if (t->out_value) t->out_value[i] = found ? dist : -1.f;
+      if (t->out_point) {
+        t->out_point[3 * i] = found ? cp.x : 0.f;
+        t->out_point[3 * i + 1] = found ? cp.y : 0.f;
+        t->out_point[3 * i + 2] = found ? cp.z : 0.f;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -257,7 +342,7 @@ struct ServeSlot {
   thea::ServeTask * h_tasks = nullptr;  // pinned mirror
   int64_t * d_off = nullptr;            // [3][MAX_TASKS + 1]
   int64_t * h_off = nullptr;
-  unsigned long long * d_counters = nullptr;  // [3]
+  unsigned long long * d_counters = nullptr;  // [5]: per query kind, then the hard queue's count and its cursor
   std::vector<ServePiece> pieces;
   bool busy = false;
   bool complete = false;  // set by the stream callback (or the test executor's clock)
@@ -452,7 +537,7 @@ void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *>
     THEA_CUDA_CHECK(cudaMemcpyAsync(s.d_off + type * (MAX_TASKS + 1), s.h_off + type * (MAX_TASKS + 1),
                                     sizeof(int64_t) * (T[type] + 1), cudaMemcpyHostToDevice, st));
   }
-  THEA_CUDA_CHECK(cudaMemsetAsync(s.d_counters, 0, 3 * sizeof(unsigned long long), st));
+  THEA_CUDA_CHECK(cudaMemsetAsync(s.d_counters, 0, 5 * sizeof(unsigned long long), st));
   int W = sv->cfg.width;
   for (int type = 0; type < 3; ++type) {
     if (!T[type]) continue;
@@ -463,10 +548,22 @@ void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *>
     int Tn = T[type];
     if (type == THEA_REQUEST_CLOSEST) {
       bool f64 = sv->cfg.precision == THEA_PRECISION_FP64_RECHECK;
+      int budget = sv->cfg.hard_query_budget;
+      size_t hn = budget > 0 ? (size_t)n : 0;
+      Scratch hq_q(hn * sizeof(int64_t), st), hq_b(hn * sizeof(float), st), hq_i(hn * sizeof(int32_t), st),
+          hq_s(hn * sizeof(int64_t), st);
+      ServeHardQueue hq{hq_q.as<int64_t>(), hq_b.as<float>(), hq_i.as<int32_t>(), hq_s.as<int64_t>(),
+                        s.d_counters + 3};
 #define THEA_SERVE_CP(WW, SS, PP)                                                                                  \
   do {                                                                                                            \
     auto k = serve_closest_kernel<WW, SS, PP>;                                                                    \
-    THEA_LAUNCH_NAMED("serve_closest_kernel", k, grid_for(k, n), SERVE_THREADS, 0, st, tk, of, Tn, n, c);        \
+    THEA_LAUNCH_NAMED("serve_closest_kernel", k, grid_for(k, n), SERVE_THREADS, 0, st, tk, of, Tn, n, c,         \
+                      budget > 0 ? budget : 0, hq);                                                               \
+    if (budget > 0) {                                                                                             \
+      auto k2 = serve_closest_phase2_kernel<WW, PP>;                                                              \
+      THEA_LAUNCH_NAMED("serve_closest_phase2_kernel", k2, grid_for(k2, n), SERVE_THREADS, 0, st, tk, of, Tn, hq, \
+                        s.d_counters + 4);                                                                        \
+    }                                                                                                             \
   } while (0)
       if (W == 4) {
         if (f64) THEA_SERVE_CP(4, 256, 1);
@@ -606,8 +703,8 @@ thea_server * server_create(thea_server_config const & c) {
   thea_server_config & cfg = sv->cfg;
   cfg = c;
   if (!cfg.memory_budget_bytes) cfg.memory_budget_bytes = int64_t(8) << 30;
-  if (!cfg.slots) cfg.slots = 3;
-  if (!cfg.max_batch_queries) cfg.max_batch_queries = 262144;
+  if (!cfg.slots) cfg.slots = 4;
+  if (!cfg.max_batch_queries) cfg.max_batch_queries = 131072;
   if (!cfg.max_piece_queries) cfg.max_piece_queries = 65536;
   cfg.max_piece_queries = std::min(cfg.max_piece_queries, cfg.max_batch_queries);
   if (!cfg.width) cfg.width = 4;
@@ -624,7 +721,7 @@ thea_server * server_create(thea_server_config const & c) {
       THEA_CUDA_CHECK(cudaMallocHost(&s->h_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
       THEA_CUDA_CHECK(cudaMalloc(&s->d_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
       THEA_CUDA_CHECK(cudaMallocHost(&s->h_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
-      THEA_CUDA_CHECK(cudaMalloc(&s->d_counters, 3 * sizeof(unsigned long long)));
+      THEA_CUDA_CHECK(cudaMalloc(&s->d_counters, 5 * sizeof(unsigned long long)));
     }
     sv->slots.push_back(std::move(s));
   }

@@ -64,7 +64,7 @@ class Ticket:
 class Server:
     def __init__(self, memory_budget_bytes=0, slots=0, max_batch_queries=0, max_piece_queries=0, precision="fp32",
                  width=4, max_leaf_size=0, small_request_queries=0, max_wait_ms=0, test_executor=False,
-                 test_ns_per_query=0):
+                 test_ns_per_query=0, hard_query_budget=0):
         cfg = N.ServerConfig()
         cfg.memory_budget_bytes = int(memory_budget_bytes)
         cfg.slots = int(slots)
@@ -77,6 +77,7 @@ class Server:
         cfg.max_wait_ms = int(max_wait_ms)
         cfg.test_executor = 1 if test_executor else 0
         cfg.test_ns_per_query = int(test_ns_per_query)
+        cfg.hard_query_budget = int(hard_query_budget)
         self._h = ctypes.c_void_p()
         N.check(N.lib().thea_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
 
