@@ -73,25 +73,50 @@ closest_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict
 //============================================================================================================================
 
 template <int W, int STACK, bool RECHECK>
-__global__ void __launch_bounds__(QUERY_THREADS)
-ray_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec, float const * __restrict__ origins,
+__device__ __forceinline__ void ray_body(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec, float const * __restrict__ origins,
            float const * __restrict__ dirs, int64_t n, float max_time, float * __restrict__ out_time,
            int32_t * __restrict__ out_index, float * __restrict__ out_normal, float * __restrict__ out_time64,
            int32_t * __restrict__ out_index64, int32_t * __restrict__ out_flags, unsigned * __restrict__ err,
            uint32_t const * __restrict__ order) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  if (order) q = order[q];
-  V3 o = load_v3(origins + 3 * q);
-  V3 d = load_v3(dirs + 3 * q);
-  RayOut r = ray_query<W, STACK, RECHECK>(nodes, rec, 0, 0, o, d, max_time, err);
-  bool found = r.idx != INT_MAX;
-  out_time[q] = found ? r.t : -1.f;
-  if (out_index) out_index[q] = found ? r.idx : -1;
+  float t;
+  int idx;
+  int64_t slot;
+  double t64 = 0.0;
+  int idx64 = INT_MAX;
+  if constexpr (RECHECK) {
+    // no early exit: the FP64 step runs with the warp's lanes together
+    __shared__ RayWarpBuf buf[QUERY_THREADS / 32];
+    bool active = q < n;
+    if (active && order) q = order[q];
+    V3 o = active ? load_v3(origins + 3 * q) : V3{0.f, 0.f, 1.f};
+    V3 d = active ? load_v3(dirs + 3 * q) : V3{0.f, 0.f, 1.f};
+    RaySearch64 s;
+    if (active) ray_search_f64<W, STACK>(nodes, rec, 0, 0, o, d, max_time, err, s);
+    else ray_search_init(s, max_time);
+    ray_resolve_warp(s, active, rec, 0, o, d, max_time, buf[threadIdx.x >> 5]);
+    if (!active) return;
+    t = s.t;
+    idx = s.idx;
+    slot = s.slot;
+    t64 = s.best64;
+    idx64 = s.idx64;
+  } else {
+    if (q >= n) return;
+    if (order) q = order[q];
+    RayOut r = ray_query<W, STACK, false>(nodes, rec, 0, 0, load_v3(origins + 3 * q), load_v3(dirs + 3 * q), max_time,
+                                          err);
+    t = r.t;
+    idx = r.idx;
+    slot = r.slot;
+  }
+  bool found = idx != INT_MAX;
+  out_time[q] = found ? t : -1.f;
+  if (out_index) out_index[q] = found ? idx : -1;
   if (out_normal) {
     V3 nn = V3{0.f, 0.f, 0.f};
     if (found) {
-      float4 const * rr = rec + r.slot * RAY_REC_F4;
+      float4 const * rr = rec + slot * RAY_REC_F4;
       nn = normalized(cross(xyz(__ldg(rr + 1)), xyz(__ldg(rr + 2))));
     }
     out_normal[3 * q] = nn.x;
@@ -99,12 +124,35 @@ ray_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ r
     out_normal[3 * q + 2] = nn.z;
   }
   if (RECHECK) {
-    bool f64 = r.idx64 != INT_MAX;
-    if (out_time64) out_time64[q] = f64 ? (float)r.t64 : -1.f;
-    if (out_index64) out_index64[q] = f64 ? r.idx64 : -1;
+    bool f64 = idx64 != INT_MAX;
+    if (out_time64) out_time64[q] = f64 ? (float)t64 : -1.f;
+    if (out_index64) out_index64[q] = f64 ? idx64 : -1;
     if (out_flags) out_flags[q] = (found != f64 ? THEA_RAY_FLAG_HIT_DIFFERS : 0) |
-                                  (found && f64 && r.idx != r.idx64 ? THEA_RAY_FLAG_ELEMENT_DIFFERS : 0);
+                                  (found && f64 && idx != idx64 ? THEA_RAY_FLAG_ELEMENT_DIFFERS : 0);
   }
+}
+
+template <int W, int STACK, bool RECHECK>
+__global__ void __launch_bounds__(QUERY_THREADS)
+ray_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec, float const * __restrict__ origins,
+           float const * __restrict__ dirs, int64_t n, float max_time, float * __restrict__ out_time,
+           int32_t * __restrict__ out_index, float * __restrict__ out_normal, float * __restrict__ out_time64,
+           int32_t * __restrict__ out_index64, int32_t * __restrict__ out_flags, unsigned * __restrict__ err,
+           uint32_t const * __restrict__ order) {
+  ray_body<W, STACK, false>(nodes, rec, origins, dirs, n, max_time, out_time, out_index, out_normal, out_time64,
+                            out_index64, out_flags, err, order);
+}
+
+// The FP64 re-check form: register use capped so that five blocks of 128 threads fit on an SM
+template <int W, int STACK>
+__global__ void __launch_bounds__(QUERY_THREADS, 5)
+ray_recheck_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                   float const * __restrict__ origins, float const * __restrict__ dirs, int64_t n, float max_time,
+                   float * __restrict__ out_time, int32_t * __restrict__ out_index, float * __restrict__ out_normal,
+                   float * __restrict__ out_time64, int32_t * __restrict__ out_index64, int32_t * __restrict__ out_flags,
+                   unsigned * __restrict__ err, uint32_t const * __restrict__ order) {
+  ray_body<W, STACK, true>(nodes, rec, origins, dirs, n, max_time, out_time, out_index, out_normal, out_time64,
+                           out_index64, out_flags, err, order);
 }
 
 //============================================================================================================================
@@ -228,8 +276,8 @@ void launch_ray(thea_bvh const * b, float const * o, float const * d, int64_t n,
                 uint32_t const * order, cudaStream_t s) {
   unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
   if (rp.recheck)
-    THEA_LAUNCH((ray_kernel<W, STACK, true>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->ray_rec, o,
-                d, n, rp.max_time, t, idx, nrm, t64, idx64, flags, err, order);
+    THEA_LAUNCH((ray_recheck_kernel<W, STACK>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->ray_rec,
+                o, d, n, rp.max_time, t, idx, nrm, t64, idx64, flags, err, order);
   else
     THEA_LAUNCH((ray_kernel<W, STACK, false>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->ray_rec, o,
                 d, n, rp.max_time, t, idx, nrm, t64, idx64, flags, err, order);

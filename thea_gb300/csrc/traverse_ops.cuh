@@ -585,6 +585,254 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
 }
 
 //============================================================================================================================
+// First ray hit with the FP64 watertight re-test, in two steps (the closest-point scheme above, for rays):
+// ray_search_f64 runs the FP32 traversal, keeps the reference's FP32 verdict, and collects the elements whose FP64
+// watertight verdict could be the nearest hit; ray_resolve_warp evaluates the collected elements of all 32 lanes in FP64
+// together.
+//
+// Which elements are collected. Every element the FP32 test accepts or rejects within an error allowance of an edge
+// (edge functions within 2^-12 of the determinant plus a bound on their FP32 rounding), every near-parallel element,
+// and nothing farther than the band B. B comes from "certain" FP32 hits: accepted with every edge function at least
+// 2^-10 of the determinant plus the rounding bound inside, and not grazing (angle between ray and plane above ~1.8
+// degrees). The FP64 test accepts a certain hit too, at a time within relative 2^-10 plus 2^-11 |o - v0|_1 / |d|_1 of
+// the FP32 time, so no element beyond B can be the FP64 nearest hit, and the traversal prunes with B.
+//============================================================================================================================
+
+constexpr int RAY_CAND = 6;
+
+struct RaySearch64 {
+  float ct[RAY_CAND];   // lower bound on each collected element's FP64 time: its FP32 hit or plane time less the
+                        // time allowance (+inf: empty)
+  int ck[RAY_CAND];     // sorted position relative to the segment start (-1: empty)
+  unsigned keep;        // bit j: entry j is grazing and kept whatever its time estimate
+  float B;              // band from certain hits (+inf if none)
+  float tcap;           // max_time with its allowance (+inf if unbounded)
+  // FP64 best of entries evaluated by the lane alone (a full list)
+  double best64;
+  int idx64;
+  int64_t slot64;
+  // the reference's FP32 verdict
+  float t;
+  int idx;
+  int64_t slot;
+};
+
+__device__ __forceinline__ float l1(V3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
+
+__device__ __forceinline__ void ray_f64_take(RaySearch64 & s, int64_t k, int idx, double t64, float max_time) {
+  if (!(t64 >= 0.0) || (max_time >= 0.f && t64 > (double)max_time)) return;
+  if (t64 < s.best64 || (t64 == s.best64 && idx < s.idx64)) {
+    s.best64 = t64;
+    s.idx64 = idx;
+    s.slot64 = k;
+  }
+}
+
+__device__ __forceinline__ void ray_search_init(RaySearch64 & s, float max_time) {
+#pragma unroll
+  for (int j = 0; j < RAY_CAND; ++j) {
+    s.ct[j] = INFINITY;
+    s.ck[j] = -1;
+  }
+  s.keep = 0;
+  s.B = INFINITY;
+  s.tcap = max_time >= 0.f ? max_time + max_time * (1.0f / 1024.0f) : INFINITY;
+  s.best64 = INFINITY;
+  s.idx64 = INT_MAX;
+  s.slot64 = -1;
+  s.t = max_time >= 0.f ? max_time : INFINITY;
+  s.idx = INT_MAX;
+  s.slot = -1;
+}
+
+template <int W, int STACK>
+__device__ __forceinline__ void ray_search_f64(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                                               int root, int64_t elem_base, V3 o, V3 d, float max_time, unsigned * err,
+                                               RaySearch64 & s) {
+  float const EPS = 1.1920928955078125e-07f;
+  ray_search_init(s, max_time);
+  float ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
+  float iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
+  float iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
+  float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+  float nd = l1(d);
+  float dd = dot(d, d);
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = root;
+  stkd[sp] = 0.f;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int code = stk[sp];
+    // the FP32 verdict needs everything up to its best; the FP64 one everything up to B
+    float bound = fminf(fmaxf(s.t, s.B), s.tcap);
+    if (stkd[sp] > bound * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd4;
+      load_node(nodes, code, nd4);
+      float lb[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        float tx0 = __fmaf_rn(nd4.lox[c], ix, ox), tx1 = __fmaf_rn(nd4.hix[c], ix, ox);
+        float ty0 = __fmaf_rn(nd4.loy[c], iy, oy), ty1 = __fmaf_rn(nd4.hiy[c], iy, oy);
+        float tz0 = __fmaf_rn(nd4.loz[c], iz, oz), tz1 = __fmaf_rn(nd4.hiz[c], iz, oz);
+        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
+        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
+      }
+      push_children<W, STACK>(nd4, lb, bound * PRUNE_SLACK, stk, stkd, sp, err);
+      continue;
+    }
+    int first, count;
+    decode_leaf(code, first, count);
+    for (int kr = first; kr < first + count; ++kr) {
+      int64_t k = elem_base + kr;
+      float4 const * r = rec + k * RAY_REC_F4;
+      float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+      V3 v0 = xyz(a), e01 = xyz(b), e02 = xyz(c);
+      int idx = __float_as_int(a.w);
+      // The reference's test (Triangle3.hpp:1466-1524: the same operations as ray_triangle_time, without its early
+      // exits, whose intermediate values the classification below reuses) ...
+      V3 diff = o - v0;
+      V3 n = cross(e01, e02);
+      float DdN = dot(d, n);
+      float sg = DdN < 0.f ? -1.f : 1.f;
+      float adn = fabsf(DdN);
+      float e1 = sg * dot(d, cross(diff, e02));
+      float e2 = sg * dot(d, cross(e01, diff));
+      float t = -1.f;
+      if (adn > EPS && e1 >= 0.f && e2 >= 0.f && e1 + e2 <= adn) {
+        float QdN = (-sg) * dot(diff, n);
+        if (QdN >= 0.f) t = QdN / adn;
+      }
+      // ... and its verdict (TriangleN<3>::rayIntersection: t >= 0 and, with a bound, t <= max_time)
+      if (t >= 0.f && t <= s.t && (t < s.t || idx < s.idx)) {
+        s.t = t;
+        s.idx = idx;
+        s.slot = k;
+      }
+      // classification for the FP64 verdict, from the same FP32 quantities. The reference's parallel threshold
+      // (|D.N| <= FLT_EPSILON with N unnormalised) is a property of its FP32 test only: a small triangle seen at a
+      // moderate angle is classified here by its geometry like any other.
+      float nn2 = dot(n, n);
+      if (!(nn2 > 0.f)) continue;  // degenerate triangle: the watertight test has no hit either
+      float e3 = adn - e1 - e2;
+      float ndiff = l1(diff);
+      // FP32 rounding allowance of an edge function (D.(diff x e), D.(e x diff) and D.N - both)
+      float le1 = l1(e01), le2 = l1(e02);
+      float E = (1.0f / 262144.0f) * nd * (ndiff * (le1 + le2) + le1 * le2);
+      bool grazing = DdN * DdN < (1.0f / 1024.0f) * dd * nn2;
+      float emin = fminf(fminf(e1, e2), e3);
+      float tabs = (1.0f / 2048.0f) * ndiff / nd;
+      float te;
+      if (grazing) {
+        te = 0.f;  // the FP32 time is unreliable: kept whatever the band
+      } else {
+        float tp = t >= 0.f ? t : (-sg * dot(diff, n)) / adn;  // plane time (the reference's formula)
+        if (tp < -tabs) continue;                             // behind the origin in FP64 too
+        if (emin >= adn * (1.0f / 1024.0f) + E && tp >= tabs) {
+          // certain: the FP64 test hits this element too, within the time allowance
+          s.B = fminf(s.B, tp + tp * (1.0f / 1024.0f) + tabs);
+        }
+        if (!(emin >= -(adn * (1.0f / 4096.0f) + E))) continue;  // clearly outside: no FP64 hit
+        te = tp - tabs;
+      }
+      float lim = fminf(s.B, s.tcap);
+      if (!grazing && te > lim) continue;
+      // the entry takes a slot that has left the band, else the farthest non-grazing slot if that is farther
+      int slot_j = -1;
+#pragma unroll
+      for (int j = 0; j < RAY_CAND; ++j)
+        if (slot_j < 0 && (s.ck[j] < 0 || (!((s.keep >> j) & 1u) && s.ct[j] > lim))) slot_j = j;
+      float worst = grazing ? INFINITY : te;
+      if (slot_j < 0) {
+        float wv = -INFINITY;
+#pragma unroll
+        for (int j = 0; j < RAY_CAND; ++j)
+          if (!((s.keep >> j) & 1u) && s.ct[j] > wv) { wv = s.ct[j]; slot_j = j; }
+        if (slot_j >= 0 && !(wv > worst)) slot_j = -1;
+      }
+      int evict = slot_j < 0 ? kr : -1;
+#pragma unroll
+      for (int j = 0; j < RAY_CAND; ++j) {
+        if (j == slot_j) {
+          if (s.ck[j] >= 0 && (((s.keep >> j) & 1u) || s.ct[j] <= lim)) evict = s.ck[j];
+          s.ct[j] = te;
+          s.ck[j] = kr;
+          s.keep = grazing ? (s.keep | (1u << j)) : (s.keep & ~(1u << j));
+        }
+      }
+      if (evict >= 0) {
+        // more entries than slots (rare): this one is evaluated by the lane alone
+        float4 const * er = rec + (elem_base + evict) * RAY_REC_F4;
+        float4 ea = __ldg(er), eb = __ldg(er + 1), ec = __ldg(er + 2);
+        double t64 = watertight_f64_call(o, d, ea, eb, ec);
+        ray_f64_take(s, elem_base + evict, __float_as_int(ea.w), t64, max_time);
+      }
+    }
+  }
+}
+
+// Shared-memory work list of one warp for ray_resolve_warp
+struct RayWarpBuf {
+  float4 const * r[32 * RAY_CAND];
+  double t[32 * RAY_CAND];
+  float o[32][3], d[32][3];
+  unsigned char owner[32 * RAY_CAND];
+};
+
+// FP64 watertight verdict over every lane's kept entries, in full-warp rounds; all 32 lanes call it together.
+__device__ __forceinline__ void ray_resolve_warp(RaySearch64 & s, bool active, float4 const * __restrict__ rec,
+                                                 int64_t elem_base, V3 o, V3 d, float max_time, RayWarpBuf & b) {
+  unsigned const FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  float lim = fminf(s.B, s.tcap);
+  bool keepj[RAY_CAND];
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < RAY_CAND; ++j) {
+    keepj[j] = active && s.ck[j] >= 0 && (((s.keep >> j) & 1u) || s.ct[j] <= lim);
+    c += keepj[j] ? 1 : 0;
+  }
+  int incl = c;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    int v = __shfl_up_sync(FULL, incl, off);
+    if (lane >= off) incl += v;
+  }
+  int total = __shfl_sync(FULL, incl, 31);
+  int base = incl - c;
+  b.o[lane][0] = o.x;
+  b.o[lane][1] = o.y;
+  b.o[lane][2] = o.z;
+  b.d[lane][0] = d.x;
+  b.d[lane][1] = d.y;
+  b.d[lane][2] = d.z;
+  int w = base;
+#pragma unroll
+  for (int j = 0; j < RAY_CAND; ++j) {
+    if (keepj[j]) {
+      b.r[w] = rec + (elem_base + s.ck[j]) * RAY_REC_F4;
+      b.owner[w] = (unsigned char)lane;
+      ++w;
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < total; i += 32) {
+    int ow = b.owner[i];
+    float4 const * r = b.r[i];
+    V3 oo = V3{b.o[ow][0], b.o[ow][1], b.o[ow][2]}, dd = V3{b.d[ow][0], b.d[ow][1], b.d[ow][2]};
+    b.t[i] = watertight_f64_call(oo, dd, __ldg(r), __ldg(r + 1), __ldg(r + 2));
+  }
+  __syncwarp();
+  for (int i = base; i < base + c; ++i)
+    ray_f64_take(s, (b.r[i] - rec) / RAY_REC_F4, __float_as_int(__ldg(b.r[i]).w), b.t[i], max_time);
+  __syncwarp();
+}
+
+//============================================================================================================================
 // k nearest points
 //============================================================================================================================
 
