@@ -54,7 +54,48 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--case", choices=sorted(CASES), help="run one small profiling case (warm-up calls, then the "
+                    "launch to capture) and exit; used by the ncu commands recorded under profiles/")
     return ap.parse_args()
+
+
+def case_ray():
+    """Config 1: three plain calls, then one call with the FP64 watertight re-test."""
+    import torch
+    import thea_gb300 as T
+    V, F, o, d = W.config1()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=2)
+    od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    for _ in range(3):
+        bvh.ray_structure_intersection(od, dd)
+    bvh.ray_structure_intersection_ex(od, dd, precision="fp64")
+    torch.cuda.synchronize()
+
+
+def case_cfg3_fp64_64():
+    """Batched closest point with FP64 re-check over 64 meshes of the config-3 distribution: two calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, foff, Q, qoff, _ = W.config3_torch(64)
+    forest = T.MeshForest(V, F, foff, width=4, max_leaf_size=1, layouts=1)
+    for _ in range(2):
+        forest.batch_closest_element(Q, qoff, precision="fp64", hard_query_budget=-1, queries_per_warp=64)
+    torch.cuda.synchronize()
+
+
+def case_gram_knn():
+    """k-NN graph (k = 16) of 1,048,576 area samples of the config-0 mesh with tensor-core candidates: two calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, _ = W.config0()
+    pos, _, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), 1 << 20, 2)
+    pb = T.PointBvh(pos)
+    for _ in range(2):
+        pb.k_closest_self(16, device=True, candidates="gram")
+    torch.cuda.synchronize()
+
+
+CASES = {"ray": case_ray, "cfg3_fp64_64": case_cfg3_fp64_64, "gram_knn": case_gram_knn}
 
 
 def peaks():
@@ -310,7 +351,22 @@ def gpu_arm(args, rank, world, local_rank):
 
     extra = {}
     if not args.no_extra:
-        extra = extra_workloads(T, torch, stream, flush, args)
+        # the same rays with the FP64 watertight re-test beside the reference's FP32 verdict (config 1 as specified)
+        T.profiling_reset()
+        T.profiling(True)
+        ms64 = timed_steps(lambda: bvh.ray_structure_intersection_ex(od, dd, precision="fp64"), args.steps,
+                           args.warmup, flush, stream)
+        T.profiling(False)
+        r_ms, r_cnt = T.profiling_read("ray_recheck_kernel")
+        T.profiling_reset()
+        _, i32, _, i64, flags = bvh.ray_structure_intersection_ex(od, dd, precision="fp64")
+        flags = flags.cpu().numpy()
+        extra["ray_fp64_recheck_cfg1"] = {
+            "value": RAYS / (statistics.mean(ms64) / 1e3) / 1e6, "unit": "Mqueries/s",
+            "ms_per_step": statistics.mean(ms64), "kernel_ms": r_ms / max(1, r_cnt),
+            "fp32_verdict_equals_plain": bool(torch.equal(i32, out_i)),
+            "rays_hit_differs": int((flags & 1).sum()), "rays_element_differs": int(((flags & 2) >> 1).sum())}
+        extra.update(extra_workloads(T, torch, stream, flush, args))
 
     line = None
     if rank == 0:
@@ -582,6 +638,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if "RANK" in os.environ else 1)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.case:
+        CASES[args.case]()
+        return
     if args.impl == "reference":
         reference_arm(args, rank, world)
         return
