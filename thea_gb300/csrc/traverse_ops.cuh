@@ -143,11 +143,105 @@ __device__ __forceinline__ int cp_record_index(float4 const * __restrict__ rec, 
   return __float_as_int(__ldg(rec + k * CP_REC_F4 + 5).w);
 }
 
-// FP64 squared distance and closest point of record k. Kept out of line: every caller shares one copy of the long FP64
-// sequence, which matters on a GPU whose FP64 pipe is narrow.
+__device__ __forceinline__ float l1(V3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
+
+// FP64 squared distance and closest point of one closest-point record: the result of closest_point_f64 on the record's
+// vertices, bit for bit, with less FP64 work. The record's FP32 data decide, with error margins, which branch
+// closest_point_f64 takes: whether the plane projection is inside the triangle (then only the normalised normal and the
+// projection are computed), and on the perimeter path, for each edge, whether the segment search clamps to an endpoint
+// (then the endpoint is the result with no square root or division) and whether the edge can be the nearest at all
+// (if its distance provably exceeds another edge's, it is left out: it cannot be the minimum, and ties are only
+// resolved among minima). Every FP64 value that is computed uses closest_point_f64's own operations; where the margins
+// do not decide a branch, closest_point_f64 itself runs. The margins are 2^5 or more times an FP32 rounding bound.
+__device__ __forceinline__ double cp_record_f64_fast(float4 const * __restrict__ r, V3 fp, D3 & out_cp) {
+  float4 a0 = __ldg(r), a1 = __ldg(r + 1), a2 = __ldg(r + 2), a3 = __ldg(r + 3);
+  float4 a4 = __ldg(r + 4), a5 = __ldg(r + 5), a6 = __ldg(r + 6);
+  V3 fv0 = xyz(a0), fv1 = xyz(a1), fv2 = xyz(a2), n32 = xyz(a3);
+  int axis = __float_as_int(a3.w);
+  // region of the plane projection, in FP32: 1 inside, 2 outside, 0 undecided
+  float sd32 = dot(fp, n32) - a0.w;
+  V3 pr = fp - sd32 * n32;
+  float v0i, v0j, v1i, v1j, v2i, v2j, pi, pj;
+  if (axis == 1) {
+    v0i = fv0.z; v0j = fv0.x; v1i = fv1.z; v1j = fv1.x; v2i = fv2.z; v2j = fv2.x; pi = pr.z; pj = pr.x;
+  } else if (axis == 2) {
+    v0i = fv0.x; v0j = fv0.y; v1i = fv1.x; v1j = fv1.y; v2i = fv2.x; v2j = fv2.y; pi = pr.x; pj = pr.y;
+  } else {
+    v0i = fv0.y; v0j = fv0.z; v1i = fv1.y; v1j = fv1.z; v2i = fv2.y; v2j = fv2.z; pi = pr.y; pj = pr.z;
+  }
+  float area = (v1i - v0i) * (v2j - v0j) - (v2i - v0i) * (v1j - v0j);
+  float len[3] = {a1.w, a2.w, a4.w};
+  int region = 0;
+  if (area != 0.f) {
+    float b0 = ((v1i - pi) * (v2j - pj) - (v2i - pi) * (v1j - pj)) / area;
+    float b1 = ((pi - v0i) * (v2j - v0j) - (v2i - v0i) * (pj - v0j)) / area;
+    float b2 = 1.0f - b0 - b1;
+    float S = fmaxf(fmaxf(fmaxf(fabsf(fp.x), fabsf(fp.y)), fabsf(fp.z)),
+                    fmaxf(fmaxf(l1(fv0), l1(fv1)), l1(fv2)));
+    float R = fmaxf(fmaxf(l1(fv0 - pr), l1(fv1 - pr)), l1(fv2 - pr));
+    float L = fmaxf(fmaxf(len[0], len[1]), len[2]);
+    float tau = (1.0f / 4096.0f) + (1.0f / 65536.0f) * (S + R) * (R + L) / fabsf(area);
+    float bmin = fminf(fminf(b0, b1), b2);
+    if (bmin >= tau) region = 1;
+    else if (bmin <= -tau) region = 2;
+  }
+  if (region == 0) return closest_point_f64(fv0, fv1, fv2, fp, out_cp);
+  D3 v0 = todd(fv0), v1 = todd(fv1), v2 = todd(fv2), p = todd(fp);
+  if (region == 1) {
+    D3 n = crossd(v1 - v0, v2 - v0);
+    double z = sqnormd(n);
+    if (z > 0.0) n = n / sqrt(z);
+    double dist = dotd(n, v0);
+    double sd = dotd(p, n) - dist;
+    D3 proj = p - sd * n;
+    out_cp = proj;
+    return sqnormd(proj - p);
+  }
+  // perimeter: edge i runs from vertex i to vertex i + 1
+  V3 fa[3] = {fv0, fv1, fv2}, fb[3] = {fv1, fv2, fv0}, fdir[3] = {xyz(a4), xyz(a5), xyz(a6)};
+  D3 da[3] = {v0, v1, v2}, db[3] = {v1, v2, v0};
+  float q32[3], qerr[3];
+  int kind[3];  // 0: clamps to the edge's start, 1: to its end, 2: undecided (closest_point_f64's segment search)
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    V3 c = fp - fa[i];
+    float t = dot(fdir[i], c);
+    float D = l1(c) + len[i];
+    float dl = (1.0f / 65536.0f) * D;
+    kind[i] = t <= -dl ? 0 : (t >= len[i] + dl ? 1 : 2);
+    V3 rr = t <= 0.f ? fa[i] : (t >= len[i] ? fb[i] : fa[i] + fdir[i] * t);
+    q32[i] = squared_norm(rr - fp);
+    qerr[i] = (1.0f / 16384.0f) * D * D;
+  }
+  float qmin = fminf(fminf(q32[0] + qerr[0], q32[1] + qerr[1]), q32[2] + qerr[2]);
+  double q[3];
+  D3 rr[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rr[i] = da[i];
+    if (q32[i] - qerr[i] > qmin) {
+      q[i] = INFINITY;  // provably farther than another edge
+      continue;
+    }
+    if (kind[i] == 1) {
+      rr[i] = db[i];
+    } else if (kind[i] == 2) {
+      D3 e = db[i] - da[i];
+      double l = sqrt(sqnormd(e));
+      rr[i] = seg_d(da[i], db[i], e / l, l, p);
+    }
+    q[i] = sqnormd(rr[i] - p);
+  }
+  D3 cp;
+  if (q[0] < q[1]) cp = (q[0] < q[2]) ? rr[0] : rr[2];
+  else cp = (q[1] < q[2]) ? rr[1] : rr[2];
+  out_cp = cp;
+  return sqnormd(cp - p);
+}
+
+// Out of line: every caller shares one copy of the FP64 sequence, which matters on a GPU whose FP64 pipe is narrow.
 static __device__ __noinline__ double cp_record_f64_call(float4 const * __restrict__ rec, int64_t k, V3 p, D3 * cp) {
-  float4 const * r = rec + k * CP_REC_F4;
-  return closest_point_f64(xyz(__ldg(r)), xyz(__ldg(r + 1)), xyz(__ldg(r + 2)), p, *cp);
+  return cp_record_f64_fast(rec + k * CP_REC_F4, p, *cp);
 }
 
 __device__ __forceinline__ float cp_record_f64(float4 const * __restrict__ rec, int64_t k, V3 p, D3 & cp, double & d2) {
@@ -617,7 +711,6 @@ struct RaySearch64 {
   int64_t slot;
 };
 
-__device__ __forceinline__ float l1(V3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
 
 __device__ __forceinline__ void ray_f64_take(RaySearch64 & s, int64_t k, int idx, double t64, float max_time) {
   if (!(t64 >= 0.0) || (max_time >= 0.f && t64 > (double)max_time)) return;
