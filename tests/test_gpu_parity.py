@@ -161,6 +161,21 @@ def test_ray_random_sphere_rays(T, oracle):
     assert np.array_equal(host(t), rt.astype(np.float32))
 
 
+@pytest.mark.parametrize("max_time", [-1.0, 1.2])
+def test_ray_large_batches_equal_small_ones(T, max_time):
+    # batches of 65,536 rays or more run on persistent lanes that take a new ray when theirs is done; smaller ones run
+    # one thread per ray: the same traversal, the same results (times, indices, normals)
+    V, F = W.noisy_icosphere(4, 43)
+    o, d = W.random_rays(150000, [-2] * 3, [2] * 3, 44)
+    bvh = T.MeshBvh(dev(V), dev(F))
+    t, idx, nrm = bvh.ray_structure_intersection(dev(o), dev(d), max_time=max_time, normals=True)
+    parts = [bvh.ray_structure_intersection(dev(o[i:i + 50000]), dev(d[i:i + 50000]), max_time=max_time, normals=True)
+             for i in range(0, len(o), 50000)]
+    assert np.array_equal(host(t), np.concatenate([host(p[0]) for p in parts]))
+    assert np.array_equal(host(idx), np.concatenate([host(p[1]) for p in parts]))
+    assert np.array_equal(host(nrm), np.concatenate([host(p[2]) for p in parts]))
+
+
 def test_ray_full_config1_subset(T, oracle):
     V, F, o, d = W.config1()
     assert len(F) == 2093058 and len(o) == 4194304

@@ -5,6 +5,8 @@
 #include "query.hpp"
 #include "traverse_ops.cuh"
 
+#include <algorithm>
+
 namespace thea {
 namespace {
 
@@ -155,6 +157,127 @@ ray_recheck_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __rest
                            out_index64, out_flags, err, order);
 }
 
+// Persistent form of ray_kernel for large batches (FP32 verdict only). Rays that leave the mesh after a few nodes and
+// rays that traverse deep share warps; with one ray per thread the finished lanes idle until their warp's last ray is
+// done. Here each lane takes a new ray as soon as its ray finishes: every loop iteration advances each busy lane by one
+// stack entry, and idle lanes are refilled from a warp-local block of 64 rays (one atomic per block). Results are the
+// same as ray_kernel's: each ray's traversal is the same sequence of steps.
+constexpr int RAY_WARP_BLOCK = 64;
+constexpr int64_t RAY_PERSISTENT_MIN = 1 << 16;
+
+template <int W, int STACK>
+__global__ void __launch_bounds__(QUERY_THREADS)
+ray_persistent_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                      float const * __restrict__ origins, float const * __restrict__ dirs, int64_t n, float max_time,
+                      float * __restrict__ out_time, int32_t * __restrict__ out_index, float * __restrict__ out_normal,
+                      unsigned * __restrict__ err, uint32_t const * __restrict__ order,
+                      unsigned long long * __restrict__ counter) {
+  unsigned const FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  int64_t qb = 0, qe = 0;  // warp-local block of ray ids [qb, qe), warp-uniform
+  bool exhausted = false;  // warp-uniform
+  int64_t q = -1;          // this lane's ray (-1: idle)
+  V3 o = V3{0.f, 0.f, 0.f};
+  float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f;
+  V3 d = V3{0.f, 0.f, 1.f};
+  float best = 0.f;
+  int best_idx = INT_MAX;
+  int64_t best_slot = -1;
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  while (true) {
+    unsigned idle = __ballot_sync(FULL, q < 0);
+    if (idle && !exhausted) {
+      if (qb >= qe) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(counter, (unsigned long long)RAY_WARP_BLOCK);
+        b = __shfl_sync(FULL, b, 0);
+        qb = (int64_t)b;
+        qe = qb + RAY_WARP_BLOCK < n ? qb + RAY_WARP_BLOCK : n;
+        if (qb >= n) exhausted = true;
+      }
+      if (!exhausted) {
+        int rank = __popc(idle & ((1u << lane) - 1));
+        int take = __popc(idle);
+        int64_t avail = qe - qb;
+        if (q < 0 && rank < avail) {
+          q = qb + rank;
+          int64_t r = order ? (int64_t)order[q] : q;
+          q = r;
+          o = load_v3(origins + 3 * r);
+          d = load_v3(dirs + 3 * r);
+          ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
+          iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
+          iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
+          ox = -o.x * ix;
+          oy = -o.y * iy;
+          oz = -o.z * iz;
+          best = max_time >= 0.f ? max_time : INFINITY;
+          best_idx = INT_MAX;
+          best_slot = -1;
+          stk[0] = 0;
+          stkd[0] = 0.f;
+          sp = 1;
+        }
+        qb += take < avail ? take : avail;
+      }
+    }
+    if (__ballot_sync(FULL, q >= 0) == 0) break;
+    if (q < 0) continue;
+    if (sp == 0) {
+      // finished: the same outputs as ray_kernel
+      bool found = best_idx != INT_MAX;
+      out_time[q] = found ? best : -1.f;
+      if (out_index) out_index[q] = found ? best_idx : -1;
+      if (out_normal) {
+        V3 nn = V3{0.f, 0.f, 0.f};
+        if (found) {
+          float4 const * rr = rec + best_slot * RAY_REC_F4;
+          nn = normalized(cross(xyz(__ldg(rr + 1)), xyz(__ldg(rr + 2))));
+        }
+        out_normal[3 * q] = nn.x;
+        out_normal[3 * q + 1] = nn.y;
+        out_normal[3 * q + 2] = nn.z;
+      }
+      q = -1;
+      continue;
+    }
+    --sp;
+    int code = stk[sp];
+    if (stkd[sp] > best * PRUNE_SLACK) continue;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        float tx0 = __fmaf_rn(nd.lox[c], ix, ox), tx1 = __fmaf_rn(nd.hix[c], ix, ox);
+        float ty0 = __fmaf_rn(nd.loy[c], iy, oy), ty1 = __fmaf_rn(nd.hiy[c], iy, oy);
+        float tz0 = __fmaf_rn(nd.loz[c], iz, oz), tz1 = __fmaf_rn(nd.hiz[c], iz, oz);
+        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
+        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
+      }
+      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      for (int64_t k = first; k < first + count; ++k) {
+        float4 const * r = rec + k * RAY_REC_F4;
+        float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+        float t = ray_triangle_time(o, d, xyz(a), xyz(b), xyz(c));
+        int idx = __float_as_int(a.w);
+        if (t >= 0.f && t <= best && (t < best || idx < best_idx)) {
+          best = t;
+          best_idx = idx;
+          best_slot = k;
+        }
+      }
+    }
+  }
+}
+
 //============================================================================================================================
 // k nearest points (BvhN::kClosestPairs + KClosestPairsFunctor + BoundedSortedArrayN; BvhN.hpp:474-500, 1139-1146;
 // BoundedSortedArrayN.hpp:137-214)
@@ -275,6 +398,23 @@ void launch_ray(thea_bvh const * b, float const * o, float const * d, int64_t n,
                 int32_t * idx, float * nrm, float * t64, int32_t * idx64, int32_t * flags, unsigned * err,
                 uint32_t const * order, cudaStream_t s) {
   unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
+  if (!rp.recheck && n >= RAY_PERSISTENT_MIN) {
+    auto k = ray_persistent_kernel<W, STACK>;
+    static int sms = 0;
+    if (!sms) {
+      int dev = 0;
+      THEA_CUDA_CHECK(cudaGetDevice(&dev));
+      THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    int per_sm = 0;
+    THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, QUERY_THREADS, 0));
+    unsigned pgrid = (unsigned)std::min<int64_t>((int64_t)std::max(1, per_sm) * sms, grid);
+    Scratch counter(sizeof(unsigned long long), s);
+    THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
+    THEA_LAUNCH_NAMED("ray_kernel_persistent", k, pgrid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes,
+                      b->ray_rec, o, d, n, rp.max_time, t, idx, nrm, err, order, counter.as<unsigned long long>());
+    return;
+  }
   if (rp.recheck)
     THEA_LAUNCH((ray_recheck_kernel<W, STACK>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->ray_rec,
                 o, d, n, rp.max_time, t, idx, nrm, t64, idx64, flags, err, order);
