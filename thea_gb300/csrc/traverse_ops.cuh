@@ -294,6 +294,26 @@ __device__ __forceinline__ void point_child_bounds(NodeRegs<W> const & nd, V3 p,
     lb[c] = point_box_d2(p.x, p.y, p.z, nd.lox[c], nd.loy[c], nd.loz[c], nd.hix[c], nd.hiy[c], nd.hiz[c]);
 }
 
+// Element tests of one leaf (segment-relative elements [first, first + count)), FP32 reference arithmetic: keeps the
+// smallest (d2, index) with d2 <= best.
+__device__ __forceinline__ void cp_leaf_fp32(float4 const * __restrict__ rec, int64_t elem_base, int first, int count,
+                                             V3 p, float & best, int & best_idx, int64_t & best_slot, V3 & best_cp) {
+  int64_t k0 = elem_base + first;
+  for (int64_t k = k0; k < k0 + count; ++k) {
+    V3 cp;
+    float d2 = cp_record_test(rec, k, p, cp);
+    if (d2 <= best) {
+      int idx = cp_record_index(rec, k);
+      if (d2 < best || idx < best_idx) {
+        best = d2;
+        best_idx = idx;
+        best_cp = cp;
+        best_slot = k;
+      }
+    }
+  }
+}
+
 // FP32 reference-arithmetic search: smallest (d2, index), accepting d2 <= thresh. With budget > 0 the search stops
 // after that many stack pops (done = false), leaving the best found so far.
 template <int W, int STACK>
@@ -329,20 +349,7 @@ __device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restri
     } else {
       int first, count;
       decode_leaf(code, first, count);
-      int64_t k0 = elem_base + first;
-      for (int64_t k = k0; k < k0 + count; ++k) {
-        V3 cp;
-        float d2 = cp_record_test(rec, k, p, cp);
-        if (d2 <= best) {
-          int idx = cp_record_index(rec, k);
-          if (d2 < best || idx < best_idx) {
-            best = d2;
-            best_idx = idx;
-            best_cp = cp;
-            best_slot = k;
-          }
-        }
-      }
+      cp_leaf_fp32(rec, elem_base, first, count, p, best, best_idx, best_slot, best_cp);
     }
   }
   ClosestOut o;
@@ -413,6 +420,62 @@ __device__ __forceinline__ void f64_take(F64Search & s, float4 const * __restric
   }
 }
 
+// Element tests of one leaf for the mixed-precision search: FP32 distances, band limit `lim` and FP32 best `best32`
+// updated, band entries kept in s (an entry pushed out of a full list is evaluated in FP64 at once).
+__device__ __forceinline__ void cp_leaf_f64(float4 const * __restrict__ rec, int64_t elem_base, int first, int count,
+                                            V3 p, double bound2, float abs_tol, float & lim, float & best32,
+                                            F64Search & s) {
+  float const REL = 1.0f + 1.0f / 16384.0f;
+  for (int kr = first; kr < first + count; ++kr) {
+    V3 cp;
+    float d2 = cp_record_test(rec, elem_base + kr, p, cp);
+    if (!(d2 <= lim)) continue;
+    if (d2 < best32) {
+      best32 = d2;
+      float lb1 = sqrtf(best32) * REL + abs_tol;
+      lim = fminf(lim, lb1 * lb1);
+    }
+    // the entry takes a slot that has left the band, else the farthest slot if that is farther than it
+    int slot_j = -1;
+    float worst = d2;
+#pragma unroll
+    for (int j = 0; j < F64_CAND; ++j)
+      if (slot_j < 0 && !(s.cand_k[j] >= 0 && s.cand_d[j] <= lim)) slot_j = j;
+    if (slot_j < 0) {
+#pragma unroll
+      for (int j = 0; j < F64_CAND; ++j)
+        if (s.cand_d[j] > worst) { worst = s.cand_d[j]; slot_j = j; }
+    }
+    int evict = slot_j < 0 ? kr : -1;
+#pragma unroll
+    for (int j = 0; j < F64_CAND; ++j) {
+      if (j == slot_j) {
+        if (s.cand_k[j] >= 0 && s.cand_d[j] <= lim) evict = s.cand_k[j];
+        s.cand_d[j] = d2;
+        s.cand_k[j] = kr;
+      }
+    }
+    if (evict >= 0) {
+      // more band entries than slots (rare): this one is evaluated by the lane alone
+      D3 c64;
+      double d64 = cp_record_f64_call(rec, elem_base + evict, p, &c64);
+      f64_take(s, rec, elem_base + evict, d64, (float)c64.x, (float)c64.y, (float)c64.z, bound2);
+    }
+  }
+}
+
+// Band limit before any element is seen: from the distance bound (or +inf), and the band's absolute term
+__device__ __forceinline__ float f64_band_start(double bound2, float scale, float & abs_tol) {
+  float const REL = 1.0f + 1.0f / 16384.0f;
+  abs_tol = scale * (1.0f / 262144.0f);
+  float lim = bound2 >= 0.0 ? __double2float_ru(bound2) : INFINITY;
+  if (bound2 >= 0.0) {
+    float lb0 = sqrtf(lim) * REL + abs_tol;
+    lim = lb0 * lb0;
+  }
+  return lim;
+}
+
 template <int W, int STACK>
 __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restrict__ nodes,
                                                    float4 const * __restrict__ rec, int root, int64_t elem_base, V3 p,
@@ -420,13 +483,8 @@ __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restric
                                                    int budget = 0) {
   f64_search_init(s);
   int pops = 0;
-  float const REL = 1.0f + 1.0f / 16384.0f;
-  float abs_tol = scale * (1.0f / 262144.0f);
-  float lim = bound2 >= 0.0 ? __double2float_ru(bound2) : INFINITY;
-  if (bound2 >= 0.0) {
-    float lb0 = sqrtf(lim) * REL + abs_tol;
-    lim = lb0 * lb0;
-  }
+  float abs_tol;
+  float lim = f64_band_start(bound2, scale, abs_tol);
   float best32 = INFINITY;
   int stk[STACK];
   float stkd[STACK];
@@ -451,42 +509,7 @@ __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restric
     } else {
       int first, count;
       decode_leaf(code, first, count);
-      for (int kr = first; kr < first + count; ++kr) {
-        V3 cp;
-        float d2 = cp_record_test(rec, elem_base + kr, p, cp);
-        if (!(d2 <= lim)) continue;
-        if (d2 < best32) {
-          best32 = d2;
-          float lb1 = sqrtf(best32) * REL + abs_tol;
-          lim = fminf(lim, lb1 * lb1);
-        }
-        // the entry takes a slot that has left the band, else the farthest slot if that is farther than it
-        int slot_j = -1;
-        float worst = d2;
-#pragma unroll
-        for (int j = 0; j < F64_CAND; ++j)
-          if (slot_j < 0 && !(s.cand_k[j] >= 0 && s.cand_d[j] <= lim)) slot_j = j;
-        if (slot_j < 0) {
-#pragma unroll
-          for (int j = 0; j < F64_CAND; ++j)
-            if (s.cand_d[j] > worst) { worst = s.cand_d[j]; slot_j = j; }
-        }
-        int evict = slot_j < 0 ? kr : -1;
-#pragma unroll
-        for (int j = 0; j < F64_CAND; ++j) {
-          if (j == slot_j) {
-            if (s.cand_k[j] >= 0 && s.cand_d[j] <= lim) evict = s.cand_k[j];
-            s.cand_d[j] = d2;
-            s.cand_k[j] = kr;
-          }
-        }
-        if (evict >= 0) {
-          // more band entries than slots (rare): this one is evaluated by the lane alone
-          D3 c64;
-          double d64 = cp_record_f64_call(rec, elem_base + evict, p, &c64);
-          f64_take(s, rec, elem_base + evict, d64, (float)c64.x, (float)c64.y, (float)c64.z, bound2);
-        }
-      }
+      cp_leaf_f64(rec, elem_base, first, count, p, bound2, abs_tol, lim, best32, s);
     }
   }
   s.lim = lim;
