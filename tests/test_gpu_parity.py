@@ -227,6 +227,25 @@ def test_sampler_bit_exact_with_reference_stream(T, golden_dir, oracle):
     assert np.array_equal(p2, rp) and np.array_equal(f2, rf) and np.array_equal(n2, rn)
 
 
+def test_sampler_areas_spanning_many_binades(T, oracle):
+    # triangles from 1e-12 to 1e+6 in area: the cumulative FP64 sum rounds, so the parallel exact sum must hand over to
+    # the sequential one; both sample streams stay bit-identical to the oracle
+    rng = np.random.default_rng(8)
+    tris = []
+    for s in 10.0 ** rng.uniform(-6, 3, 3000):
+        c = rng.uniform(-100, 100, 3)
+        tris.append(c + s * rng.normal(size=(3, 3)))
+    V = np.concatenate(tris).astype(np.float32)
+    F = np.arange(len(V), dtype=np.int32).reshape(-1, 3)
+    for rng_mode in ("thea", "counter"):
+        p, n, f = T.sample_evenly_by_area(V, F, 50000, 13, rng=rng_mode)
+        if rng_mode == "thea":
+            rp, rn, rf = oracle.sample_by_area(V, F, 50000, 13)
+            assert np.array_equal(p, rp) and np.array_equal(f, rf) and np.array_equal(n, rn)
+        else:
+            assert len(p) == 50000 and np.all(f >= 0)
+
+
 def test_sampler_counter_mode_distribution(T, oracle):
     V, F = W.noisy_icosphere(2, 61)
     p, n, f = T.sample_evenly_by_area(V, F, 200000, 5, rng="counter")

@@ -13,6 +13,7 @@
 #include "device_util.cuh"
 #include "query.hpp"
 
+#include <climits>
 #include <mutex>
 #include <string>
 
@@ -106,6 +107,138 @@ __global__ void serial_cdf_kernel(float const * __restrict__ area, int64_t nf, d
     for (int j = threadIdx.x; j < m; j += blockDim.x) cum[base + j] = c[j];
     __syncthreads();
   }
+}
+
+// Parallel form of the same cumulative sum. A sum of FP32 values in an FP64 accumulator does not round as long as every
+// running total fits in 53 significant bits, which holds for any mesh whose triangle areas are within a factor 2^29 of
+// each other up to its size (each area has 24 significant bits, and the running total stays below 2^29 times the
+// smallest of them). Then cum[i] is the exact prefix sum, which a parallel scan of the areas as 128-bit fixed-point
+// integers (units of the smallest area's last bit) computes exactly. Every prefix is checked for exact representability
+// in FP64; if one is not (areas spanning too many binades), the caller runs serial_cdf_kernel instead, so the result
+// is always the sequential one bit for bit.
+struct U128 {
+  uint64_t lo, hi;
+  U128() = default;
+  __host__ __device__ constexpr U128(int v) : lo((uint64_t)(int64_t)v), hi(v < 0 ? ~0ull : 0ull) {}
+};
+__device__ __forceinline__ U128 operator+(U128 a, U128 b) {
+  U128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+  return r;
+}
+__device__ __forceinline__ U128 operator-(U128 a, U128 b) {
+  U128 r;
+  r.lo = a.lo - b.lo;
+  r.hi = a.hi - b.hi - (a.lo < b.lo ? 1ull : 0ull);
+  return r;
+}
+__device__ __forceinline__ U128 & operator+=(U128 & a, U128 b) { return a = a + b; }
+__device__ __forceinline__ U128 __shfl_up_sync(unsigned mask, U128 v, unsigned d) {
+  v.lo = ::__shfl_up_sync(mask, v.lo, d);
+  v.hi = ::__shfl_up_sync(mask, v.hi, d);
+  return v;
+}
+
+// a = m * 2^e exactly (a >= 0 finite)
+__device__ __forceinline__ void float_parts(float a, uint32_t & m, int & e) {
+  uint32_t b = __float_as_uint(a);
+  uint32_t ex = (b >> 23) & 0xffu, mt = b & 0x7fffffu;
+  if (ex == 0) {
+    m = mt;
+    e = -149;
+  } else {
+    m = mt | 0x800000u;
+    e = (int)ex - 150;
+  }
+}
+
+// st[0] = smallest exponent of a nonzero area, st[1] = largest, st[2] = 1 if an area is negative, infinite or NaN
+__global__ void cdf_init_kernel(int * st) {
+  st[0] = INT_MAX;
+  st[1] = INT_MIN;
+  st[2] = 0;
+}
+
+__global__ void cdf_range_kernel(float const * __restrict__ area, int64_t nf, int * st) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int lo = INT_MAX, hi = INT_MIN, bad = 0;
+  if (i < nf) {
+    float a = area[i];
+    if (!(a >= 0.f) || isinf(a)) {
+      bad = 1;
+    } else if (a > 0.f) {
+      uint32_t m;
+      int e;
+      float_parts(a, m, e);
+      lo = hi = e;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (lo != INT_MAX) atomicMin(st, lo);
+    if (hi != INT_MIN) atomicMax(st + 1, hi);
+    if (bad) atomicOr(st + 2, 1);
+  }
+}
+
+// Largest spread of exponents for which 2^24-bit areas and up to 2^31 of them sum within 127 bits
+constexpr int CDF_MAX_SPREAD = 127 - 24 - 31;
+
+__global__ void cdf_fixed_kernel(float const * __restrict__ area, int64_t nf, int const * __restrict__ st,
+                                 U128 * __restrict__ v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  U128 r(0);
+  int emin = st[0];
+  if (!st[2] && st[1] - emin <= CDF_MAX_SPREAD) {
+    float a = area[i];
+    if (a > 0.f) {
+      uint32_t m;
+      int e;
+      float_parts(a, m, e);
+      int sh = e - emin;  // 0..CDF_MAX_SPREAD
+      if (sh < 64) {
+        r.lo = (uint64_t)m << sh;
+        r.hi = sh == 0 ? 0ull : (uint64_t)m >> (64 - sh);
+      } else {
+        r.lo = 0;
+        r.hi = (uint64_t)m << (sh - 64);
+      }
+    }
+  }
+  v[i] = r;
+}
+
+// cum[i] = (excl[i] + v[i]) * 2^emin, exactly; st[2] set if some total has more than 53 significant bits
+__global__ void cdf_convert_kernel(U128 const * __restrict__ excl, U128 const * __restrict__ v, int64_t nf, int * st,
+                                   double * __restrict__ cum) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  if (st[2] || st[1] - st[0] > CDF_MAX_SPREAD) {
+    if (i == 0) st[2] = 1;
+    return;
+  }
+  U128 x = excl[i] + v[i];
+  if (x.lo == 0 && x.hi == 0) {
+    cum[i] = 0.0;
+    return;
+  }
+  int tz = x.lo ? __ffsll((long long)x.lo) - 1 : 64 + __ffsll((long long)x.hi) - 1;
+  int bl = x.hi ? 128 - __clzll((long long)x.hi) : 64 - __clzll((long long)x.lo);
+  if (bl - tz > 53) {
+    atomicOr(st + 2, 1);
+    return;
+  }
+  uint64_t mant;
+  if (tz >= 64) mant = x.hi >> (tz - 64);
+  else if (tz == 0) mant = x.lo;
+  else mant = (x.lo >> tz) | (x.hi << (64 - tz));
+  cum[i] = ldexp((double)mant, tz + st[0]);
 }
 
 // Philox-4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3", SC'11)
@@ -321,7 +454,21 @@ int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64
   Scratch area((size_t)nf * sizeof(float), s);
   Scratch cum((size_t)nf * sizeof(double), s);
   THEA_LAUNCH(tri_area_kernel, (unsigned)ceil_div(nf, 256), 256, 0, s, V, F, nf, area.as<float>());
-  THEA_LAUNCH(serial_cdf_kernel, 1, 256, 0, s, area.as<float>(), nf, cum.as<double>());
+  {
+    // exact parallel cumulative areas; the serial kernel where they would not be exact
+    Scratch st(4 * sizeof(int), s), fixed((size_t)nf * sizeof(U128), s), excl((size_t)nf * sizeof(U128), s);
+    unsigned g = (unsigned)ceil_div(nf, 256);
+    THEA_LAUNCH(cdf_init_kernel, 1, 1, 0, s, st.as<int>());
+    THEA_LAUNCH(cdf_range_kernel, g, 256, 0, s, area.as<float>(), nf, st.as<int>());
+    THEA_LAUNCH(cdf_fixed_kernel, g, 256, 0, s, area.as<float>(), nf, st.as<int>(), fixed.as<U128>());
+    exclusive_scan<U128>(fixed.as<U128>(), excl.as<U128>(), nf, s);
+    THEA_LAUNCH(cdf_convert_kernel, g, 256, 0, s, excl.as<U128>(), fixed.as<U128>(), nf, st.as<int>(),
+                cum.as<double>());
+    int flag = 0;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&flag, st.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (flag) THEA_LAUNCH(serial_cdf_kernel, 1, 256, 0, s, area.as<float>(), nf, cum.as<double>());
+  }
   double total = 0.0;
   THEA_CUDA_CHECK(cudaMemcpyAsync(&total, cum.as<double>() + nf - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
   THEA_CUDA_CHECK(cudaStreamSynchronize(s));
