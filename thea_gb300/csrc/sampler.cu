@@ -40,38 +40,40 @@ __device__ __forceinline__ uint32_t mt_temper(uint32_t r) {
 
 // Writes `count` tempered words of Random(seed): Random::Random(seed) then bits() repeatedly.
 __global__ void __launch_bounds__(MT_THREADS) thea_mt_stream_kernel(uint32_t seed, int64_t count, uint32_t * __restrict__ out) {
-  __shared__ uint32_t s[MT_N];
+  // The twisted state is written to the other half of a ping-pong buffer, so each phase needs one barrier (its inputs
+  // are the old state and the new words of the phase before), not two. One word per thread and phase: the twist is a
+  // chain of three dependent phases, and their latency is the cost (a single warp with eight words per lane and
+  // phase measured 4.6x slower).
+  __shared__ uint32_t buf[2][MT_N];
   int t = threadIdx.x;
   if (t == 0) {
-    s[0] = seed;
-    for (int i = 1; i < MT_N; ++i) s[i] = 1812433253u * (s[i - 1] ^ (s[i - 1] >> 30)) + (uint32_t)i;
+    buf[0][0] = seed;
+    for (int i = 1; i < MT_N; ++i) buf[0][i] = 1812433253u * (buf[0][i - 1] ^ (buf[0][i - 1] >> 30)) + (uint32_t)i;
   }
   __syncthreads();
   int64_t twists = ceil_div(count, MT_N);
+  int cur = 0;
   for (int64_t k = 0; k < twists; ++k) {
-    uint32_t v;
-    // phase A: i in [0, N - M): uses old words i, i + 1, i + M
-    if (t < MT_N - MT_M) v = mt_mix(s[t], s[t + 1], s[t + MT_M]);
+    uint32_t const * X = buf[cur];
+    uint32_t * Y = buf[cur ^ 1];
+    // phase A: i in [0, N - M) from old words i, i + 1, i + M; word N - M is left as it is by Thea's twist
+    if (t < MT_N - MT_M) Y[t] = mt_mix(X[t], X[t + 1], X[t + MT_M]);
+    if (t == 0) Y[MT_N - MT_M] = X[MT_N - MT_M];
     __syncthreads();
-    if (t < MT_N - MT_M) s[t] = v;
-    __syncthreads();
-    // phase B: i in [N - M + 1, 2 (N - M)): uses new word i - (N - M) and old words i, i + 1
+    // phase B: i in [N - M + 1, 2 (N - M)) from old words i, i + 1 and new word i - (N - M)
     int i = MT_N - MT_M + 1 + t;
-    if (i < 2 * (MT_N - MT_M)) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
+    if (i < 2 * (MT_N - MT_M)) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
     __syncthreads();
-    if (i < 2 * (MT_N - MT_M)) s[i] = v;
-    __syncthreads();
-    // phase C: i in [2 (N - M), N - 1) and i = N - 1 (which pairs old word N - 1 with new word 0 and new word M - 1)
+    // phase C: i in [2 (N - M), N - 1), and i = N - 1 (old word N - 1 with new words 0 and M - 1)
     i = 2 * (MT_N - MT_M) + t;
-    if (i < MT_N - 1) v = mt_mix(s[i], s[i + 1], s[i - (MT_N - MT_M)]);
-    else if (i == MT_N - 1) v = mt_mix(s[MT_N - 1], s[0], s[MT_M - 1]);
-    __syncthreads();
-    if (i < MT_N) s[i] = v;
+    if (i < MT_N - 1) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
+    else if (i == MT_N - 1) Y[i] = mt_mix(X[MT_N - 1], Y[0], Y[MT_M - 1]);
     __syncthreads();
     int64_t base = k * MT_N;
     for (int j = t; j < MT_N; j += MT_THREADS)
-      if (base + j < count) out[base + j] = mt_temper(s[j]);
-    // the next twist's phase A only reads s, and its first write follows a barrier
+      if (base + j < count) out[base + j] = mt_temper(Y[j]);
+    // the next twist reads Y and writes the other buffer, whose last readers finished before the barrier above
+    cur ^= 1;
   }
 }
 
