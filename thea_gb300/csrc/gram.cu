@@ -2,8 +2,8 @@
 // bounded by the re-ranked k-th distance.
 //
 // Points are taken in the point BVH's leaf order (a Morton order), so a block of 128 consecutive points and the 512
-// points around it are spatial neighbours. One CTA scores its 128 query points against that 512-point window with two
-// tcgen05.mma (M = 128, N = 256, K = 16, FP16 operands, FP32 accumulators in tensor memory):
+// points around it are spatial neighbours. One CTA scores its 128 query points against that 512-point window with four
+// tcgen05.mma (M = 128, N = 128, K = 16, FP16 operands, FP32 accumulators in tensor memory):
 //   A row r = (a_r, 1, 0, ...)          B row j = (-2 b_j, |b_j|^2, 0, ...)        (A B^T)[r][j] = |b_j|^2 - 2 a_r . b_j
 // with coordinates taken relative to the block's first point and scaled to the window's extent. Per row that is
 // |a_r - b_j|^2 - |a_r|^2, so the row's order of the keys is the order of the squared distances (up to FP16 rounding).
@@ -28,12 +28,12 @@ namespace thea {
 namespace {
 
 constexpr int GRAM_M = 128;      // query rows per CTA (tensor-memory lanes)
-constexpr int GRAM_N = 256;      // candidates per MMA
-constexpr int GRAM_PASSES = 2;
+constexpr int GRAM_N = 128;      // candidates per MMA
+constexpr int GRAM_PASSES = 4;
 constexpr int GRAM_WINDOW = GRAM_N * GRAM_PASSES;
 constexpr int GRAM_K = 16;       // K of one f16 MMA; coordinates use 4 of it
 constexpr int GRAM_THREADS = 128;
-constexpr uint32_t GRAM_TMEM_COLS = 256;
+constexpr uint32_t GRAM_TMEM_COLS = 128;
 constexpr int GRAM_SPIN_LIMIT = 1 << 20;  // try_wait rounds before a wait is declared failed
 
 // Operand tiles in the no-swizzle K-major core-matrix layout: 8 rows x 16 bytes per core matrix (128 B contiguous), the
@@ -389,14 +389,14 @@ bool gram_supported(int64_t n) { return n >= GRAM_WINDOW; }
 void run_gram_bounds(thea_bvh const * b, int k, float * bound, cudaStream_t s) {
   int64_t n = b->n;
   float4 const * pts = b->pt_rec;
-  // two CTAs per SM: each holds half of the SM's tensor memory (256 of 512 columns) for its whole life
+  // four CTAs per SM: each holds a quarter of the SM's tensor memory (128 of 512 columns) for its whole life
   static int sms = 0;
   if (!sms) {
     int dev = 0;
     THEA_CUDA_CHECK(cudaGetDevice(&dev));
     THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  int blocks = (int)std::min<int64_t>(ceil_div(n, GRAM_M), 2 * (int64_t)sms);
+  int blocks = (int)std::min<int64_t>(ceil_div(n, GRAM_M), 4 * (int64_t)sms);
   Scratch counter(sizeof(unsigned long long), s);
   THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
   unsigned long long * next = counter.as<unsigned long long>();
