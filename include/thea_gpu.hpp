@@ -105,6 +105,22 @@ class MeshBvh : public BvhHandle {
   }
 
   // BvhN::rayIntersectionTime<RayIntersectionTester>(ray, max_time), batched.
+  // closestElement with a precision mode (THEA_PRECISION_*) and the per-query |distance - FP64 distance| (nullable)
+  void closestElementEx(float const * queries, int64_t n, int32_t precision, int32_t * indices,
+                        float * distances = nullptr, float * closest_points = nullptr, float * errors = nullptr,
+                        double dist_bound = -1, void * stream = nullptr) const {
+    check(thea_closest_element_ex(h_, queries, n, (float)dist_bound, precision, indices, distances, closest_points,
+                                  errors, stream));
+  }
+
+  // rayStructureIntersection with the FP64 watertight verdict beside the reference's FP32 one (flags: THEA_RAY_FLAG_*)
+  void rayStructureIntersectionEx(float const * origins, float const * directions, int64_t n, float * times,
+                                  int32_t * indices, float * times_fp64, int32_t * indices_fp64, int32_t * flags,
+                                  float max_time = -1, void * stream = nullptr) const {
+    check(thea_ray_intersection_ex(h_, origins, directions, n, max_time, THEA_PRECISION_FP64_RECHECK, times, indices,
+                                   nullptr, times_fp64, indices_fp64, flags, stream));
+  }
+
   void rayIntersectionTime(float const * origins, float const * directions, int64_t n, float * times,
                            float max_time = -1, void * stream = nullptr) const {
     check(thea_ray_intersection(h_, origins, directions, n, max_time, times, nullptr, nullptr, stream));
@@ -132,6 +148,114 @@ class PointBvh : public BvhHandle {
   void kClosestSelf(int32_t k, int32_t * indices, float * sq_distances, void * stream = nullptr) const {
     check(thea_k_closest_self(h_, k, indices, sq_distances, stream));
   }
+
+  // The same graph with a choice of candidate generation (THEA_KNN_CANDIDATES_*); results are identical.
+  void kClosestSelf(int32_t k, int32_t candidates, int32_t * indices, float * sq_distances,
+                    void * stream = nullptr) const {
+    check(thea_k_closest_self_ex(h_, k, candidates, indices, sq_distances, stream));
+  }
+};
+
+// Many meshes (or point sets) in one structure, queried in one persistent launch. Faces index the shared vertex array;
+// mesh m owns faces [mesh_face_offsets[m], mesh_face_offsets[m + 1]) (host array, num_meshes + 1 entries). Queries
+// are grouped by mesh through device-resident query_offsets.
+class MeshForest : public BvhHandle {
+ public:
+  MeshForest(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t const * mesh_face_offsets,
+             int32_t num_meshes, BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
+    thea_build_config c = opt.config();
+    check(thea_mesh_forest_build(vertices, num_vertices, faces, mesh_face_offsets, num_meshes, &c, stream, &h_));
+  }
+
+  // hard_query_budget: 0 = default two-phase search, negative = one thread per query throughout
+  void batchClosestElement(float const * queries, int64_t const * query_offsets, int64_t n, int32_t * indices,
+                           float * distances = nullptr, float * closest_points = nullptr, float * errors = nullptr,
+                           int32_t precision = THEA_PRECISION_FP32_REFERENCE, double dist_bound = -1,
+                           int32_t queries_per_warp = 0, int32_t hard_query_budget = 0,
+                           void * stream = nullptr) const {
+    check(thea_batch_closest_element(h_, queries, query_offsets, n, (float)dist_bound, precision, queries_per_warp,
+                                     hard_query_budget, indices, distances, closest_points, errors, stream));
+  }
+
+  void batchRayIntersection(float const * origins, float const * directions, int64_t const * query_offsets, int64_t n,
+                            float * times, int32_t * indices = nullptr, float max_time = -1,
+                            int32_t queries_per_warp = 0, void * stream = nullptr) const {
+    check(thea_batch_ray_intersection(h_, origins, directions, query_offsets, n, max_time, queries_per_warp, times,
+                                      indices, stream));
+  }
+};
+
+class PointForest : public BvhHandle {
+ public:
+  PointForest(float const * points, int64_t const * set_offsets, int32_t num_sets,
+              BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
+    thea_build_config c = opt.config();
+    check(thea_point_forest_build(points, set_offsets, num_sets, &c, stream, &h_));
+  }
+
+  void batchKClosest(float const * queries, int64_t const * query_offsets, int64_t n, int32_t k, int32_t * indices,
+                     float * sq_distances, double dist_bound = -1, int32_t queries_per_warp = 0,
+                     void * stream = nullptr) const {
+    check(thea_batch_k_closest(h_, queries, query_offsets, n, k, (float)dist_bound, queries_per_warp, indices,
+                               sq_distances, stream));
+  }
+};
+
+// CUDA-graph capture of asynchronous (device-array) calls on one stream, replayed with launch().
+class Graph {
+ public:
+  explicit Graph(void * stream) : stream_(stream) { check(thea_graph_capture_begin(stream)); }
+  Graph(Graph const &) = delete;
+  Graph & operator=(Graph const &) = delete;
+  void end() { check(thea_graph_capture_end(stream_, &g_)); }
+  void launch(void * stream) const { check(thea_graph_launch(g_, stream)); }
+  ~Graph() {
+    if (g_) thea_graph_destroy(g_);
+  }
+
+ private:
+  void * stream_;
+  thea_graph * g_ = nullptr;
+};
+
+// The serving loop (thea_server_*): resident meshes, memory-budget admission, continuous batching.
+class Server {
+ public:
+  explicit Server(thea_server_config const & config) { check(thea_server_create(&config, &s_)); }
+  Server(Server const &) = delete;
+  Server & operator=(Server const &) = delete;
+  ~Server() {
+    if (s_) thea_server_destroy(s_);
+  }
+
+  int32_t addMesh(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t num_faces) {
+    int32_t id = -1;
+    check(thea_server_add_mesh(s_, vertices, num_vertices, faces, num_faces, &id));
+    return id;
+  }
+  void removeMesh(int32_t mesh) { check(thea_server_remove_mesh(s_, mesh)); }
+  uint64_t submit(thea_request const & request) {
+    uint64_t t = 0;
+    check(thea_server_submit(s_, &request, &t));
+    return t;
+  }
+  // true when the request ended (its outcome in *request_status); false if timeout_us passed first
+  bool wait(uint64_t ticket, thea_status * request_status = nullptr, double * latency_ms = nullptr,
+            int64_t timeout_us = -1) {
+    thea_status r = thea_server_wait(s_, ticket, timeout_us, request_status, latency_ms);
+    if (r == THEA_ERR_WAIT_TIMEOUT) return false;
+    check(r);
+    return true;
+  }
+  void cancel(uint64_t ticket) { check(thea_server_cancel(s_, ticket)); }
+  thea_server_stats stats() const {
+    thea_server_stats st{};
+    check(thea_server_get_stats(s_, &st));
+    return st;
+  }
+
+ private:
+  thea_server * s_ = nullptr;
 };
 
 // MeshSampler::sampleEvenlyByArea (EXACT count mode), drawing from Random(seed).

@@ -15,6 +15,39 @@ int main(int argc, char ** argv) {
   } catch (thea_gpu::Exception const & e) {
     if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 3;
   }
+  // the serving wrapper on the test executor (no CUDA call): admission, submit, wait, stats
+  {
+    thea_server_config cfg{};
+    cfg.test_executor = 1;
+    cfg.test_ns_per_query = 100;
+    thea_gpu::Server server(cfg);
+    float sv[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+    int32_t sf[] = {0, 1, 2, 0, 1, 3, 0, 2, 3, 1, 2, 3};
+    int32_t mesh = server.addMesh(sv, 4, sf, 4);
+    float q[30] = {0};
+    int32_t idx[80];
+    float val[80];
+    thea_request r{};
+    r.type = THEA_REQUEST_KNN;
+    r.mesh = mesh;
+    r.num_queries = 10;
+    r.queries = q;
+    r.k = 8;
+    r.out_index = idx;
+    r.out_value = val;
+    uint64_t t = server.submit(r);
+    thea_status st = THEA_ERR_INTERNAL;
+    double ms = -1;
+    if (!server.wait(t, &st, &ms) || st != THEA_OK || ms < 0) return 7;
+    thea_server_stats s = server.stats();
+    if (s.completed != 1 || s.queries_completed != 10 || s.resident_meshes != 1) return 8;
+    try {
+      server.submit(thea_request{});
+      return 9;  // must have thrown
+    } catch (thea_gpu::Exception const & e) {
+      if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 10;
+    }
+  }
   if (no_device) return 0;
 
   float V[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
