@@ -248,6 +248,17 @@ THEA_API thea_status thea_autotune_batch_closest(const float * vertices, int64_t
                                                  int64_t num_queries, int32_t precision, void * stream,
                                                  thea_tuning * out_tuning);
 
+/* All points within `radius` of each query, inclusive (squared FP32 distance <= radius * radius, as BallN::contains):
+ * replaces BvhN::rangeQueryIndices / processRange with a Ball3 range (BvhN.hpp:1208-1219, 2118-2171), the query behind
+ * PointSet3's proximity graph. Output is a CSR list in two calls. Call 1, with out_index == NULL: writes out_offsets
+ * (num_queries + 1 entries; out_offsets[num_queries] = total). Call 2, with the same queries, radius and exclusions and
+ * the offsets of call 1: writes out_index (total entries; query q's neighbours in [out_offsets[q], out_offsets[q + 1]),
+ * in ascending element index) and, if not NULL, out_sq_distance. exclude_index (nullable): per-query element to skip.
+ * All arrays are device memory. Call 2 synchronizes the stream (it reads the total). */
+THEA_API thea_status thea_radius_neighbors(const thea_bvh * point_bvh, const float * queries, int64_t num_queries,
+                                           float radius, const int32_t * exclude_index, int64_t * out_offsets,
+                                           int32_t * out_index, float * out_sq_distance, void * stream);
+
 /* ---- tensor-core k-NN candidates ----------------------------------------------------------------------------------- */
 
 #define THEA_KNN_CANDIDATES_TRAVERSAL 0  /* best-first BVH traversal from an unbounded start (thea_k_closest_self) */

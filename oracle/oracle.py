@@ -56,6 +56,10 @@ def lib():
         for name in ("oracle_knn_ref", "oracle_knn_contract"):
             getattr(L, name).argtypes = [_vp, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
                                          ctypes.c_int]
+        L.oracle_range_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_float, _i32p,
+                                         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), _i32p, _f32p,
+                                         ctypes.c_int]
+        L.oracle_range_brute.restype = None
         L.oracle_knn_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
                                        ctypes.c_int, ctypes.c_int]
         L.oracle_sample_by_area.restype = _i64
@@ -224,6 +228,25 @@ def knn_brute(P, q, k, dist_bound=-1.0, exclude=None, fp64=False, threads=None):
     lib().oracle_knn_brute(_p(P, _f32p), len(P), _p(q, _f32p), n, int(k), float(dist_bound), _p(ex, _i32p),
                            _p(idx, _i32p), _p(d2, _f64p), int(fp64), threads or default_threads())
     return idx, d2
+
+
+def range_brute(P, q, radius, exclude=None, threads=None):
+    """Every point within `radius` (inclusive, FP32) of each query, by brute force: CSR (offsets, indices, d2)."""
+    P = _f32(P).reshape(-1, 3)
+    q = _f32(q).reshape(-1, 3)
+    n = len(q)
+    ex = None if exclude is None else _i32(exclude)
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    counts = np.zeros(n, np.int64)
+    lib().oracle_range_brute(_p(P, _f32p), len(P), _p(q, _f32p), n, float(radius), _p(ex, _i32p), _p(counts, i64p),
+                             None, None, None, threads or default_threads())
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    idx = np.empty(int(off[-1]), np.int32)
+    d2 = np.empty(int(off[-1]), np.float32)
+    if len(idx):
+        lib().oracle_range_brute(_p(P, _f32p), len(P), _p(q, _f32p), n, float(radius), _p(ex, _i32p), None,
+                                 _p(off, i64p), _p(idx, _i32p), _p(d2, _f32p), threads or default_threads())
+    return off, idx, d2
 
 
 def sample_by_area(V, F, n, seed):

@@ -286,6 +286,32 @@ static void knnBruteImpl(float const * P, int64_t np, float const * q, int64_t n
 }
 }  // extern "C++"
 
+// Points within a ball (BallN::contains, BallN.hpp:83: (p - center).squaredNorm() <= radius * radius in FP32), as
+// used by BvhN::rangeQueryIndices (BvhN.hpp:1208-1219). Pass 1 (idx == nullptr): counts[i]. Pass 2: fills query i's
+// neighbours in ascending index at offsets[i].
+void oracle_range_brute(float const * P, int64_t np, float const * q, int64_t n, float radius, int32_t const * exclude,
+                        int64_t * counts, int64_t const * offsets, int32_t * idx, float * d2, int nthreads) {
+  float r2 = radius * radius;
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      V3<float> c = q3<float>(q, i);
+      int64_t w = idx ? offsets[i] : 0, cnt = 0;
+      for (int64_t j = 0; j < np; ++j) {
+        if (exclude && exclude[i] == j) continue;
+        float dd = squaredNorm(q3<float>(P, j) - c);
+        if (dd <= r2) {
+          if (idx) {
+            idx[w + cnt] = (int32_t)j;
+            d2[w + cnt] = dd;
+          }
+          ++cnt;
+        }
+      }
+      if (!idx) counts[i] = cnt;
+    }
+  });
+}
+
 void oracle_knn_brute(float const * P, int64_t np, float const * q, int64_t n, int k, double dist_bound,
                       int32_t const * exclude, int32_t * idx, double * d2, int fp64, int nthreads) {
   if (fp64) knnBruteImpl<double>(P, np, q, n, k, dist_bound, exclude, idx, d2, nthreads);

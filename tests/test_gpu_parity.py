@@ -336,3 +336,42 @@ def test_reference_testbvh_scenario(T, golden_dir):
     t, i, n = tb.ray_structure_intersection(np.zeros((1, 3), np.float32), z["ray_dir"][None], normals=True)
     assert np.array_equal(i, z["ray_index"]) and np.array_equal(t, z["ray_time"])
     assert np.array_equal(n, z["ref_ray_normal"])
+
+
+def test_cpp_wrapper_on_device(T):
+    # the header-only C++ wrapper drives the library end to end: closest point, ray, k-NN on a tetrahedron
+    import subprocess
+    from tests.conftest import ROOT
+    src = os.path.join(ROOT, "tests", "cpp", "wrapper_compile.cpp")
+    out = os.path.join(ROOT, "tests", "cpp", "_build", "wrapper_device")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), src, "-o", out,
+                        "-L", os.path.join(ROOT, "thea_gb300", "_lib"), "-lthea_gpu",
+                        "-Wl,-rpath," + os.path.join(ROOT, "thea_gb300", "_lib")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([out], capture_output=True, text=True)
+    assert r.returncode == 0 and "wrapper ok" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("radius", [0.0, 0.03, 0.12])
+def test_radius_neighbors_equal_brute_force(T, oracle, radius):
+    import torch
+    P = W.uniform_box_points(20000, [0] * 3, [1] * 3, 81)
+    P[1000:1040] = P[7]  # duplicates: zero distances
+    Q = np.concatenate([P[:3000], W.uniform_box_points(2000, [-0.2] * 3, [1.2] * 3, 82)])
+    ex = np.concatenate([np.arange(1500, dtype=np.int32), -np.ones(3500, np.int32)])
+    pb = T.PointBvh(dev(P), max_leaf_size=4)
+    off, idx, d2 = pb.radius_neighbors(dev(Q), radius, exclude=dev(ex))
+    roff, ridx, rd2 = oracle.range_brute(P, Q, radius, exclude=ex)
+    assert np.array_equal(host(off), roff)
+    assert np.array_equal(host(idx), ridx)
+    assert np.array_equal(host(d2), rd2)
+    assert pb.info()["device_error_bits"] == 0
+    # the same on a k-NN graph's surface samples without exclusions
+    if radius == 0.03:
+        V, F, _ = W.config0()
+        pos, _, _ = T.sample_evenly_by_area(dev(V), dev(F), 30000, 4)
+        pb2 = T.PointBvh(pos)
+        off, idx, d2 = pb2.radius_neighbors(pos[:5000], 0.01)
+        roff, ridx, rd2 = oracle.range_brute(host(pos), host(pos[:5000]), 0.01)
+        assert np.array_equal(host(off), roff) and np.array_equal(host(idx), ridx)

@@ -174,3 +174,21 @@ def test_golden_fixtures_reproduce(oracle, golden_dir, name):
     else:
         assert np.array_equal(oracle.thea_random_bits(5489, 2000), z["seed_5489"])
         assert np.array_equal(oracle.thea_random_bits(0xFFFF, 2000), z["seed_ffff"])
+
+
+def test_range_brute_matches_numpy_restatement(oracle):
+    # BallN::contains: (p - center).squaredNorm() <= radius * radius, FP32, Eigen's e0 + (e1 + e2) order
+    rng = np.random.default_rng(12)
+    P = rng.uniform(0, 1, (3000, 3)).astype(np.float32)
+    P[100:110] = P[5]
+    q = np.concatenate([P[:50], rng.uniform(-0.2, 1.2, (50, 3)).astype(np.float32)])
+    ex = np.concatenate([np.arange(50, dtype=np.int32), -np.ones(50, np.int32)])
+    r = np.float32(0.07)
+    off, idx, d2 = oracle.range_brute(P, q, r, exclude=ex)
+    for i in range(len(q)):
+        diff = P - q[i]
+        dd = diff[:, 0] * diff[:, 0] + (diff[:, 1] * diff[:, 1] + diff[:, 2] * diff[:, 2])
+        want = np.nonzero(dd <= r * r)[0]
+        want = want[want != ex[i]]
+        assert np.array_equal(idx[off[i]:off[i + 1]], want)
+        assert np.array_equal(d2[off[i]:off[i + 1]], dd[want])

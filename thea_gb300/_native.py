@@ -120,6 +120,7 @@ SIGNATURES = {
     "thea_autotune_batch_closest": (ctypes.c_int, [_vp, _i64, _vp, _i64p, _i32, _vp, _vp, _i64, _i32, _vp,
                                                    ctypes.POINTER(Tuning)]),
     "thea_k_closest_self_ex": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
+    "thea_radius_neighbors": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp]),
     "thea_point_gram_tile": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp]),
     "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "thea_server_destroy": (ctypes.c_int, [_vp]),

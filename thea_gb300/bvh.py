@@ -318,6 +318,27 @@ class PointBvh(_Bvh):
                                        _stream_of(io.device)))
         return idx, d2
 
+    def radius_neighbors(self, queries, radius, exclude=None):
+        """BvhN::rangeQueryIndices with a Ball3: every point within `radius` (inclusive) of each CUDA-tensor query, as
+        CSR (offsets [n + 1] int64, indices [total] int32 in ascending order per query, squared distances [total])."""
+        import torch
+        q = queries.to(torch.float32).contiguous()
+        n = q.shape[0]
+        ex = exclude.to(torch.int32).contiguous() if exclude is not None else None
+        off = torch.empty(n + 1, dtype=torch.int64, device=q.device)
+        pex = ctypes.c_void_p(ex.data_ptr()) if ex is not None else None
+        st = _stream_of(True)
+        N.check(N.lib().thea_radius_neighbors(self._h, ctypes.c_void_p(q.data_ptr()), n, float(radius), pex,
+                                              ctypes.c_void_p(off.data_ptr()), None, None, st))
+        total = int(off[-1].item()) if n else 0
+        idx = torch.empty(total, dtype=torch.int32, device=q.device)
+        d2 = torch.empty(total, dtype=torch.float32, device=q.device)
+        if total:
+            N.check(N.lib().thea_radius_neighbors(self._h, ctypes.c_void_p(q.data_ptr()), n, float(radius), pex,
+                                                  ctypes.c_void_p(off.data_ptr()), ctypes.c_void_p(idx.data_ptr()),
+                                                  ctypes.c_void_p(d2.data_ptr()), st))
+        return off, idx, d2
+
     def k_closest_self(self, k, device=False, candidates="traversal"):
         """k-nearest-neighbour graph of the indexed points, each excluding itself; rows in point order.
         candidates="gram": tensor-core Gram tiles seed the search with an exact bound (same results)."""

@@ -530,6 +530,24 @@ static void knn_self_impl(const thea_bvh * point_bvh, int32_t k, int32_t candida
   if (hi || hd) THEA_CUDA_CHECK(cudaStreamSynchronize(s));
 }
 
+THEA_API thea_status thea_radius_neighbors(const thea_bvh * point_bvh, const float * queries, int64_t num_queries,
+                                           float radius, const int32_t * exclude_index, int64_t * out_offsets,
+                                           int32_t * out_index, float * out_sq_distance, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "radius_neighbors: a point BVH is required");
+    THEA_REQUIRE(num_queries >= 0, "radius_neighbors: negative query count");
+    THEA_REQUIRE(radius >= 0.f, "radius_neighbors: negative or NaN radius");
+    if (num_queries == 0) return;
+    THEA_REQUIRE(queries && out_offsets, "radius_neighbors: null queries or out_offsets");
+    void const * arrays[5] = {queries, exclude_index, out_offsets, out_index, out_sq_distance};
+    for (void const * p : arrays)
+      THEA_REQUIRE(!p || !is_host_pointer(p), "radius_neighbors: every array must be device memory");
+    THEA_REQUIRE(out_index || !out_sq_distance, "radius_neighbors: out_sq_distance needs out_index");
+    run_range(point_bvh, queries, num_queries, radius, exclude_index, out_offsets, out_index, out_sq_distance,
+              handle_error_word(point_bvh), (cudaStream_t)stream);
+  });
+}
+
 THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,
                                          float * out_sq_distance, void * stream) {
   return guarded([&] {

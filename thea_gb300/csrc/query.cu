@@ -322,6 +322,108 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
 }
 
 //============================================================================================================================
+// Points within a radius (BvhN::rangeQueryIndices with a Ball3 range, BvhN.hpp:1208-1219, 2118-2171; BallN::contains,
+// BallN.hpp:83: (p - center).squaredNorm() <= radius * radius, inclusive, FP32). Counting pass, then a filling pass into
+// each query's slice of a CSR list; the slices are then put in ascending element order by one key sort.
+//============================================================================================================================
+
+template <int W, int STACK, bool FILL>
+__global__ void __launch_bounds__(QUERY_THREADS)
+range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
+             int64_t n, float r2, int32_t const * __restrict__ exclude, int64_t * __restrict__ count_or_offset,
+             uint64_t * __restrict__ keys, float * __restrict__ out_d2, unsigned * __restrict__ err) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  V3 p = load_v3(queries + 3 * q);
+  int ex = exclude ? exclude[q] : -1;
+  int64_t w = FILL ? count_or_offset[q] : 0;
+  int64_t c = 0;
+  int stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  stk[sp] = 0;
+  stkd[sp] = 0.f;
+  ++sp;
+  float lim = r2 * PRUNE_SLACK;
+  while (sp > 0) {
+    --sp;
+    int code = stk[sp];
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children<W, STACK>(nd, lb, lim, stk, stkd, sp, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      for (int64_t k = first; k < first + count; ++k) {
+        float4 a = __ldg(pts + k);
+        int idx = __float_as_int(a.w);
+        if (idx == ex) continue;
+        float d2 = squared_norm(xyz(a) - p);
+        if (d2 <= r2) {
+          if (FILL) {
+            keys[w + c] = ((uint64_t)q << 32) | (uint32_t)idx;
+            out_d2[w + c] = d2;
+          }
+          ++c;
+        }
+      }
+    }
+  }
+  if (!FILL) count_or_offset[q] = c;
+}
+
+__global__ void range_total_kernel(int64_t const * __restrict__ counts, int64_t n, int64_t * __restrict__ offsets) {
+  offsets[n] = offsets[n - 1] + counts[n - 1];
+}
+
+__global__ void range_iota_kernel(int64_t total, uint32_t * __restrict__ v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) v[i] = (uint32_t)i;
+}
+
+// After the key sort: element index from the low key bits, squared distance gathered through the permutation
+__global__ void range_emit_kernel(uint64_t const * __restrict__ keys, uint32_t const * __restrict__ perm,
+                                  float const * __restrict__ d2_unsorted, int64_t total, int32_t * __restrict__ out_idx,
+                                  float * __restrict__ out_d2) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  out_idx[i] = (int32_t)(uint32_t)(keys[i] & 0xffffffffu);
+  if (out_d2) out_d2[i] = d2_unsorted[perm[i]];
+}
+
+template <int W, int STACK>
+void launch_range(thea_bvh const * b, float const * q, int64_t n, float r2, int32_t const * ex, int64_t * offsets,
+                  int32_t * out_idx, float * out_d2, unsigned * err, cudaStream_t s) {
+  unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
+  if (!out_idx) {
+    Scratch counts((size_t)n * sizeof(int64_t), s);
+    THEA_LAUNCH((range_kernel<W, STACK, false>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec,
+                q, n, r2, ex, counts.as<int64_t>(), (uint64_t *)nullptr, (float *)nullptr, err);
+    exclusive_scan<int64_t>(counts.as<int64_t>(), offsets, n, s);
+    THEA_LAUNCH(range_total_kernel, 1, 1, 0, s, counts.as<int64_t>(), n, offsets);
+    return;
+  }
+  int64_t total = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&total, offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (total <= 0) return;
+  THEA_REQUIRE(total < (int64_t(1) << 32), "radius_neighbors: more than 2^32 neighbours in one call");
+  Scratch keys((size_t)total * sizeof(uint64_t), s), d2((size_t)total * sizeof(float), s);
+  Scratch perm((size_t)total * sizeof(uint32_t), s);
+  THEA_LAUNCH((range_kernel<W, STACK, true>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec, q,
+              n, r2, ex, offsets, keys.as<uint64_t>(), d2.as<float>(), err);
+  THEA_LAUNCH(range_iota_kernel, (unsigned)ceil_div(total, 256), 256, 0, s, total, perm.as<uint32_t>());
+  int qbits = 1;
+  while ((int64_t(1) << qbits) < n) ++qbits;
+  radix_sort_pairs(keys.as<uint64_t>(), perm.as<uint32_t>(), total, 32 + qbits, s);
+  THEA_LAUNCH(range_emit_kernel, (unsigned)ceil_div(total, 256), 256, 0, s, keys.as<uint64_t>(), perm.as<uint32_t>(),
+              d2.as<float>(), total, out_idx, out_d2);
+}
+
+//============================================================================================================================
 // Query ordering: large batches can be traversed in the order of a Morton code of the query point (rays: of the
 // origin, with the direction octant as the top bits). Results are written to each query's own slot.
 //============================================================================================================================
@@ -470,6 +572,17 @@ void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, Ra
                         : launch_ray<4, 256>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s);
   else sm ? launch_ray<8, 128>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s)
           : launch_ray<8, 512>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s);
+}
+
+void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex, int64_t * offsets,
+               int32_t * idx, float * d2, unsigned * err, cudaStream_t s) {
+  if (n <= 0) return;
+  float r2 = radius * radius;  // BallN::contains compares with radius * radius in FP32
+  bool sm = small_stack_ok(b);
+  if (b->width == 4) sm ? launch_range<4, 64>(b, q, n, r2, ex, offsets, idx, d2, err, s)
+                        : launch_range<4, 256>(b, q, n, r2, ex, offsets, idx, d2, err, s);
+  else sm ? launch_range<8, 128>(b, q, n, r2, ex, offsets, idx, d2, err, s)
+          : launch_range<8, 512>(b, q, n, r2, ex, offsets, idx, d2, err, s);
 }
 
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
