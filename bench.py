@@ -21,6 +21,7 @@ the only exchange is the max-over-ranks of the timed region.
 """
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -95,7 +96,31 @@ def case_gram_knn():
     torch.cuda.synchronize()
 
 
-CASES = {"ray": case_ray, "cfg3_fp64_64": case_cfg3_fp64_64, "gram_knn": case_gram_knn}
+def case_cfg0():
+    """Config 0: closest point of 262,144 queries on the noisy icosphere, three calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, Q = W.config0()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1)
+    Qd = torch.from_numpy(Q).cuda()
+    for _ in range(3):
+        bvh.closest_element(Qd)
+    torch.cuda.synchronize()
+
+
+def case_cfg3_fp32_64():
+    """Batched closest point (FP32, one thread per query throughout) over 64 meshes of the config-3 distribution."""
+    import torch
+    import thea_gb300 as T
+    V, F, foff, Q, qoff, _ = W.config3_torch(64)
+    forest = T.MeshForest(V, F, foff, width=4, max_leaf_size=1, layouts=1)
+    for _ in range(2):
+        forest.batch_closest_element(Q, qoff, hard_query_budget=-1, queries_per_warp=64)
+    torch.cuda.synchronize()
+
+
+CASES = {"ray": case_ray, "cfg0": case_cfg0, "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64,
+         "gram_knn": case_gram_knn}
 
 
 def peaks():
@@ -410,17 +435,19 @@ def extra_workloads(T, torch, stream, flush, args):
     steps = max(3, min(args.steps, 5))
     # config 0: closest point on the noisy icosphere
     V, F, Q = W.config0()
-    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1)
+    # leaf size 1: the autotuner's choice for closest point on these meshes (config 3)
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1, max_leaf_size=1)
     Qd = torch.from_numpy(Q).cuda()
     T.profiling_reset()
     T.profiling(True)
     ms = timed_steps(lambda: bvh.closest_element(Qd), steps, 2, flush, stream)
     T.profiling(False)
-    k_ms, k_cnt = T.profiling_read("closest_kernel")
-    kms = k_ms / max(1, k_cnt)
+    # large batches run as two kernels (persistent lanes with a step budget, then one warp per query over budget)
+    k_ms, k_cnt = T.profiling_read("batch_closest_phase")
+    kms = k_ms / max(1, k_cnt // 2) if k_cnt else 0.0
     out["closest_point_cfg0"] = {"value": CP_QUERIES / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
                                  "ms_per_step": statistics.mean(ms), "kernel_ms": kms,
-                                 "roofline_frac": ALGO_BYTES_CFG0 / (kms / 1e3) / 1e9 / peaks()[0]}
+                                 "roofline_frac": ALGO_BYTES_CFG0 / (max(kms, 1e-9) / 1e3) / 1e9 / peaks()[0]}
     bvh.close()
     # config 2: 1,048,576 area samples of the config-0 mesh (reference Random stream), k = 16 graph excluding self
     torch.cuda.synchronize()
@@ -469,6 +496,8 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     each with a log-uniform 1..1,048,576 queries uniform in its mesh's box grown by 50% (rays: origins there, uniform
     directions). Query and result arrays are pinned host memory; latency runs from submit to results written back."""
     res = {}
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     V, F, foff, _, _, levels = W.config3_torch(num_meshes, seed=seed, min_q=1, max_q=2)
     srv = T.Server(memory_budget_bytes=8 << 30)
     t0 = time.perf_counter()
@@ -518,6 +547,9 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     tickets = [None] * n_req
     srv.reset_stats()
     torch.cuda.synchronize()
+    # the client is this Python loop: keep the garbage collector from pausing it in the middle of the arrival stream
+    gc.collect()
+    gc.disable()
     with ClockSampler(torch.cuda.current_device()) as clk:
         start = time.perf_counter()
         for r in range(n_req):
@@ -537,6 +569,7 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
             lat[r] = t.latency_ms
             assert t.status == 0
         total_s = time.perf_counter() - start
+    gc.enable()
     st = srv.stats()
     srv.close()
     small = nq <= 65536

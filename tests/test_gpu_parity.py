@@ -375,3 +375,17 @@ def test_radius_neighbors_equal_brute_force(T, oracle, radius):
         off, idx, d2 = pb2.radius_neighbors(pos[:5000], 0.01)
         roff, ridx, rd2 = oracle.range_brute(host(pos), host(pos[:5000]), 0.01)
         assert np.array_equal(host(off), roff) and np.array_equal(host(idx), ridx)
+
+
+@pytest.mark.parametrize("dist_bound", [-1.0, 0.05])
+def test_closest_large_batches_equal_small_ones(T, dist_bound):
+    # batches of 65,536 queries or more run as persistent lanes with a step budget plus one warp per query over budget;
+    # smaller ones run one thread per query: the same searches, the same results
+    V, F = W.noisy_icosphere(5, 45)
+    Q = W.uniform_box_points(150000, [-1.5] * 3, [1.5] * 3, 46)
+    bvh = T.MeshBvh(dev(V), dev(F))
+    i, d, c = bvh.closest_element(dev(Q), dist_bound=dist_bound)
+    parts = [bvh.closest_element(dev(Q[k:k + 50000]), dist_bound=dist_bound) for k in range(0, len(Q), 50000)]
+    assert np.array_equal(host(i), np.concatenate([host(p[0]) for p in parts]))
+    assert np.array_equal(host(d), np.concatenate([host(p[1]) for p in parts]))
+    assert np.array_equal(host(c), np.concatenate([host(p[2]) for p in parts]))

@@ -163,7 +163,8 @@ constexpr int REFILL_RESOLVE_AT = 8;
 
 template <int W, int STACK, int PREC>
 __global__ void __launch_bounds__(BATCH_THREADS)
-batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned long long * counter) {
+batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned long long * counter, int budget,
+                            HardQueue hq) {
   F64WarpBuf * buf = nullptr;
   if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
     __shared__ F64WarpBuf s_buf[BATCH_THREADS / 32];
@@ -187,6 +188,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
   V3 best_cp = V3{0.f, 0.f, 0.f};
   F64Search s;
   float best32 = INFINITY, abs_tol = 0.f;
+  int pops = 0;  // stack entries taken by this lane's query (two-phase form: budget > 0)
   if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) f64_search_init(s);
   while (true) {
     unsigned idle = __ballot_sync(FULL, q < 0);
@@ -211,6 +213,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
           stk[0] = __ldg(f.seg_root + m);
           stkd[0] = 0.f;
           sp = 1;
+          pops = 0;
           if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
             f64_search_init(s);
             float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
@@ -252,6 +255,22 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
                       nullptr);
         q = -1;
       }
+      continue;
+    }
+    if (budget > 0 && ++pops > budget) {
+      // over budget: queued with the best element so far, finished by a warp of its own in the second kernel
+      unsigned long long pos = atomicAdd(hq.count, 1ull);
+      hq.q[pos] = q;
+      if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
+        hq.bound[pos] = best32;
+        hq.idx[pos] = INT_MAX;
+        hq.slot[pos] = -1;
+      } else {
+        hq.bound[pos] = best;
+        hq.idx[pos] = best_idx;
+        hq.slot[pos] = best_slot;
+      }
+      q = -1;
       continue;
     }
     --sp;
@@ -397,21 +416,29 @@ template <int W, int STACK, int PREC>
 void launch_closest_prec(BatchForest const & f, ClosestArgs const & a, int64_t nq, int budget,
                          unsigned long long * counters, int chunk, HardQueue const & hq, cudaStream_t s) {
   auto k1 = batch_closest_kernel<W, STACK, PREC>;
+  // FP32 without error estimates: persistent lanes (1.5x on the 256-mesh case), also as the first phase of the
+  // two-phase form. The mixed-precision search stays on rounds: it is bound by the FP64 pipe, and rounds fill the FP64
+  // step better (27.5 against 25.7 ms measured).
+  bool refill = PREC != THEA_PRECISION_FP64_RECHECK && !a.out_err;
   if (budget <= 0) {
-    // FP32 without error estimates: persistent lanes (1.5x on the 256-mesh case). The mixed-precision search stays on
-    // rounds: it is bound by the FP64 pipe, and rounds fill the FP64 step better (27.5 against 25.7 ms measured).
-    if (PREC != THEA_PRECISION_FP64_RECHECK && !a.out_err) {
+    if (refill) {
       auto kr = batch_closest_refill_kernel<W, STACK, PREC>;
-      THEA_LAUNCH_NAMED(PREC == THEA_PRECISION_FP64_RECHECK ? "batch_closest_kernel_fp64" : "batch_closest_kernel_fp32",
-                        kr, persistent_grid((void const *)kr), BATCH_THREADS, 0, s, f, a, nq, counters);
+      THEA_LAUNCH_NAMED("batch_closest_kernel_fp32", kr, persistent_grid((void const *)kr), BATCH_THREADS, 0, s, f, a,
+                        nq, counters, 0, hq);
       return;
     }
-    THEA_LAUNCH_NAMED("batch_closest_kernel_fp32", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a, nq,
-                      counters, chunk, 0, hq);
+    THEA_LAUNCH_NAMED(PREC == THEA_PRECISION_FP64_RECHECK ? "batch_closest_kernel_fp64" : "batch_closest_kernel_fp32",
+                      k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a, nq, counters, chunk, 0, hq);
     return;
   }
-  THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a, nq,
-                    counters, chunk, budget, hq);
+  if (refill) {
+    auto kr = batch_closest_refill_kernel<W, STACK, PREC>;
+    THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", kr, persistent_grid((void const *)kr), BATCH_THREADS, 0, s, f, a,
+                      nq, counters, budget, hq);
+  } else {
+    THEA_LAUNCH_NAMED("batch_closest_phase1_kernel", k1, persistent_grid((void const *)k1), BATCH_THREADS, 0, s, f, a,
+                      nq, counters, chunk, budget, hq);
+  }
   auto k2 = batch_closest_phase2_kernel<W, PREC>;
   THEA_LAUNCH_NAMED("batch_closest_phase2_kernel", k2, persistent_grid((void const *)k2), BATCH_THREADS, 0, s, f, a, hq,
                     counters + 1);
