@@ -398,7 +398,7 @@ def gpu_arm(args, rank, world, local_rank):
         cpu = None
         if not args.no_cpu and world == 1:
             cpu = cpu_ray_baseline(V, F, o, d)
-        traffic = ncu_traffic("ray_kernel")
+        traffic = ncu_traffic("ray_persistent_kernel")
         line = {
             "metric": "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)",
             "value": value, "unit": "Mqueries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -413,7 +413,7 @@ def gpu_arm(args, rank, world, local_rank):
                     "d2h_bytes_per_step": RAYS * 8},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "ray_kernel", "kernel_ms": kernel_ms,
+                         "kernel": "ray_persistent_kernel", "kernel_ms": kernel_ms,
                          "algorithmic_bytes_per_launch": ALGO_BYTES_CFG1},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
