@@ -267,6 +267,17 @@ def reference_arm(args, rank, world):
 # GPU arm
 # ---------------------------------------------------------------------------------------------------------------------
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over all ranks (x itself without a process group): the whole job's time is its slowest
+    rank's."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def timed_steps(fn, steps, warmup, flush, stream):
     """Runs warmup steps, then `steps` timed steps each preceded by an L2 flush; returns per-step ms (CUDA events)."""
     import torch
@@ -336,11 +347,7 @@ def gpu_arm(args, rank, world, local_rank):
     T.profiling(False)
     k_ms, k_cnt = T.profiling_read("ray_kernel")
     T.profiling_reset()
-    step_ms = sum(ms) / len(ms)
-    if dist:
-        tt = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        step_ms = float(tt.item())
+    step_ms = max_over_ranks(sum(ms) / len(ms), dist, "cuda")
     value = world * RAYS / (step_ms / 1000.0) / 1e6
     kernel_ms = k_ms / max(1, k_cnt)
     peak, peak_kind = peaks()
@@ -366,11 +373,7 @@ def gpu_arm(args, rank, world, local_rank):
         t0 = time.perf_counter()
         e2e_step()  # synchronous: returns once results are in host memory
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_times)
-    if dist:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(statistics.mean(e2e_times), dist, "cuda")
     assert np.array_equal(hi.numpy(), out_i.cpu().numpy()), "host and device paths disagree"
     hits = int((hi.numpy() >= 0).sum())
 
