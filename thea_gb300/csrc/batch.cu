@@ -401,12 +401,7 @@ batch_knn_kernel(BatchForest f, float const * __restrict__ queries, int64_t cons
 }
 
 int persistent_grid(void const * kernel) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    THEA_CUDA_CHECK(cudaGetDevice(&dev));
-    THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  int sms = sm_count();
   int per_sm = 0;
   THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BATCH_THREADS, 0));
   return std::max(1, per_sm) * sms;

@@ -8,6 +8,8 @@
 
 #include "common.cuh"
 
+#include <mutex>
+
 #include <algorithm>
 #include <cstring>
 
@@ -18,6 +20,18 @@ namespace thea {
 cudaMemPool_t scratch_pool();
 
 // A device buffer taken from the library's stream-ordered pool and returned to it when the owner goes out of scope.
+// Multiprocessor count of the current device (cached per device; safe to call from several threads)
+inline int sm_count() {
+  static std::mutex m;
+  static int counts[64] = {0};
+  int dev = 0;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(m);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!counts[dev]) THEA_CUDA_CHECK(cudaDeviceGetAttribute(&counts[dev], cudaDevAttrMultiProcessorCount, dev));
+  return counts[dev];
+}
+
 struct Scratch {
   void * ptr = nullptr;
   size_t bytes = 0;

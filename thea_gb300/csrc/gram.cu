@@ -390,12 +390,7 @@ void run_gram_bounds(thea_bvh const * b, int k, float * bound, cudaStream_t s) {
   int64_t n = b->n;
   float4 const * pts = b->pt_rec;
   // four CTAs per SM: each holds a quarter of the SM's tensor memory (128 of 512 columns) for its whole life
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    THEA_CUDA_CHECK(cudaGetDevice(&dev));
-    THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  int sms = sm_count();
   int blocks = (int)std::min<int64_t>(ceil_div(n, GRAM_M), 4 * (int64_t)sms);
   Scratch counter(sizeof(unsigned long long), s);
   THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));

@@ -511,12 +511,7 @@ void launch_ray(thea_bvh const * b, float const * o, float const * d, int64_t n,
   unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
   if (!rp.recheck && n >= RAY_PERSISTENT_MIN) {
     auto k = ray_persistent_kernel<W, STACK>;
-    static int sms = 0;
-    if (!sms) {
-      int dev = 0;
-      THEA_CUDA_CHECK(cudaGetDevice(&dev));
-      THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int sms = sm_count();
     int per_sm = 0;
     THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, QUERY_THREADS, 0));
     unsigned pgrid = (unsigned)std::min<int64_t>((int64_t)std::max(1, per_sm) * sms, grid);

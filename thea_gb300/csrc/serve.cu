@@ -257,12 +257,7 @@ serve_knn_kernel(ServeTask const * __restrict__ tasks, int64_t const * __restric
 }
 
 template <class K> int grid_for(K kernel, int64_t nq) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    THEA_CUDA_CHECK(cudaGetDevice(&dev));
-    THEA_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  int sms = sm_count();
   int per_sm = 0;
   THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, SERVE_THREADS, 0));
   int64_t need = ceil_div(nq, SERVE_THREADS);

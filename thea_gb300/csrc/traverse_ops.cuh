@@ -596,21 +596,19 @@ struct RayOut {
   float t;       // FP32 reference verdict: hit time, or the initial bound when nothing was hit
   int idx;       // INT_MAX if none
   int64_t slot;
-  double t64;    // watertight FP64 verdict (re-check mode): hit time or +inf
-  int idx64;
-  int64_t slot64;
 };
 
 static __device__ __noinline__ double watertight_f64_call(V3 o, V3 d, float4 a, float4 b, float4 c) {
   return ray_triangle_watertight_f64(o, d, xyz(a), xyz(b), xyz(c));
 }
 
-// Reference verdict (FP32 Eberly test with the parallel threshold) and, when `recheck` is set, the watertight FP64
-// verdict over every element the FP32 test accepted or rejected by a narrow margin (within 2^-12 of the determinant on
-// an edge test, or near the parallel threshold).
+// The reference's verdict: FP32 Eberly test with its parallel threshold (TriangleN<3>::rayIntersection), nearest hit
+// with t >= 0 and, with a bound, t <= max_time; ties to the lowest index. (The FP64 watertight verdict is
+// ray_search_f64 + ray_resolve_warp below.) The template flag is kept for the callers' signatures and must be false.
 template <int W, int STACK, bool RECHECK>
 __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
                                             int root, int64_t elem_base, V3 o, V3 d, float max_time, unsigned * err) {
+  static_assert(!RECHECK, "the FP64 re-test is ray_search_f64 + ray_resolve_warp");
   float ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
   float iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
   float iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
@@ -618,9 +616,6 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
   float best = max_time >= 0.f ? max_time : INFINITY;
   int best_idx = INT_MAX;
   int64_t best_slot = -1;
-  double best64 = max_time >= 0.f ? (double)max_time : INFINITY;
-  int idx64 = INT_MAX;
-  int64_t slot64 = -1;
   int stk[STACK];
   float stkd[STACK];
   int sp = 0;
@@ -630,8 +625,7 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
   while (sp > 0) {
     --sp;
     int code = stk[sp];
-    float bound = RECHECK ? fmaxf(best, (float)best64) : best;
-    if (stkd[sp] > bound * PRUNE_SLACK) continue;
+    if (stkd[sp] > best * PRUNE_SLACK) continue;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
@@ -645,7 +639,7 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
         float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
         lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
       }
-      push_children<W, STACK>(nd, lb, bound * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, err);
     } else {
       int first, count;
       decode_leaf(code, first, count);
@@ -655,38 +649,10 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
         float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
         float t = ray_triangle_time(o, d, xyz(a), xyz(b), xyz(c));
         int idx = __float_as_int(a.w);
-        // TriangleN<3>::rayIntersection accepts t >= 0 and, with a bound, t <= max_time
-        if (t >= 0.f && t <= best) {
-          if (t < best || idx < best_idx) {
-            best = t;
-            best_idx = idx;
-            best_slot = k;
-          }
-        }
-        if (RECHECK) {
-          bool candidate = t >= 0.f;
-          if (!candidate) {
-            // narrow FP32 rejections: recompute the edge tests' margins
-            V3 diff = o - xyz(a);
-            V3 nrm = cross(xyz(b), xyz(c));
-            float DdN = dot(d, nrm);
-            float s = DdN < 0.f ? -1.f : 1.f;
-            float adn = fabsf(DdN);
-            float e1 = s * dot(d, cross(diff, xyz(c)));
-            float e2 = s * dot(d, cross(xyz(b), diff));
-            float eta = adn * (1.0f / 4096.0f);
-            candidate = adn <= 4.f * 1.1920928955078125e-07f ||
-                        (fminf(fminf(e1, e2), adn - e1 - e2) >= -eta && fmaxf(fabsf(e1), fabsf(e2)) <= 2.f * adn);
-          }
-          if (candidate) {
-            double t64 = watertight_f64_call(o, d, a, b, c);
-            if (t64 >= 0.0 && (max_time < 0.f || t64 <= (double)max_time) &&
-                (t64 < best64 || (t64 == best64 && idx < idx64))) {
-              best64 = t64;
-              idx64 = idx;
-              slot64 = k;
-            }
-          }
+        if (t >= 0.f && t <= best && (t < best || idx < best_idx)) {
+          best = t;
+          best_idx = idx;
+          best_slot = k;
         }
       }
     }
@@ -695,9 +661,6 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
   out.t = best;
   out.idx = best_idx;
   out.slot = best_slot;
-  out.t64 = best64;
-  out.idx64 = idx64;
-  out.slot64 = slot64;
   return out;
 }
 
