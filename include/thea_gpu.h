@@ -76,7 +76,7 @@ typedef struct thea_bvh_info {
   float bounds_lo[3];        /* bounds of all elements */
   float bounds_hi[3];
   uint32_t device_error_bits; /* nonzero if a query kernel hit an internal limit (reading it synchronizes) */
-  int32_t reserved;
+  int32_t num_segments;      /* BVHs in the handle: 1, or the meshes / point sets of a forest */
 } thea_bvh_info;
 
 /* ---- library ------------------------------------------------------------------------------------------------------- */
@@ -109,6 +109,17 @@ THEA_API thea_status thea_point_bvh_build(const float * points, int64_t num_poin
 
 /* Releases the handle after all work on `stream`-ordered queries using it has completed (synchronizes the device). */
 THEA_API thea_status thea_bvh_destroy(thea_bvh * bvh);
+
+/* Byte image of a built BVH (any kind: mesh, points, forest), for warm starts without a rebuild: a versioned header
+ * (magic "THEABVH", version 1), the handle's parameters, then its arrays. out_image == NULL: *out_bytes = the image
+ * size. Otherwise the image is written to host memory out_image (capacity bytes). Synchronizes the stream. The
+ * reference has no counterpart (its BvhN is not Serializable). */
+THEA_API thea_status thea_bvh_serialize(const thea_bvh * bvh, void * out_image, int64_t capacity, int64_t * out_bytes,
+                                        void * stream);
+/* A new handle on the current device from an image made by thea_bvh_serialize (host memory). The header and section
+ * sizes are checked before anything is allocated (THEA_ERR_INVALID_ARGUMENT for a foreign, truncated or newer image).
+ * Queries on the new handle return what they return on the original. Synchronizes the stream. */
+THEA_API thea_status thea_bvh_deserialize(const void * image, int64_t bytes, void * stream, thea_bvh ** out_bvh);
 
 THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * info);
 
@@ -278,6 +289,13 @@ THEA_API thea_status thea_k_closest_self_ex(const thea_bvh * point_bvh, int32_t 
  * columns j >= num_b are padding. */
 THEA_API thea_status thea_point_gram_tile(const float * a, int32_t num_a, const float * b, int32_t num_b,
                                           float * out_keys, void * stream);
+
+/* Diagnostic of the failure path of the library's bounded device-side waits (the tensor-core kernels wait on an mbarrier
+ * for their MMAs; every such wait gives up after a fixed number of rounds and reports instead of hanging). One warp
+ * waits on a barrier phase that nothing completes, with the given round limit (1..2^20). Returns
+ * THEA_ERR_DEVICE_TIMEOUT when the wait gave up (the expected outcome; the context stays usable), THEA_OK if the phase
+ * completed. No counterpart in the reference. Synchronizes the stream. */
+THEA_API thea_status thea_selftest_bounded_wait(int32_t spin_limit, void * stream);
 
 /* ---- sampling ------------------------------------------------------------------------------------------------------ */
 

@@ -11,6 +11,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <vector>
 
 namespace thea_gpu {
 
@@ -64,14 +65,38 @@ class BvhHandle {
     check(thea_bvh_get_info(h_, &i));
     return i;
   }
+  // Byte image of the built BVH (thea_bvh_serialize); the class's fromImage reloads it without a rebuild.
+  std::vector<unsigned char> serialize(void * stream = nullptr) const {
+    int64_t n = 0;
+    check(thea_bvh_serialize(h_, nullptr, 0, &n, stream));
+    std::vector<unsigned char> out((size_t)n);
+    check(thea_bvh_serialize(h_, out.data(), n, &n, stream));
+    return out;
+  }
 
  protected:
+  template <class T>
+  static T loadImage(void const * image, int64_t bytes, bool mesh, void * stream) {
+    T t;
+    check(thea_bvh_deserialize(image, bytes, stream, &static_cast<BvhHandle &>(t).h_));
+    if ((t.info().is_mesh != 0) != mesh)
+      throw Exception(THEA_ERR_INVALID_ARGUMENT, "bvh image holds the other kind of BVH");
+    return t;
+  }
+
   thea_bvh * h_ = nullptr;
 };
 
 // MeshBvh: a BVH over the triangles of a mesh; element index = face index (MeshBvh::add + MeshBvh::init).
 class MeshBvh : public BvhHandle {
+  friend class BvhHandle;
+  MeshBvh() = default;
+
  public:
+  // A handle on the current device from a byte image made by serialize() of a MeshBvh
+  static MeshBvh fromImage(void const * image, int64_t bytes, void * stream = nullptr) {
+    return loadImage<MeshBvh>(image, bytes, true, stream);
+  }
   MeshBvh(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t num_faces,
           BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
     thea_build_config c = opt.config();
@@ -129,7 +154,14 @@ class MeshBvh : public BvhHandle {
 
 // BvhN<Vector3, 3>: a BVH over points; element index = point index.
 class PointBvh : public BvhHandle {
+  friend class BvhHandle;
+  PointBvh() = default;
+
  public:
+  // A handle on the current device from a byte image made by serialize() of a PointBvh
+  static PointBvh fromImage(void const * image, int64_t bytes, void * stream = nullptr) {
+    return loadImage<PointBvh>(image, bytes, false, stream);
+  }
   PointBvh(float const * points, int64_t num_points, BuildOptions const & opt = BuildOptions(),
            void * stream = nullptr) {
     thea_build_config c = opt.config();
@@ -160,7 +192,14 @@ class PointBvh : public BvhHandle {
 // mesh m owns faces [mesh_face_offsets[m], mesh_face_offsets[m + 1]) (host array, num_meshes + 1 entries). Queries
 // are grouped by mesh through device-resident query_offsets.
 class MeshForest : public BvhHandle {
+  friend class BvhHandle;
+  MeshForest() = default;
+
  public:
+  // A handle on the current device from a byte image made by serialize() of a MeshForest
+  static MeshForest fromImage(void const * image, int64_t bytes, void * stream = nullptr) {
+    return loadImage<MeshForest>(image, bytes, true, stream);
+  }
   MeshForest(float const * vertices, int64_t num_vertices, int32_t const * faces, int64_t const * mesh_face_offsets,
              int32_t num_meshes, BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
     thea_build_config c = opt.config();
@@ -186,7 +225,14 @@ class MeshForest : public BvhHandle {
 };
 
 class PointForest : public BvhHandle {
+  friend class BvhHandle;
+  PointForest() = default;
+
  public:
+  // A handle on the current device from a byte image made by serialize() of a PointForest
+  static PointForest fromImage(void const * image, int64_t bytes, void * stream = nullptr) {
+    return loadImage<PointForest>(image, bytes, false, stream);
+  }
   PointForest(float const * points, int64_t const * set_offsets, int32_t num_sets,
               BuildOptions const & opt = BuildOptions(), void * stream = nullptr) {
     thea_build_config c = opt.config();

@@ -48,6 +48,14 @@ int main(int argc, char ** argv) {
       if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 10;
     }
   }
+  // a foreign image is refused before any CUDA call
+  try {
+    unsigned char junk[256] = {0};
+    thea_gpu::MeshBvh::fromImage(junk, sizeof(junk));
+    return 11;  // must have thrown
+  } catch (thea_gpu::Exception const & e) {
+    if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 12;
+  }
   if (no_device) return 0;
 
   float V[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -62,6 +70,11 @@ int main(int argc, char ** argv) {
   int32_t ti = -1;
   mesh.rayStructureIntersection(o, d, 1, &t, &ti);
   if (ti != 3) { std::printf("ray %d %f\n", ti, t); return 5; }
+  // the reloaded image answers like the original
+  std::vector<unsigned char> image = mesh.serialize();
+  thea_gpu::MeshBvh again = thea_gpu::MeshBvh::fromImage(image.data(), (int64_t)image.size());
+  double dist2 = -1;
+  if (again.closestElement(q, -1, &dist2, cp) != idx || dist2 != dist) return 13;
   thea_gpu::PointBvh pts(V, 4);
   int32_t ki[2];
   float kd[2];

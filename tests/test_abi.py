@@ -51,10 +51,14 @@ def test_library_is_built_for_sm_103a(lib):
     # ptxas -v reports the target of every compiled entry function in the build logs
     from thea_gb300 import build as B
     logs = [os.path.join(B.BUILD, f[:-3] + ".log") for f in B.sources()]
+    with_kernels = 0
     for log in logs:
         text = open(log).read()
         assert "arch=compute_103a,code=sm_103a" in text.splitlines()[0]
-        assert "for 'sm_103a'" in text
+        targets = set(re.findall(r"Compiling entry function '\w+' for '(\w+)'", text))
+        assert targets <= {"sm_103a"}, (log, targets)
+        with_kernels += bool(targets)
+    assert with_kernels >= len(logs) - 1  # serialize.cu is host code only
 
 
 def test_status_strings_and_version(lib):
@@ -109,3 +113,37 @@ def test_cpp_wrapper_compiles():
     assert r.returncode == 0, r.stderr
     r = subprocess.run([out, "--no-device"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def _image_header(version=1, width=4, n=4, num_nodes=1, segments=1, is_mesh=1, layouts=3, sections=None):
+    """A serialized-BVH header (the fixed layout thea_bvh_serialize writes), for rejection tests without a device."""
+    import struct
+    node, cp, ray, pt = sections if sections is not None else (num_nodes * 128, n * 128, n * 48, 0)
+    return struct.pack("<8sI5iIi3q6f4q", b"THEABVH\0", version, is_mesh, width, 4, 1, 0, layouts, segments, n,
+                       num_nodes, 0, 0, 0, 0, 1, 1, 1, node, cp, ray, pt)
+
+
+def test_bvh_images_are_checked_before_any_device_call(lib):
+    """thea_bvh_deserialize refuses foreign, newer, inconsistent and truncated images with INVALID_ARGUMENT, and
+    never allocates for them (no device here)."""
+    from thea_gb300 import MeshBvh, PointBvh
+    from thea_gb300 import _native as N
+    h = ctypes.c_void_p()
+    size = ctypes.c_int64()
+    assert lib.thea_bvh_serialize(None, None, 0, ctypes.byref(size), None) == N.THEA_ERR_INVALID_ARGUMENT
+    cases = {
+        "not a BVH image": b"x" * 256,
+        "buffer shorter than a header": _image_header()[:40],
+        "version 2 is not supported": _image_header(version=2) + bytes(4096),
+        "inconsistent header": _image_header(width=5) + bytes(4096),
+        "inconsistent section sizes": _image_header(sections=(128, 4 * 128, 0, 0)) + bytes(4096),
+        "shorter than the image": _image_header() + bytes(64),
+    }
+    for why, img in cases.items():
+        buf = ctypes.create_string_buffer(img, len(img))
+        assert lib.thea_bvh_deserialize(buf, len(img), None, ctypes.byref(h)) == N.THEA_ERR_INVALID_ARGUMENT, why
+        assert why.encode() in lib.thea_last_error_message(), (why, lib.thea_last_error_message())
+        assert not h.value
+    for cls in (MeshBvh, PointBvh):
+        with pytest.raises(N.TheaError):
+            cls.from_bytes(b"")

@@ -81,3 +81,19 @@ def test_gram_mode_on_small_sets_falls_back(T):
     i0, d0 = pb.k_closest_self(5, device=True)
     i1, d1 = pb.k_closest_self(5, device=True, candidates="gram")
     assert torch.equal(i0, i1) and torch.equal(d0, d1)
+
+
+def test_bounded_device_wait_gives_up_and_context_survives(T):
+    # failure path of the bounded mbarrier waits: a phase nothing completes; the wait reports instead of hanging
+    import torch
+    from thea_gb300 import _native as N
+    r = N.lib().thea_selftest_bounded_wait(2000, None)
+    assert r == N.THEA_ERR_DEVICE_TIMEOUT
+    # the context is still usable
+    P = torch.rand((1000, 3), device="cuda")
+    pb = T.PointBvh(P)
+    i0, d0 = pb.k_closest_self(4, device=True)
+    i1, d1 = pb.k_closest_self(4, device=True, candidates="gram")
+    assert torch.equal(i0, i1) and torch.equal(d0, d1)
+    # invalid limits are refused on the host
+    assert N.lib().thea_selftest_bounded_wait(0, None) == N.THEA_ERR_INVALID_ARGUMENT

@@ -16,6 +16,7 @@ STATUS_NAMES = {0: "THEA_OK", 1: "THEA_ERR_INVALID_ARGUMENT", 2: "THEA_ERR_OUT_O
                 9: "THEA_ERR_WAIT_TIMEOUT"}
 THEA_ERR_INVALID_ARGUMENT = 1
 THEA_ERR_ADMISSION_REFUSED = 3
+THEA_ERR_DEVICE_TIMEOUT = 4
 THEA_ERR_CANCELLED = 8
 THEA_ERR_WAIT_TIMEOUT = 9
 
@@ -43,7 +44,7 @@ class BvhInfo(ctypes.Structure):
     _fields_ = [("num_elements", ctypes.c_int64), ("num_nodes", ctypes.c_int64), ("width", ctypes.c_int32),
                 ("max_leaf_size", ctypes.c_int32), ("is_mesh", ctypes.c_int32), ("depth", ctypes.c_int32),
                 ("device_bytes", ctypes.c_int64), ("bounds_lo", ctypes.c_float * 3), ("bounds_hi", ctypes.c_float * 3),
-                ("device_error_bits", ctypes.c_uint32), ("reserved", ctypes.c_int32)]
+                ("device_error_bits", ctypes.c_uint32), ("num_segments", ctypes.c_int32)]
 
 
 class Tuning(ctypes.Structure):
@@ -96,6 +97,8 @@ SIGNATURES = {
     "thea_point_bvh_build": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(BuildConfig), _vp, ctypes.POINTER(_vp)]),
     "thea_bvh_destroy": (ctypes.c_int, [_vp]),
     "thea_bvh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(BvhInfo)]),
+    "thea_bvh_serialize": (ctypes.c_int, [_vp, _vp, _i64, _i64p, _vp]),
+    "thea_bvh_deserialize": (ctypes.c_int, [_vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "thea_closest_element": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp]),
     "thea_ray_intersection": (ctypes.c_int, [_vp, _vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp]),
     "thea_k_closest": (ctypes.c_int, [_vp, _vp, _i64, _i32, _f32, _vp, _vp, _vp, _vp]),
@@ -121,6 +124,7 @@ SIGNATURES = {
                                                    ctypes.POINTER(Tuning)]),
     "thea_k_closest_self_ex": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "thea_radius_neighbors": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp]),
+    "thea_selftest_bounded_wait": (ctypes.c_int, [_i32, _vp]),
     "thea_point_gram_tile": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp]),
     "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "thea_server_destroy": (ctypes.c_int, [_vp]),

@@ -81,7 +81,35 @@ class _Bvh:
         return {"num_elements": inf.num_elements, "num_nodes": inf.num_nodes, "width": inf.width,
                 "max_leaf_size": inf.max_leaf_size, "is_mesh": bool(inf.is_mesh), "depth": inf.depth,
                 "device_bytes": inf.device_bytes, "bounds_lo": list(inf.bounds_lo), "bounds_hi": list(inf.bounds_hi),
-                "device_error_bits": inf.device_error_bits}
+                "device_error_bits": inf.device_error_bits, "num_segments": inf.num_segments}
+
+    def to_bytes(self):
+        """Byte image of the built BVH (thea_bvh_serialize); ``type(self).from_bytes`` reloads it without a rebuild."""
+        size = ctypes.c_int64()
+        N.check(N.lib().thea_bvh_serialize(self._h, None, 0, ctypes.byref(size), None))
+        buf = ctypes.create_string_buffer(size.value)
+        N.check(N.lib().thea_bvh_serialize(self._h, buf, size.value, ctypes.byref(size), None))
+        return buf.raw[:size.value]
+
+    @classmethod
+    def from_bytes(cls, image):
+        """A handle on the current device from a byte image (thea_bvh_deserialize); the image's kind (mesh or points)
+        must match the class."""
+        image = bytes(image)
+        buf = (ctypes.c_char * max(len(image), 1)).from_buffer_copy(image or b"\0")
+        obj = cls.__new__(cls)
+        _Bvh.__init__(obj)
+        N.check(N.lib().thea_bvh_deserialize(buf, len(image), None, ctypes.byref(obj._h)))
+        inf = obj.info()
+        if inf["is_mesh"] != issubclass(cls, (MeshBvh, MeshForest)):
+            obj.close()
+            raise N.TheaError(N.THEA_ERR_INVALID_ARGUMENT, "bvh_deserialize: the image holds a %s BVH, not a %s" %
+                              ("mesh" if inf["is_mesh"] else "point", cls.__name__))
+        obj._restored(inf)
+        return obj
+
+    def _restored(self, inf):
+        pass
 
     def close(self):
         if self._h:
@@ -192,6 +220,9 @@ class MeshForest(_Bvh):
         cfg = _config(width, max_leaf_size, layouts)
         N.check(N.lib().thea_mesh_forest_build(pv, nv, pf, poff, self.num_meshes, ctypes.byref(cfg),
                                                _stream_of(io.device), ctypes.byref(self._h)))
+
+    def _restored(self, inf):
+        self.num_meshes = inf["num_segments"]
 
     def batch_closest_element(self, queries, query_offsets, dist_bound=-1.0, precision="fp32", queries_per_warp=0,
                               hard_query_budget=0, closest_points=False, errors=False, out=None):
@@ -306,6 +337,9 @@ class PointBvh(_Bvh):
         cfg = _config(width, max_leaf_size, 0, query_order)
         N.check(N.lib().thea_point_bvh_build(pp, n, ctypes.byref(cfg), _stream_of(io.device), ctypes.byref(self._h)))
         self.n = n
+
+    def _restored(self, inf):
+        self.n = inf["num_elements"]
 
     def k_closest_pairs(self, queries, k, dist_bound=-1.0, exclude=None):
         """BvhN::kClosestPairs: (indices [n, k], squared distances [n, k]); unused slots -1."""

@@ -6,6 +6,7 @@
 #include "batch.hpp"
 #include "serve.hpp"
 #include "gram.hpp"
+#include "serialize.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -369,6 +370,23 @@ THEA_API thea_status thea_bvh_destroy(thea_bvh * bvh) {
   });
 }
 
+THEA_API thea_status thea_bvh_serialize(const thea_bvh * bvh, void * out_image, int64_t capacity, int64_t * out_bytes,
+                                        void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(bvh && out_bytes, "bvh_serialize: null argument");
+    THEA_REQUIRE(!out_image || is_host_pointer(out_image), "bvh_serialize: the image buffer must be host memory");
+    *out_bytes = serialize_bvh(bvh, out_image, capacity, (cudaStream_t)stream);
+  });
+}
+
+THEA_API thea_status thea_bvh_deserialize(const void * image, int64_t bytes, void * stream, thea_bvh ** out_bvh) {
+  return guarded([&] {
+    THEA_REQUIRE(out_bvh, "bvh_deserialize: null output");
+    *out_bvh = nullptr;
+    *out_bvh = deserialize_bvh(image, bytes, (cudaStream_t)stream);
+  });
+}
+
 THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * info) {
   return guarded([&] {
     THEA_REQUIRE(bvh && info, "bvh_get_info: null argument");
@@ -379,6 +397,7 @@ THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * inf
     info->max_leaf_size = bvh->leaf_size;
     info->is_mesh = bvh->is_mesh;
     info->depth = bvh->depth;
+    info->num_segments = bvh->num_segments;
     info->device_bytes = bvh->device_bytes;
     for (int i = 0; i < 3; ++i) {
       info->bounds_lo[i] = bvh->lo[i];
@@ -546,6 +565,18 @@ THEA_API thea_status thea_radius_neighbors(const thea_bvh * point_bvh, const flo
     run_range(point_bvh, queries, num_queries, radius, exclude_index, out_offsets, out_index, out_sq_distance,
               handle_error_word(point_bvh), (cudaStream_t)stream);
   });
+}
+
+THEA_API thea_status thea_selftest_bounded_wait(int32_t spin_limit, void * stream) {
+  thea_status r = THEA_OK;
+  thea_status g = guarded([&] {
+    THEA_REQUIRE(spin_limit >= 1 && spin_limit <= (1 << 20), "selftest_bounded_wait: spin_limit must be 1..2^20");
+    if (run_wait_probe(spin_limit, (cudaStream_t)stream)) {
+      g_error = "selftest_bounded_wait: the device wait gave up as designed";
+      r = THEA_ERR_DEVICE_TIMEOUT;
+    }
+  });
+  return g != THEA_OK ? g : r;
 }
 
 THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,

@@ -103,10 +103,10 @@ __device__ __forceinline__ void mma_commit(unsigned long long * bar) {
                : "memory");
 }
 
-// Bounded wait for the barrier phase `parity`; false if it did not complete within GRAM_SPIN_LIMIT rounds.
-__device__ __forceinline__ bool mbar_wait(unsigned long long * bar, uint32_t parity) {
+// Bounded wait for the barrier phase `parity`; false if it did not complete within `limit` rounds.
+__device__ __forceinline__ bool mbar_wait(unsigned long long * bar, uint32_t parity, int limit = GRAM_SPIN_LIMIT) {
   uint32_t a = smem_addr(bar);
-  for (int i = 0; i < GRAM_SPIN_LIMIT; ++i) {
+  for (int i = 0; i < limit; ++i) {
     uint32_t ok;
     asm volatile(
         "{\n"
@@ -374,12 +374,34 @@ gram_tile_kernel(float4 const * __restrict__ a, int na, float4 const * __restric
   gram_teardown(s, err);
 }
 
+// Self-test of the bounded wait above: one warp waits on a barrier phase that nothing completes. The wait must give up
+// after `limit` rounds and report it (out = 1), leaving the context usable.
+__global__ void wait_probe_kernel(int limit, int * out) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  bool ok = mbar_wait(&bar, 0u, limit);
+  if (threadIdx.x == 0) *out = ok ? 0 : 1;
+}
+
 __global__ void to_float4_kernel(float const * __restrict__ p, int n, float4 * __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = make_float4(p[3 * i], p[3 * i + 1], p[3 * i + 2], __int_as_float(i));
 }
 
 }  // namespace
+
+bool run_wait_probe(int limit, cudaStream_t s) {
+  Scratch flag(sizeof(int), s);
+  THEA_LAUNCH(wait_probe_kernel, 1, 32, 0, s, limit, flag.as<int>());
+  int h = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&h, flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  return h != 0;
+}
 
 int gram_tile_rows() { return GRAM_M; }
 int gram_tile_cols() { return GRAM_WINDOW; }

@@ -16,4 +16,8 @@ void run_gram_bounds(thea_bvh const * b, int k, float * bound, cudaStream_t s);
 // a: na <= 128 points, b: nb <= 512 points, device arrays of 3 floats each.
 void run_gram_tile(float const * a, int na, float const * b, int nb, float * keys, unsigned * err, cudaStream_t s);
 
+// Runs the bounded device-side wait of these kernels on a barrier that nothing completes; true if it gave up (the
+// expected outcome) within `limit` try-wait rounds. Synchronizes the stream.
+bool run_wait_probe(int limit, cudaStream_t s);
+
 }  // namespace thea
