@@ -110,6 +110,19 @@ THEA_API thea_status thea_point_bvh_build(const float * points, int64_t num_poin
 /* Releases the handle after all work on `stream`-ordered queries using it has completed (synchronizes the device). */
 THEA_API thea_status thea_bvh_destroy(thea_bvh * bvh);
 
+/* Affine transform of a built BVH (BvhN::setTransform / clearTransform / getTransformInv, BvhN.hpp:903-929), for
+ * queries against the transformed elements without rebuilding from the caller's arrays. affine_3x4: row-major [L | t],
+ * p -> L p + t; L must be invertible. As in the reference, rays are moved into object space with the FP32 inverse
+ * (t' = L^-1 (-t)) and hit normals are returned in world space (normalised inverse-transpose); closest-point, k-NN and
+ * radius queries are answered on the elements transformed into world space (the handle builds a world-space copy of
+ * its records on the device: about twice the handle's memory while a transform is set). Single BVHs only (forests:
+ * THEA_ERR_INVALID_ARGUMENT). Synchronizes the stream; must not run while queries on the handle are in flight. */
+THEA_API thea_status thea_bvh_set_transform(thea_bvh * bvh, const float * affine_3x4, void * stream);
+THEA_API thea_status thea_bvh_clear_transform(thea_bvh * bvh);
+/* *has_transform = 0 or 1; affine_3x4 / inverse_3x4 (nullable) receive the map and its FP32 inverse (identity if none) */
+THEA_API thea_status thea_bvh_get_transform(const thea_bvh * bvh, int32_t * has_transform, float * affine_3x4,
+                                            float * inverse_3x4);
+
 /* Byte image of a built BVH (any kind: mesh, points, forest), for warm starts without a rebuild: a versioned header
  * (magic "THEABVH", version 1), the handle's parameters, then its arrays. out_image == NULL: *out_bytes = the image
  * size. Otherwise the image is written to host memory out_image (capacity bytes). Synchronizes the stream. The

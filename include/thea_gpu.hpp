@@ -65,6 +65,16 @@ class BvhHandle {
     check(thea_bvh_get_info(h_, &i));
     return i;
   }
+  // BvhN::setTransform / clearTransform: affine_3x4 row-major [L | t]
+  void setTransform(float const * affine_3x4, void * stream = nullptr) {
+    check(thea_bvh_set_transform(h_, affine_3x4, stream));
+  }
+  void clearTransform() { check(thea_bvh_clear_transform(h_)); }
+  bool hasTransform() const {
+    int32_t has = 0;
+    check(thea_bvh_get_transform(h_, &has, nullptr, nullptr));
+    return has != 0;
+  }
   // Byte image of the built BVH (thea_bvh_serialize); the class's fromImage reloads it without a rebuild.
   std::vector<unsigned char> serialize(void * stream = nullptr) const {
     int64_t n = 0;

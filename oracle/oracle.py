@@ -73,6 +73,10 @@ def lib():
         L.oracle_box_ray_time.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_float]
         L.oracle_tree_depth.restype = _i64
         L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
+        L.oracle_affine_inverse.restype = ctypes.c_int
+        L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
+        for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
+            getattr(L, name).argtypes = [_f32p, _f32p, _i64, _f32p]
         _lib = L
     return _lib
 
@@ -306,3 +310,44 @@ def triangle_props(tris):
 
 def tree_depth(n, max_leaf=5):
     return lib().oracle_tree_depth(int(n), int(max_leaf))
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# Affine transforms (BvhN::setTransform semantics): row-major 3x4 [L | t] in FP32
+# ---------------------------------------------------------------------------------------------------------------------
+
+def _affine(m):
+    m = _f32(m)
+    if m.shape == (4, 4):
+        m = np.ascontiguousarray(m[:3])
+    return m.reshape(3, 4)
+
+
+def affine_inverse(m):
+    """AffineTransformN::inverse in FP32 (Eigen's 3x3 cofactor inverse); None if the linear part is singular."""
+    m = _affine(m)
+    inv = np.empty((3, 4), np.float32)
+    return inv if lib().oracle_affine_inverse(_p(m, _f32p), _p(inv, _f32p)) else None
+
+
+def _apply(name, m, v):
+    m = _affine(m)
+    v = _f32(v).reshape(-1, 3)
+    out = np.empty_like(v)
+    getattr(lib(), name)(_p(m, _f32p), _p(v, _f32p), len(v), _p(out, _f32p))
+    return out
+
+
+def affine_points(m, p):
+    """L p + t per point (AffineTransformN::operator*)."""
+    return _apply("oracle_affine_points", m, p)
+
+
+def affine_vectors(m, v):
+    """L v per vector (the linear part, as for ray directions)."""
+    return _apply("oracle_affine_vectors", m, v)
+
+
+def normals_to_world(inv, n):
+    """normalToWorldSpace: (L^-1)^T n normalised, with inv the inverse transform."""
+    return _apply("oracle_normals_to_world", inv, n)

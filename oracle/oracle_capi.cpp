@@ -377,4 +377,26 @@ float oracle_box_ray_time(float const * lo, float const * hi, float const * o, f
 
 int64_t oracle_tree_depth(int64_t n, int max_leaf) { return treeDepth(n, max_leaf, 0.5f); }
 
+// Affine transforms (FP32): the inverse (returns 0 if singular), points through [L | t], vectors through L, normals
+// through the inverse transpose (m then holds the inverse)
+int oracle_affine_inverse(float const * m, float * inv) { return affineInverse(m, inv) ? 1 : 0; }
+void oracle_affine_points(float const * m, float const * p, int64_t n, float * out) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> w = affinePoint(m, q3<float>(p, i));
+    out[3 * i] = w.x; out[3 * i + 1] = w.y; out[3 * i + 2] = w.z;
+  }
+}
+void oracle_affine_vectors(float const * m, float const * v, int64_t n, float * out) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> w = affineLinear(m, q3<float>(v, i));
+    out[3 * i] = w.x; out[3 * i + 1] = w.y; out[3 * i + 2] = w.z;
+  }
+}
+void oracle_normals_to_world(float const * inv, float const * nrm, int64_t n, float * out) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> w = normalToWorld(inv, q3<float>(nrm, i));
+    out[3 * i] = w.x; out[3 * i + 1] = w.y; out[3 * i + 2] = w.z;
+  }
+}
+
 }  // extern "C"

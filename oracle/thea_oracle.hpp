@@ -798,4 +798,41 @@ template <class F> void parallelFor(int64_t n, int nthreads, F f) {
   for (auto & x : th) x.join();
 }
 
+//============================================================================================================================
+// Affine transforms (BvhN::setTransform, BvhN.hpp:903-912; AffineTransformN.hpp:133-137,160; toObjectSpace and
+// normalToWorldSpace, BvhN.hpp:2175-2184). Matrices are row-major 3x4 [L | t].
+//
+// Products follow Eigen's coefficient-wise evaluation of a fixed 3x3 by 3-vector product (row(i) . v, reduced as
+// e0 + (e1 + e2)). The inverse restates Eigen 3.4's 3x3 inverse (Eigen/src/LU/InverseImpl.h, compute_inverse for size 3;
+// Eigen is not present here, so this step is the published algorithm, unpinned): cofactor(i, j) =
+// L(i+1, j+1) L(i+2, j+2) - L(i+1, j+2) L(i+2, j+1) (indices mod 3), det = the cofactors of column 0 dotted with column 0,
+// inverse(j, i) = cofactor(i, j) * (1 / det); then the translation L^-1 (-t) (AffineTransformN::inverse).
+//============================================================================================================================
+
+template <class S> inline V3<S> affinePoint(S const * m, V3<S> const & v) {
+  return V3<S>((m[0] * v.x + (m[1] * v.y + m[2] * v.z)) + m[3], (m[4] * v.x + (m[5] * v.y + m[6] * v.z)) + m[7],
+               (m[8] * v.x + (m[9] * v.y + m[10] * v.z)) + m[11]);
+}
+template <class S> inline V3<S> affineLinear(S const * m, V3<S> const & v) {
+  return V3<S>(m[0] * v.x + (m[1] * v.y + m[2] * v.z), m[4] * v.x + (m[5] * v.y + m[6] * v.z),
+               m[8] * v.x + (m[9] * v.y + m[10] * v.z));
+}
+template <class S> inline bool affineInverse(S const * m, S * inv) {
+  auto L = [&](int i, int j) { return m[4 * (i % 3) + (j % 3)]; };
+  auto cof = [&](int i, int j) { return L(i + 1, j + 1) * L(i + 2, j + 2) - L(i + 1, j + 2) * L(i + 2, j + 1); };
+  S det = cof(0, 0) * m[0] + (cof(1, 0) * m[4] + cof(2, 0) * m[8]);
+  if (!(det != S(0)) || !std::isfinite(det)) return false;
+  S invdet = S(1) / det;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) inv[4 * j + i] = cof(i, j) * invdet;
+  S nt[3] = {-m[3], -m[7], -m[11]};
+  for (int r = 0; r < 3; ++r) inv[4 * r + 3] = inv[4 * r] * nt[0] + (inv[4 * r + 1] * nt[1] + inv[4 * r + 2] * nt[2]);
+  return true;
+}
+// (L^-1)^T n, normalised; inv is the inverse transform's 3x4 matrix
+template <class S> inline V3<S> normalToWorld(S const * inv, V3<S> const & n) {
+  return normalized(V3<S>(inv[0] * n.x + (inv[4] * n.y + inv[8] * n.z), inv[1] * n.x + (inv[5] * n.y + inv[9] * n.z),
+                          inv[2] * n.x + (inv[6] * n.y + inv[10] * n.z)));
+}
+
 }  // namespace oracle

@@ -84,6 +84,10 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.thea_k_closest_self(None, 4, None, None, None) == 1
     assert lib.thea_sample_by_area(None, 0, None, 0, 5, 1, 9, None, None, None, None, None) == 1
     assert lib.thea_bvh_destroy(None) == 0
+    eye = np.eye(3, 4, dtype=np.float32)
+    assert lib.thea_bvh_set_transform(None, eye.ctypes.data, None) == 1
+    assert lib.thea_bvh_clear_transform(None) == 1
+    assert lib.thea_bvh_get_transform(None, None, None, None) == 1
     with pytest.raises(N.TheaError):
         N.check(lib.thea_k_closest_self(None, 4, None, None, None))
 
@@ -119,8 +123,8 @@ def _image_header(version=1, width=4, n=4, num_nodes=1, segments=1, is_mesh=1, l
     """A serialized-BVH header (the fixed layout thea_bvh_serialize writes), for rejection tests without a device."""
     import struct
     node, cp, ray, pt = sections if sections is not None else (num_nodes * 128, n * 128, n * 48, 0)
-    return struct.pack("<8sI5iIi3q6f4q", b"THEABVH\0", version, is_mesh, width, 4, 1, 0, layouts, segments, n,
-                       num_nodes, 0, 0, 0, 0, 1, 1, 1, node, cp, ray, pt)
+    return struct.pack("<8sI5iIi3q6f4q2i12f", b"THEABVH\0", version, is_mesh, width, 4, 1, 0, layouts, segments, n,
+                       num_nodes, 0, 0, 0, 0, 1, 1, 1, node, cp, ray, pt, 0, 0, *([0.0] * 12))
 
 
 def test_bvh_images_are_checked_before_any_device_call(lib):

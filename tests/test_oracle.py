@@ -192,3 +192,34 @@ def test_range_brute_matches_numpy_restatement(oracle):
         want = want[want != ex[i]]
         assert np.array_equal(idx[off[i]:off[i + 1]], want)
         assert np.array_equal(d2[off[i]:off[i + 1]], dd[want])
+
+
+def test_affine_restatement(oracle):
+    """The transform arithmetic (AffineTransformN::inverse / operator*, normalToWorldSpace): exact on a map whose inverse
+    is representable, within FP32 rounding of the FP64 inverse on a general map, identity leaves points bit-identical."""
+    m = np.array([[2, 0, 0, 1], [0, 4, 0, 2], [0, 0, 8, 3]], np.float32)
+    inv = oracle.affine_inverse(m)
+    assert np.array_equal(inv, np.array([[0.5, 0, 0, -0.5], [0, 0.25, 0, -0.5], [0, 0, 0.125, -0.375]], np.float32))
+    P = W.uniform_box_points(1000, [-5] * 3, [5] * 3, 1)
+    assert np.array_equal(oracle.affine_points(np.eye(3, 4, dtype=np.float32), P), P)
+    m0 = m.copy()
+    m0[:, 3] = 0
+    assert np.array_equal(oracle.affine_points(oracle.affine_inverse(m0), oracle.affine_points(m0, P)), P)  # exact
+    rng = np.random.default_rng(2)
+    for _ in range(20):
+        g = rng.normal(size=(3, 4)).astype(np.float32)
+        inv = oracle.affine_inverse(g)
+        g64 = np.vstack([g.astype(np.float64), [0, 0, 0, 1]])
+        ref = np.linalg.inv(g64)[:3]
+        cond = np.linalg.cond(g64[:3, :3])
+        assert np.allclose(inv, ref, rtol=0, atol=1e-5 * cond * np.abs(ref).max())
+        # a point mapped there and back returns within rounding
+        back = oracle.affine_points(inv, oracle.affine_points(g, P))
+        assert np.allclose(back, P, atol=1e-4 * cond * 5)
+    assert oracle.affine_inverse(np.array([[1, 2, 3, 0], [2, 4, 6, 0], [0, 0, 1, 0]], np.float32)) is None
+    # a rotation maps unit normals like vectors
+    c, s = np.float32(0.6), np.float32(0.8)
+    rot = np.array([[c, -s, 0, 3], [s, c, 0, -1], [0, 0, 1, 2]], np.float32)
+    n = np.array([[1, 0, 0], [0, 0, 1]], np.float32)
+    w = oracle.normals_to_world(oracle.affine_inverse(rot), n)
+    assert np.allclose(w, oracle.affine_vectors(rot, n), atol=1e-6)

@@ -97,6 +97,9 @@ SIGNATURES = {
     "thea_point_bvh_build": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(BuildConfig), _vp, ctypes.POINTER(_vp)]),
     "thea_bvh_destroy": (ctypes.c_int, [_vp]),
     "thea_bvh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(BvhInfo)]),
+    "thea_bvh_set_transform": (ctypes.c_int, [_vp, _vp, _vp]),
+    "thea_bvh_clear_transform": (ctypes.c_int, [_vp]),
+    "thea_bvh_get_transform": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "thea_bvh_serialize": (ctypes.c_int, [_vp, _vp, _i64, _i64p, _vp]),
     "thea_bvh_deserialize": (ctypes.c_int, [_vp, _i64, _vp, ctypes.POINTER(_vp)]),
     "thea_closest_element": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp]),

@@ -18,8 +18,9 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libthea_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-              "-Xptxas", "-v"]
+# host code too is compiled without floating-point contraction (aarch64 hosts would otherwise fuse multiply-adds)
+NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo",
+              "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-Xptxas", "-v"]
 
 
 def nvcc():

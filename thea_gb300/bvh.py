@@ -19,6 +19,11 @@ def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
 
+def _cuda_ready():
+    import torch
+    return torch.cuda.is_available() and torch.cuda.is_initialized()
+
+
 def _stream_of(on_device):
     if not on_device:
         return None
@@ -82,6 +87,29 @@ class _Bvh:
                 "max_leaf_size": inf.max_leaf_size, "is_mesh": bool(inf.is_mesh), "depth": inf.depth,
                 "device_bytes": inf.device_bytes, "bounds_lo": list(inf.bounds_lo), "bounds_hi": list(inf.bounds_hi),
                 "device_error_bits": inf.device_error_bits, "num_segments": inf.num_segments}
+
+    def set_transform(self, affine):
+        """BvhN::setTransform: queries then act on the elements mapped by ``affine`` (3x4 [L | t], or 4x4 with last row
+        0 0 0 1). Rays go into object space with the FP32 inverse, closest-point / k-NN / radius queries run on a
+        world-space copy of the records built on the device."""
+        m = np.asarray(affine, np.float32)
+        if m.shape == (4, 4):
+            m = m[:3]
+        if m.shape != (3, 4):
+            raise ValueError("affine must be 3x4 or 4x4")
+        m = np.ascontiguousarray(m)
+        N.check(N.lib().thea_bvh_set_transform(self._h, m.ctypes.data, _stream_of(_cuda_ready())))
+
+    def clear_transform(self):
+        N.check(N.lib().thea_bvh_clear_transform(self._h))
+
+    def transform(self):
+        """(affine 3x4, its FP32 inverse 3x4), or None without a transform."""
+        has = ctypes.c_int32()
+        m = np.empty((3, 4), np.float32)
+        inv = np.empty((3, 4), np.float32)
+        N.check(N.lib().thea_bvh_get_transform(self._h, ctypes.byref(has), m.ctypes.data, inv.ctypes.data))
+        return (m, inv) if has.value else None
 
     def to_bytes(self):
         """Byte image of the built BVH (thea_bvh_serialize); ``type(self).from_bytes`` reloads it without a rebuild."""

@@ -7,6 +7,7 @@
 #include "serve.hpp"
 #include "gram.hpp"
 #include "serialize.hpp"
+#include "transform.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -387,6 +388,28 @@ THEA_API thea_status thea_bvh_deserialize(const void * image, int64_t bytes, voi
   });
 }
 
+THEA_API thea_status thea_bvh_set_transform(thea_bvh * bvh, const float * affine_3x4, void * stream) {
+  return guarded([&] { set_transform(bvh, affine_3x4, (cudaStream_t)stream); });
+}
+
+THEA_API thea_status thea_bvh_clear_transform(thea_bvh * bvh) {
+  return guarded([&] {
+    THEA_REQUIRE(bvh, "bvh_clear_transform: null handle");
+    clear_transform(bvh);
+  });
+}
+
+THEA_API thea_status thea_bvh_get_transform(const thea_bvh * bvh, int32_t * has_transform, float * affine_3x4,
+                                            float * inverse_3x4) {
+  return guarded([&] {
+    THEA_REQUIRE(bvh && has_transform, "bvh_get_transform: null argument");
+    *has_transform = bvh->has_transform;
+    float const id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    if (affine_3x4) std::memcpy(affine_3x4, bvh->has_transform ? bvh->xf : id, sizeof(id));
+    if (inverse_3x4) std::memcpy(inverse_3x4, bvh->has_transform ? bvh->xf_inv : id, sizeof(id));
+  });
+}
+
 THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * info) {
   return guarded([&] {
     THEA_REQUIRE(bvh && info, "bvh_get_info: null argument");
@@ -402,6 +425,24 @@ THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * inf
     for (int i = 0; i < 3; ++i) {
       info->bounds_lo[i] = bvh->lo[i];
       info->bounds_hi[i] = bvh->hi[i];
+    }
+    if (bvh->world) {
+      for (int i = 0; i < 3; ++i) {
+        info->bounds_lo[i] = bvh->world->lo[i];
+        info->bounds_hi[i] = bvh->world->hi[i];
+      }
+    } else if (bvh->has_transform) {
+      // world-space box of the transformed corners (AxisAlignedBoxN::transformAndBound)
+      for (int i = 0; i < 3; ++i) info->bounds_lo[i] = INFINITY, info->bounds_hi[i] = -INFINITY;
+      for (int c = 0; c < 8; ++c) {
+        V3 w = affine_point(bvh->xf, V3{(c & 1) ? bvh->hi[0] : bvh->lo[0], (c & 2) ? bvh->hi[1] : bvh->lo[1],
+                                        (c & 4) ? bvh->hi[2] : bvh->lo[2]});
+        float wc[3] = {w.x, w.y, w.z};
+        for (int i = 0; i < 3; ++i) {
+          info->bounds_lo[i] = std::min(info->bounds_lo[i], wc[i]);
+          info->bounds_hi[i] = std::max(info->bounds_hi[i], wc[i]);
+        }
+      }
     }
     unsigned * w = handle_error_word(bvh);
     unsigned bits = 0;
@@ -420,6 +461,7 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
   THEA_REQUIRE(num_queries >= 0, "closest_element: negative query count");
   if (num_queries == 0) return;
   THEA_REQUIRE(queries && out_index, "closest_element: null queries or out_index");
+  mesh_bvh = query_target(mesh_bvh);
   ClosestParams cp;
   cp.thresh = bound_threshold(dist_bound);
   cp.bound2 = dist_bound >= 0.f ? (double)dist_bound * (double)dist_bound : -1.0;
@@ -455,8 +497,19 @@ static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const flo
               {out_index64, 4, true, false}, {out_flags, 4, true, false}},
              num_rays, (cudaStream_t)stream,
              [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
-               run_ray(mesh_bvh, (float const *)p[0], (float const *)p[1], cnt, rp, (float *)p[2], (int32_t *)p[3],
-                       (float *)p[4], (float *)p[5], (int32_t *)p[6], (int32_t *)p[7], err, s);
+               float const * o = (float const *)p[0];
+               float const * d = (float const *)p[1];
+               Scratch o_obj, d_obj;
+               if (mesh_bvh->has_transform) {
+                 o_obj = Scratch((size_t)cnt * 12, s);
+                 d_obj = Scratch((size_t)cnt * 12, s);
+                 rays_to_object(mesh_bvh, o, d, cnt, o_obj.as<float>(), d_obj.as<float>(), s);
+                 o = o_obj.as<float>();
+                 d = d_obj.as<float>();
+               }
+               run_ray(mesh_bvh, o, d, cnt, rp, (float *)p[2], (int32_t *)p[3], (float *)p[4], (float *)p[5],
+                       (int32_t *)p[6], (int32_t *)p[7], err, s);
+               if (mesh_bvh->has_transform) normals_to_world(mesh_bvh, (float *)p[4], cnt, s);
              });
 }
 
@@ -508,6 +561,7 @@ THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * qu
     THEA_REQUIRE(num_queries >= 0, "k_closest: negative query count");
     if (num_queries == 0) return;
     THEA_REQUIRE(queries && out_index && out_sq_distance, "k_closest: null queries or outputs");
+    point_bvh = query_target(point_bvh);
     float thresh = bound_threshold(dist_bound);
     unsigned * err = handle_error_word(point_bvh);
     run_staged({{(void *)queries, 12, false, false}, {(void *)exclude_index, 4, false, false},
@@ -527,6 +581,7 @@ static void knn_self_impl(const thea_bvh * point_bvh, int32_t k, int32_t candida
   THEA_REQUIRE(candidates == THEA_KNN_CANDIDATES_TRAVERSAL || candidates == THEA_KNN_CANDIDATES_GRAM,
                "k_closest_self: unknown candidate mode");
   THEA_REQUIRE(out_index && out_sq_distance, "k_closest_self: null outputs");
+  point_bvh = query_target(point_bvh);
   cudaStream_t s = (cudaStream_t)stream;
   unsigned * err = handle_error_word(point_bvh);
   int64_t n = point_bvh->n;
@@ -562,8 +617,8 @@ THEA_API thea_status thea_radius_neighbors(const thea_bvh * point_bvh, const flo
     for (void const * p : arrays)
       THEA_REQUIRE(!p || !is_host_pointer(p), "radius_neighbors: every array must be device memory");
     THEA_REQUIRE(out_index || !out_sq_distance, "radius_neighbors: out_sq_distance needs out_index");
-    run_range(point_bvh, queries, num_queries, radius, exclude_index, out_offsets, out_index, out_sq_distance,
-              handle_error_word(point_bvh), (cudaStream_t)stream);
+    run_range(query_target(point_bvh), queries, num_queries, radius, exclude_index, out_offsets, out_index,
+              out_sq_distance, handle_error_word(point_bvh), (cudaStream_t)stream);
   });
 }
 

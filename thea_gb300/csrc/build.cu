@@ -666,6 +666,11 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
 
 void destroy_bvh(thea_bvh * b) {
   if (!b) return;
+  if (b->world) {
+    b->world->err = nullptr;  // shared with b
+    destroy_bvh(b->world);
+    b->world = nullptr;
+  }
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(b->device);

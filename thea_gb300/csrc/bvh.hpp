@@ -30,6 +30,11 @@ struct thea_bvh {
   int32_t * seg_root = nullptr;      // device, num_segments: root wide node of each segment
   std::vector<int64_t> seg_start_host;
   std::vector<float> seg_lo, seg_hi;  // per-segment element bounds (3 floats each)
+  // affine transform (BvhN::setTransform): row-major 3x4 [L | t] and its FP32 inverse; `world` is the world-space copy
+  // of the element records that closest-point, k-NN and radius queries read (it shares this handle's error word)
+  int32_t has_transform = 0;
+  float xf[12] = {0}, xf_inv[12] = {0};
+  thea_bvh * world = nullptr;
 };
 
 namespace thea {

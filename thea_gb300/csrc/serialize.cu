@@ -2,6 +2,7 @@
 // then its device arrays in a fixed order. Reloading an image skips the build: a serving process can warm-start its
 // resident meshes. The reference has no counterpart (its BvhN is not Serializable).
 #include "serialize.hpp"
+#include "transform.hpp"
 
 #include "common.cuh"
 
@@ -25,6 +26,8 @@ struct ImageHeader {
   int64_t n, num_nodes, device_bytes;
   float lo[3], hi[3];
   int64_t node_bytes, cp_bytes, ray_bytes, pt_bytes;  // sizes of the array sections
+  int32_t has_transform, reserved;
+  float xf[12];  // affine transform (row-major 3x4); the world-space copy is rebuilt on load
 };
 
 int64_t node_size(int width) { return width == 4 ? (int64_t)sizeof(WideNode<4>) : (int64_t)sizeof(WideNode<8>); }
@@ -58,6 +61,8 @@ ImageHeader header_of(thea_bvh const * b) {
   h.cp_bytes = b->cp_rec ? b->n * CP_REC_F4 * 16 : 0;
   h.ray_bytes = b->ray_rec ? b->n * RAY_REC_F4 * 16 : 0;
   h.pt_bytes = b->pt_rec ? b->n * 16 : 0;
+  h.has_transform = b->has_transform;
+  std::memcpy(h.xf, b->xf, sizeof(h.xf));
   return h;
 }
 
@@ -106,6 +111,8 @@ thea_bvh * deserialize_bvh(void const * in, int64_t bytes, cudaStream_t s) {
                    h.ray_bytes == (h.is_mesh && (h.layouts & THEA_LAYOUT_RAY) ? h.n * RAY_REC_F4 * 16 : 0) &&
                    h.pt_bytes == (h.is_mesh ? 0 : h.n * 16),
                "bvh_deserialize: inconsistent section sizes");
+  THEA_REQUIRE(h.has_transform == 0 || (h.has_transform == 1 && h.num_segments == 1),
+               "bvh_deserialize: inconsistent transform");
   THEA_REQUIRE(bytes >= image_bytes(h), "bvh_deserialize: buffer shorter than the image");
   thea_bvh * b = new thea_bvh;
   try {
@@ -153,6 +160,7 @@ thea_bvh * deserialize_bvh(void const * in, int64_t bytes, cudaStream_t s) {
     THEA_CUDA_CHECK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), s));
     // the host image may be reused by the caller as soon as this returns
     THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (h.has_transform) set_transform(b, h.xf, s);
     return b;
   } catch (...) {
     cudaStreamSynchronize(s);
