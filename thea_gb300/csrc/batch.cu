@@ -179,9 +179,9 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
   bool pending = false;    // mixed precision: traversal done, waiting for the warp's FP64 step
   int64_t ebase = 0;
   V3 p = V3{0.f, 0.f, 0.f};
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
+  int next = CHILD_EMPTY;  // nearest child of the last node, visited next without a stack round trip
   float best = 0.f;  // FP32 mode: best squared distance; mixed mode: band limit
   int best_idx = INT_MAX;
   int64_t best_slot = -1;
@@ -210,9 +210,8 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
           int m = mesh_of_query(a.qoff, f.M, q);
           ebase = __ldg(f.seg_start + m);
           p = load_v3(a.queries + 3 * q);
-          stk[0] = __ldg(f.seg_root + m);
-          stkd[0] = 0.f;
-          sp = 1;
+          sp = 0;
+          next = __ldg(f.seg_root + m);
           pops = 0;
           if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
             f64_search_init(s);
@@ -245,7 +244,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
     }
     if (__ballot_sync(FULL, q >= 0) == 0) break;
     if (q < 0 || pending) continue;
-    if (sp == 0) {
+    if (next == CHILD_EMPTY && sp == 0) {
       if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
         s.lim = best;
         s.best32 = best32;
@@ -258,7 +257,8 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
       continue;
     }
     if (budget > 0 && ++pops > budget) {
-      // over budget: queued with the best element so far, finished by a warp of its own in the second kernel
+      // over budget (steps taken, the register-held child included): queued with the best element so far, finished
+      // by a warp of its own in the second kernel
       unsigned long long pos = atomicAdd(hq.count, 1ull);
       hq.q[pos] = q;
       if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
@@ -273,15 +273,19 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
       q = -1;
       continue;
     }
-    --sp;
-    int code = stk[sp];
-    if (stkd[sp] > best * PRUNE_SLACK) continue;
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > best * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, f.err);
+      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, f.err);
     } else {
       int first, count;
       decode_leaf(code, first, count);

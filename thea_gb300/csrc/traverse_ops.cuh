@@ -287,6 +287,35 @@ __device__ __forceinline__ void push_children(NodeRegs<W> const & nd, float cons
   }
 }
 
+// push_children for the persistent-lane loops: the nearest kept child is returned in `next` (it would be popped right
+// away) and the others are pushed farthest first as packed (code, bound bits) entries, one 8-byte access each.
+// `next` is CHILD_EMPTY when no child is kept.
+template <int W, int STACK>
+__device__ __forceinline__ void push_children_next(NodeRegs<W> const & nd, float const (&lb)[W], float lim,
+                                                   int2 (&stk)[STACK], int & sp, int & next, unsigned * err) {
+  uint32_t key[W];
+  int cc[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    bool keep = nd.child[c] != CHILD_EMPTY && lb[c] <= lim;
+    key[c] = keep ? __float_as_uint(lb[c]) : 0xffffffffu;
+    cc[c] = nd.child[c];
+  }
+  sort_children<W>(key, cc);
+  next = key[0] != 0xffffffffu ? cc[0] : CHILD_EMPTY;
+#pragma unroll
+  for (int c = W - 1; c >= 1; --c) {
+    if (key[c] != 0xffffffffu) {
+      if (sp < STACK) {
+        stk[sp] = make_int2(cc[c], (int)key[c]);
+        ++sp;
+      } else {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+      }
+    }
+  }
+}
+
 template <int W>
 __device__ __forceinline__ void point_child_bounds(NodeRegs<W> const & nd, V3 p, float (&lb)[W]) {
 #pragma unroll
