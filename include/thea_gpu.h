@@ -185,6 +185,21 @@ THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const f
                                               float * out_normal, float * out_time_fp64, int32_t * out_index_fp64,
                                               int32_t * out_flags, void * stream);
 
+/* BvhN::rayIntersects (BvhN.hpp:1266-1269): out_hit[i] = 1 iff rayIntersectionTime(ray i, max_time) >= 0, i.e. some
+ * element is hit at a time in [0, max_time] (any time if max_time < 0). An any-hit search that stops at the first
+ * accepted element. Host or device arrays. */
+THEA_API thea_status thea_ray_intersects(const thea_bvh * mesh_bvh, const float * origins, const float * directions,
+                                         int64_t num_rays, float max_time, uint8_t * out_hit, void * stream);
+/* `count` unit directions of Random(seed).sphere() (Random.cpp:225-250), in stream order: xyz triples, host or device */
+THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * out_directions, void * stream);
+/* Visibility::compute (Algorithms/SurfaceFeatures/Local/Visibility.hpp:104-126) for many points: the fraction of
+ * num_rays rays from each point (origin pushed out by 0.001 |extent of the padded root box| along the direction) with no
+ * hit. Random(seed) replaces the reference's process-wide Random::common(): point i uses directions
+ * [i * num_rays, (i + 1) * num_rays) of the thea_random_sphere stream, so the result equals the reference run with that
+ * generator. num_rays <= 0: 100, as in the reference. Host or device arrays; synchronizes the stream. */
+THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * positions, int64_t num_points,
+                                     int32_t num_rays, uint32_t seed, double * out_fraction, void * stream);
+
 /* k nearest points of a point BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
  * index first). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
  * Code/Source/Algorithms/PointSet3.hpp:576-583). dist_bound < 0: unbounded; else only squared distances strictly below

@@ -73,6 +73,8 @@ def lib():
         L.oracle_box_ray_time.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_float]
         L.oracle_tree_depth.restype = _i64
         L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
+        L.oracle_random_sphere.argtypes = [ctypes.c_uint32, _i64, _f32p]
+        L.oracle_visibility.argtypes = [_vp, _f32p, _i64, _i64, ctypes.c_uint32, _f32p, _f64p, ctypes.c_int]
         L.oracle_affine_inverse.restype = ctypes.c_int
         L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
         for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
@@ -155,6 +157,16 @@ class MeshIndex:
         lib().oracle_ray_ref(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f32p), _p(idx, _i32p),
                              _p(nrm, _f32p), threads or default_threads())
         return t, idx, nrm
+
+    def visibility(self, positions, num_rays, seed, transform=None, threads=None):
+        """Visibility::compute per position with Random(seed) in place of Random::common() (FP32 handle only);
+        transform: an affine map (3x4) set on the BVH."""
+        p = _f32(positions).reshape(-1, 3)
+        out = np.empty(len(p), np.float64)
+        xf = _affine(transform) if transform is not None else None
+        lib().oracle_visibility(self.h, _p(p, _f32p), len(p), int(num_rays), int(seed),
+                                _p(xf, _f32p) if xf is not None else None, _p(out, _f64p), threads or default_threads())
+        return out
 
     def ray_contract(self, o, d, max_time=-1.0, threads=None):
         o = _f32(o).reshape(-1, 3)
@@ -351,3 +363,10 @@ def affine_vectors(m, v):
 def normals_to_world(inv, n):
     """normalToWorldSpace: (L^-1)^T n normalised, with inv the inverse transform."""
     return _apply("oracle_normals_to_world", inv, n)
+
+
+def random_sphere(seed, n):
+    """Random(seed).sphere() directions in stream order (Knop's method)."""
+    out = np.empty((int(n), 3), np.float32)
+    lib().oracle_random_sphere(int(seed), int(n), _p(out, _f32p))
+    return out

@@ -377,6 +377,43 @@ float oracle_box_ray_time(float const * lo, float const * hi, float const * o, f
 
 int64_t oracle_tree_depth(int64_t n, int max_leaf) { return treeDepth(n, max_leaf, 0.5f); }
 
+// Random(seed).sphere() directions in stream order
+void oracle_random_sphere(uint32_t seed, int64_t n, float * out) {
+  TheaRandom r(seed);
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> u = theaSphere(r);
+    out[3 * i] = u.x; out[3 * i + 1] = u.y; out[3 * i + 2] = u.z;
+  }
+}
+
+// Visibility::compute for each position with Random(seed): point i draws directions [i * num_rays, (i + 1) * num_rays)
+// xf (nullable): an affine transform set on the BVH (row-major 3x4)
+void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t num_rays, uint32_t seed,
+                       float const * xf, double * out, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  if (num_rays <= 0) num_rays = 100;
+  std::vector<V3<float>> dirs((size_t)(n * num_rays));
+  TheaRandom r(seed);
+  for (auto & u : dirs) u = theaSphere(r);
+  // getBounds(): the padded root box, or with a transform the box of its eight mapped corners (transformAndBound)
+  Box<float> box = h->f.tree.nodes[0].bounds;
+  float inv[12];
+  if (xf) {
+    affineInverse(xf, inv);
+    Box<float> w;
+    for (int c = 0; c < 8; ++c)
+      w.merge(affinePoint(xf, V3<float>((c & 1) ? box.hi.x : box.lo.x, (c & 2) ? box.hi.y : box.lo.y,
+                                        (c & 4) ? box.hi.z : box.lo.z)));
+    box = w;
+  }
+  float scale = norm(box.extent());
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i)
+      out[i] = visibilityFraction(h->f, q3<float>(positions, i), dirs.data() + i * num_rays, num_rays, scale,
+                                  xf ? inv : nullptr);
+  });
+}
+
 // Affine transforms (FP32): the inverse (returns 0 if singular), points through [L | t], vectors through L, normals
 // through the inverse transpose (m then holds the inverse)
 int oracle_affine_inverse(float const * m, float * inv) { return affineInverse(m, inv) ? 1 : 0; }

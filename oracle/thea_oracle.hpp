@@ -835,4 +835,38 @@ template <class S> inline V3<S> normalToWorld(S const * inv, V3<S> const & n) {
                           inv[2] * n.x + (inv[6] * n.y + inv[10] * n.z)));
 }
 
+//============================================================================================================================
+// Random::sphere (Random.cpp:225-250; Knop, CACM 13, 1970) and Visibility::compute
+// (Algorithms/SurfaceFeatures/Local/Visibility.hpp:104-126) with a given generator in place of Random::common().
+//============================================================================================================================
+
+inline V3<float> theaSphere(TheaRandom & r) {
+  float x, y, m2;
+  do {
+    x = 2 * r.uniform01() - 1;
+    y = 2 * r.uniform01() - 1;
+    m2 = x * x + y * y;
+  } while (m2 > 1 || m2 < 1e-10);
+  float z = 2 * m2 - 1;
+  float s = 2 * std::sqrt(1 - m2);
+  return V3<float>(x * s, y * s, z);
+}
+
+// Escaped fraction of the rays along dirs[0 .. num_rays) from `position`, with `scale` the |extent| of the BVH's
+// getBounds(); inv (nullable): the inverse of the BVH's transform, which moves each ray into object space
+// (toObjectSpace, BvhN.hpp:2175-2178)
+inline double visibilityFraction(MeshIndex<float> const & m, V3<float> const & position, V3<float> const * dirs,
+                                 int64_t num_rays, float scale, float const * inv) {
+  int64_t escaped = 0;
+  for (int64_t i = 0; i < num_rays; ++i) {
+    V3<float> u = dirs[i];
+    V3<float> offset = 0.001f * scale * u;
+    V3<float> o = position + offset, d = u;
+    if (inv) o = affinePoint(inv, o), d = affineLinear(inv, d);
+    bool hit = m.rayRef(o, d, -1.f).idx >= 0;  // rayIntersects = rayIntersectionTime >= 0
+    if (!hit) ++escaped;
+  }
+  return (double)escaped / num_rays;
+}
+
 }  // namespace oracle

@@ -223,3 +223,37 @@ def test_affine_restatement(oracle):
     n = np.array([[1, 0, 0], [0, 0, 1]], np.float32)
     w = oracle.normals_to_world(oracle.affine_inverse(rot), n)
     assert np.allclose(w, oracle.affine_vectors(rot, n), atol=1e-6)
+
+
+def test_random_sphere_restatement(oracle):
+    """Random::sphere (Knop's method) in the oracle equals a NumPy FP32 restatement over the same uniform stream, and
+    gives unit vectors."""
+    n = 3000
+    words = oracle.thea_random_bits(99, 4 * n).astype(np.uint64)
+    u = words.astype(np.float32) * np.float32(1.0 / 0xFFFFFFFF)
+    out = []
+    k = 0
+    while len(out) < n:
+        x = np.float32(2) * u[k] - np.float32(1)
+        y = np.float32(2) * u[k + 1] - np.float32(1)
+        k += 2
+        m2 = np.float32(x * x) + np.float32(y * y)
+        if m2 > 1 or float(m2) < 1e-10:
+            continue
+        z = np.float32(2) * m2 - np.float32(1)
+        s = np.float32(2) * np.sqrt(np.float32(1) - m2)
+        out.append([x * s, y * s, z])
+    ref = np.array(out, np.float32)
+    got = oracle.random_sphere(99, n)
+    assert np.array_equal(got, ref)
+    assert np.allclose(np.linalg.norm(got, axis=1), 1, atol=1e-6)
+
+
+def test_visibility_restatement_limits(oracle):
+    """Visibility of points far outside a sphere is near 1, inside it is 0, on it about one half."""
+    V, F = W.noisy_icosphere(3, 5)
+    m = oracle.MeshIndex(V, F)
+    assert np.all(m.visibility(V[:50] * np.float32(0.5), 100, 7) == 0)
+    assert np.all(m.visibility(V[:50] * np.float32(4), 100, 7) > 0.9)
+    on = m.visibility(V[:200], 100, 7)
+    assert 0.4 < on.mean() < 0.6

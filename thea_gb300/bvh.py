@@ -196,6 +196,39 @@ class MeshBvh(_Bvh):
         """BvhN::rayIntersectionTime: hit time per ray, -1 on a miss."""
         return self.ray_structure_intersection(origins, directions, max_time)[0]
 
+    def ray_intersects(self, origins, directions, max_time=-1.0):
+        """BvhN::rayIntersects: per ray, whether some element is hit at a time in [0, max_time] (any-hit search)."""
+        io = _Arrays(origins)
+        po, n = io.input(origins, np.float32, 3)
+        pd, nd = io.input(directions, np.float32, 3)
+        if nd != n:
+            raise ValueError("origins and directions differ in length")
+        if io.device:
+            import torch
+            hit = torch.empty(n, dtype=torch.uint8, device="cuda")
+            ph = ctypes.c_void_p(hit.data_ptr() if n else 0)
+        else:
+            hit = np.empty(n, np.uint8)
+            ph = ctypes.c_void_p(hit.ctypes.data if n else 0)
+        N.check(N.lib().thea_ray_intersects(self._h, po, pd, n, float(max_time), ph, _stream_of(io.device)))
+        return hit.bool() if io.device else hit.astype(bool)
+
+    def visibility(self, positions, num_rays=100, seed=0):
+        """Visibility::compute for each position (fraction of num_rays rays that escape), with Random(seed) in place of
+        the reference's Random::common(); float64 per point (CUDA tensor for CUDA input)."""
+        io = _Arrays(positions)
+        pp, n = io.input(positions, np.float32, 3)
+        if io.device:
+            import torch
+            out = torch.empty(n, dtype=torch.float64, device="cuda")
+            po = ctypes.c_void_p(out.data_ptr() if n else 0)
+        else:
+            out = np.empty(n, np.float64)
+            po = ctypes.c_void_p(out.ctypes.data if n else 0)
+        N.check(N.lib().thea_visibility(self._h, pp, n, int(num_rays), int(seed) & 0xffffffff, po,
+                                        _stream_of(io.device)))
+        return out
+
     def closest_element_ex(self, queries, dist_bound=-1.0, precision="fp32", closest_points=True, errors=True):
         """closest_element with a precision mode ("fp32": the reference's arithmetic; "fp64": FP64 re-check band) and
         per-query |returned distance - FP64 distance of the returned element|: (index, distance, cp, error)."""
@@ -426,6 +459,19 @@ def point_gram_tile(a, b):
     N.check(N.lib().thea_point_gram_tile(ctypes.c_void_p(a.data_ptr()), a.shape[0], ctypes.c_void_p(b.data_ptr()),
                                          b.shape[0], ctypes.c_void_p(keys.data_ptr()), _stream_of(True)))
     return keys
+
+
+def random_sphere(seed, count, device=False):
+    """`count` directions of Random(seed).sphere() in stream order (float32 [count, 3])."""
+    if device:
+        import torch
+        out = torch.empty((count, 3), dtype=torch.float32, device="cuda")
+        N.check(N.lib().thea_random_sphere(int(seed) & 0xffffffff, int(count), ctypes.c_void_p(out.data_ptr()),
+                                           _stream_of(True)))
+        return out
+    out = np.empty((count, 3), np.float32)
+    N.check(N.lib().thea_random_sphere(int(seed) & 0xffffffff, int(count), ctypes.c_void_p(out.ctypes.data), None))
+    return out
 
 
 def sample_evenly_by_area(vertices, faces, num_samples, seed, rng="thea"):

@@ -8,6 +8,7 @@
 #include "gram.hpp"
 #include "serialize.hpp"
 #include "transform.hpp"
+#include "visibility.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -549,6 +550,72 @@ THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const f
   return guarded([&] {
     ray_impl(mesh_bvh, origins, directions, num_rays, max_time, precision, out_time, out_index, out_normal,
              out_time_fp64, out_index_fp64, out_flags, stream);
+  });
+}
+
+THEA_API thea_status thea_ray_intersects(const thea_bvh * mesh_bvh, const float * origins, const float * directions,
+                                         int64_t num_rays, float max_time, uint8_t * out_hit, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "ray_intersects: a mesh BVH is required");
+    THEA_REQUIRE(mesh_bvh->ray_rec, "ray_intersects: the BVH was built without THEA_LAYOUT_RAY");
+    THEA_REQUIRE(num_rays >= 0, "ray_intersects: negative ray count");
+    if (num_rays == 0) return;
+    THEA_REQUIRE(origins && directions && out_hit, "ray_intersects: null origins, directions or out_hit");
+    float mt = max_time >= 0.f ? max_time : -1.f;
+    run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_hit, 1, true, false}},
+               num_rays, (cudaStream_t)stream,
+               [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
+                 run_ray_intersects(mesh_bvh, (float const *)p[0], (float const *)p[1], cnt, mt, (uint8_t *)p[2], s);
+               });
+  });
+}
+
+THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * out_directions, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(count >= 0, "random_sphere: negative count");
+    if (count == 0) return;
+    THEA_REQUIRE(out_directions, "random_sphere: null output");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (is_host_pointer(out_directions)) {
+      Scratch d((size_t)count * 12, s);
+      run_random_sphere(seed, count, d.as<float>(), s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(out_directions, d.ptr, (size_t)count * 12, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    } else {
+      run_random_sphere(seed, count, out_directions, s);
+    }
+  });
+}
+
+THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * positions, int64_t num_points,
+                                     int32_t num_rays, uint32_t seed, double * out_fraction, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "visibility: a mesh BVH is required");
+    THEA_REQUIRE(mesh_bvh->ray_rec, "visibility: the BVH was built without THEA_LAYOUT_RAY");
+    THEA_REQUIRE(num_points >= 0, "visibility: negative point count");
+    if (num_points == 0) return;
+    THEA_REQUIRE(positions && out_fraction, "visibility: null positions or out_fraction");
+    if (num_rays <= 0) num_rays = 100;  // Visibility::compute: DEFAULT_NUM_RAYS for a non-positive count
+    THEA_REQUIRE((int64_t)num_points * num_rays < ((int64_t)1 << 31), "visibility: too many rays for one call");
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch pin, pout;
+    float const * pos = positions;
+    double * out = out_fraction;
+    if (is_host_pointer(positions)) {
+      pin = Scratch((size_t)num_points * 12, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(pin.ptr, positions, (size_t)num_points * 12, cudaMemcpyHostToDevice, s));
+      pos = pin.as<float>();
+    }
+    bool host_out = is_host_pointer(out_fraction);
+    if (host_out) {
+      pout = Scratch((size_t)num_points * 8, s);
+      out = pout.as<double>();
+    }
+    run_visibility(mesh_bvh, pos, num_points, num_rays, seed, out, s);
+    if (host_out) {
+      THEA_CUDA_CHECK(cudaMemcpyAsync(out_fraction, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
   });
 }
 

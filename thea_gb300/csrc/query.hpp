@@ -34,6 +34,9 @@ void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
              float * d2, unsigned * err, cudaStream_t s, float const * init_bound = nullptr);
 
+// `count` tempered words of Random(seed) (Random::Random(seed), then bits() repeatedly), in stream order
+void run_thea_random_words(uint32_t seed, int64_t count, uint32_t * out, cudaStream_t s);
+
 // Returns the number of samples written (0 when the total area is not positive); synchronizes the stream.
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
                            float * pos, float * nrm, int32_t * face, cudaStream_t s);

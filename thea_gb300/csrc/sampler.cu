@@ -449,6 +449,11 @@ int64_t run_sample_by_area_noalloc(float const * V, int64_t nv, int32_t const * 
   return n;
 }
 
+void run_thea_random_words(uint32_t seed, int64_t count, uint32_t * out, cudaStream_t s) {
+  if (count <= 0) return;
+  THEA_LAUNCH(thea_mt_stream_kernel, 1, MT_THREADS, 0, s, seed, count, out);
+}
+
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
                            float * pos, float * nrm, int32_t * face, cudaStream_t s) {
   (void)nv;
