@@ -394,6 +394,12 @@ def gpu_arm(args, rank, world, local_rank):
             "ms_per_step": statistics.mean(ms64), "kernel_ms": r_ms / max(1, r_cnt),
             "fp32_verdict_equals_plain": bool(torch.equal(i32, out_i)),
             "rays_hit_differs": int((flags & 1).sum()), "rays_element_differs": int(((flags & 2) >> 1).sum())}
+        # the same rays as occlusion queries (rayIntersects: any-hit search)
+        ms_any = timed_steps(lambda: bvh.ray_intersects(od, dd), args.steps, args.warmup, flush, stream)
+        extra["ray_intersects_cfg1"] = {
+            "value": RAYS / (statistics.mean(ms_any) / 1e3) / 1e6, "unit": "Mqueries/s",
+            "ms_per_step": statistics.mean(ms_any),
+            "equals_first_hit": bool(torch.equal(bvh.ray_intersects(od, dd), out_t >= 0))}
         extra.update(extra_workloads(T, torch, stream, flush, args))
 
     line = None
@@ -487,6 +493,22 @@ def extra_workloads(T, torch, stream, flush, args):
         "bounded_search_ms": k_ms / max(1, k_cnt), "tensor_flop_per_step": 2 * 16 * 512 * KNN_POINTS,
         "identical_to_traversal": bool(torch.equal(i0, i1) and torch.equal(d0, d1))}
     pb.close()
+    # Visibility of 65,536 of the surface samples, 100 rays each (directions of Random(seed).sphere())
+    mesh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=2)
+    vis_pts = pos[:65536].contiguous()
+    T.profiling_reset()
+    T.profiling(True)
+    ms = timed_steps(lambda: mesh.visibility(vis_pts, num_rays=100, seed=3), steps, 2, flush, stream)
+    T.profiling(False)
+    a_ms, a_cnt = T.profiling_read("any_hit_kernel")
+    m_ms, m_cnt = T.profiling_read("thea_mt_stream_kernel")
+    vis = mesh.visibility(vis_pts, num_rays=100, seed=3)
+    out["visibility_cfg0_mesh"] = {
+        "value": 65536 * 100 / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mrays/s", "points": 65536,
+        "rays_per_point": 100, "ms_per_step": statistics.mean(ms), "any_hit_kernel_ms": a_ms / max(1, a_cnt),
+        "direction_stream_ms": m_ms / max(1, m_cnt), "mean_visibility": float(vis.mean().item())}
+    mesh.close()
+    T.profiling_reset()
     T.profiling_reset()
     out["batched_closest_cfg3"] = batched_config3(T, torch, stream, flush, args)
     out["serving_cfg4"] = serving_config4(T, torch, args)

@@ -200,6 +200,22 @@ THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * ou
 THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * positions, int64_t num_points,
                                      int32_t num_rays, uint32_t seed, double * out_fraction, void * stream);
 
+/* Sample proximity graph: PointSet3::updateGraph (Algorithms/PointSet3.hpp:324-391, no oversampling) with options
+ * max_degree (1..64). Random(seed) replaces the reference's Random::common() in the mean-separation estimate (100
+ * samples' nearest-neighbour distances); everything else is the reference's: radius sqrt(max_degree) x estimate,
+ * doubled up to twice for samples with fewer than clamp(max_degree / 4, 4, max_degree) neighbours; a candidate is kept
+ * unless its normal makes a dot product below -0.5 with the sample's (when normals are given) or, with normals and a
+ * surface (mesh BVH with the ray layout), the segment between the two samples lifted by 5 x separation along the mean
+ * normal hits the surface. Separations are Math::fastSqrt of the squared distance. Row i of out_neighbors
+ * (num_samples x max_degree) lists sample i's neighbours by ascending (separation, index), -1 past its degree;
+ * out_separations (nullable) the separations, 0 past the degree; out_degree (nullable) the degrees;
+ * out_avg_separation (nullable, 2 floats): the estimate and the final mean edge length (updateAverageSeparation).
+ * Host or device arrays; synchronizes the stream. */
+THEA_API thea_status thea_sample_graph(const float * positions, const float * normals, int64_t num_samples,
+                                       int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                       int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
+                                       float * out_avg_separation, void * stream);
+
 /* k nearest points of a point BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
  * index first). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
  * Code/Source/Algorithms/PointSet3.hpp:576-583). dist_bound < 0: unbounded; else only squared distances strictly below

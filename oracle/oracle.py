@@ -74,6 +74,8 @@ def lib():
         L.oracle_tree_depth.restype = _i64
         L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
         L.oracle_random_sphere.argtypes = [ctypes.c_uint32, _i64, _f32p]
+        L.oracle_sample_graph.argtypes = [_f32p, _f32p, _i64, ctypes.c_int, ctypes.c_uint32, _vp, _i32p, _f32p, _i32p,
+                                          _f32p, ctypes.c_int]
         L.oracle_visibility.argtypes = [_vp, _f32p, _i64, _i64, ctypes.c_uint32, _f32p, _f64p, ctypes.c_int]
         L.oracle_affine_inverse.restype = ctypes.c_int
         L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
@@ -370,3 +372,19 @@ def random_sphere(seed, n):
     out = np.empty((int(n), 3), np.float32)
     lib().oracle_random_sphere(int(seed), int(n), _p(out, _f32p))
     return out
+
+
+def sample_graph(P, N=None, max_degree=8, seed=0, surface=None, threads=None):
+    """PointSet3::updateGraph (no oversampling) with Random(seed): (neighbours, separations, degrees, (estimate, final
+    mean separation)); surface: a MeshIndex for the reachability test (used with normals)."""
+    P = _f32(P).reshape(-1, 3)
+    n = len(P)
+    Nn = _f32(N).reshape(-1, 3) if N is not None else None
+    nbr = np.empty((n, max_degree), np.int32)
+    sep = np.empty((n, max_degree), np.float32)
+    deg = np.empty(n, np.int32)
+    avg = np.empty(2, np.float32)
+    lib().oracle_sample_graph(_p(P, _f32p), _p(Nn, _f32p), n, int(max_degree), int(seed),
+                              surface.h if surface is not None else None, _p(nbr, _i32p), _p(sep, _f32p),
+                              _p(deg, _i32p), _p(avg, _f32p), threads or default_threads())
+    return nbr, sep, deg, (float(avg[0]), float(avg[1]))

@@ -414,6 +414,31 @@ void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t nu
   });
 }
 
+// Sample proximity graph with Random(seed); surface: nullable mesh handle. Outputs as thea_sample_graph.
+void oracle_sample_graph(float const * P, float const * N, int64_t n, int max_degree, uint32_t seed, void * surface,
+                         int32_t * out_nbr, float * out_sep, int32_t * out_deg, float * out_avg, int nthreads) {
+  std::vector<V3<float>> pts((size_t)n), nrm;
+  for (int64_t i = 0; i < n; ++i) pts[(size_t)i] = q3<float>(P, i);
+  if (N) {
+    nrm.resize((size_t)n);
+    for (int64_t i = 0; i < n; ++i) nrm[(size_t)i] = q3<float>(N, i);
+  }
+  TheaRandom r(seed);
+  MeshIndex<float> const * m = surface ? &static_cast<MeshHandle *>(surface)->f : nullptr;
+  SampleGraphResult g = sampleGraph(pts, N ? &nrm : nullptr, max_degree, r, m, nthreads);
+  for (int64_t i = 0; i < n; ++i) {
+    auto const & v = g.nbrs[(size_t)i];
+    for (int k = 0; k < max_degree; ++k) {
+      bool in = k < (int)v.size();
+      out_nbr[i * max_degree + k] = in ? v[(size_t)k].second : -1;
+      out_sep[i * max_degree + k] = in ? v[(size_t)k].first : 0.f;
+    }
+    out_deg[i] = (int32_t)v.size();
+  }
+  out_avg[0] = g.estimate;
+  out_avg[1] = g.final_avg;
+}
+
 // Affine transforms (FP32): the inverse (returns 0 if singular), points through [L | t], vectors through L, normals
 // through the inverse transpose (m then holds the inverse)
 int oracle_affine_inverse(float const * m, float * inv) { return affineInverse(m, inv) ? 1 : 0; }

@@ -738,6 +738,12 @@ struct TheaRandom {
     return r;
   }
 
+  // integer(low, high): Random.cpp:147-157
+  int32_t integer(int32_t low, int32_t high) {
+    int32_t r = (int32_t)std::floor(low + (high - low + 1) * (double)bits() / 0xFFFFFFFFUL);
+    return r > high ? high : r;
+  }
+
   // uniform01(): Random.hpp:126-131 -- (float)bits() * (1.0f / (float)0xFFFFFFFF)
   float uniform01() {
     static float const NORM = 1.0f / (float)0xFFFFFFFFul;
@@ -867,6 +873,90 @@ inline double visibilityFraction(MeshIndex<float> const & m, V3<float> const & p
     if (!hit) ++escaped;
   }
   return (double)escaped / num_rays;
+}
+
+//============================================================================================================================
+// Sample proximity graph: PointSet3::updateGraph without oversampling (Algorithms/PointSet3.hpp:324-391), with
+// findSampleNeighbors / NeighborFunctor (:586-681) and updateAverageSeparation (:688-702). The separation estimate draws
+// from the given generator in place of Random::common(). Candidates by brute force (every other sample inside the
+// ball); neighbour sets keep the max_degree smallest (separation, index), SamplePoint3's order.
+//============================================================================================================================
+
+// Math::fastRsq (Math.hpp:193-208) and fastSqrt (:218-223)
+inline float fastRsq(float x) {
+  float x2 = x * 0.5f;
+  float y = x;
+  int32_t i;
+  std::memcpy(&i, &y, 4);
+  i = 0x5f3759df - (i >> 1);
+  std::memcpy(&y, &i, 4);
+  y = y * (1.5f - (x2 * y * y));
+  return y;
+}
+inline float fastSqrt(float x) { return 1.0f / fastRsq(x); }
+
+struct SampleGraphResult {
+  std::vector<std::vector<std::pair<float, int32_t>>> nbrs;  // per sample, ascending (separation, index)
+  float estimate = 0, final_avg = 0;
+};
+
+inline SampleGraphResult sampleGraph(std::vector<V3<float>> const & P, std::vector<V3<float>> const * N, int max_degree,
+                                     TheaRandom & rng, MeshIndex<float> const * surface, int nthreads) {
+  SampleGraphResult g;
+  int64_t n = (int64_t)P.size();
+  g.nbrs.resize((size_t)n);
+  int64_t trials = std::min<int64_t>(100, n);
+  float avg = 0;
+  for (int64_t t = 0; t < trials; ++t) {
+    int32_t i = rng.integer(0, (int32_t)n - 1);
+    float best = std::numeric_limits<float>::infinity();
+    for (int64_t j = 0; j < n; ++j)
+      if (j != i) best = std::min(best, squaredNorm(P[(size_t)j] - P[(size_t)i]));
+    avg += best;
+  }
+  avg = std::sqrt(avg / (float)trials);
+  g.estimate = avg;
+  float init_radius = std::sqrt((float)max_degree) * avg;
+  int d4 = (int)(0.25 * max_degree);
+  int min_degree = d4 < 4 ? 4 : (d4 > max_degree ? max_degree : d4);
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      float radius = init_radius;
+      auto & out = g.nbrs[(size_t)i];
+      for (int it = 0; it < 3; ++it) {
+        out.clear();
+        float r2 = radius * radius;
+        for (int64_t j = 0; j < n; ++j) {
+          if (j == i) continue;
+          V3<float> diff = P[(size_t)j] - P[(size_t)i];
+          float sq = squaredNorm(diff);
+          if (!(sq <= r2)) continue;  // BallN::contains
+          if (N && dot((*N)[(size_t)i], (*N)[(size_t)j]) < -0.5f) continue;
+          float sep = fastSqrt(sq);
+          if (surface && N) {
+            V3<float> lift = normalized((*N)[(size_t)i] + (*N)[(size_t)j]);
+            V3<float> o = P[(size_t)i] + 5.0f * sep * lift;
+            if (surface->rayRef(o, diff, 1.f).idx >= 0) continue;
+          }
+          std::pair<float, int32_t> c(sep, (int32_t)j);
+          auto pos = std::lower_bound(out.begin(), out.end(), c);
+          if ((int)out.size() < max_degree) out.insert(pos, c);
+          else if (pos != out.end()) { out.insert(pos, c); out.pop_back(); }
+        }
+        if ((int)out.size() >= min_degree) break;
+        radius *= 2.0f;
+      }
+    }
+  });
+  float s = 0;
+  int64_t edges = 0;
+  for (auto const & v : g.nbrs) {
+    for (auto const & c : v) s += c.first;
+    edges += (int64_t)v.size();
+  }
+  if (edges > 0) s /= (float)edges;
+  g.final_avg = s;
+  return g;
 }
 
 }  // namespace oracle

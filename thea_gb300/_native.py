@@ -98,6 +98,8 @@ SIGNATURES = {
     "thea_bvh_destroy": (ctypes.c_int, [_vp]),
     "thea_bvh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(BvhInfo)]),
     "thea_ray_intersects": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, _vp, _vp]),
+    "thea_sample_graph": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp,
+                                         _vp]),
     "thea_random_sphere": (ctypes.c_int, [ctypes.c_uint32, _i64, _vp, _vp]),
     "thea_visibility": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32, _vp, _vp]),
     "thea_bvh_set_transform": (ctypes.c_int, [_vp, _vp, _vp]),

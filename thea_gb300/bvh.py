@@ -461,6 +461,39 @@ def point_gram_tile(a, b):
     return keys
 
 
+def sample_graph(positions, normals=None, max_degree=8, seed=0, surface=None):
+    """PointSet3::updateGraph (no oversampling) with Random(seed) for the separation estimate. Returns (neighbours
+    [n, max_degree] int32 with -1 past the degree, separations [n, max_degree], degrees [n], (estimate, final mean
+    separation)). surface: a MeshBvh for the reachability test (used with normals, as in the reference)."""
+    io = _Arrays(positions)
+    pp, n = io.input(positions, np.float32, 3)
+    pn, _ = io.input(normals, np.float32, 3) if normals is not None else (None, 0)
+    nbr, pnb = io.output((n, max_degree), np.int32)
+    sep, psp = io.output((n, max_degree), np.float32)
+    deg, pdg = io.output((n,), np.int32)
+    avg = np.zeros(2, np.float32)
+    N.check(N.lib().thea_sample_graph(pp, pn, n, int(max_degree), int(seed) & 0xffffffff,
+                                      surface.handle if surface is not None else None, pnb, psp, pdg,
+                                      avg.ctypes.data, _stream_of(io.device)))
+    return nbr, sep, deg, (float(avg[0]), float(avg[1]))
+
+
+def write_sample_graph(path, neighbors, separations, degrees, max_degree, write_distances=True):
+    """PointSet3::save's graph file (PointSet3.cpp:321-348): the maximum degree, then one line per sample: its degree,
+    its neighbours' indices and (optionally) their separations, formatted as C++ streams print floats (%g)."""
+    nb = np.asarray(neighbors)
+    sp = np.asarray(separations)
+    dg = np.asarray(degrees)
+    with open(path, "w", newline="\n") as f:
+        f.write("%d\n" % max_degree)
+        for i in range(len(dg)):
+            k = int(dg[i])
+            parts = [str(k)] + [str(int(x)) for x in nb[i, :k]]
+            if write_distances:
+                parts += ["%g" % float(x) for x in sp[i, :k]]
+            f.write(" ".join(parts) + "\n")
+
+
 def random_sphere(seed, count, device=False):
     """`count` directions of Random(seed).sphere() in stream order (float32 [count, 3])."""
     if device:

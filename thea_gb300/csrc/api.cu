@@ -9,6 +9,7 @@
 #include "serialize.hpp"
 #include "transform.hpp"
 #include "visibility.hpp"
+#include "sample_graph.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -616,6 +617,57 @@ THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * po
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_fraction, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaStreamSynchronize(s));
     }
+  });
+}
+
+THEA_API thea_status thea_sample_graph(const float * positions, const float * normals, int64_t num_samples,
+                                       int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                       int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
+                                       float * out_avg_separation, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(positions && out_neighbors, "sample_graph: null positions or out_neighbors");
+    THEA_REQUIRE(!surface || (surface->is_mesh && surface->ray_rec),
+                 "sample_graph: the surface must be a mesh BVH with THEA_LAYOUT_RAY");
+    THEA_REQUIRE(num_samples >= 2, "sample_graph: at least two samples are needed");
+    THEA_REQUIRE(max_degree >= 1 && max_degree <= 64, "sample_graph: max_degree must be in 1..64");
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t n = (size_t)num_samples, m = (size_t)max_degree;
+    DeviceView pos(positions, n * 12, s), nrm(normals, n * 12, s);
+    // outputs: device buffers, copied out when the caller's arrays are host memory; separations and degrees are
+    // always produced when the final mean separation is asked for
+    bool need_sep = out_separations || out_avg_separation, need_deg = out_degree || out_avg_separation;
+    bool hn = is_host_pointer(out_neighbors);
+    bool hs = out_separations && is_host_pointer(out_separations), hd = out_degree && is_host_pointer(out_degree);
+    Scratch bn, bs, bd;
+    SampleGraphOut o;
+    o.neighbors = out_neighbors;
+    o.separations = out_separations;
+    o.degree = out_degree;
+    if (hn) { bn = Scratch(n * m * 4, s); o.neighbors = bn.as<int32_t>(); }
+    if (need_sep && (!out_separations || hs)) { bs = Scratch(n * m * 4, s); o.separations = bs.as<float>(); }
+    if (need_deg && (!out_degree || hd)) { bd = Scratch(n * 4, s); o.degree = bd.as<int32_t>(); }
+    run_sample_graph((float const *)pos.ptr, (float const *)nrm.ptr, num_samples, max_degree, seed, surface, o, s);
+    if (hn) THEA_CUDA_CHECK(cudaMemcpyAsync(out_neighbors, o.neighbors, n * m * 4, cudaMemcpyDeviceToHost, s));
+    if (hs) THEA_CUDA_CHECK(cudaMemcpyAsync(out_separations, o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
+    if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_degree, o.degree, n * 4, cudaMemcpyDeviceToHost, s));
+    if (out_avg_separation) {
+      // updateAverageSeparation (PointSet3.hpp:688-702): FP32 sum over samples and their sorted neighbours, in order
+      std::vector<float> sep(n * m);
+      std::vector<int32_t> deg(n);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(sep.data(), o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaMemcpyAsync(deg.data(), o.degree, n * 4, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      float avg = 0.f;
+      int64_t edges = 0;
+      for (size_t i = 0; i < n; ++i) {
+        for (int32_t k = 0; k < deg[i]; ++k) avg += sep[i * m + (size_t)k];
+        edges += deg[i];
+      }
+      if (edges > 0) avg /= (float)edges;
+      out_avg_separation[0] = o.avg_separation_estimate;
+      out_avg_separation[1] = avg;
+    }
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
   });
 }
 

@@ -1,0 +1,236 @@
+// Sample proximity graph: PointSet3::updateGraph (Algorithms/PointSet3.hpp:324-391) without oversampling, with
+// findSampleNeighbors and NeighborFunctor (PointSet3.hpp:586-681) and updateAverageSeparation (:688-702).
+//
+// The reference estimates the mean sample separation from 100 samples drawn with Random::common().integer(0, n - 1);
+// Random(seed) takes its place here so that the graph is reproducible. Every other step is deterministic: each sample
+// keeps the max_degree smallest (separation, index) pairs among its valid candidates (SamplePoint3's bounded sorted
+// neighbour set orders by separation, then by sample address, i.e. array index), which does not depend on the order
+// in which the range query visits them.
+//
+// GPU form, per radius round (at most three, doubling the radius for samples with fewer than min_degree neighbours):
+// a radius query of the active samples gives candidate pairs (CSR); one thread per pair applies the angle test and
+// computes the separation (Math::fastSqrt: the one-step inverse-square-root approximation); the reachability rays of
+// all pairs go through the any-hit kernel; one thread per sample then selects its neighbours.
+#include "sample_graph.hpp"
+
+#include "any_hit.cuh"
+#include "device_util.cuh"
+#include "query.hpp"
+#include "traverse_ops.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace thea {
+namespace {
+
+constexpr int GRAPH_THREADS = 256;
+constexpr int MAX_GRAPH_DEGREE = 64;
+
+// Math::fastRsq (Math.hpp:193-208): one Newton step from the 0x5f3759df estimate; Math::fastSqrt = 1 / fastRsq
+__device__ __forceinline__ float fast_sqrt(float x) {
+  float x2 = x * 0.5f;
+  int i = 0x5f3759df - (__float_as_int(x) >> 1);
+  float y = __int_as_float(i);
+  y = y * (1.5f - ((x2 * y) * y));
+  return 1.0f / y;
+}
+
+__global__ void gather_kernel(float const * __restrict__ p, int32_t const * __restrict__ ids, int64_t n,
+                              float * __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t j = ids[i];
+  out[3 * i] = p[3 * j];
+  out[3 * i + 1] = p[3 * j + 1];
+  out[3 * i + 2] = p[3 * j + 2];
+}
+
+__global__ void owner_kernel(int64_t const * __restrict__ off, int64_t n, int32_t * __restrict__ owner) {
+  int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  for (int64_t p = off[a]; p < off[a + 1]; ++p) owner[p] = (int32_t)a;
+}
+
+// NeighborFunctor::isValidNeighbor up to the reachability test: identity (excluded by the range query), angle,
+// separation
+__global__ void pair_kernel(float const * __restrict__ pos, float const * __restrict__ nrm,
+                            int32_t const * __restrict__ active, int32_t const * __restrict__ owner,
+                            int32_t const * __restrict__ cand, int64_t total, float * __restrict__ sep,
+                            uint8_t * __restrict__ ok) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= total) return;
+  int64_t s = active[owner[p]], j = cand[p];
+  bool valid = true;
+  if (nrm) valid = !(dot(load_v3(nrm + 3 * s), load_v3(nrm + 3 * j)) < -0.5f);  // MIN_DOT
+  V3 diff = load_v3(pos + 3 * j) - load_v3(pos + 3 * s);
+  sep[p] = fast_sqrt(squared_norm(diff));
+  ok[p] = valid ? 1 : 0;
+}
+
+// Reachability rays: from the sample lifted by 5 * separation along the normalised normal sum, along the difference,
+// bounded by time 1 (the segment between the lifted points)
+struct ReachRays {
+  float const * pos;
+  float const * nrm;
+  int32_t const * active;
+  int32_t const * owner;
+  int32_t const * cand;
+  float const * sep;
+  Inverse inv;
+  __device__ __forceinline__ void get(int64_t p, V3 & o, V3 & d) const {
+    int64_t s = active[owner[p]], j = cand[p];
+    V3 ps = load_v3(pos + 3 * s);
+    V3 lift = normalized(load_v3(nrm + 3 * s) + load_v3(nrm + 3 * j));
+    o = ps + (5.0f * sep[p]) * lift;  // LIFT_FACTOR * sep * lift_dir
+    d = load_v3(pos + 3 * j) - ps;
+    if (inv.on) {
+      o = affine_point(inv.m, o);
+      d = affine_vector(inv.m, d);
+    }
+  }
+};
+
+struct BlockedFlags {
+  uint8_t * ok;
+  __device__ __forceinline__ void put(int64_t p, bool hit) const {
+    if (hit) ok[p] = 0;
+  }
+};
+
+// Per active sample: the max_degree smallest (separation, index) among valid candidates; final if at least min_degree
+// (or in the last round), else the sample goes to the next round
+__global__ void select_kernel(int32_t const * __restrict__ active, int64_t n_active, int64_t const * __restrict__ off,
+                              int32_t const * __restrict__ cand, float const * __restrict__ sep,
+                              uint8_t const * __restrict__ ok, int max_degree, int min_degree, int last,
+                              int32_t * __restrict__ out_nbr, float * __restrict__ out_sep,
+                              int32_t * __restrict__ out_deg, uint8_t * __restrict__ again) {
+  int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n_active) return;
+  float bs[MAX_GRAPH_DEGREE];
+  int bi[MAX_GRAPH_DEGREE];
+  int cnt = 0;
+  for (int64_t p = off[a]; p < off[a + 1]; ++p) {
+    if (!ok[p]) continue;
+    float v = sep[p];
+    int j = cand[p];
+    if (cnt == max_degree && !(v < bs[cnt - 1] || (v == bs[cnt - 1] && j < bi[cnt - 1]))) continue;
+    int k = cnt < max_degree ? cnt++ : cnt - 1;
+    while (k > 0 && (v < bs[k - 1] || (v == bs[k - 1] && j < bi[k - 1]))) {
+      bs[k] = bs[k - 1];
+      bi[k] = bi[k - 1];
+      --k;
+    }
+    bs[k] = v;
+    bi[k] = j;
+  }
+  bool fin = cnt >= min_degree || last;
+  again[a] = fin ? 0 : 1;
+  if (!fin) return;
+  int64_t s = active[a];
+  for (int k = 0; k < max_degree; ++k) {
+    out_nbr[s * max_degree + k] = k < cnt ? bi[k] : -1;
+    if (out_sep) out_sep[s * max_degree + k] = k < cnt ? bs[k] : 0.f;
+  }
+  if (out_deg) out_deg[s] = cnt;
+}
+
+}  // namespace
+
+void run_sample_graph(float const * positions, float const * normals, int64_t n, int max_degree, uint32_t seed,
+                      thea_bvh const * surface, SampleGraphOut & out, cudaStream_t s) {
+  THEA_REQUIRE(n >= 2, "sample_graph: at least two samples are needed");
+  THEA_REQUIRE(n < ((int64_t)1 << 31), "sample_graph: too many samples");
+  THEA_REQUIRE(max_degree >= 1 && max_degree <= MAX_GRAPH_DEGREE, "sample_graph: max_degree must be in 1..64");
+  thea_build_config cfg{};
+  cfg.width = 4;
+  thea_bvh * pts = build_bvh(false, positions, n, nullptr, 0, cfg, s);
+  try {
+    // mean separation estimate (RMS nearest-neighbour distance of num_trials samples drawn by Random::integer)
+    int64_t trials = std::min<int64_t>(100, n);
+    std::vector<uint32_t> words((size_t)trials);
+    {
+      Scratch w((size_t)trials * 4, s);
+      run_thea_random_words(seed, trials, w.as<uint32_t>(), s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(words.data(), w.ptr, (size_t)trials * 4, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    std::vector<int32_t> tid((size_t)trials);
+    int32_t hi = (int32_t)n - 1;
+    for (int64_t t = 0; t < trials; ++t) {
+      // Random::integer(low, high) (Random.cpp:147-157)
+      int32_t r = (int32_t)std::floor(0 + (hi - 0 + 1) * (double)words[(size_t)t] / 0xFFFFFFFFUL);
+      tid[(size_t)t] = r > hi ? hi : r;
+    }
+    std::vector<float> nd2((size_t)trials);
+    {
+      Scratch ids((size_t)trials * 4, s), q((size_t)trials * 12, s), ki((size_t)trials * 4, s), kd((size_t)trials * 4, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(ids.ptr, tid.data(), (size_t)trials * 4, cudaMemcpyHostToDevice, s));
+      THEA_LAUNCH(gather_kernel, (unsigned)ceil_div(trials, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions,
+                  ids.as<int32_t>(), trials, q.as<float>());
+      run_knn(pts, q.as<float>(), trials, 1, INFINITY, ids.as<int32_t>(), ki.as<int32_t>(), kd.as<float>(), pts->err,
+              s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(nd2.data(), kd.ptr, (size_t)trials * 4, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    float avg = 0.f;
+    for (int64_t t = 0; t < trials; ++t) avg += nd2[(size_t)t];
+    avg = std::sqrt(avg / (float)trials);
+    out.avg_separation_estimate = avg;
+
+    float radius = std::sqrt((float)max_degree) * avg;
+    int d4 = (int)(0.25 * max_degree);
+    int min_degree = d4 < 4 ? 4 : (d4 > max_degree ? max_degree : d4);  // Math::clamp(x, 4, max_degree)
+    bool reach = surface && normals;
+    // round 0: every sample
+    std::vector<int32_t> act((size_t)n);
+    for (int64_t i = 0; i < n; ++i) act[(size_t)i] = (int32_t)i;
+    for (int round = 0; round < 3 && !act.empty(); ++round, radius *= 2.0f) {
+      int64_t na = (int64_t)act.size();
+      bool last = round == 2;
+      Scratch ids((size_t)na * 4, s), q((size_t)na * 12, s), off((size_t)(na + 1) * 8, s), again((size_t)na, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(ids.ptr, act.data(), (size_t)na * 4, cudaMemcpyHostToDevice, s));
+      THEA_LAUNCH(gather_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions,
+                  ids.as<int32_t>(), na, q.as<float>());
+      // candidates: Ball3(position, radius), the sample itself excluded (the identity test)
+      run_range(pts, q.as<float>(), na, radius, ids.as<int32_t>(), off.as<int64_t>(), nullptr, nullptr, pts->err, s);
+      int64_t total = 0;
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&total, off.as<int64_t>() + na, 8, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      Scratch cand((size_t)std::max<int64_t>(total, 1) * 4, s), owner((size_t)std::max<int64_t>(total, 1) * 4, s);
+      Scratch sep((size_t)std::max<int64_t>(total, 1) * 4, s), ok((size_t)std::max<int64_t>(total, 1), s);
+      if (total > 0) {
+        run_range(pts, q.as<float>(), na, radius, ids.as<int32_t>(), off.as<int64_t>(), cand.as<int32_t>(), nullptr,
+                  pts->err, s);
+        THEA_LAUNCH(owner_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, off.as<int64_t>(), na,
+                    owner.as<int32_t>());
+        THEA_LAUNCH(pair_kernel, (unsigned)ceil_div(total, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions, normals,
+                    ids.as<int32_t>(), owner.as<int32_t>(), cand.as<int32_t>(), total, sep.as<float>(),
+                    ok.as<uint8_t>());
+        if (reach)
+          dispatch_any(surface,
+                       ReachRays{positions, normals, ids.as<int32_t>(), owner.as<int32_t>(), cand.as<int32_t>(),
+                                 sep.as<float>(), inverse_of(surface)},
+                       BlockedFlags{ok.as<uint8_t>()}, total, 1.0f, s);
+      }
+      THEA_LAUNCH(select_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, ids.as<int32_t>(), na,
+                  off.as<int64_t>(), cand.as<int32_t>(), sep.as<float>(), ok.as<uint8_t>(), max_degree, min_degree,
+                  last ? 1 : 0, out.neighbors, out.separations, out.degree, again.as<uint8_t>());
+      std::vector<uint8_t> h((size_t)na);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(h.data(), again.ptr, (size_t)na, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      std::vector<int32_t> next;
+      for (int64_t a = 0; a < na; ++a)
+        if (h[(size_t)a]) next.push_back(act[(size_t)a]);
+      act.swap(next);
+    }
+  } catch (...) {
+    cudaStreamSynchronize(s);
+    destroy_bvh(pts);
+    throw;
+  }
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  destroy_bvh(pts);
+}
+
+}  // namespace thea
