@@ -507,6 +507,16 @@ def extra_workloads(T, torch, stream, flush, args):
         "value": 65536 * 100 / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mrays/s", "points": 65536,
         "rays_per_point": 100, "ms_per_step": statistics.mean(ms), "any_hit_kernel_ms": a_ms / max(1, a_cnt),
         "direction_stream_ms": m_ms / max(1, m_cnt), "mean_visibility": float(vis.mean().item())}
+    # sample proximity graph of 262,144 of the surface samples with face normals, reachability against the mesh
+    g_pts = pos[:262144].contiguous()
+    _, g_nrm, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), KNN_POINTS, 2)
+    g_nrm = g_nrm[:262144].contiguous()
+    ms = timed_steps(lambda: T.sample_graph(g_pts, g_nrm, max_degree=8, seed=1, surface=mesh), 3, 1, flush, stream)
+    _, _, g_deg, g_avg = T.sample_graph(g_pts, g_nrm, max_degree=8, seed=1, surface=mesh)
+    out["sample_graph_cfg0_mesh"] = {
+        "value": 262144 / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Msamples/s", "samples": 262144,
+        "max_degree": 8, "ms_per_step": statistics.mean(ms), "mean_degree": float(g_deg.float().mean().item()),
+        "separation_estimate": g_avg[0], "mean_separation": g_avg[1], "reachability": "against the mesh"}
     mesh.close()
     T.profiling_reset()
     T.profiling_reset()
