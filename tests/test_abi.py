@@ -84,6 +84,17 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.thea_k_closest_self(None, 4, None, None, None) == 1
     assert lib.thea_sample_by_area(None, 0, None, 0, 5, 1, 9, None, None, None, None, None) == 1
     assert lib.thea_bvh_destroy(None) == 0
+    # occlusion, visibility, sphere stream and sample graph: argument checks before any device call
+    P = np.zeros((4, 3), np.float32)
+    out = np.zeros(64, np.int32)
+    assert lib.thea_ray_intersects(None, None, None, 0, -1.0, None, None) == 1
+    assert lib.thea_visibility(None, P.ctypes.data, 4, 10, 1, None, None) == 1
+    assert lib.thea_random_sphere(1, -1, None, None) == 1
+    assert lib.thea_random_sphere(1, 0, None, None) == 0
+    assert lib.thea_sample_graph(None, None, 4, 8, 1, None, out.ctypes.data, None, None, None, None) == 1
+    assert lib.thea_sample_graph(P.ctypes.data, None, 1, 8, 1, None, out.ctypes.data, None, None, None, None) == 1
+    assert lib.thea_sample_graph(P.ctypes.data, None, 4, 0, 1, None, out.ctypes.data, None, None, None, None) == 1
+    assert lib.thea_sample_graph(P.ctypes.data, None, 4, 65, 1, None, out.ctypes.data, None, None, None, None) == 1
     eye = np.eye(3, 4, dtype=np.float32)
     assert lib.thea_bvh_set_transform(None, eye.ctypes.data, None) == 1
     assert lib.thea_bvh_clear_transform(None) == 1

@@ -87,3 +87,13 @@ def test_graph_file_format(T, oracle, tmp_path):
         k = int(rd[i])
         want = " ".join([str(k)] + [str(x) for x in rn[i, :k]] + ["%g" % x for x in rs[i, :k]])
         assert lines[i + 1] == want
+
+
+def test_graph_with_duplicate_samples(T, oracle):
+    """Coincident samples (separation 0, where fastSqrt gives a tiny positive value) and a small set."""
+    _, _, P, _ = sphere_samples(600, 241, T)
+    P = np.concatenate([P, P[:50], P[:5]]).astype(np.float32)
+    got = T.sample_graph(dev(P), max_degree=8, seed=8)
+    same(got, oracle.sample_graph(P, None, 8, 8))
+    tiny = P[:6]
+    same(T.sample_graph(tiny, max_degree=4, seed=1), oracle.sample_graph(tiny, None, 4, 1))

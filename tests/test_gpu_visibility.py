@@ -85,3 +85,17 @@ def test_visibility_with_a_transform(T, oracle):
     bvh.set_transform(M)
     got = bvh.visibility(dev(Pw), num_rays=50, seed=3).cpu().numpy()
     assert np.array_equal(got, oracle.MeshIndex(V, F).visibility(Pw, 50, 3, transform=M))
+
+
+def test_empty_and_degenerate_inputs(T, oracle):
+    V, F = W.noisy_icosphere(2, 151)
+    bvh = T.MeshBvh(dev(V), dev(F))
+    assert len(bvh.ray_intersects(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))) == 0
+    assert len(bvh.visibility(np.zeros((0, 3), np.float32))) == 0
+    assert T.random_sphere(3, 0).shape == (0, 3)
+    # zero directions and origins on vertices
+    O = np.concatenate([V[:100], np.zeros((10, 3), np.float32)])
+    D = np.concatenate([np.zeros((50, 3), np.float32), -V[50:100], np.ones((10, 3), np.float32)])
+    hit = bvh.ray_intersects(dev(O), dev(D)).cpu().numpy()
+    rt, _ = oracle.MeshIndex(V, F).ray_contract(O, D)
+    assert np.array_equal(hit, rt >= 0)
