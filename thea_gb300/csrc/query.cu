@@ -291,8 +291,12 @@ ray_persistent_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __r
 // BoundedSortedArrayN.hpp:137-214)
 //============================================================================================================================
 
+// Resident blocks per SM requested from the register allocator: the K-best lists live in registers, and for K = 16
+// the allocation otherwise rounds up past five blocks of 128 threads
+template <int K> constexpr int knn_min_blocks() { return K <= 8 ? 8 : (K <= 16 ? 5 : 3); }
+
 template <int W, int K, int STACK>
-__global__ void __launch_bounds__(QUERY_THREADS)
+__global__ void __launch_bounds__(QUERY_THREADS, knn_min_blocks<K>())
 knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
            int64_t n, int k_out, float thresh, int32_t const * __restrict__ exclude, int32_t * __restrict__ out_index,
            float * __restrict__ out_d2, unsigned * __restrict__ err, uint32_t const * __restrict__ order,

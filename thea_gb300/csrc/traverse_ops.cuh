@@ -962,22 +962,23 @@ template <int W, int K, int STACK>
 __device__ __forceinline__ void knn_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts,
                                           int root, int64_t elem_base, V3 p, int excl, float (&bd)[K], int (&bi)[K],
                                           unsigned * err) {
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
-  stk[sp] = root;
-  stkd[sp] = 0.f;
-  ++sp;
-  while (sp > 0) {
-    --sp;
-    int code = stk[sp];
-    if (stkd[sp] > bd[K - 1] * PRUNE_SLACK) continue;
+  int next = root;  // nearest child of the last node, visited without a stack round trip
+  while (next != CHILD_EMPTY || sp > 0) {
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > bd[K - 1] * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children<W, STACK>(nd, lb, bd[K - 1] * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children_next<W, STACK>(nd, lb, bd[K - 1] * PRUNE_SLACK, stk, sp, next, err);
     } else {
       int first, count;
       decode_leaf(code, first, count);
