@@ -358,22 +358,25 @@ range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__
   int ex = exclude ? exclude[q] : -1;
   int64_t w = FILL ? count_or_offset[q] : 0;
   int64_t c = 0;
+  // every child within the radius is visited whatever the order, so children are pushed unsorted
   int stk[STACK];
-  float stkd[STACK];
   int sp = 0;
-  stk[sp] = 0;
-  stkd[sp] = 0.f;
-  ++sp;
+  stk[sp++] = 0;
   float lim = r2 * PRUNE_SLACK;
   while (sp > 0) {
-    --sp;
-    int code = stk[sp];
+    int code = stk[--sp];
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children<W, STACK>(nd, lb, lim, stk, stkd, sp, err);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        if (nd.child[c] != CHILD_EMPTY && lb[c] <= lim) {
+          if (sp < STACK) stk[sp++] = nd.child[c];
+          else atomicOr(err, ERR_STACK_OVERFLOW);
+        }
+      }
     } else {
       int first, count;
       decode_leaf(code, first, count);

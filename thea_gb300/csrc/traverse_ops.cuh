@@ -259,37 +259,10 @@ struct ClosestOut {
   bool done;     // false when the pop budget ran out before the search finished
 };
 
-// Pushes the children of an expanded node whose lower bound passes `lim` (misses carry a NaN bound and never pass),
-// nearest on top. Leaves go on the stack too, so every child is visited in order of its bound.
-template <int W, int STACK>
-__device__ __forceinline__ void push_children(NodeRegs<W> const & nd, float const (&lb)[W], float lim,
-                                              int (&stk)[STACK], float (&stkd)[STACK], int & sp, unsigned * err) {
-  uint32_t key[W];
-  int cc[W];
-#pragma unroll
-  for (int c = 0; c < W; ++c) {
-    bool keep = nd.child[c] != CHILD_EMPTY && lb[c] <= lim;
-    key[c] = keep ? __float_as_uint(lb[c]) : 0xffffffffu;
-    cc[c] = nd.child[c];
-  }
-  sort_children<W>(key, cc);
-#pragma unroll
-  for (int c = W - 1; c >= 0; --c) {
-    if (key[c] != 0xffffffffu) {
-      if (sp < STACK) {
-        stk[sp] = cc[c];
-        stkd[sp] = __uint_as_float(key[c]);
-        ++sp;
-      } else {
-        atomicOr(err, ERR_STACK_OVERFLOW);
-      }
-    }
-  }
-}
-
-// push_children for the persistent-lane loops: the nearest kept child is returned in `next` (it would be popped right
-// away) and the others are pushed farthest first as packed (code, bound bits) entries, one 8-byte access each.
-// `next` is CHILD_EMPTY when no child is kept.
+// Children of a node whose lower bound passes `lim` (misses carry a NaN bound and never pass), in ascending bound
+// order: the nearest is returned in `next` (the
+// next step visits it without a stack round trip) and the others are pushed farthest first as packed (code, bound bits)
+// entries, one 8-byte access each. `next` is CHILD_EMPTY when no child is kept.
 template <int W, int STACK>
 __device__ __forceinline__ void push_children_next(NodeRegs<W> const & nd, float const (&lb)[W], float lim,
                                                    int2 (&stk)[STACK], int & sp, int & next, unsigned * err) {
@@ -354,27 +327,28 @@ __device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restri
   int best_idx = INT_MAX;
   int64_t best_slot = -1;
   V3 best_cp = V3{0.f, 0.f, 0.f};
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
-  stk[sp] = root;
-  stkd[sp] = 0.f;
-  ++sp;
+  int next = root;  // nearest child of the last node, visited without a stack round trip
   int pops = 0;
-  while (sp > 0) {
+  while (next != CHILD_EMPTY || sp > 0) {
     if (budget > 0 && ++pops > budget) {
       done = false;
       break;
     }
-    --sp;
-    int code = stk[sp];
-    if (stkd[sp] > best * PRUNE_SLACK) continue;
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > best * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, err);
     } else {
       int first, count;
       decode_leaf(code, first, count);
@@ -515,26 +489,27 @@ __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restric
   float abs_tol;
   float lim = f64_band_start(bound2, scale, abs_tol);
   float best32 = INFINITY;
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
-  stk[sp] = root;
-  stkd[sp] = 0.f;
-  ++sp;
-  while (sp > 0) {
+  int next = root;  // nearest child of the last node, visited without a stack round trip
+  while (next != CHILD_EMPTY || sp > 0) {
     if (budget > 0 && ++pops > budget) {
       s.done = false;
       break;
     }
-    --sp;
-    int code = stk[sp];
-    if (stkd[sp] > lim * PRUNE_SLACK) continue;
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > lim * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children<W, STACK>(nd, lb, lim * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children_next<W, STACK>(nd, lb, lim * PRUNE_SLACK, stk, sp, next, err);
     } else {
       int first, count;
       decode_leaf(code, first, count);
@@ -645,16 +620,17 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
   float best = max_time >= 0.f ? max_time : INFINITY;
   int best_idx = INT_MAX;
   int64_t best_slot = -1;
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
-  stk[sp] = root;
-  stkd[sp] = 0.f;
-  ++sp;
-  while (sp > 0) {
-    --sp;
-    int code = stk[sp];
-    if (stkd[sp] > best * PRUNE_SLACK) continue;
+  int next = root;  // nearest child of the last node, visited without a stack round trip
+  while (next != CHILD_EMPTY || sp > 0) {
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > best * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd;
       load_node(nodes, code, nd);
@@ -668,7 +644,7 @@ __device__ __forceinline__ RayOut ray_query(WideNode<W> const * __restrict__ nod
         float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
         lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
       }
-      push_children<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, err);
     } else {
       int first, count;
       decode_leaf(code, first, count);
@@ -765,18 +741,19 @@ __device__ __forceinline__ void ray_search_f64(WideNode<W> const * __restrict__ 
   float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
   float nd = l1(d);
   float dd = dot(d, d);
-  int stk[STACK];
-  float stkd[STACK];
+  int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
-  stk[sp] = root;
-  stkd[sp] = 0.f;
-  ++sp;
-  while (sp > 0) {
-    --sp;
-    int code = stk[sp];
+  int next = root;  // nearest child of the last node, visited without a stack round trip
+  while (next != CHILD_EMPTY || sp > 0) {
     // the FP32 verdict needs everything up to its best; the FP64 one everything up to B
     float bound = fminf(fmaxf(s.t, s.B), s.tcap);
-    if (stkd[sp] > bound * PRUNE_SLACK) continue;
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > bound * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
     if (code >= 0) {
       NodeRegs<W> nd4;
       load_node(nodes, code, nd4);
@@ -790,7 +767,7 @@ __device__ __forceinline__ void ray_search_f64(WideNode<W> const * __restrict__ 
         float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
         lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);  // a miss: NaN passes no bound
       }
-      push_children<W, STACK>(nd4, lb, bound * PRUNE_SLACK, stk, stkd, sp, err);
+      push_children_next<W, STACK>(nd4, lb, bound * PRUNE_SLACK, stk, sp, next, err);
       continue;
     }
     int first, count;
