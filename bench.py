@@ -10,8 +10,10 @@ are seeded synthetic data with the benchmark's shapes and distributions (no data
              device->host copies of (time, index) inside the timed region.
   roofline   algorithmic bytes per launch / mean ray-kernel duration (CUDA events recorded around each launch).
   cpu_baseline  the oracle's restatement of the reference's CPU traversal (reference kd-tree, reference tie order) on a
-             bounded sample, all host threads.
-  extra      the other workloads (closest point, k-NN graph) measured the same way, device-resident.
+             bounded sample, all host threads (and one thread on a smaller sample).
+  extra      the other workloads measured the same way, device-resident: the FP64 ray re-test and occlusion queries
+             on config 1, closest point (config 0), the k-NN graph (config 2), Visibility and the sample graph on the
+             config-0 mesh, the batched forest (config 3) and the serving loop (config 4).
 
 --impl reference times the reference's algorithm on the host cores instead (the CPU restatement, since the reference
 itself needs Eigen, which is absent).
@@ -220,9 +222,17 @@ def cpu_ray_baseline(V, F, o, d, target_s=12.0, threads=None):
     t0 = time.perf_counter()
     m.ray_ref(o[sel], d[sel], threads=threads)
     dt = time.perf_counter() - t0
+    # one core as well, on a smaller strided sample (the reference itself runs single-threaded)
+    n1 = int(min(len(o), max(4096, n2 // max(1, threads) // 4)))
+    sel1 = np.linspace(0, len(o) - 1, n1).astype(np.int64)
+    t0 = time.perf_counter()
+    m.ray_ref(o[sel1], d[sel1], threads=1)
+    dt1 = time.perf_counter() - t0
     return {"value": n2 / dt / 1e6, "unit": "Mqueries/s", "cores": threads, "kind": "port",
+            "one_core_value": n1 / dt1 / 1e6, "one_core_sample": n1,
             "sample": "%d of the %d rays (evenly strided), reference kd-tree and traversal restated in C++ (oracle), "
-                      "%d threads; kd-tree build %.2f s not included" % (n2, len(o), threads, build_s)}
+                      "%d threads (and %d rays on one thread); kd-tree build %.2f s not included"
+                      % (n2, len(o), threads, n1, build_s)}
 
 
 def reference_arm(args, rank, world):
