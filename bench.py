@@ -6,8 +6,8 @@ are seeded synthetic data with the benchmark's shapes and distributions (no data
 
   value      Mqueries/s with rays and mesh resident in HBM (device pointers), CUDA events on the launching stream,
              L2 flushed (256 MB write) before every timed step.
-  e2e        the same metric through the C ABI with host (pinned) buffers: host->device copies of the rays and
-             device->host copies of (time, index) inside the timed region.
+  e2e        the same metric through the C ABI with host (pinned) buffers, inside the timed region: the rays go to the
+             GPU and (time, index) come back (the library reads and writes pinned arrays in place over NVLink-C2C).
   roofline   algorithmic bytes per launch / mean ray-kernel duration (CUDA events recorded around each launch).
   cpu_baseline  the oracle's restatement of the reference's CPU traversal (reference kd-tree, reference tie order) on a
              bounded sample, all host threads (and one thread on a smaller sample).

@@ -389,3 +389,32 @@ def test_closest_large_batches_equal_small_ones(T, dist_bound):
     assert np.array_equal(host(i), np.concatenate([host(p[0]) for p in parts]))
     assert np.array_equal(host(d), np.concatenate([host(p[1]) for p in parts]))
     assert np.array_equal(host(c), np.concatenate([host(p[2]) for p in parts]))
+
+
+def test_ray_pinned_host_arrays_are_read_in_place(T):
+    """Rays and results in pinned host memory take the one-launch path that reads and writes them in place; results
+    equal the device-resident call's, for a batch that is not a multiple of the 64-ray block, with and without the index
+    output and with a time bound."""
+    import ctypes
+    import torch
+    from thea_gb300 import _native as N
+    V, F = W.heightfield(256, 301)
+    o, d = W.cosine_rays_down(200003, 302)
+    n = len(o)
+    bvh = T.MeshBvh(dev(V), dev(F), layouts=2)
+    L = N.lib()
+    ho, hd = torch.from_numpy(o).pin_memory(), torch.from_numpy(d).pin_memory()
+    ptr = lambda x: ctypes.c_void_p(x.data_ptr()) if x is not None else None  # noqa: E731
+    for max_time, with_index in ((-1.0, True), (0.3, True), (-1.0, False)):
+        t_dev, i_dev, _ = bvh.ray_structure_intersection(dev(o), dev(d), max_time=max_time)
+        ht = torch.full((n,), 7.0).pin_memory()
+        hi = torch.full((n,), 7, dtype=torch.int32).pin_memory() if with_index else None
+        N.check(L.thea_ray_intersection(bvh.handle, ptr(ho), ptr(hd), n, max_time, ptr(ht), ptr(hi), None,
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        assert torch.equal(ht, t_dev.cpu())
+        if with_index:
+            assert torch.equal(hi, i_dev.cpu())
+    # pageable arrays take the staged path and agree too
+    t_h, i_h, _ = bvh.ray_structure_intersection(o, d)
+    t_dev, i_dev, _ = bvh.ray_structure_intersection(dev(o), dev(d))
+    assert np.array_equal(t_h, t_dev.cpu().numpy()) and np.array_equal(i_h, i_dev.cpu().numpy())

@@ -494,6 +494,29 @@ static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const flo
   rp.max_time = max_time >= 0.f ? max_time : -1.f;
   rp.recheck = precision == THEA_PRECISION_FP64_RECHECK;
   if (!rp.recheck) out_time64 = nullptr, out_index64 = nullptr, out_flags = nullptr;
+  // rays and results all in pinned host memory: one launch reads and writes them in place
+  if (!rp.recheck && !out_normal && !mesh_bvh->has_transform && num_rays >= (1 << 16)) {
+    void const * hp[4] = {origins, directions, out_time, out_index};
+    void * dp[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool direct = true;
+    for (int i = 0; i < 4 && direct; ++i) {
+      if (!hp[i]) continue;
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, hp[i]) != cudaSuccess) {
+        cudaGetLastError();
+        direct = false;
+      } else {
+        direct = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+        dp[i] = at.devicePointer;
+      }
+    }
+    if (direct) {
+      run_ray_stream(mesh_bvh, (float const *)dp[0], (float const *)dp[1], num_rays, rp.max_time, (float *)dp[2],
+                     (int32_t *)dp[3], err, (cudaStream_t)stream);
+      THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+      return;
+    }
+  }
   run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
               {out_index, 4, true, false}, {out_normal, 12, true, false}, {out_time64, 4, true, false},
               {out_index64, 4, true, false}, {out_flags, 4, true, false}},

@@ -286,6 +286,180 @@ ray_persistent_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __r
   }
 }
 
+// Host-resident form of ray_persistent_kernel, for rays and results in pinned host memory read and written by the
+// kernel itself (Grace-Blackwell reaches host memory coherently over NVLink-C2C). Instead of staging the batch through
+// device buffers in chunks (each launch then ends with its own tail of long rays), one launch covers the batch: a warp
+// copies each 64-ray block into shared memory once when it takes the block (one wait per block instead of one per ray),
+// and results go to a per-warp ring of block buffers in shared memory that are written out, in ray order and with
+// coalesced stores, once every ray of the block is done. A warp takes a new block only when a ring slot is free; the
+// lanes then idle until their warp's oldest block completes, which always happens because its rays are in flight on
+// lanes of the same warp. Time and index only (the normal variant keeps the staged path).
+constexpr int STREAM_RING = 4;
+constexpr int STREAM_WARPS = QUERY_THREADS / 32;
+
+template <int W, int STACK>
+__global__ void __launch_bounds__(QUERY_THREADS)
+ray_stream_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                  float const * __restrict__ origins, float const * __restrict__ dirs, int64_t n, float max_time,
+                  float * __restrict__ out_time, int32_t * __restrict__ out_index, unsigned * __restrict__ err,
+                  unsigned long long * __restrict__ counter) {
+  __shared__ float s_in[STREAM_WARPS][RAY_WARP_BLOCK * 6];
+  __shared__ float s_t[STREAM_WARPS][STREAM_RING][RAY_WARP_BLOCK];
+  __shared__ int s_i[STREAM_WARPS][STREAM_RING][RAY_WARP_BLOCK];
+  __shared__ int s_left[STREAM_WARPS][STREAM_RING];
+  __shared__ long long s_base[STREAM_WARPS][STREAM_RING];
+  __shared__ int s_cnt[STREAM_WARPS][STREAM_RING];
+  unsigned const FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float * in = s_in[warp];
+  int64_t qb = 0, qe = 0;   // rays of the current block not yet handed out, warp-uniform
+  bool exhausted = false;   // warp-uniform
+  long long taken = 0;      // blocks taken by this warp, warp-uniform
+  long long oldest = 0;     // oldest block not written out yet, warp-uniform
+  int64_t q = -1;           // this lane's ray (-1: idle)
+  int slot = 0;             // ring slot of this lane's ray
+  int64_t qbase = 0;        // first ray of that slot's block
+  V3 o = V3{0.f, 0.f, 0.f};
+  float ix = 0.f, iy = 0.f, iz = 0.f, ox = 0.f, oy = 0.f, oz = 0.f;
+  V3 d = V3{0.f, 0.f, 1.f};
+  float best = 0.f;
+  int best_idx = INT_MAX;
+  int2 stk[STACK];
+  int sp = 0;
+  int next = CHILD_EMPTY;
+  while (true) {
+    __syncwarp();
+    // write out completed blocks, oldest first
+    while (oldest < taken && s_left[warp][oldest % STREAM_RING] == 0) {
+      int sl = (int)(oldest % STREAM_RING);
+      long long base = s_base[warp][sl];
+      int cnt = s_cnt[warp][sl];
+      for (int j = lane; j < cnt; j += 32) {
+        out_time[base + j] = s_t[warp][sl][j];
+        if (out_index) out_index[base + j] = s_i[warp][sl][j];
+      }
+      ++oldest;
+    }
+    __syncwarp();
+    unsigned idle = __ballot_sync(FULL, q < 0);
+    if (idle && !exhausted) {
+      if (qb >= qe && taken - oldest < STREAM_RING) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(counter, (unsigned long long)RAY_WARP_BLOCK);
+        b = __shfl_sync(FULL, b, 0);
+        if ((int64_t)b >= n) {
+          exhausted = true;
+        } else {
+          qb = (int64_t)b;
+          qe = qb + RAY_WARP_BLOCK < n ? qb + RAY_WARP_BLOCK : n;
+          int cnt = (int)(qe - qb);
+          // one coalesced copy of the block's origins and directions
+          for (int k = lane; k < 3 * cnt; k += 32) {
+            in[(k / 3) * 6 + k % 3] = origins[3 * qb + k];
+            in[(k / 3) * 6 + 3 + k % 3] = dirs[3 * qb + k];
+          }
+          int sl = (int)(taken % STREAM_RING);
+          if (lane == 0) {
+            s_base[warp][sl] = qb;
+            s_cnt[warp][sl] = cnt;
+            s_left[warp][sl] = cnt;
+          }
+          ++taken;
+          __syncwarp();
+        }
+      }
+      if (!exhausted && qb < qe) {
+        int rank = __popc(idle & ((1u << lane) - 1));
+        int take = __popc(idle);
+        int64_t avail = qe - qb;
+        if (q < 0 && rank < avail) {
+          q = qb + rank;
+          slot = (int)((taken - 1) % STREAM_RING);
+          qbase = s_base[warp][slot];
+          float const * r = in + (q - qbase) * 6;
+          o = V3{r[0], r[1], r[2]};
+          d = V3{r[3], r[4], r[5]};
+          ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
+          iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
+          iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
+          ox = -o.x * ix;
+          oy = -o.y * iy;
+          oz = -o.z * iz;
+          best = max_time >= 0.f ? max_time : INFINITY;
+          best_idx = INT_MAX;
+          sp = 0;
+          next = 0;
+        }
+        qb += take < avail ? take : avail;
+      }
+    }
+    bool busy = __ballot_sync(FULL, q >= 0) != 0;
+    if (!busy && oldest == taken && (exhausted || qb >= qe)) {
+      if (exhausted) break;
+      continue;  // every block written out and no ray in flight: take the next block
+    }
+    if (q < 0) continue;
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      if (sp == 0) {
+        bool found = best_idx != INT_MAX;
+        int j = (int)(q - qbase);
+        s_t[warp][slot][j] = found ? best : -1.f;
+        s_i[warp][slot][j] = found ? best_idx : -1;
+        atomicSub(&s_left[warp][slot], 1);
+        q = -1;
+        continue;
+      }
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > best * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        float tx0 = __fmaf_rn(nd.lox[c], ix, ox), tx1 = __fmaf_rn(nd.hix[c], ix, ox);
+        float ty0 = __fmaf_rn(nd.loy[c], iy, oy), ty1 = __fmaf_rn(nd.hiy[c], iy, oy);
+        float tz0 = __fmaf_rn(nd.loz[c], iz, oz), tz1 = __fmaf_rn(nd.hiz[c], iz, oz);
+        float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.f));
+        float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        lb[c] = tmin <= tmax ? tmin : __int_as_float(0x7fffffff);
+      }
+      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      for (int64_t k = first; k < first + count; ++k) {
+        float4 const * r = rec + k * RAY_REC_F4;
+        float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+        float t = ray_triangle_time(o, d, xyz(a), xyz(b), xyz(c));
+        int idx = __float_as_int(a.w);
+        if (t >= 0.f && t <= best && (t < best || idx < best_idx)) {
+          best = t;
+          best_idx = idx;
+        }
+      }
+    }
+  }
+}
+
+template <int W, int STACK>
+void launch_ray_stream(thea_bvh const * b, float const * o, float const * d, int64_t n, float max_time, float * t,
+                       int32_t * idx, unsigned * err, cudaStream_t s) {
+  auto k = ray_stream_kernel<W, STACK>;
+  int per_sm = 0;
+  THEA_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, QUERY_THREADS, 0));
+  int64_t need = ceil_div(ceil_div(n, RAY_WARP_BLOCK) * 32, QUERY_THREADS);
+  unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(1, per_sm) * sm_count(), need));
+  Scratch counter(sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counter.ptr, 0, sizeof(unsigned long long), s));
+  THEA_LAUNCH_NAMED("ray_stream_kernel", k, grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->ray_rec, o, d,
+                    n, max_time, t, idx, err, counter.as<unsigned long long>());
+}
+
 //============================================================================================================================
 // k nearest points (BvhN::kClosestPairs + KClosestPairsFunctor + BoundedSortedArrayN; BvhN.hpp:474-500, 1139-1146;
 // BoundedSortedArrayN.hpp:137-214)
@@ -600,6 +774,16 @@ void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, Ra
                         : launch_ray<4, 256>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s);
   else sm ? launch_ray<8, 128>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s)
           : launch_ray<8, 512>(b, o, d, n, rp, t, idx, nrm, t64, idx64, flags, err, od, s);
+}
+
+void run_ray_stream(thea_bvh const * b, float const * o, float const * d, int64_t n, float max_time, float * t,
+                    int32_t * idx, unsigned * err, cudaStream_t s) {
+  if (n <= 0) return;
+  bool sm = small_stack_ok(b);
+  if (b->width == 4) sm ? launch_ray_stream<4, 64>(b, o, d, n, max_time, t, idx, err, s)
+                        : launch_ray_stream<4, 256>(b, o, d, n, max_time, t, idx, err, s);
+  else sm ? launch_ray_stream<8, 128>(b, o, d, n, max_time, t, idx, err, s)
+          : launch_ray_stream<8, 512>(b, o, d, n, max_time, t, idx, err, s);
 }
 
 void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex, int64_t * offsets,

@@ -22,6 +22,9 @@ bool small_stack_ok(thea_bvh const * b);
 
 void run_closest(thea_bvh const * b, float const * q, int64_t n, ClosestParams const & cp, int32_t * idx, float * dist,
                  float * cpt, float * errout, unsigned * err, cudaStream_t s);
+// FP32 first hit with rays and results in pinned host memory accessed by the kernel (device-usable pointers).
+void run_ray_stream(thea_bvh const * b, float const * o, float const * d, int64_t n, float max_time, float * t,
+                    int32_t * idx, unsigned * err, cudaStream_t s);
 void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, RayParams const & rp, float * t,
              int32_t * idx, float * nrm, float * t64, int32_t * idx64, int32_t * flags, unsigned * err, cudaStream_t s);
 // q == nullptr: self mode over the BVH's own points (n = number of points, rows in element order)
