@@ -121,8 +121,24 @@ def case_cfg3_fp32_64():
     torch.cuda.synchronize()
 
 
-CASES = {"ray": case_ray, "cfg0": case_cfg0, "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64,
-         "gram_knn": case_gram_knn}
+def case_ray_host():
+    """Config 1 through the C ABI with rays and results in pinned host memory (the in-place e2e kernel): three calls."""
+    import ctypes
+    import torch
+    import thea_gb300 as T
+    from thea_gb300 import _native as N
+    V, F, o, d = W.config1()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=2, max_leaf_size=2)
+    ho, hd = torch.from_numpy(o).pin_memory(), torch.from_numpy(d).pin_memory()
+    ht, hi = torch.empty(len(o)).pin_memory(), torch.empty(len(o), dtype=torch.int32).pin_memory()
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    for _ in range(3):
+        N.check(N.lib().thea_ray_intersection(bvh.handle, p(ho), p(hd), len(o), -1.0, p(ht), p(hi), None,
+                                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+
+CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg3_fp64_64": case_cfg3_fp64_64,
+         "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
 
 
 def peaks():
