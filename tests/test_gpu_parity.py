@@ -418,3 +418,43 @@ def test_ray_pinned_host_arrays_are_read_in_place(T):
     t_h, i_h, _ = bvh.ray_structure_intersection(o, d)
     t_dev, i_dev, _ = bvh.ray_structure_intersection(dev(o), dev(d))
     assert np.array_equal(t_h, t_dev.cpu().numpy()) and np.array_equal(i_h, i_dev.cpu().numpy())
+
+
+def test_non_finite_and_huge_inputs(T, oracle):
+    """NaN, infinite and huge coordinates in queries and rays end like the oracle's traversal (no element where no
+    comparison can succeed), without stalling a kernel."""
+    V, F = W.noisy_icosphere(3, 71)
+    Q = W.uniform_box_points(2000, [-1.5] * 3, [1.5] * 3, 72)
+    Q[::50] = np.nan
+    Q[1::50] = np.inf
+    Q[2::50, 0] = -np.inf
+    Q[3::50] = 1e30
+    Q[4::50, 1] = np.nan
+    bvh = T.MeshBvh(dev(V), dev(F))
+    idx, dist, cp = bvh.closest_element(dev(Q))
+    ri, rd2, rcp = oracle.MeshIndex(V, F).closest_contract(Q)
+    idx, dist = host(idx), host(dist)
+    assert np.array_equal(idx, ri)
+    ok = ri >= 0
+    assert np.array_equal(dist[ok], np.sqrt(rd2[ok].astype(np.float32)))
+    O, D = W.random_rays(2000, [-2] * 3, [2] * 3, 73)
+    O[::40] = np.nan
+    D[1::40] = np.nan
+    D[2::40] = 0.0
+    D[3::40] = np.inf
+    O[4::40] = 1e30
+    t, ti, _ = bvh.ray_structure_intersection(dev(O), dev(D))
+    rt, rti = oracle.MeshIndex(V, F).ray_contract(O, D)
+    assert np.array_equal(host(ti), rti)
+    assert np.array_equal(host(t), rt.astype(np.float32))
+    P = W.uniform_box_points(5000, [0] * 3, [1] * 3, 74)
+    pb = T.PointBvh(dev(P))
+    ki, kd = pb.k_closest_pairs(dev(Q), 4)
+    rki, rkd = oracle.PointIndex(P).knn_contract(Q, 4)
+    ki = host(ki)
+    # a query with a NaN coordinate has no neighbours here; the reference (and the oracle) fill its list with the first
+    # points their traversal admits while the list is not full, at NaN distance
+    nan_rows = np.isnan(Q).any(axis=1)
+    assert np.all(ki[nan_rows] == -1)
+    assert np.array_equal(ki[~nan_rows], rki[~nan_rows])
+    assert bvh.info()["device_error_bits"] == 0 and pb.info()["device_error_bits"] == 0
