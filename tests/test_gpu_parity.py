@@ -458,3 +458,31 @@ def test_non_finite_and_huge_inputs(T, oracle):
     assert np.all(ki[nan_rows] == -1)
     assert np.array_equal(ki[~nan_rows], rki[~nan_rows])
     assert bvh.info()["device_error_bits"] == 0 and pb.info()["device_error_bits"] == 0
+
+
+def test_closest_pinned_host_arrays_are_read_in_place(T, oracle):
+    """Queries and results in pinned host memory take the in-place path (FP32, large batch); results equal the
+    device-resident call's (and the oracle's on a subset), with all outputs, with the index alone and with a bound."""
+    import ctypes
+    import torch
+    from thea_gb300 import _native as N
+    V, F = W.noisy_icosphere(4, 311)
+    Q = W.uniform_box_points(100003, [-1.5] * 3, [1.5] * 3, 312)
+    n = len(Q)
+    bvh = T.MeshBvh(dev(V), dev(F), layouts=1)
+    L = N.lib()
+    hq = torch.from_numpy(Q).pin_memory()
+    ptr = lambda x: ctypes.c_void_p(x.data_ptr()) if x is not None else None  # noqa: E731
+    for bound, all_outputs in ((-1.0, True), (0.2, True), (-1.0, False)):
+        i_dev, d_dev, c_dev = bvh.closest_element(dev(Q), dist_bound=bound)
+        hi = torch.full((n,), 7, dtype=torch.int32).pin_memory()
+        hd = torch.full((n,), 7.0).pin_memory() if all_outputs else None
+        hc = torch.full((n, 3), 7.0).pin_memory() if all_outputs else None
+        N.check(L.thea_closest_element(bvh.handle, ptr(hq), n, bound, ptr(hi), ptr(hd), ptr(hc),
+                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        assert torch.equal(hi, i_dev.cpu())
+        if all_outputs:
+            assert torch.equal(hd, d_dev.cpu()) and torch.equal(hc, c_dev.cpu())
+    sel = np.arange(0, n, 37)
+    ri, _, rcp = oracle.MeshIndex(V, F).closest_contract(Q[sel])
+    assert np.array_equal(hi.numpy()[sel], ri)

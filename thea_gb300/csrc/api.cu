@@ -126,6 +126,26 @@ static bool is_host_pointer(void const * p) {
   return !(a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged);
 }
 
+// Device-usable addresses of caller arrays that are all pinned host memory (null entries are skipped); false if any
+// array is device or pageable memory.
+static bool pinned_host_views(std::initializer_list<void const *> ptrs, std::vector<void *> & out) {
+  out.clear();
+  for (void const * p : ptrs) {
+    if (!p) {
+      out.push_back(nullptr);
+      continue;
+    }
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return false;
+    out.push_back(at.devicePointer);
+  }
+  return true;
+}
+
 // Two non-blocking copy/compute streams per device, created once, used to overlap chunk transfers with kernels.
 static std::array<cudaStream_t, 2> staging_streams() {
   static std::mutex m;
@@ -470,6 +490,18 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
   cp.precision = precision;
   cp.scene_scale = scene_scale_of(mesh_bvh);
   unsigned * err = handle_error_word(mesh_bvh);
+  // queries and results all in pinned host memory (FP32, large batch): read and written in place by the kernels
+  std::vector<void *> dp;
+  if (precision == THEA_PRECISION_FP32_REFERENCE && !out_error && !mesh_bvh->query_order &&
+      mesh_bvh->num_segments == 1 && num_queries >= (1 << 16) &&
+      pinned_host_views({queries, out_index, out_distance, out_closest_point}, dp)) {
+    ClosestParams c2 = cp;
+    c2.budget = 256;  // the step budget of the device-resident two-phase path
+    run_closest_stream(mesh_bvh, (float const *)dp[0], num_queries, c2, (int32_t *)dp[1], (float *)dp[2],
+                       (float *)dp[3], (cudaStream_t)stream);
+    THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    return;
+  }
   run_staged({{(void *)queries, 12, false, false}, {out_index, 4, true, false}, {out_distance, 4, true, false},
               {out_closest_point, 12, true, false}, {out_error, 4, true, false}},
              num_queries, (cudaStream_t)stream,
@@ -495,27 +527,13 @@ static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const flo
   rp.recheck = precision == THEA_PRECISION_FP64_RECHECK;
   if (!rp.recheck) out_time64 = nullptr, out_index64 = nullptr, out_flags = nullptr;
   // rays and results all in pinned host memory: one launch reads and writes them in place
-  if (!rp.recheck && !out_normal && !mesh_bvh->has_transform && num_rays >= (1 << 16)) {
-    void const * hp[4] = {origins, directions, out_time, out_index};
-    void * dp[4] = {nullptr, nullptr, nullptr, nullptr};
-    bool direct = true;
-    for (int i = 0; i < 4 && direct; ++i) {
-      if (!hp[i]) continue;
-      cudaPointerAttributes at;
-      if (cudaPointerGetAttributes(&at, hp[i]) != cudaSuccess) {
-        cudaGetLastError();
-        direct = false;
-      } else {
-        direct = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
-        dp[i] = at.devicePointer;
-      }
-    }
-    if (direct) {
-      run_ray_stream(mesh_bvh, (float const *)dp[0], (float const *)dp[1], num_rays, rp.max_time, (float *)dp[2],
-                     (int32_t *)dp[3], err, (cudaStream_t)stream);
-      THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
-      return;
-    }
+  std::vector<void *> dp;
+  if (!rp.recheck && !out_normal && !mesh_bvh->has_transform && num_rays >= (1 << 16) &&
+      pinned_host_views({origins, directions, out_time, out_index}, dp)) {
+    run_ray_stream(mesh_bvh, (float const *)dp[0], (float const *)dp[1], num_rays, rp.max_time, (float *)dp[2],
+                   (int32_t *)dp[3], err, (cudaStream_t)stream);
+    THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    return;
   }
   run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
               {out_index, 4, true, false}, {out_normal, 12, true, false}, {out_time64, 4, true, false},

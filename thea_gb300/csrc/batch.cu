@@ -358,6 +358,153 @@ batch_closest_phase2_kernel(BatchForest f, ClosestArgs a, HardQueue hq, unsigned
   }
 }
 
+// Closest point of one BVH with queries and results in pinned host memory, read and written by the kernel (the
+// in-place form of the first phase above, FP32 reference arithmetic): a warp copies each 64-query block into shared
+// memory once, results collect in a per-warp ring of block buffers and are written out in query order with coalesced
+// stores once the block is done. A query over the step budget is queued as in the first phase and counts as done for
+// its block; the warp-per-query kernel then writes its result over the block's placeholder.
+constexpr int CP_STREAM_RING = 4;
+constexpr int CP_STREAM_WARPS = BATCH_THREADS / 32;
+
+template <int W, int STACK>
+__global__ void __launch_bounds__(BATCH_THREADS)
+closest_stream_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned long long * counter, int budget,
+                      HardQueue hq) {
+  __shared__ float s_in[CP_STREAM_WARPS][REFILL_BLOCK * 3];
+  __shared__ int s_i[CP_STREAM_WARPS][CP_STREAM_RING][REFILL_BLOCK];
+  __shared__ float s_d[CP_STREAM_WARPS][CP_STREAM_RING][REFILL_BLOCK];
+  __shared__ float s_c[CP_STREAM_WARPS][CP_STREAM_RING][REFILL_BLOCK * 3];
+  __shared__ int s_left[CP_STREAM_WARPS][CP_STREAM_RING];
+  __shared__ long long s_base[CP_STREAM_WARPS][CP_STREAM_RING];
+  __shared__ int s_cnt[CP_STREAM_WARPS][CP_STREAM_RING];
+  unsigned const FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WideNode<W> const * nodes = (WideNode<W> const *)f.nodes;
+  int const root = __ldg(f.seg_root);
+  float * in = s_in[warp];
+  int64_t qb = 0, qe = 0;  // queries of the current block not yet handed out, warp-uniform
+  bool exhausted = false;  // warp-uniform
+  long long taken = 0, oldest = 0;  // blocks taken / oldest block not written out, warp-uniform
+  int64_t q = -1;
+  int slot = 0;
+  int64_t qbase = 0;
+  V3 p = V3{0.f, 0.f, 0.f};
+  int2 stk[STACK];
+  int sp = 0;
+  int next = CHILD_EMPTY;
+  float best = 0.f;
+  int best_idx = INT_MAX;
+  int64_t best_slot = -1;
+  V3 best_cp = V3{0.f, 0.f, 0.f};
+  int pops = 0;
+  while (true) {
+    __syncwarp();
+    while (oldest < taken && s_left[warp][oldest % CP_STREAM_RING] == 0) {
+      int sl = (int)(oldest % CP_STREAM_RING);
+      long long base = s_base[warp][sl];
+      int cnt = s_cnt[warp][sl];
+      for (int j = lane; j < cnt; j += 32) {
+        a.out_index[base + j] = s_i[warp][sl][j];
+        if (a.out_dist) a.out_dist[base + j] = s_d[warp][sl][j];
+      }
+      if (a.out_cp)
+        for (int j = lane; j < 3 * cnt; j += 32) a.out_cp[3 * base + j] = s_c[warp][sl][j];
+      ++oldest;
+    }
+    __syncwarp();
+    unsigned idle = __ballot_sync(FULL, q < 0);
+    if (idle && !exhausted) {
+      if (qb >= qe && taken - oldest < CP_STREAM_RING) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(counter, (unsigned long long)REFILL_BLOCK);
+        b = __shfl_sync(FULL, b, 0);
+        if ((int64_t)b >= nq) {
+          exhausted = true;
+        } else {
+          qb = (int64_t)b;
+          qe = qb + REFILL_BLOCK < nq ? qb + REFILL_BLOCK : nq;
+          int cnt = (int)(qe - qb);
+          for (int k = lane; k < 3 * cnt; k += 32) in[k] = a.queries[3 * qb + k];
+          int sl = (int)(taken % CP_STREAM_RING);
+          if (lane == 0) {
+            s_base[warp][sl] = qb;
+            s_cnt[warp][sl] = cnt;
+            s_left[warp][sl] = cnt;
+          }
+          ++taken;
+          __syncwarp();
+        }
+      }
+      if (!exhausted && qb < qe) {
+        int rank = __popc(idle & ((1u << lane) - 1));
+        int take = __popc(idle);
+        int64_t avail = qe - qb;
+        if (q < 0 && rank < avail) {
+          q = qb + rank;
+          slot = (int)((taken - 1) % CP_STREAM_RING);
+          qbase = s_base[warp][slot];
+          float const * r = in + (q - qbase) * 3;
+          p = V3{r[0], r[1], r[2]};
+          best = a.thresh;
+          best_idx = INT_MAX;
+          best_slot = -1;
+          sp = 0;
+          next = root;
+          pops = 0;
+        }
+        qb += take < avail ? take : avail;
+      }
+    }
+    bool busy = __ballot_sync(FULL, q >= 0) != 0;
+    if (!busy && oldest == taken && (exhausted || qb >= qe)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (q < 0) continue;
+    if (next == CHILD_EMPTY && sp == 0) {
+      bool found = best_idx != INT_MAX;
+      int j = (int)(q - qbase);
+      s_i[warp][slot][j] = found ? best_idx : -1;
+      s_d[warp][slot][j] = found ? sqrtf(best) : -1.f;
+      s_c[warp][slot][3 * j] = found ? best_cp.x : 0.f;
+      s_c[warp][slot][3 * j + 1] = found ? best_cp.y : 0.f;
+      s_c[warp][slot][3 * j + 2] = found ? best_cp.z : 0.f;
+      atomicSub(&s_left[warp][slot], 1);
+      q = -1;
+      continue;
+    }
+    if (budget > 0 && ++pops > budget) {
+      // over budget: queued with its best element; the warp-per-query kernel writes its result in place later
+      unsigned long long pos = atomicAdd(hq.count, 1ull);
+      hq.q[pos] = q;
+      hq.bound[pos] = best;
+      hq.idx[pos] = best_idx;
+      hq.slot[pos] = best_slot;
+      atomicSub(&s_left[warp][slot], 1);
+      q = -1;
+      continue;
+    }
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > best * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, f.err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      cp_leaf_fp32(f.cp_rec, 0, first, count, p, best, best_idx, best_slot, best_cp);
+    }
+  }
+}
+
 template <int W, int STACK>
 __global__ void __launch_bounds__(BATCH_THREADS)
 batch_ray_kernel(BatchForest f, float const * __restrict__ origins, float const * __restrict__ dirs,
@@ -513,6 +660,39 @@ void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff
                         : launch_batch_closest<4, 256>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
   else sm ? launch_batch_closest<8, 128>(f, a, nq, cp.precision, budget, c, chunk, hq, s)
           : launch_batch_closest<8, 512>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
+}
+
+template <int W, int STACK>
+void launch_closest_stream(BatchForest const & f, ClosestArgs const & a, int64_t nq, int budget,
+                           unsigned long long * counters, HardQueue const & hq, cudaStream_t s) {
+  auto k1 = closest_stream_kernel<W, STACK>;
+  int64_t need = ceil_div(ceil_div(nq, REFILL_BLOCK) * 32, BATCH_THREADS);
+  unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(persistent_grid((void const *)k1), need));
+  THEA_LAUNCH_NAMED("closest_stream_kernel", k1, grid, BATCH_THREADS, 0, s, f, a, nq, counters, budget, hq);
+  auto k2 = batch_closest_phase2_kernel<W, THEA_PRECISION_FP32_REFERENCE>;
+  THEA_LAUNCH_NAMED("batch_closest_phase2_kernel", k2, persistent_grid((void const *)k2), BATCH_THREADS, 0, s, f, a, hq,
+                    counters + 1);
+}
+
+void run_closest_stream(thea_bvh const * b, float const * q, int64_t nq, ClosestParams const & cp, int32_t * idx,
+                        float * dist, float * cpt, cudaStream_t s) {
+  if (nq <= 0) return;
+  THEA_REQUIRE(b->num_segments == 1, "closest_stream: one BVH only");
+  BatchForest f = forest_view(b);
+  bool sm = small_stack_ok(b);
+  ClosestArgs a{q, nullptr, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, nullptr};
+  int budget = cp.budget > 0 ? cp.budget : 0;
+  Scratch counters(3 * sizeof(unsigned long long), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));
+  auto * c = counters.as<unsigned long long>();
+  size_t hq_n = budget > 0 ? (size_t)nq : 1;
+  Scratch hq_q(hq_n * sizeof(int64_t), s), hq_b(hq_n * sizeof(float), s);
+  Scratch hq_i(hq_n * sizeof(int32_t), s), hq_s(hq_n * sizeof(int64_t), s);
+  HardQueue hq{hq_q.as<int64_t>(), hq_b.as<float>(), hq_i.as<int32_t>(), hq_s.as<int64_t>(), c + 2};
+  if (b->width == 4) sm ? launch_closest_stream<4, 64>(f, a, nq, budget, c, hq, s)
+                        : launch_closest_stream<4, 256>(f, a, nq, budget, c, hq, s);
+  else sm ? launch_closest_stream<8, 128>(f, a, nq, budget, c, hq, s)
+          : launch_closest_stream<8, 512>(f, a, nq, budget, c, hq, s);
 }
 
 void run_batch_ray(thea_bvh const * b, float const * o, float const * d, int64_t const * qoff, int64_t nq,
