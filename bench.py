@@ -483,6 +483,31 @@ def extra_workloads(T, torch, stream, flush, args):
     out["closest_point_cfg0"] = {"value": CP_QUERIES / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
                                  "ms_per_step": statistics.mean(ms), "kernel_ms": kms,
                                  "roofline_frac": ALGO_BYTES_CFG0 / (max(kms, 1e-9) / 1e3) / 1e9 / peaks()[0]}
+    # end to end through the C ABI with the queries and all three outputs in pinned host memory
+    import ctypes
+    from thea_gb300 import _native as N
+    hq = torch.from_numpy(Q).pin_memory()
+    hi = torch.empty(CP_QUERIES, dtype=torch.int32).pin_memory()
+    hd, hc = torch.empty(CP_QUERIES).pin_memory(), torch.empty((CP_QUERIES, 3)).pin_memory()
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+
+    def cp_e2e():
+        N.check(N.lib().thea_closest_element(bvh.handle, p(hq), CP_QUERIES, -1.0, p(hi), p(hd), p(hc),
+                                             ctypes.c_void_p(stream.cuda_stream)))
+
+    for _ in range(2):
+        cp_e2e()
+    e2e_t = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cp_e2e()
+        e2e_t.append(time.perf_counter() - t0)
+    out["closest_point_cfg0"]["e2e"] = {"value": CP_QUERIES / statistics.mean(e2e_t) / 1e6, "unit": "Mqueries/s",
+                                        "ms": 1e3 * statistics.mean(e2e_t), "h2d_bytes": 12 * CP_QUERIES,
+                                        "d2h_bytes": 20 * CP_QUERIES, "same_as_device":
+                                        bool(torch.equal(hi, bvh.closest_element(Qd)[0].cpu()))}
     bvh.close()
     # config 2: 1,048,576 area samples of the config-0 mesh (reference Random stream), k = 16 graph excluding self
     torch.cuda.synchronize()
