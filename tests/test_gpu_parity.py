@@ -486,3 +486,28 @@ def test_closest_pinned_host_arrays_are_read_in_place(T, oracle):
     sel = np.arange(0, n, 37)
     ri, _, rcp = oracle.MeshIndex(V, F).closest_contract(Q[sel])
     assert np.array_equal(hi.numpy()[sel], ri)
+
+
+def test_knn_with_pinned_host_arrays(T):
+    """k-NN with pinned host arrays (query mode with exclusions, and the self graph) equals the device-resident calls."""
+    import ctypes
+    import torch
+    from thea_gb300 import _native as N
+    P = W.uniform_box_points(60000, [0] * 3, [1] * 3, 321)
+    Q = W.uniform_box_points(70001, [0] * 3, [1] * 3, 322)
+    ex = np.random.default_rng(323).integers(-1, len(P), size=len(Q)).astype(np.int32)
+    pb = T.PointBvh(dev(P))
+    L = N.lib()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ptr = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    ki, kd = pb.k_closest_pairs(dev(Q), 8, exclude=dev(ex))
+    hq, he = torch.from_numpy(Q).pin_memory(), torch.from_numpy(ex).pin_memory()
+    hi = torch.empty((len(Q), 8), dtype=torch.int32).pin_memory()
+    hd = torch.empty((len(Q), 8)).pin_memory()
+    N.check(L.thea_k_closest(pb.handle, ptr(hq), len(Q), 8, -1.0, ptr(he), ptr(hi), ptr(hd), st))
+    assert torch.equal(hi, ki.cpu()) and torch.equal(hd, kd.cpu())
+    si, sd = pb.k_closest_self(16, device=True)
+    hi = torch.empty((len(P), 16), dtype=torch.int32).pin_memory()
+    hd = torch.empty((len(P), 16)).pin_memory()
+    N.check(L.thea_k_closest_self(pb.handle, 16, ptr(hi), ptr(hd), st))
+    assert torch.equal(hi, si.cpu()) and torch.equal(hd, sd.cpu())
