@@ -137,8 +137,26 @@ def case_ray_host():
                                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
 
 
-CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg3_fp64_64": case_cfg3_fp64_64,
-         "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
+def case_cfg0_host():
+    """Config 0 through the C ABI with queries and results in pinned host memory (the in-place kernels): three calls."""
+    import ctypes
+    import torch
+    import thea_gb300 as T
+    from thea_gb300 import _native as N
+    V, F, Q = W.config0()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1, max_leaf_size=1)
+    n = len(Q)
+    hq = torch.from_numpy(Q).pin_memory()
+    hi, hd = torch.empty(n, dtype=torch.int32).pin_memory(), torch.empty(n).pin_memory()
+    hc = torch.empty((n, 3)).pin_memory()
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    for _ in range(3):
+        N.check(N.lib().thea_closest_element(bvh.handle, p(hq), n, -1.0, p(hi), p(hd), p(hc),
+                                             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+
+CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host,
+         "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
 
 
 def peaks():
