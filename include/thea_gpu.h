@@ -6,9 +6,12 @@
  * a thea_status, and thea_last_error_message() gives a human-readable detail for the calling thread.
  *
  * Pointers. Array arguments may point to device memory or to host memory (pinned or pageable); the library detects which
- * with cudaPointerGetAttributes. Device-resident arrays are used in place. When any array of a query call is host
- * memory, the call stages the work through device buffers in chunks on the given stream and returns after the results
- * have been written back (the call then synchronizes the stream). Device-only calls are asynchronous on the stream.
+ * with cudaPointerGetAttributes. Device-resident arrays are used in place. When every array of a large FP32 first-hit
+ * call (no normals) or closest-point call (no error output) is pinned host memory, the kernels read and write those
+ * arrays in place over NVLink-C2C (one launch, block-sized coalesced accesses). Otherwise, when any array of a query
+ * call is host memory, the call stages the work through device buffers in chunks on the given stream. Calls with host
+ * arrays return after the results are in host memory (they synchronize the stream); device-only calls are
+ * asynchronous on the stream.
  *
  * Streams. `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.
  *
