@@ -219,6 +219,42 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
                                        int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
                                        float * out_avg_separation, void * stream);
 
+/* ---- mesh files --------------------------------------------------------------------------------------------------- */
+
+/* A mesh file read into host arrays in the reference's element order, ready for thea_mesh_bvh_build. */
+typedef struct thea_mesh thea_mesh;
+
+typedef struct thea_mesh_info {
+  int64_t num_vertices;  /* vertices of all submeshes */
+  int64_t num_triangles;
+  int64_t num_faces;     /* faces that produced at least one triangle */
+  int64_t num_submeshes;
+} thea_mesh_info;
+
+/* MeshGroup<DisplayMesh>::load(path) (Graphics/MeshGroup.hpp:471-497) with the default codec options, for the OFF
+ * (ASCII and binary, Graphics/MeshCodecOff.hpp) and OBJ (Graphics/MeshCodecObj.hpp) codecs, chosen by the file
+ * extension. Submeshes come in file order (OBJ: one per g/o group that has faces; each submesh's vertices are the
+ * distinct vertex/texcoord/normal references of its faces in ascending order). Faces are triangulated as
+ * DisplayMesh::addFace does (Graphics/DisplayMesh.cpp:249-320); faces the non-strict readers skip (bad, out-of-range or,
+ * in OFF, repeated indices) are skipped. The PLY and 3DS codecs are not built: THEA_ERR_INVALID_ARGUMENT. */
+THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh);
+THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info);
+/* Copies the arrays to host buffers (each nullable): vertices (3 x num_vertices floats), vertex_source (file vertex index
+ * of each vertex, 0-based), triangles (3 x num_triangles indices into vertices), triangle_face (source face index of each
+ * triangle: the OFF face number, or the OBJ reader's running face count), submesh_vertex_offsets and
+ * submesh_triangle_offsets (num_submeshes + 1 entries each). */
+THEA_API thea_status thea_mesh_copy(const thea_mesh * mesh, float * vertices, int32_t * vertex_source,
+                                    int32_t * triangles, int32_t * triangle_face, int64_t * submesh_vertex_offsets,
+                                    int64_t * submesh_triangle_offsets);
+THEA_API thea_status thea_mesh_destroy(thea_mesh * mesh);
+
+/* Triangles of one polygon of num_vertices host positions (xyz) as DisplayMesh::addFace makes them: a triangle as is,
+ * a quad by Polygon3::triangulateQuad (Polygon3.hpp:245-285), more vertices by Polygon3::triangulate
+ * (Polygon3.cpp:179-270). Writes local vertex indices, three per triangle, to out_triangles (room for
+ * 3 x (num_vertices - 2)) and the triangle count (0: a degenerate face, which the mesh skips) to out_count. */
+THEA_API thea_status thea_triangulate_face(const float * positions, int32_t num_vertices, int32_t * out_triangles,
+                                           int32_t * out_count);
+
 /* k nearest points of a point BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
  * index first). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
  * Code/Source/Algorithms/PointSet3.hpp:576-583). dist_bound < 0: unbounded; else only squared distances strictly below

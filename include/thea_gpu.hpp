@@ -336,6 +336,39 @@ class MeshSampler {
   int64_t nf_;
 };
 
+// MeshGroup<DisplayMesh>::load for OFF and OBJ files, flattened into host arrays in the reference's element order;
+// MeshBvh(file.vertices.data(), file.numVertices(), file.triangles.data(), file.numTriangles()) indexes its triangles.
+class MeshFile {
+ public:
+  explicit MeshFile(std::string const & path) {
+    thea_mesh * m = nullptr;
+    check(thea_mesh_read(path.c_str(), &m));
+    thea_mesh_info info{};
+    thea_status s = thea_mesh_get_info(m, &info);
+    if (s == THEA_OK) {
+      vertices.resize((size_t)(3 * info.num_vertices));
+      vertex_source.resize((size_t)info.num_vertices);
+      triangles.resize((size_t)(3 * info.num_triangles));
+      triangle_face.resize((size_t)info.num_triangles);
+      submesh_vertex_offsets.resize((size_t)(info.num_submeshes + 1));
+      submesh_triangle_offsets.resize((size_t)(info.num_submeshes + 1));
+      s = thea_mesh_copy(m, vertices.data(), vertex_source.data(), triangles.data(), triangle_face.data(),
+                         submesh_vertex_offsets.data(), submesh_triangle_offsets.data());
+      num_faces = info.num_faces;
+    }
+    thea_mesh_destroy(m);
+    check(s);
+  }
+
+  int64_t numVertices() const { return (int64_t)vertex_source.size(); }
+  int64_t numTriangles() const { return (int64_t)triangle_face.size(); }
+
+  std::vector<float> vertices;
+  std::vector<int32_t> vertex_source, triangles, triangle_face;
+  std::vector<int64_t> submesh_vertex_offsets, submesh_triangle_offsets;
+  int64_t num_faces = 0;
+};
+
 }  // namespace thea_gpu
 
 #endif  // THEA_GPU_HPP

@@ -56,6 +56,25 @@ int main(int argc, char ** argv) {
   } catch (thea_gpu::Exception const & e) {
     if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 12;
   }
+  // a quad in an OFF file becomes two triangles of face 0 (host code only)
+  {
+    std::string path = std::string(argv[0]) + ".off";
+    FILE * f = std::fopen(path.c_str(), "w");
+    if (!f) return 14;
+    std::fputs("OFF\n4 1 0\n0 0 0\n1 0 0\n1 1 0\n0 1 0\n4 0 1 2 3\n", f);
+    std::fclose(f);
+    thea_gpu::MeshFile mf(path);
+    std::remove(path.c_str());
+    int32_t const want[6] = {0, 1, 2, 2, 3, 0};
+    if (mf.numVertices() != 4 || mf.numTriangles() != 2 || mf.num_faces != 1) return 15;
+    if (std::memcmp(mf.triangles.data(), want, sizeof(want)) != 0 || mf.triangle_face[1] != 0) return 16;
+    try {
+      thea_gpu::MeshFile missing(path);
+      return 17;  // must have thrown
+    } catch (thea_gpu::Exception const & e) {
+      if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 18;
+    }
+  }
   if (no_device) return 0;
 
   float V[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};

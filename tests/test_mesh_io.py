@@ -1,0 +1,275 @@
+"""CPU tests of the mesh-file readers and face triangulation (host code of the library) against the pure-Python
+restatement in oracle/mesh_oracle.py, plus hand-derived answers for small cases."""
+
+import struct
+
+import numpy as np
+import pytest
+
+from oracle import mesh_oracle as MO
+
+
+@pytest.fixture(scope="module")
+def T():
+    from thea_gb300 import build as B
+    B.build()
+    import thea_gb300
+    return thea_gb300
+
+
+def _lib_tris(T, pts):
+    return [tuple(int(x) for x in t) for t in T.triangulate_face(np.asarray(pts, np.float32))]
+
+
+def _same_mesh(got, want):
+    np.testing.assert_array_equal(got.vertices, want["vertices"])
+    np.testing.assert_array_equal(got.vertex_source, want["vertex_source"])
+    np.testing.assert_array_equal(got.triangles, want["triangles"])
+    np.testing.assert_array_equal(got.triangle_face, want["triangle_face"])
+    np.testing.assert_array_equal(got.submesh_vertex_offsets, want["submesh_vertex_offsets"])
+    np.testing.assert_array_equal(got.submesh_triangle_offsets, want["submesh_triangle_offsets"])
+    assert got.num_faces == want["num_faces"]
+
+
+# ---- triangulation ---------------------------------------------------------------------------------------------------
+
+def test_known_triangulations(T):
+    sq = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)]
+    assert _lib_tris(T, sq) == MO.triangulate_face(sq) == [(0, 1, 2), (2, 3, 0)]
+    # a dart whose diagonal 0-2 lies outside: the quad splits along 1-3
+    dart = [(0, 0, 0), (2, 1, 0), (0, 2, 0), (1, 1, 0)]
+    assert _lib_tris(T, dart) == MO.triangulate_face(dart) == [(1, 2, 3), (3, 0, 1)]
+    # collinear quad: no triangle; half-degenerate quad: one
+    line = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (3, 0, 0)]
+    assert _lib_tris(T, line) == MO.triangulate_face(line) == []
+    half = [(0, 0, 0), (1, 0, 0), (2, 0, 0), (1, 1, 0)]
+    assert _lib_tris(T, half) == MO.triangulate_face(half) == [(2, 3, 0)]
+    # convex counter-clockwise pentagon: ears (4, 0, 1), (1, 2, 3), (3, 4, 1)
+    pent = [(np.cos(a), np.sin(a), 0.0) for a in np.arange(5) * 2 * np.pi / 5]
+    assert _lib_tris(T, pent) == MO.triangulate_face(pent) == [(4, 0, 1), (1, 2, 3), (3, 4, 1)]
+    # the same pentagon clockwise: the polygon is walked reversed and each triangle emitted reversed
+    cw = pent[::-1]
+    assert _lib_tris(T, cw) == MO.triangulate_face(cw)
+    assert len(_lib_tris(T, cw)) == 3
+    # fewer than three vertices and a plain triangle
+    assert _lib_tris(T, pent[:2]) == [] and _lib_tris(T, pent[:3]) == [(0, 1, 2)]
+
+
+def _random_polygon(rng, n, concave):
+    ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+    rad = rng.uniform(0.3, 1.0, n) if concave else np.ones(n)
+    xy = np.stack([rad * np.cos(ang), rad * np.sin(ang), np.zeros(n)], 1)
+    if rng.random() < 0.5:
+        xy = xy[::-1]
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    return (xy @ q.T * rng.uniform(0.01, 100) + rng.normal(size=3) * 10).astype(np.float32)
+
+
+@pytest.mark.parametrize("concave", [False, True])
+def test_random_polygons_match_the_restatement(T, concave):
+    rng = np.random.default_rng(11 + concave)
+    for _ in range(400):
+        n = int(rng.integers(3, 13))
+        p = _random_polygon(rng, n, concave)
+        got, want = _lib_tris(T, p), MO.triangulate_face(p)
+        assert got == want, (p.tolist(), got, want)
+        if not concave:
+            assert len(got) == n - 2
+
+
+def test_degenerate_polygons_match_the_restatement(T):
+    rng = np.random.default_rng(5)
+    for _ in range(200):
+        n = int(rng.integers(4, 9))
+        p = _random_polygon(rng, n, True)
+        k = int(rng.integers(0, n))
+        p[(k + 1) % n] = p[k]                      # a repeated vertex
+        if rng.random() < 0.3:
+            p[:, 2] = p[0, 2]; p[:, 1] = p[0, 1]   # all collinear
+        assert _lib_tris(T, p) == MO.triangulate_face(p)
+
+
+# ---- OFF -------------------------------------------------------------------------------------------------------------
+
+OFF_TEXT = """OFF
+# a comment, then a blank line
+
+7 8 0
+0 0 0
+1 0 0
+1 1 0
+0 1 0
+2 0.5 0.25
+# another comment
+1.5 2 1e-3
+-1 -1 -1
+4 0 1 2 3
+3 1 4 2
+5 0 1 4 5 3
+3 0 1 9
+3 0 1 1
+2 0 1
+0
+6 0 1 4 2 5 6 7 8
+"""
+
+
+def test_off_ascii(T, tmp_path):
+    path = tmp_path / "m.off"
+    path.write_bytes(OFF_TEXT.replace("\n", "\r\n").encode())
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    assert m.vertices.shape == (7, 3) and m.vertex_source.tolist() == list(range(7))
+    # faces 0 (quad), 1 (triangle), 2 (pentagon) and 7 (hexagon; extra indices on the line are ignored) produce
+    # triangles; 3 (index out of range), 4 (repeated vertex), 5 (two vertices) and 6 (empty) do not
+    assert sorted(set(m.triangle_face.tolist())) == [0, 1, 2, 7]
+    assert m.triangles[:2].tolist() == [[0, 1, 2], [2, 3, 0]] and m.triangles[2].tolist() == [1, 4, 2]
+    assert m.num_faces == 4 and m.submesh_triangle_offsets.tolist() == [0, len(m.triangle_face)]
+
+
+def _binary_off(nv_list, faces, trailing=b""):
+    b = b"OFF BINARY\n" + struct.pack(">iii", len(nv_list), len(faces), 0)
+    for v in nv_list:
+        b += struct.pack(">fff", *v)
+    for f in faces:
+        b += f
+    return b + trailing
+
+
+def test_off_binary(T, tmp_path):
+    V = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0.5, 2, 0.5)]
+    faces = [
+        struct.pack(">iiiii", 4, 0, 1, 2, 3) + struct.pack(">i", 0),            # quad, no colour
+        struct.pack(">iiii", 3, 1, 4, 2) + struct.pack(">ifff", 3, 1, 0, 0),    # triangle with an RGB colour
+        struct.pack(">iiii", 3, 0, 0, 2) + struct.pack(">i", 0),                # repeated vertex: skipped
+        # an out-of-range index ends the face's indices; the next word (index 1) is taken as the colour count and
+        # skips the real colour count, so the stream stays aligned
+        struct.pack(">iiii", 3, 0, 99, 1) + struct.pack(">i", 0),
+        struct.pack(">iiii", 3, 2, 3, 4) + struct.pack(">i", 0),
+    ]
+    path = tmp_path / "m.off"
+    path.write_bytes(_binary_off(V, faces))
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    assert m.triangle_face.tolist() == [0, 0, 1, 4]
+    assert m.triangles.tolist() == [[0, 1, 2], [2, 3, 0], [1, 4, 2], [2, 3, 4]]
+
+
+def test_off_errors(T, tmp_path):
+    from thea_gb300 import TheaError
+    bad = tmp_path / "bad.off"
+    bad.write_text("COFF\n1 0 0\n0 0 0\n")
+    with pytest.raises(TheaError, match="does not start with 'OFF'"):
+        T.read_mesh(str(bad))
+    short = tmp_path / "short.off"
+    short.write_text("OFF\n3 1 0\n0 0 0\n1 0 0\n")
+    with pytest.raises(TheaError, match="end of input"):
+        T.read_mesh(str(short))
+    empty = tmp_path / "empty.off"
+    empty.write_text("OFF\n0 0 0\n")
+    m = T.read_mesh(str(empty))
+    assert m.vertices.shape == (0, 3) and m.submesh_triangle_offsets.tolist() == [0]
+    for name in ("m.ply", "m.3ds", "m.stl"):
+        (tmp_path / name).write_text("x")
+        with pytest.raises(TheaError):
+            T.read_mesh(str(tmp_path / name))
+    with pytest.raises(TheaError, match="cannot open"):
+        T.read_mesh(str(tmp_path / "missing.obj"))
+
+
+# ---- OBJ -------------------------------------------------------------------------------------------------------------
+
+OBJ_TEXT = """# header comment
+mtllib ignored.mtl
+v 0 0 0
+v 1 0 0
+v 1 1 0
+v 0 1 0
+v 2 0.5 0.5
+vt 0 0
+vt 1 0
+vt 1 1
+vn 0 0 1
+vn 0 0 -1
+f 1/1/1 2/2/1 3/3/1 4/1/1
+f 2//2 5//2 3//2
+usemtl whatever
+g second
+f -1 -4 -3
+f 1/2 2/3 5/1 3/2 4/3
+p 1
+f 1 0 2
+f 1 2 7
+o third
+f 1 2 2
+f 1 2 3 4/9/9
+g
+s off
+f 4 3 2
+"""
+
+
+def test_obj_groups_and_references(T, tmp_path):
+    path = tmp_path / "m.obj"
+    path.write_text(OBJ_TEXT)
+    m = T.read_mesh(str(path))
+    want = MO.read_mesh(str(path))
+    _same_mesh(m, want)
+    # the first submesh's vertices are its distinct (v, t, n) references in ascending order: (1,1,1) (2,0,2) (2,2,1)
+    # (3,0,2) (3,3,1) (4,1,1) (5,0,2)
+    s0 = slice(m.submesh_vertex_offsets[0], m.submesh_vertex_offsets[1])
+    assert m.vertex_source[s0].tolist() == [0, 1, 1, 2, 2, 3, 4]
+    # four submeshes: the anonymous one, 'second', 'third' and the bare 'g'. Faces are numbered over the whole file;
+    # the bad faces (index 0, index 7) are not numbered, the point 'p 1' (face 4) is but makes no triangle, and the
+    # degenerate 'f 1 2 2' (face 5) is kept as a triangle
+    assert m.submesh_triangle_offsets.tolist()[0] == 0 and len(m.submesh_triangle_offsets) == 5
+    assert sorted(set(m.triangle_face.tolist())) == [0, 1, 2, 3, 5, 6, 7]
+
+
+def test_obj_drops_groups_without_triangles(T, tmp_path):
+    path = tmp_path / "m.obj"
+    path.write_text("v 0 0 0\nv 1 0 0\nv 2 0 0\nv 0 1 0\ng a\nf 1 2 3 1/1\np 4\ng b\nf 1 2 4\n")
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    # group a: a quad whose references 1 and 1/1 are the same vertex (no texture coordinates exist, so /1 is dropped)
+    # is collinear, and a point: no triangle, so the group is dropped; group b's face is the file's third
+    assert m.submesh_vertex_offsets.tolist() == [0, 3] and m.triangle_face.tolist() == [2]
+
+
+def _random_obj(rng, n_vertices, n_faces):
+    V = rng.normal(size=(n_vertices, 3)).astype(np.float32)
+    lines = ["v %.9g %.9g %.9g" % tuple(v) for v in V] + ["vt 0.5 0.5", "vn 0 0 1"]
+    for f in range(n_faces):
+        if rng.random() < 0.05:
+            lines.append("g grp%d" % f)
+        k = int(rng.integers(1, 9))
+        ids = rng.choice(n_vertices, size=k, replace=False) + 1
+        forms = ["%d", "%d/1", "%d//1", "%d/1/1"]
+        fields = []
+        for i in ids:
+            i = int(i) if rng.random() < 0.8 else int(i) - n_vertices - 1   # some negative references
+            fields.append(forms[int(rng.integers(0, 4))] % i)
+        lines.append(("p " if k == 1 else "f ") + " ".join(fields))
+    return "\n".join(lines) + "\n"
+
+
+def test_random_obj_matches_the_restatement(T, tmp_path):
+    rng = np.random.default_rng(3)
+    for trial in range(6):
+        path = tmp_path / ("r%d.obj" % trial)
+        path.write_text(_random_obj(rng, 60, 300))
+        _same_mesh(T.read_mesh(str(path)), MO.read_mesh(str(path)))
+
+
+def test_random_off_matches_the_restatement(T, tmp_path):
+    rng = np.random.default_rng(4)
+    for trial in range(4):
+        V = rng.normal(size=(50, 3)).astype(np.float32)
+        lines = ["OFF", "50 200 0"] + ["%.9g %.9g %.9g" % tuple(v) for v in V]
+        for _ in range(200):
+            k = int(rng.integers(1, 8))
+            ids = rng.integers(0, 52, size=k)   # some out of range, some repeated
+            lines.append(" ".join(str(int(x)) for x in [k, *ids]))
+        path = tmp_path / ("r%d.off" % trial)
+        path.write_text("\n".join(lines) + "\n")
+        _same_mesh(T.read_mesh(str(path)), MO.read_mesh(str(path)))

@@ -3,6 +3,7 @@ build and area-weighted mesh sampling, as hand-written sm_103a CUDA behind a C A
 
 from .bvh import (MeshBvh, PointBvh, MeshForest, PointForest, Graph, autotune_batch_closest,  # noqa: F401
                   sample_evenly_by_area, launch_count, profiling, profiling_reset,  # noqa: F401
-                  profiling_read, point_gram_tile, random_sphere, sample_graph, write_sample_graph)
+                  profiling_read, point_gram_tile, random_sphere, sample_graph, write_sample_graph,  # noqa: F401
+                  MeshData, read_mesh, triangulate_face)
 from .serve import Server  # noqa: F401
 from ._native import TheaError, LIB_PATH  # noqa: F401

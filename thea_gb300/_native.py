@@ -47,6 +47,11 @@ class BvhInfo(ctypes.Structure):
                 ("device_error_bits", ctypes.c_uint32), ("num_segments", ctypes.c_int32)]
 
 
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_int64), ("num_triangles", ctypes.c_int64), ("num_faces", ctypes.c_int64),
+                ("num_submeshes", ctypes.c_int64)]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int32), ("max_leaf_size", ctypes.c_int32), ("queries_per_warp", ctypes.c_int32),
                 ("milliseconds", ctypes.c_float), ("candidates", ctypes.c_int32),
@@ -101,6 +106,11 @@ SIGNATURES = {
     "thea_sample_graph": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "thea_random_sphere": (ctypes.c_int, [ctypes.c_uint32, _i64, _vp, _vp]),
+    "thea_mesh_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "thea_mesh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(MeshInfo)]),
+    "thea_mesh_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "thea_mesh_destroy": (ctypes.c_int, [_vp]),
+    "thea_triangulate_face": (ctypes.c_int, [_vp, ctypes.c_int32, _vp, ctypes.POINTER(ctypes.c_int32)]),
     "thea_visibility": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32, _vp, _vp]),
     "thea_bvh_set_transform": (ctypes.c_int, [_vp, _vp, _vp]),
     "thea_bvh_clear_transform": (ctypes.c_int, [_vp]),

@@ -167,6 +167,12 @@ class MeshBvh(_Bvh):
         N.check(N.lib().thea_mesh_bvh_build(pv, nv, pf, nf, ctypes.byref(cfg), _stream_of(io.device),
                                             ctypes.byref(self._h)))
 
+    @classmethod
+    def from_file(cls, path, **kwargs):
+        """BVH over the triangles of an OFF or OBJ file, in the order MeshGroup::load + MeshBvh::add give them."""
+        m = read_mesh(path)
+        return cls(m.vertices, m.triangles, **kwargs)
+
     def closest_element(self, queries, dist_bound=-1.0, closest_points=True):
         """BvhN::closestElement<MetricL2>: (index, distance, closest point or None) per query."""
         io = _Arrays(queries)
@@ -505,6 +511,55 @@ def random_sphere(seed, count, device=False):
     out = np.empty((count, 3), np.float32)
     N.check(N.lib().thea_random_sphere(int(seed) & 0xffffffff, int(count), ctypes.c_void_p(out.ctypes.data), None))
     return out
+
+
+class MeshData:
+    """A mesh file read as MeshGroup<DisplayMesh>::load reads it (OFF or OBJ, by extension), flattened: vertices
+    [nv, 3] float32, vertex_source [nv] (file vertex index), triangles [nt, 3] int32, triangle_face [nt] (source face
+    index), submesh_vertex_offsets and submesh_triangle_offsets [submeshes + 1] int64, num_faces (faces that produced
+    triangles). Pass (vertices, triangles) to MeshBvh for the reference's element order."""
+
+    def __init__(self, vertices, vertex_source, triangles, triangle_face, submesh_vertex_offsets,
+                 submesh_triangle_offsets, num_faces):
+        self.vertices = vertices
+        self.vertex_source = vertex_source
+        self.triangles = triangles
+        self.triangle_face = triangle_face
+        self.submesh_vertex_offsets = submesh_vertex_offsets
+        self.submesh_triangle_offsets = submesh_triangle_offsets
+        self.num_faces = num_faces
+
+
+def read_mesh(path):
+    """Reads an OFF or OBJ file into host arrays (MeshData)."""
+    lib = N.lib()
+    h = ctypes.c_void_p()
+    N.check(lib.thea_mesh_read(str(path).encode(), ctypes.byref(h)))
+    try:
+        inf = N.MeshInfo()
+        N.check(lib.thea_mesh_get_info(h, ctypes.byref(inf)))
+        nv, nt, ns = inf.num_vertices, inf.num_triangles, inf.num_submeshes
+        v = np.empty((nv, 3), np.float32)
+        vs = np.empty(nv, np.int32)
+        t = np.empty((nt, 3), np.int32)
+        tf = np.empty(nt, np.int32)
+        svo = np.empty(ns + 1, np.int64)
+        sto = np.empty(ns + 1, np.int64)
+        N.check(lib.thea_mesh_copy(h, v.ctypes.data, vs.ctypes.data, t.ctypes.data, tf.ctypes.data, svo.ctypes.data,
+                                   sto.ctypes.data))
+        return MeshData(v, vs, t, tf, svo, sto, int(inf.num_faces))
+    finally:
+        lib.thea_mesh_destroy(h)
+
+
+def triangulate_face(positions):
+    """Triangles of one polygon (positions [n, 3]) as DisplayMesh::addFace makes them: int32 [t, 3] local indices."""
+    p = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    n = len(p)
+    out = np.empty((max(n - 2, 0), 3), np.int32)
+    cnt = ctypes.c_int32(0)
+    N.check(N.lib().thea_triangulate_face(p.ctypes.data, n, out.ctypes.data if n >= 3 else None, ctypes.byref(cnt)))
+    return out[:cnt.value]
 
 
 def sample_evenly_by_area(vertices, faces, num_samples, seed, rng="thea"):

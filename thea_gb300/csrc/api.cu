@@ -10,6 +10,7 @@
 #include "transform.hpp"
 #include "visibility.hpp"
 #include "sample_graph.hpp"
+#include "mesh_io.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -1197,6 +1198,64 @@ THEA_API thea_status thea_server_reset_stats(thea_server * server) {
   return guarded([&] {
     THEA_REQUIRE(server, "server_reset_stats: null server");
     server_reset_stats(server);
+  });
+}
+
+THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh) {
+  return guarded([&] {
+    THEA_REQUIRE(out_mesh, "mesh_read: null output");
+    *out_mesh = nullptr;
+    THEA_REQUIRE(path, "mesh_read: null path");
+    thea::MeshData data = thea::read_mesh_file(path);
+    *out_mesh = reinterpret_cast<thea_mesh *>(new thea::MeshData(std::move(data)));
+  });
+}
+
+THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh && info, "mesh_get_info: null argument");
+    auto const & m = *reinterpret_cast<thea::MeshData const *>(mesh);
+    info->num_vertices = (int64_t)m.vertex_source.size();
+    info->num_triangles = (int64_t)m.triangle_face.size();
+    info->num_faces = m.num_faces;
+    info->num_submeshes = (int64_t)m.submesh_triangle_offsets.size() - 1;
+  });
+}
+
+THEA_API thea_status thea_mesh_copy(const thea_mesh * mesh, float * vertices, int32_t * vertex_source,
+                                    int32_t * triangles, int32_t * triangle_face, int64_t * submesh_vertex_offsets,
+                                    int64_t * submesh_triangle_offsets) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh, "mesh_copy: null mesh");
+    auto const & m = *reinterpret_cast<thea::MeshData const *>(mesh);
+    auto put = [](void * dst, auto const & v) {
+      if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+    };
+    put(vertices, m.vertices);
+    put(vertex_source, m.vertex_source);
+    put(triangles, m.triangles);
+    put(triangle_face, m.triangle_face);
+    put(submesh_vertex_offsets, m.submesh_vertex_offsets);
+    put(submesh_triangle_offsets, m.submesh_triangle_offsets);
+  });
+}
+
+THEA_API thea_status thea_mesh_destroy(thea_mesh * mesh) {
+  return guarded([&] { delete reinterpret_cast<thea::MeshData *>(mesh); });
+}
+
+THEA_API thea_status thea_triangulate_face(const float * positions, int32_t num_vertices, int32_t * out_triangles,
+                                           int32_t * out_count) {
+  return guarded([&] {
+    THEA_REQUIRE(out_count, "triangulate_face: null count");
+    *out_count = 0;
+    THEA_REQUIRE(num_vertices >= 0, "triangulate_face: negative vertex count");
+    if (num_vertices < 3) return;
+    THEA_REQUIRE(positions && out_triangles, "triangulate_face: null argument");
+    std::vector<int32_t> tris;
+    int nt = thea::triangulate_face(positions, num_vertices, tris);
+    std::copy(tris.begin(), tris.end(), out_triangles);
+    *out_count = nt;
   });
 }
 

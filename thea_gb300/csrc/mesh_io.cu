@@ -1,0 +1,466 @@
+// Mesh file readers and face triangulation (host code).
+//
+// Restates, as far as geometry goes, the reference's non-strict OFF reader (Graphics/MeshCodecOff.hpp:154-330: ASCII and
+// big-endian binary), its OBJ reader (Graphics/MeshCodecObj.hpp:210-545: one submesh per g/o group, each submesh's
+// vertices being the distinct (vertex, texcoord, normal) references of its faces in sorted order) and the triangulation
+// of DisplayMesh::addFace (Graphics/DisplayMesh.cpp:249-320): quads by Polygon3::triangulateQuad (Polygon3.hpp:245-285),
+// larger polygons by Polygon3::triangulate (Polygon3.cpp:109-288: ear clipping after projecting onto the plane of
+// Polygon3::computeNormal, Polygon3.hpp:180-208, in the basis of Math::orthonormalBasis, MatrixUtil.hpp:225-249).
+// FP32 arithmetic in the reference's operation order; this file is compiled without floating-point contraction.
+#include "mesh_io.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cctype>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <fstream>
+#include <iterator>
+#include <map>
+#include <sstream>
+
+namespace thea {
+namespace {
+
+float const FLT_EPS = 1.1920928955078125e-07f;  // Math::eps<float>()
+
+struct V2 {
+  float x, y;
+};
+
+// Polygon3::triangulateQuad: the diagonal p0-p2 unless its two triangles face opposite ways, then the degeneracy test
+// against eps^2
+int triangulate_quad(V3 p0, V3 p1, V3 p2, V3 p3, int (&t)[6]) {
+  V3 n0 = cross(p1 - p0, p2 - p0);
+  V3 n1 = cross(p2 - p0, p3 - p0);
+  static int const diag02[6] = {0, 1, 2, 2, 3, 0};
+  static int const diag13[6] = {1, 2, 3, 3, 0, 1};
+  if (dot(n0, n1) < 0.f) {
+    n0 = cross(p2 - p1, p3 - p1);
+    n1 = cross(p3 - p1, p0 - p1);
+    std::copy(diag13, diag13 + 6, t);
+  } else {
+    std::copy(diag02, diag02 + 6, t);
+  }
+  float e2 = FLT_EPS * FLT_EPS;
+  if (squared_norm(n0) < e2) {
+    if (squared_norm(n1) < e2) return 0;
+    std::copy(t + 3, t + 6, t);  // the second triangle is the only non-degenerate one
+    return 1;
+  }
+  return squared_norm(n1) < e2 ? 1 : 2;
+}
+
+// Polygon3::computeNormal: the first (p2 - p1) x (p0 - p1) over consecutive vertex triples (n tries, wrapping around)
+// with squared norm >= 1e-10, normalised; zero if there is none
+V3 polygon_normal(std::vector<V3> const & p) {
+  size_t n = p.size();
+  V3 p0 = p[0], p1 = p[1];
+  size_t i2 = 2 % n;
+  for (size_t k = 0; k < n; ++k) {
+    V3 p2 = p[i2];
+    V3 nrm = cross(p2 - p1, p0 - p1);
+    if (squared_norm(nrm) >= 1e-10f) return normalized(nrm);
+    p0 = p1;
+    p1 = p2;
+    i2 = (i2 + 1) % n;
+  }
+  return V3{0.f, 0.f, 0.f};
+}
+
+// P inside or on the triangle ABC (counter-clockwise), by the signs of three edge cross products
+bool inside_triangle2(V2 A, V2 B, V2 C, V2 P) {
+  float ax = C.x - B.x, ay = C.y - B.y;
+  float bx = A.x - C.x, by = A.y - C.y;
+  float cx = B.x - A.x, cy = B.y - A.y;
+  float apx = P.x - A.x, apy = P.y - A.y;
+  float bpx = P.x - B.x, bpy = P.y - B.y;
+  float cpx = P.x - C.x, cpy = P.y - C.y;
+  float a_bp = ax * bpy - ay * bpx;
+  float c_ap = cx * apy - cy * apx;
+  float b_cp = bx * cpy - by * cpx;
+  return a_bp >= 0.f && b_cp >= 0.f && c_ap >= 0.f;
+}
+
+// An ear (u, v, w) of the remaining polygon: convex by more than eps and containing none of its other vertices
+bool is_ear(std::vector<V2> const & q, size_t u, size_t v, size_t w, size_t n, std::vector<size_t> const & idx) {
+  V2 A = q[idx[u]], B = q[idx[v]], C = q[idx[w]];
+  if (FLT_EPS > (((B.x - A.x) * (C.y - A.y)) - ((B.y - A.y) * (C.x - A.x)))) return false;
+  for (size_t p = 0; p < n; ++p) {
+    if (p == u || p == v || p == w) continue;
+    if (inside_triangle2(A, B, C, q[idx[p]])) return false;
+  }
+  return true;
+}
+
+// Polygon3::triangulate with the default epsilon
+int triangulate_polygon(std::vector<V3> const & p, std::vector<int32_t> & tris) {
+  size_t n = p.size();
+  size_t before = tris.size();
+  // Math::orthonormalBasis(normal): u = orthogonalDirection(normal), v = normalized(normal) x u
+  V3 normal = polygon_normal(p);
+  V3 w = normalized(normal);
+  V3 u = max_abs_axis(normal) == 0 ? normalized(V3{normal.y, -normal.x, 0.f}) : normalized(V3{0.f, normal.z, -normal.y});
+  V3 v = cross(w, u);
+  std::vector<V2> q(n);
+  for (size_t i = 0; i < n; ++i) {
+    V3 d = p[i] - p[0];
+    q[i] = V2{dot(d, u), dot(d, v)};
+  }
+  // signed area of the projected polygon (Polygon3::projArea)
+  float area = 0.f;
+  for (size_t a = n - 1, b = 0; b < n; a = b++) area += q[a].x * q[b].y - q[b].x * q[a].y;
+  area = 0.5f * area;
+  bool flipped = !(area > 0.f);
+  std::vector<size_t> idx(n);
+  for (size_t i = 0; i < n; ++i) idx[i] = flipped ? (n - 1) - i : i;
+  // clip ears walking around the polygon; give up after two fruitless laps
+  size_t nv = n;
+  size_t tries = 2 * nv;
+  for (size_t cur = nv - 1; nv > 2;) {
+    if (tries-- == 0) break;
+    size_t a = cur < nv ? cur : 0;
+    cur = a + 1 < nv ? a + 1 : 0;
+    size_t c = cur + 1 < nv ? cur + 1 : 0;
+    if (is_ear(q, a, cur, c, nv, idx)) {
+      int32_t ia = (int32_t)idx[a], ib = (int32_t)idx[cur], ic = (int32_t)idx[c];
+      if (flipped) std::swap(ia, ic);
+      tris.push_back(ia);
+      tris.push_back(ib);
+      tris.push_back(ic);
+      idx.erase(idx.begin() + (std::ptrdiff_t)cur);
+      --nv;
+      tries = 2 * nv;
+    }
+  }
+  return (int)((tris.size() - before) / 3);
+}
+
+std::string trim(std::string const & s) {
+  size_t b = s.find_first_not_of(" \t\r\n\f\v");
+  if (b == std::string::npos) return std::string();
+  size_t e = s.find_last_not_of(" \t\r\n\f\v");
+  return s.substr(b, e - b + 1);
+}
+
+[[noreturn]] void fail(std::string const & path, std::string const & why) {
+  throw Error(THEA_ERR_INVALID_ARGUMENT, "mesh_read: " + path + ": " + why);
+}
+
+// The whole file with a read cursor: lines for the text formats, big-endian words for binary OFF
+struct Input {
+  std::string data;
+  size_t pos = 0;
+  std::string path;
+
+  bool has_more() const { return pos < data.size(); }
+  std::string line() {
+    size_t e = data.find('\n', pos);
+    std::string s = data.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+    pos = e == std::string::npos ? data.size() : e + 1;
+    return s;
+  }
+  uint32_t be32() {
+    if (data.size() - pos < 4) fail(path, "unexpected end of input");
+    uint32_t w = 0;
+    for (int i = 0; i < 4; ++i) w = (w << 8) | (uint32_t)(unsigned char)data[pos + (size_t)i];
+    pos += 4;
+    return w;
+  }
+  int32_t int32() { return (int32_t)be32(); }
+  float float32() {
+    uint32_t w = be32();
+    float f;
+    std::memcpy(&f, &w, 4);
+    return f;
+  }
+  void skip(int64_t bytes) {
+    if (bytes < 0 || (uint64_t)bytes > data.size() - pos) fail(path, "unexpected end of input");
+    pos += (size_t)bytes;
+  }
+};
+
+// The next line that is neither blank nor a comment (the OFF reader's loop)
+std::string off_data_line(Input & in) {
+  std::string line = trim(in.line());
+  while (line.empty() || line[0] == '#') {
+    if (!in.has_more()) fail(in.path, "unexpected end of input");
+    line = trim(in.line());
+  }
+  return line;
+}
+
+// Builds the display mesh of one submesh: vertices appended, faces added in order with running source indices
+struct SubmeshBuilder {
+  MeshData & m;
+  int64_t first_vertex, first_triangle, faces_before;
+
+  explicit SubmeshBuilder(MeshData & m_)
+      : m(m_), first_vertex((int64_t)m_.vertices.size() / 3), first_triangle((int64_t)m_.triangle_face.size()),
+        faces_before(m_.num_faces) {}
+
+  void add_vertex(float x, float y, float z, int32_t source) {
+    m.vertices.push_back(x);
+    m.vertices.push_back(y);
+    m.vertices.push_back(z);
+    m.vertex_source.push_back(source);
+  }
+
+  // DisplayMesh::addFace with local vertex indices
+  void add_face(std::vector<int32_t> const & face, int32_t src_face) {
+    int n = (int)face.size();
+    if (n < 3) return;
+    std::vector<float> pos((size_t)3 * n);
+    for (int i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c) pos[(size_t)3 * i + c] = m.vertices[(size_t)(3 * (first_vertex + face[(size_t)i]) + c)];
+    std::vector<int32_t> local;
+    int nt = triangulate_face(pos.data(), n, local);
+    if (nt <= 0) return;
+    for (int t = 0; t < nt; ++t) {
+      for (int k = 0; k < 3; ++k) m.triangles.push_back((int32_t)first_vertex + face[(size_t)local[(size_t)3 * t + k]]);
+      m.triangle_face.push_back(src_face);
+    }
+    ++m.num_faces;
+  }
+
+  // Ends the submesh; the mesh group keeps it only if it has faces (skip_empty_meshes)
+  void end() {
+    if (m.num_faces == faces_before) {
+      m.vertices.resize((size_t)(3 * first_vertex));
+      m.vertex_source.resize((size_t)first_vertex);
+      m.triangles.resize((size_t)(3 * first_triangle));
+      m.triangle_face.resize((size_t)first_triangle);
+      return;
+    }
+    m.submesh_vertex_offsets.push_back((int64_t)m.vertex_source.size());
+    m.submesh_triangle_offsets.push_back((int64_t)m.triangle_face.size());
+  }
+};
+
+MeshData read_off_ascii(Input & in) {
+  MeshData m;
+  std::istringstream counts(off_data_line(in));
+  long long nv = 0, nf = 0, ne = 0;
+  if (!(counts >> nv >> nf >> ne)) fail(in.path, "could not read the mesh statistics");
+  if (nv <= 0) return m;
+  SubmeshBuilder b(m);
+  for (long long v = 0; v < nv; ++v) {
+    std::istringstream vs(off_data_line(in));
+    double x, y, z;
+    if (!(vs >> x >> y >> z)) fail(in.path, "could not read a vertex");
+    b.add_vertex((float)x, (float)y, (float)z, (int32_t)v);
+  }
+  std::vector<int32_t> face;
+  for (long long f = 0; f < nf; ++f) {
+    std::istringstream fs(off_data_line(in));
+    long long k = 0;
+    if (!(fs >> k)) fail(in.path, "could not read the number of vertices of a face");
+    if (k <= 0) continue;
+    face.clear();
+    bool skip = false;
+    for (long long v = 0; v < k && !skip; ++v) {
+      long long index;
+      if (!(fs >> index) || index < 0 || index >= nv) {
+        skip = true;  // unreadable or out of range: the face is skipped
+        break;
+      }
+      skip = std::find(face.begin(), face.end(), (int32_t)index) != face.end();  // repeated vertex
+      face.push_back((int32_t)index);
+    }
+    if (!skip) b.add_face(face, (int32_t)f);
+  }
+  m.submesh_vertex_offsets.push_back((int64_t)m.vertex_source.size());  // the OFF mesh is kept even without faces
+  m.submesh_triangle_offsets.push_back((int64_t)m.triangle_face.size());
+  return m;
+}
+
+MeshData read_off_binary(Input & in) {
+  MeshData m;
+  int64_t nv = in.int32(), nf = in.int32();
+  in.int32();  // number of edges
+  if (nv <= 0) return m;
+  SubmeshBuilder b(m);
+  for (int64_t v = 0; v < nv; ++v) {
+    float x = in.float32(), y = in.float32(), z = in.float32();
+    b.add_vertex(x, y, z, (int32_t)v);
+  }
+  std::vector<int32_t> face;
+  for (int64_t f = 0; f < nf; ++f) {
+    int32_t k = in.int32();
+    if (k <= 0) continue;
+    face.clear();
+    bool skip = false;
+    for (int32_t v = 0; v < k; ++v) {
+      if (skip) {
+        in.skip(4);  // the rest of a face with a repeated vertex
+        continue;
+      }
+      int32_t index = in.int32();
+      if (index < 0 || index >= nv) {
+        // The reference stops reading this face's indices here and takes the next word as the colour count; the same
+        // words are consumed here so that files read identically.
+        skip = true;
+        break;
+      }
+      skip = std::find(face.begin(), face.end(), index) != face.end();
+      face.push_back(index);
+    }
+    int32_t colours = in.int32();
+    if (colours > 0) in.skip(4 * (int64_t)colours);
+    if (!skip) b.add_face(face, (int32_t)f);
+  }
+  m.submesh_vertex_offsets.push_back((int64_t)m.vertex_source.size());
+  m.submesh_triangle_offsets.push_back((int64_t)m.triangle_face.size());
+  return m;
+}
+
+MeshData read_off(Input & in) {
+  std::string header = trim(in.line());
+  if (header != "OFF" && header.rfind("OFF ", 0) != 0) fail(in.path, "invalid OFF stream (does not start with 'OFF')");
+  bool binary = header == "OFF BINARY" || header.rfind("OFF BINARY ", 0) == 0;
+  return binary ? read_off_binary(in) : read_off_ascii(in);
+}
+
+using VTN = std::array<long long, 3>;  // 1-based vertex, texcoord, normal (0: none), compared lexicographically
+
+// Adds one OBJ submesh: its vertices are the distinct VTN references of its faces in sorted order
+void construct_obj_submesh(MeshData & m, std::vector<float> const & positions, std::vector<VTN> const & refs,
+                           std::vector<size_t> const & face_starts, int64_t & num_faces) {
+  std::map<VTN, int32_t> local;
+  for (VTN const & r : refs) local.emplace(r, 0);
+  SubmeshBuilder b(m);
+  int32_t next = 0;
+  for (auto & kv : local) {
+    size_t p = (size_t)(kv.first[0] - 1);
+    b.add_vertex(positions[3 * p], positions[3 * p + 1], positions[3 * p + 2], (int32_t)p);
+    kv.second = next++;
+  }
+  std::vector<int32_t> face;
+  for (size_t i = 0; i < face_starts.size(); ++i) {
+    size_t e = i + 1 < face_starts.size() ? face_starts[i + 1] : refs.size();
+    face.clear();
+    for (size_t j = face_starts[i]; j < e; ++j) face.push_back(local[refs[j]]);
+    b.add_face(face, (int32_t)num_faces);
+    ++num_faces;  // every face is numbered, including those the triangulation drops
+  }
+  b.end();
+}
+
+MeshData read_obj(Input & in) {
+  MeshData m;
+  std::vector<float> positions;
+  long long num_tex = 0, num_nrm = 0;
+  std::vector<VTN> refs;          // references of the current submesh's faces, concatenated
+  std::vector<size_t> face_starts;
+  int64_t num_faces = 0;
+  while (in.has_more()) {
+    std::string line = trim(in.line());
+    if (line.empty()) continue;
+    char c0 = line[0];
+    if (c0 == 'v' && line.size() >= 2) {
+      if (line[1] == 't') {
+        std::istringstream vs(line.substr(2));
+        double x, y;
+        if (!(vs >> x >> y)) fail(in.path, "could not read a texture coordinate on line '" + line + "'");
+        ++num_tex;
+      } else if (line[1] == 'n') {
+        std::istringstream vs(line.substr(2));
+        double x, y, z;
+        if (!(vs >> x >> y >> z)) fail(in.path, "could not read a normal on line '" + line + "'");
+        ++num_nrm;
+      } else if (line[1] == ' ' || line[1] == '\t') {
+        std::istringstream vs(line.substr(1));
+        double x, y, z;
+        if (!(vs >> x >> y >> z)) fail(in.path, "could not read a vertex position on line '" + line + "'");
+        positions.push_back((float)x);
+        positions.push_back((float)y);
+        positions.push_back((float)z);
+      }
+    } else if ((c0 == 'f' || c0 == 'p') && line.size() >= 2 && (line[1] == ' ' || line[1] == '\t')) {
+      size_t start = refs.size();
+      long long nvtx = (long long)(positions.size() / 3);
+      size_t b = line.find_first_not_of("fp \t");
+      if (b == std::string::npos) fail(in.path, "malformed face '" + line + "'");
+      bool bad_face = false;
+      for (size_t e = 0; e != std::string::npos;) {
+        e = line.find_first_of(" \t", b);
+        std::istringstream fs(line.substr(b, e == std::string::npos ? std::string::npos : e - b));
+        VTN r{0, 0, 0};
+        bool bad = !(fs >> r[0]);
+        if (!bad && fs.get() == '/') {
+          if (fs.peek() == '/') {
+            fs.get();
+            bad = !(fs >> r[2]);
+          } else {
+            bad = !(fs >> r[1]);
+            if (!bad && fs.get() == '/') bad = !(fs >> r[2]);
+          }
+        }
+        if (bad || std::llabs(r[0]) < 1 || std::llabs(r[0]) > nvtx) {
+          bad_face = true;
+          break;
+        }
+        if (std::llabs(r[1]) > num_tex) r[1] = 0;
+        if (std::llabs(r[2]) > num_nrm) r[2] = 0;
+        if (r[0] < 0) r[0] = nvtx + 1 + r[0];
+        if (r[1] < 0) r[1] = num_tex + 1 + r[1];
+        if (r[2] < 0) r[2] = num_nrm + 1 + r[2];
+        refs.push_back(r);
+        if (e != std::string::npos) b = line.find_first_not_of(" \t", e);
+      }
+      if (bad_face)
+        refs.resize(start);  // the non-strict reader drops the face
+      else
+        face_starts.push_back(start);
+    } else if ((c0 == 'g' || c0 == 'o') && (line.size() < 2 || line[1] == ' ' || line[1] == '\t')) {
+      if (!face_starts.empty()) construct_obj_submesh(m, positions, refs, face_starts, num_faces);
+      refs.clear();
+      face_starts.clear();
+    }
+  }
+  if (!face_starts.empty()) construct_obj_submesh(m, positions, refs, face_starts, num_faces);
+  return m;
+}
+
+}  // namespace
+
+int triangulate_face(float const * pos, int n, std::vector<int32_t> & tris) {
+  if (n < 3) return 0;
+  auto P = [&](int i) { return V3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}; };
+  if (n == 3) {
+    tris.insert(tris.end(), {0, 1, 2});
+    return 1;
+  }
+  if (n == 4) {
+    int t[6];
+    int nt = triangulate_quad(P(0), P(1), P(2), P(3), t);
+    tris.insert(tris.end(), t, t + 3 * nt);
+    return nt;
+  }
+  std::vector<V3> p((size_t)n);
+  for (int i = 0; i < n; ++i) p[(size_t)i] = P(i);
+  return triangulate_polygon(p, tris);
+}
+
+MeshData read_mesh_file(std::string const & path) {
+  std::string lower = path;
+  for (char & ch : lower) ch = (char)std::tolower((unsigned char)ch);
+  auto ends_with = [&](char const * ext) {
+    size_t n = std::strlen(ext);
+    return lower.size() >= n && lower.compare(lower.size() - n, n, ext) == 0;
+  };
+  bool obj = ends_with(".obj"), off = ends_with(".off");
+  if (!obj && !off) {
+    if (ends_with(".ply") || ends_with(".3ds")) fail(path, "only the OFF and OBJ codecs are built");
+    fail(path, "could not detect the codec from the file extension");
+  }
+  std::ifstream f(path, std::ios::binary);
+  if (!f) fail(path, "cannot open the file");
+  Input in;
+  in.path = path;
+  in.data.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  return obj ? read_obj(in) : read_off(in);
+}
+
+}  // namespace thea
