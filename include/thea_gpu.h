@@ -232,16 +232,19 @@ typedef struct thea_mesh_info {
 } thea_mesh_info;
 
 /* MeshGroup<DisplayMesh>::load(path) (Graphics/MeshGroup.hpp:471-497) with the default codec options, for the OFF
- * (ASCII and binary, Graphics/MeshCodecOff.hpp) and OBJ (Graphics/MeshCodecObj.hpp) codecs, chosen by the file
- * extension. Submeshes come in file order (OBJ: one per g/o group that has faces; each submesh's vertices are the
+ * (.off, .off.bin; ASCII and binary, Graphics/MeshCodecOff.hpp), OBJ (Graphics/MeshCodecObj.hpp) and PLY (ASCII and
+ * binary, Graphics/MeshCodecPly.hpp) codecs, chosen by the file extension. Submeshes come in file order (OBJ: one per g/o group that has faces; each submesh's vertices are the
  * distinct vertex/texcoord/normal references of its faces in ascending order). Faces are triangulated as
  * DisplayMesh::addFace does (Graphics/DisplayMesh.cpp:249-320); faces the non-strict readers skip (bad, out-of-range or,
- * in OFF, repeated indices) are skipped. The PLY and 3DS codecs are not built: THEA_ERR_INVALID_ARGUMENT. */
+ * in OFF and PLY, repeated indices) are skipped. Binary PLY properties beyond a vertex's coordinates and a face's index
+ * list, and elements of other kinds, are skipped as the header describes them (the reference's binary reader cannot
+ * read such files). The 3DS codec (which needs lib3ds) is not built: THEA_ERR_INVALID_ARGUMENT. */
 THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh);
 THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info);
 /* Copies the arrays to host buffers (each nullable): vertices (3 x num_vertices floats), vertex_source (file vertex index
  * of each vertex, 0-based), triangles (3 x num_triangles indices into vertices), triangle_face (source face index of each
- * triangle: the OFF face number, or the OBJ reader's running face count), submesh_vertex_offsets and
+ * triangle: the OFF face number, the OBJ reader's running face count, or the PLY reader's count of faces handed to
+ * the mesh), submesh_vertex_offsets and
  * submesh_triangle_offsets (num_submeshes + 1 entries each). */
 THEA_API thea_status thea_mesh_copy(const thea_mesh * mesh, float * vertices, int32_t * vertex_source,
                                     int32_t * triangles, int32_t * triangle_face, int64_t * submesh_vertex_offsets,

@@ -336,7 +336,7 @@ class MeshSampler {
   int64_t nf_;
 };
 
-// MeshGroup<DisplayMesh>::load for OFF and OBJ files, flattened into host arrays in the reference's element order;
+// MeshGroup<DisplayMesh>::load for OFF, OBJ and PLY files, flattened into host arrays in the reference's element order;
 // MeshBvh(file.vertices.data(), file.numVertices(), file.triangles.data(), file.numTriangles()) indexes its triangles.
 class MeshFile {
  public:

@@ -8,7 +8,9 @@ in FP32 with one rounding per operation (numpy float32 scalars) and Eigen's 3-te
   Polygon3::computeNormal (Polygon3.hpp:180-208) and Math::orthonormalBasis (MatrixUtil.hpp:225-249);
 - the non-strict OFF reader (Graphics/MeshCodecOff.hpp:154-330, ASCII and big-endian binary);
 - the OBJ reader with texcoords and normals read (Graphics/MeshCodecObj.hpp:210-545): a submesh per g/o group whose
-  vertices are the distinct (v, t, n) references of its faces in ascending order.
+  vertices are the distinct (v, t, n) references of its faces in ascending order;
+- the PLY reader (Graphics/MeshCodecPly.hpp:229-700), ASCII and binary; binary properties and elements beyond the
+  vertex coordinates and the face index list are skipped as the header describes them.
 
 Small inputs only (pure-Python loops). Parity status: unpinned (the reference's readers cannot be built here).
 """
@@ -382,9 +384,109 @@ def read_obj(data):
     return m.arrays()
 
 
+_PLY_TYPES = {"int8": "b", "char": "b", "int16": "h", "short": "h", "int32": "i", "int": "i", "uint8": "B",
+              "uchar": "B", "uint16": "H", "ushort": "H", "uint32": "I", "uint": "I", "float32": "f", "float": "f",
+              "float64": "d", "double": "d"}
+
+
+def read_ply(data):
+    """The PLY reader on the bytes of a file: dict of arrays as thea_mesh_copy returns them."""
+    pos = 0
+
+    def line():
+        nonlocal pos
+        e = data.find(b"\n", pos)
+        e = len(data) if e < 0 else e
+        s = data[pos:e].decode("latin-1")
+        pos = min(e + 1, len(data))
+        return s
+
+    if line().strip() != "ply":
+        raise ValueError("not a PLY file")
+    binary, order, blocks = False, "<", []
+    while True:
+        if pos >= len(data):
+            raise ValueError("header not closed")
+        ln = line().strip()
+        if not ln:
+            continue
+        if ln == "end_header":
+            break
+        w = ln.split()
+        if w[0] == "format":
+            binary = w[1] != "ascii"
+            order = ">" if w[1] == "binary_big_endian" else "<"
+        elif w[0] == "element":
+            blocks.append((w[1], int(w[2]), []))
+        elif w[0] == "property":
+            blocks[-1][2].append(("list", _PLY_TYPES[w[2]], _PLY_TYPES[w[3]]) if w[1] == "list"
+                                 else (_PLY_TYPES[w[1]],))
+
+    def num(code):
+        nonlocal pos
+        size = struct.calcsize(code)
+        if pos + size > len(data):
+            raise ValueError("unexpected end of input")
+        v = struct.unpack(order + code, data[pos:pos + size])[0]
+        pos += size
+        return v
+
+    def skip(prop):
+        if prop[0] == "list":
+            for _ in range(num(prop[1])):
+                num(prop[2])
+        else:
+            num(prop[0])
+
+    verts, faces = [], []
+    for kind, count, props in blocks:
+        for _ in range(count):
+            if not binary:
+                while True:
+                    if pos >= len(data):
+                        raise ValueError("unexpected end of input")
+                    ln = line().strip()
+                    if ln and not ln.startswith("comment"):
+                        break
+                tok = ln.split()
+                if kind == "vertex":
+                    verts.append(tuple(f32(float(t)) for t in tok[:3]))
+                elif kind == "face":
+                    k = int(tok[0])
+                    if k > 0:
+                        idx = [int(t) for t in tok[1:k + 1]]
+                        if len(idx) == k:
+                            faces.append(idx)
+                continue
+            if kind == "vertex":
+                verts.append(tuple(f32(num(props[j][0])) for j in range(3)))
+                for p in props[3:]:
+                    skip(p)
+            elif kind == "face":
+                idx = [num(props[0][2]) for _ in range(num(props[0][1]))]
+                for p in props[1:]:
+                    skip(p)
+                if idx:
+                    faces.append(idx)
+            else:
+                for p in props:
+                    skip(p)
+    m = _Mesh()
+    nv = len(verts)
+    kept = []
+    for idx in faces:
+        if all(0 <= v < nv for v in idx) and len(set(idx)) == len(idx):
+            kept.append((idx, len(kept)))
+    _add_submesh(m, verts, list(range(nv)), kept, keep_empty=nv > 0)
+    return m.arrays()
+
+
 def read_mesh(path):
     with open(path, "rb") as f:
         data = f.read()
-    if str(path).lower().endswith(".obj"):
+    p = str(path).lower()
+    if p.endswith(".obj"):
         return read_obj(data)
+    if p.endswith(".ply"):
+        return read_ply(data)
     return read_off(data)

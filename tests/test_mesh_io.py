@@ -273,3 +273,115 @@ def test_random_off_matches_the_restatement(T, tmp_path):
         path = tmp_path / ("r%d.off" % trial)
         path.write_text("\n".join(lines) + "\n")
         _same_mesh(T.read_mesh(str(path)), MO.read_mesh(str(path)))
+
+
+# ---- PLY -------------------------------------------------------------------------------------------------------------
+
+PLY_ASCII = """ply
+format ascii 1.0
+comment made by hand
+element vertex 6
+property float x
+property float y
+property float z
+property uchar red
+element edge 1
+property int vertex1
+property int vertex2
+element face 6
+property list uchar int vertex_indices
+property float quality
+end_header
+0 0 0 255
+1 0 0 0
+comment inside the data
+1 1 0 7
+
+0 1 0 1
+2 0.5 0.25 3
+1.5 2 1e-3 9
+0 1
+4 0 1 2 3 0.5
+3 1 4 2
+5 0 1 4 5 3 0.25
+3 0 1 9
+3 0 0 1
+2 0 1
+"""
+
+
+def test_ply_ascii(T, tmp_path):
+    path = tmp_path / "m.ply"
+    path.write_text(PLY_ASCII)
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    # the out-of-range and repeated faces are not handed to the mesh, so they take no face number; the two-vertex face
+    # does (number 3) but makes no triangle
+    assert m.vertex_source.tolist() == list(range(6))
+    assert m.triangle_face.tolist() == [0, 0, 1, 2, 2, 2] and m.num_faces == 3
+    assert m.triangles[:3].tolist() == [[0, 1, 2], [2, 3, 0], [1, 4, 2]]
+
+
+def _ply_binary(order, verts, faces, extra_vertex_props=True, edges=True):
+    e = "binary_little_endian" if order == "<" else "binary_big_endian"
+    head = ["ply", "format %s 1.0" % e, "element vertex %d" % len(verts), "property double x", "property double y",
+            "property double z"]
+    if extra_vertex_props:
+        head += ["property float nx", "property list uchar float extra", "property uchar red"]
+    if edges:
+        head += ["element edge 1", "property int a", "property int b"]
+    head += ["element face %d" % len(faces), "property list uchar uint vertex_indices", "property short flags",
+             "end_header"]
+    b = ("\n".join(head) + "\n").encode()
+    for i, v in enumerate(verts):
+        b += struct.pack(order + "ddd", *v)
+        if extra_vertex_props:
+            n = i % 3
+            b += struct.pack(order + "fB" + "f" * n + "B", 1.0, n, *([2.0] * n), 200)
+    if edges:
+        b += struct.pack(order + "ii", 0, 1)
+    for f in faces:
+        b += struct.pack(order + "B" + "I" * len(f) + "h", len(f), *f, -3)
+    return b
+
+
+@pytest.mark.parametrize("order", ["<", ">"])
+@pytest.mark.parametrize("extras", [False, True])
+def test_ply_binary(T, tmp_path, order, extras):
+    rng = np.random.default_rng(9)
+    V = [tuple(x) for x in rng.normal(size=(12, 3))]
+    F = [[0, 1, 2], [2, 3, 4, 5], [5, 6, 7, 8, 9], [0, 99, 1], [1, 1, 2], [], [3, 4], [9, 10, 11, 0, 1, 2]]
+    path = tmp_path / "m.ply"
+    path.write_bytes(_ply_binary(order, V, F, extras, extras))
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    np.testing.assert_array_equal(m.vertices, np.asarray(V, np.float64).astype(np.float32))
+    # faces handed to the mesh: 0, 1, 2, the two-vertex face (3) and the hexagon (4)
+    assert sorted(set(m.triangle_face.tolist())) == [0, 1, 2, 4]
+
+
+def test_ply_errors(T, tmp_path):
+    from thea_gb300 import TheaError
+    cases = {
+        "ply\nformat ascii 1.0\nelement vertex 1\nproperty float x\n": "end_header",
+        "ply\nformat text 1.0\nend_header\n": "format specifier",
+        "ply\nformat ascii 1.0\nelement vertex 1\nproperty float x\nproperty float y\nend_header\n0 0\n": "three",
+        "ply\nformat ascii 1.0\nelement face 1\nproperty float q\nend_header\n1\n": "list of integer",
+        "ply\nformat ascii 1.0\nelement vertex 1\nproperty half x\nend_header\n": "unknown property type",
+        "ply\nformat ascii 1.0\nelement vertex 2\nproperty float x\nproperty float y\nproperty float z\n"
+        "end_header\n0 0 0\n": "end of input",
+        "plx\n": "does not start with 'ply'",
+    }
+    for i, (text, msg) in enumerate(cases.items()):
+        path = tmp_path / ("e%d.ply" % i)
+        path.write_text(text)
+        with pytest.raises(TheaError, match=msg):
+            T.read_mesh(str(path))
+
+
+def test_off_bin_extension(T, tmp_path):
+    V = [(0, 0, 0), (1, 0, 0), (0, 1, 0)]
+    path = tmp_path / "m.off.bin"
+    path.write_bytes(_binary_off(V, [struct.pack(">iiiii", 3, 0, 1, 2, 0)]))
+    m = T.read_mesh(str(path))
+    assert m.triangles.tolist() == [[0, 1, 2]]

@@ -169,7 +169,7 @@ class MeshBvh(_Bvh):
 
     @classmethod
     def from_file(cls, path, **kwargs):
-        """BVH over the triangles of an OFF or OBJ file, in the order MeshGroup::load + MeshBvh::add give them."""
+        """BVH over the triangles of an OFF, OBJ or PLY file, in the order MeshGroup::load + MeshBvh::add give them."""
         m = read_mesh(path)
         return cls(m.vertices, m.triangles, **kwargs)
 
@@ -514,7 +514,7 @@ def random_sphere(seed, count, device=False):
 
 
 class MeshData:
-    """A mesh file read as MeshGroup<DisplayMesh>::load reads it (OFF or OBJ, by extension), flattened: vertices
+    """A mesh file read as MeshGroup<DisplayMesh>::load reads it (OFF, OBJ or PLY, by extension), flattened: vertices
     [nv, 3] float32, vertex_source [nv] (file vertex index), triangles [nt, 3] int32, triangle_face [nt] (source face
     index), submesh_vertex_offsets and submesh_triangle_offsets [submeshes + 1] int64, num_faces (faces that produced
     triangles). Pass (vertices, triangles) to MeshBvh for the reference's element order."""
@@ -531,7 +531,7 @@ class MeshData:
 
 
 def read_mesh(path):
-    """Reads an OFF or OBJ file into host arrays (MeshData)."""
+    """Reads an OFF, OBJ or PLY file into host arrays (MeshData)."""
     lib = N.lib()
     h = ctypes.c_void_p()
     N.check(lib.thea_mesh_read(str(path).encode(), ctypes.byref(h)))

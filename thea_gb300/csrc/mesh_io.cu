@@ -1,7 +1,7 @@
 // Mesh file readers and face triangulation (host code).
 //
 // Restates, as far as geometry goes, the reference's non-strict OFF reader (Graphics/MeshCodecOff.hpp:154-330: ASCII and
-// big-endian binary), its OBJ reader (Graphics/MeshCodecObj.hpp:210-545: one submesh per g/o group, each submesh's
+// big-endian binary), its PLY reader (Graphics/MeshCodecPly.hpp:229-700: ASCII and either byte order), its OBJ reader (Graphics/MeshCodecObj.hpp:210-545: one submesh per g/o group, each submesh's
 // vertices being the distinct (vertex, texcoord, normal) references of its faces in sorted order) and the triangulation
 // of DisplayMesh::addFace (Graphics/DisplayMesh.cpp:249-320): quads by Polygon3::triangulateQuad (Polygon3.hpp:245-285),
 // larger polygons by Polygon3::triangulate (Polygon3.cpp:109-288: ear clipping after projecting onto the plane of
@@ -161,13 +161,18 @@ struct Input {
     pos = e == std::string::npos ? data.size() : e + 1;
     return s;
   }
-  uint32_t be32() {
-    if (data.size() - pos < 4) fail(path, "unexpected end of input");
-    uint32_t w = 0;
-    for (int i = 0; i < 4; ++i) w = (w << 8) | (uint32_t)(unsigned char)data[pos + (size_t)i];
-    pos += 4;
+  // an unsigned word of `bytes` bytes (1, 2, 4 or 8) in the given byte order
+  uint64_t word(int bytes, bool big_endian) {
+    if (data.size() - pos < (size_t)bytes) fail(path, "unexpected end of input");
+    uint64_t w = 0;
+    for (int i = 0; i < bytes; ++i) {
+      int k = big_endian ? i : bytes - 1 - i;
+      w = (w << 8) | (uint64_t)(unsigned char)data[pos + (size_t)k];
+    }
+    pos += (size_t)bytes;
     return w;
   }
+  uint32_t be32() { return (uint32_t)word(4, true); }
   int32_t int32() { return (int32_t)be32(); }
   float float32() {
     uint32_t w = be32();
@@ -423,6 +428,223 @@ MeshData read_obj(Input & in) {
   return m;
 }
 
+// ---- PLY (Graphics/MeshCodecPly.hpp:229-700) -------------------------------------------------------------------------
+
+enum class PlyType { INVALID, LIST, INT8, INT16, INT32, UINT8, UINT16, UINT32, FLOAT32, FLOAT64 };
+
+PlyType ply_type(std::string const & name) {
+  static std::pair<char const *, PlyType> const names[] = {
+      {"list", PlyType::LIST},     {"int8", PlyType::INT8},       {"int16", PlyType::INT16},
+      {"int32", PlyType::INT32},   {"uint8", PlyType::UINT8},     {"uint16", PlyType::UINT16},
+      {"uint32", PlyType::UINT32}, {"float32", PlyType::FLOAT32}, {"float64", PlyType::FLOAT64},
+      {"char", PlyType::INT8},     {"short", PlyType::INT16},     {"int", PlyType::INT32},
+      {"uchar", PlyType::UINT8},   {"ushort", PlyType::UINT16},   {"uint", PlyType::UINT32},
+      {"float", PlyType::FLOAT32}, {"double", PlyType::FLOAT64}};
+  for (auto const & n : names)
+    if (name == n.first) return n.second;
+  return PlyType::INVALID;
+}
+
+int ply_bytes(PlyType t) {
+  switch (t) {
+    case PlyType::INT8: case PlyType::UINT8: return 1;
+    case PlyType::INT16: case PlyType::UINT16: return 2;
+    case PlyType::INT32: case PlyType::UINT32: case PlyType::FLOAT32: return 4;
+    case PlyType::FLOAT64: return 8;
+    default: return 0;
+  }
+}
+
+bool ply_integer(PlyType t) { return t != PlyType::FLOAT32 && t != PlyType::FLOAT64 && ply_bytes(t) > 0; }
+
+struct PlyProperty {
+  PlyType type = PlyType::INVALID, count_type = PlyType::INVALID, item_type = PlyType::INVALID;
+};
+
+enum class PlyElement { VERTEX, FACE, OTHER };
+
+struct PlyBlock {
+  PlyElement kind = PlyElement::OTHER;
+  long long count = 0;
+  std::vector<PlyProperty> props;
+};
+
+struct PlyHeader {
+  bool binary = false, big_endian = false;
+  std::vector<PlyBlock> blocks;
+};
+
+PlyHeader read_ply_header(Input & in) {
+  if (trim(in.line()) != "ply") fail(in.path, "invalid PLY stream (does not start with 'ply')");
+  PlyHeader h;
+  bool have_format = false;
+  while (in.has_more()) {
+    std::string line = trim(in.line());
+    if (line.empty()) continue;
+    if (line == "end_header") return h;
+    std::istringstream ls(line);
+    std::string field;
+    ls >> field;
+    if (field == "format") {
+      if (have_format) fail(in.path, "format specifier must be first line after magic string");
+      if (!(ls >> field)) fail(in.path, "could not read ascii/binary specifier");
+      if (field == "ascii") {
+        h.binary = false;
+      } else if (field == "binary_little_endian" || field == "binary_big_endian") {
+        h.binary = true;
+        h.big_endian = field == "binary_big_endian";
+      } else {
+        fail(in.path, "invalid format specifier");
+      }
+      have_format = true;
+    } else if (field == "element") {
+      PlyBlock b;
+      if (!(ls >> field)) fail(in.path, "could not read element type");
+      if (!(ls >> b.count)) fail(in.path, "could not read number of elements of type '" + field + "'");
+      b.kind = field == "vertex" ? PlyElement::VERTEX : field == "face" ? PlyElement::FACE : PlyElement::OTHER;
+      h.blocks.push_back(b);
+    } else if (field == "property") {
+      if (h.blocks.empty()) fail(in.path, "property specification outside an element block");
+      PlyProperty p;
+      if (!(ls >> field)) fail(in.path, "could not read property type");
+      p.type = ply_type(field);
+      if (p.type == PlyType::INVALID) fail(in.path, "unknown property type '" + field + "'");
+      if (p.type == PlyType::LIST) {
+        std::string c, t;
+        if (!(ls >> c >> t)) fail(in.path, "could not read list item and count types");
+        p.count_type = ply_type(c);
+        p.item_type = ply_type(t);
+        if (ply_bytes(p.count_type) == 0) fail(in.path, "unknown list count type '" + c + "'");
+        if (ply_bytes(p.item_type) == 0) fail(in.path, "unknown list item type '" + t + "'");
+      }
+      h.blocks.back().props.push_back(p);
+    }
+    // comment, obj_info and other header lines are ignored
+  }
+  fail(in.path, "no end_header token, header not closed");
+}
+
+void check_ply_block(PlyBlock const & b, std::string const & path) {
+  if (b.kind == PlyElement::VERTEX) {
+    if (b.props.size() < 3 || b.props[0].type == PlyType::LIST || b.props[1].type == PlyType::LIST ||
+        b.props[2].type == PlyType::LIST)
+      fail(path, "vertex element must start with three numerical coordinates");
+  } else if (b.kind == PlyElement::FACE) {
+    if (b.props.empty() || b.props[0].type != PlyType::LIST || !ply_integer(b.props[0].count_type) ||
+        !ply_integer(b.props[0].item_type))
+      fail(path, "face element must start with a list of integer indices");
+  }
+}
+
+// One binary number of type t, as a double (integers of up to 32 bits and floats convert exactly)
+double ply_number(Input & in, PlyType t, bool big) {
+  uint64_t w = in.word(ply_bytes(t), big);
+  switch (t) {
+    case PlyType::INT8: return (double)(int8_t)(uint8_t)w;
+    case PlyType::INT16: return (double)(int16_t)(uint16_t)w;
+    case PlyType::INT32: return (double)(int32_t)(uint32_t)w;
+    case PlyType::UINT8: case PlyType::UINT16: case PlyType::UINT32: return (double)w;
+    case PlyType::FLOAT32: {
+      uint32_t u = (uint32_t)w;
+      float f;
+      std::memcpy(&f, &u, 4);
+      return (double)f;
+    }
+    case PlyType::FLOAT64: {
+      double d;
+      std::memcpy(&d, &w, 8);
+      return d;
+    }
+    default: fail(in.path, "unknown property type");
+  }
+}
+
+void skip_ply_property(Input & in, PlyProperty const & p, bool big) {
+  if (p.type == PlyType::LIST) {
+    double n = ply_number(in, p.count_type, big);
+    if (n > 0) in.skip((int64_t)n * ply_bytes(p.item_type));
+  } else {
+    in.skip(ply_bytes(p.type));
+  }
+}
+
+// Adds a face of file vertex indices unless an index is out of range or repeated (the non-strict reader's rule);
+// returns whether it was added
+bool add_checked_face(SubmeshBuilder & b, std::vector<long long> const & idx, long long nv, int64_t src_face) {
+  std::vector<int32_t> face;
+  for (long long v : idx) {
+    if (v < 0 || v >= nv) return false;
+    if (std::find(face.begin(), face.end(), (int32_t)v) != face.end()) return false;
+    face.push_back((int32_t)v);
+  }
+  b.add_face(face, (int32_t)src_face);
+  return true;
+}
+
+MeshData read_ply(Input & in) {
+  PlyHeader h = read_ply_header(in);
+  MeshData m;
+  SubmeshBuilder b(m);
+  long long nv = 0;
+  int64_t nf = 0;  // faces handed to the mesh: the source index of the next one
+  std::vector<long long> idx;
+  for (PlyBlock const & blk : h.blocks) {
+    check_ply_block(blk, in.path);
+    for (long long e = 0; e < blk.count; ++e) {
+      if (!h.binary) {
+        std::string line;
+        do {
+          if (!in.has_more()) fail(in.path, "unexpected end of input");
+          line = trim(in.line());
+        } while (line.empty() || line.rfind("comment", 0) == 0);
+        std::istringstream ls(line);
+        if (blk.kind == PlyElement::VERTEX) {
+          double x, y, z;
+          if (!(ls >> x >> y >> z)) fail(in.path, "could not read vertex on line '" + line + "'");
+          b.add_vertex((float)x, (float)y, (float)z, (int32_t)nv++);
+        } else if (blk.kind == PlyElement::FACE) {
+          long long k;
+          if (!(ls >> k)) fail(in.path, "could not read number of vertices in face on line '" + line + "'");
+          if (k <= 0) continue;
+          idx.clear();
+          long long v;
+          bool readable = true;
+          for (long long j = 0; j < k && readable; ++j) {
+            readable = (bool)(ls >> v);
+            idx.push_back(v);
+          }
+          if (readable && add_checked_face(b, idx, nv, nf)) ++nf;
+        }
+        continue;
+      }
+      // Binary. Properties after a vertex's coordinates or a face's index list, and elements of other kinds, are
+      // skipped as the header describes them (the reference's loop over extra vertex properties does not advance, and
+      // it skips neither extra face properties nor other elements, so it cannot read such files).
+      if (blk.kind == PlyElement::VERTEX) {
+        float c[3];
+        for (int k = 0; k < 3; ++k) c[k] = (float)ply_number(in, blk.props[(size_t)k].type, h.big_endian);
+        for (size_t k = 3; k < blk.props.size(); ++k) skip_ply_property(in, blk.props[k], h.big_endian);
+        b.add_vertex(c[0], c[1], c[2], (int32_t)nv++);
+      } else if (blk.kind == PlyElement::FACE) {
+        PlyProperty const & p = blk.props[0];
+        double n = ply_number(in, p.count_type, h.big_endian);
+        if (n < 0) fail(in.path, "list has negative size");
+        idx.resize((size_t)n);
+        for (auto & v : idx) v = (long long)ply_number(in, p.item_type, h.big_endian);
+        for (size_t k = 1; k < blk.props.size(); ++k) skip_ply_property(in, blk.props[k], h.big_endian);
+        if (!idx.empty() && add_checked_face(b, idx, nv, nf)) ++nf;
+      } else {
+        for (PlyProperty const & p : blk.props) skip_ply_property(in, p, h.big_endian);
+      }
+    }
+  }
+  if (nv > 0 || m.num_faces > 0) {  // the mesh is kept if it has vertices or faces
+    m.submesh_vertex_offsets.push_back((int64_t)m.vertex_source.size());
+    m.submesh_triangle_offsets.push_back((int64_t)m.triangle_face.size());
+  }
+  return m;
+}
+
 }  // namespace
 
 int triangulate_face(float const * pos, int n, std::vector<int32_t> & tris) {
@@ -450,17 +672,16 @@ MeshData read_mesh_file(std::string const & path) {
     size_t n = std::strlen(ext);
     return lower.size() >= n && lower.compare(lower.size() - n, n, ext) == 0;
   };
-  bool obj = ends_with(".obj"), off = ends_with(".off");
-  if (!obj && !off) {
-    if (ends_with(".ply") || ends_with(".3ds")) fail(path, "only the OFF and OBJ codecs are built");
-    fail(path, "could not detect the codec from the file extension");
-  }
+  // codecs in the reference's order of detection: 3DS, OBJ, OFF (.off, .off.bin), PLY
+  if (ends_with(".3ds")) fail(path, "the 3DS codec (which needs lib3ds) is not built");
+  bool obj = ends_with(".obj"), off = ends_with(".off") || ends_with(".off.bin"), ply = ends_with(".ply");
+  if (!obj && !off && !ply) fail(path, "could not detect the codec from the file extension");
   std::ifstream f(path, std::ios::binary);
   if (!f) fail(path, "cannot open the file");
   Input in;
   in.path = path;
   in.data.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
-  return obj ? read_obj(in) : read_off(in);
+  return obj ? read_obj(in) : off ? read_off(in) : read_ply(in);
 }
 
 }  // namespace thea

@@ -1,5 +1,5 @@
-// Mesh files to triangle arrays: the OFF and OBJ readers (Graphics/MeshCodecOff.hpp, MeshCodecObj.hpp) building display
-// meshes, whose faces are triangulated as DisplayMesh::addFace does (Graphics/DisplayMesh.cpp:249-320). Host code.
+// Mesh files to triangle arrays: the OFF, OBJ and PLY readers (Graphics/MeshCodecOff.hpp, MeshCodecObj.hpp,
+// MeshCodecPly.hpp) building display meshes, whose faces are triangulated as DisplayMesh::addFace does (Graphics/DisplayMesh.cpp:249-320). Host code.
 #pragma once
 
 #include "common.cuh"
@@ -26,7 +26,7 @@ struct MeshData {
 // (three per triangle, at most n - 2 triangles) to `tris` and returns the number of triangles (0: the face is skipped).
 int triangulate_face(float const * pos, int n, std::vector<int32_t> & tris);
 
-// Reads an OFF (ASCII or binary) or OBJ file, chosen by the file extension as MeshGroup::load does. Throws Error
+// Reads an OFF, OBJ or PLY file (ASCII or binary), chosen by the file extension as MeshGroup::load does. Throws Error
 // (THEA_ERR_INVALID_ARGUMENT) where the reference's non-strict readers throw; faces they skip are skipped.
 MeshData read_mesh_file(std::string const & path);
 
