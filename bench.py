@@ -12,8 +12,8 @@ are seeded synthetic data with the benchmark's shapes and distributions (no data
   cpu_baseline  the oracle's restatement of the reference's CPU traversal (reference kd-tree, reference tie order) on a
              bounded sample, all host threads (and one thread on a smaller sample).
   extra      the other workloads measured the same way, device-resident: the FP64 ray re-test and occlusion queries
-             on config 1, closest point (config 0), the k-NN graph (config 2), Visibility and the sample graph on the
-             config-0 mesh, the batched forest (config 3) and the serving loop (config 4).
+             on config 1, closest point (config 0), the k-NN graph (config 2), Visibility, the sample graph and
+             ShapeDiameter on the config-0 mesh, the batched forest (config 3) and the serving loop (config 4).
 
 --impl reference times the reference's algorithm on the host cores instead (the CPU restatement, since the reference
 itself needs Eigen, which is absent).
@@ -586,6 +586,18 @@ def extra_workloads(T, torch, stream, flush, args):
         "value": 262144 / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Msamples/s", "samples": 262144,
         "max_degree": 8, "ms_per_step": statistics.mean(ms), "mean_degree": float(g_deg.float().mean().item()),
         "separation_estimate": g_avg[0], "mean_separation": g_avg[1], "reachability": "against the mesh"}
+    # ShapeDiameter of 65,536 of the surface samples with their face normals (30 cone rays each)
+    sd_pts, sd_nrm = g_pts[:65536].contiguous(), g_nrm[:65536].contiguous()
+    T.profiling_reset()
+    T.profiling(True)
+    ms = timed_steps(lambda: mesh.shape_diameter(sd_pts, sd_nrm), steps, 2, flush, stream)
+    T.profiling(False)
+    r_ms, r_cnt = T.profiling_read("ray_kernel")
+    sdf = mesh.shape_diameter(sd_pts, sd_nrm)
+    out["shape_diameter_cfg0_mesh"] = {
+        "value": 65536 * 30 / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mrays/s", "points": 65536,
+        "rays_per_point": 30, "ms_per_step": statistics.mean(ms), "ray_kernel_ms": r_ms / max(1, r_cnt),
+        "points_with_value": int((sdf >= 0).sum().item()), "mean_sdf": float(sdf[sdf >= 0].mean().item())}
     mesh.close()
     T.profiling_reset()
     T.profiling_reset()

@@ -203,6 +203,19 @@ THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * ou
 THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * positions, int64_t num_points,
                                      int32_t num_rays, uint32_t seed, double * out_fraction, void * stream);
 
+/* ShapeDiameter::compute (Algorithms/SurfaceFeatures/Local/ShapeDiameter.hpp:143-217) for many points, as the
+ * ShapeDiameter(ExternalBvh const *, scale) constructor sets it up (ShapeDiameter.hpp:94-101): per point, 30 rays along
+ * the reference's fixed cone about the inward normal, from the point pushed 0.001 x scale inwards; first hits whose
+ * element normal faces along the ray are kept (all hits when only_interior == 0); the median is selected with
+ * libstdc++'s std::nth_element permutation, values beyond one standard deviation from it are rejected and the rest
+ * averaged with cosine weights, divided by scale and clamped to [0, 1] (FP64). out_sdf[i] = -1 when no ray is kept.
+ * normals (nullable, unnormalised is fine): the outward normals; NULL takes each point's closest element's own normal
+ * (ShapeDiameter::compute(position); lowest element index among equidistant elements). scale <= 0: the |extent| of
+ * the BVH's bounds, the constructor's default. Host or device arrays; synchronizes the stream. */
+THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float * positions, const float * normals,
+                                         int64_t num_points, float scale, int32_t only_interior, double * out_sdf,
+                                         void * stream);
+
 /* Sample proximity graph: PointSet3::updateGraph (Algorithms/PointSet3.hpp:324-391, no oversampling) with options
  * max_degree (1..64). Random(seed) replaces the reference's Random::common() in the mean-separation estimate (100
  * samples' nearest-neighbour distances); everything else is the reference's: radius sqrt(max_degree) x estimate,

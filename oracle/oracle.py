@@ -77,6 +77,8 @@ def lib():
         L.oracle_sample_graph.argtypes = [_f32p, _f32p, _i64, ctypes.c_int, ctypes.c_uint32, _vp, _i32p, _f32p, _i32p,
                                           _f32p, ctypes.c_int]
         L.oracle_visibility.argtypes = [_vp, _f32p, _i64, _i64, ctypes.c_uint32, _f32p, _f64p, ctypes.c_int]
+        L.oracle_shape_diameter.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, ctypes.c_int, _f32p, _f64p,
+                                             ctypes.c_int]
         L.oracle_affine_inverse.restype = ctypes.c_int
         L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
         for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
@@ -168,6 +170,19 @@ class MeshIndex:
         xf = _affine(transform) if transform is not None else None
         lib().oracle_visibility(self.h, _p(p, _f32p), len(p), int(num_rays), int(seed),
                                 _p(xf, _f32p) if xf is not None else None, _p(out, _f64p), threads or default_threads())
+        return out
+
+    def shape_diameter(self, positions, normals=None, scale=-1.0, only_interior=True, transform=None, threads=None):
+        """ShapeDiameter::compute per position (FP32 handle; normals None: the closest element's normal, which needs
+        no transform); transform: an affine map (3x4) set on the BVH."""
+        p = _f32(positions).reshape(-1, 3)
+        nr = _f32(normals).reshape(-1, 3) if normals is not None else None
+        out = np.empty(len(p), np.float64)
+        xf = _affine(transform) if transform is not None else None
+        lib().oracle_shape_diameter(self.h, _p(p, _f32p), _p(nr, _f32p) if nr is not None else None, len(p),
+                                    float(scale), 1 if only_interior else 0,
+                                    _p(xf, _f32p) if xf is not None else None, _p(out, _f64p),
+                                    threads or default_threads())
         return out
 
     def ray_contract(self, o, d, max_time=-1.0, threads=None):

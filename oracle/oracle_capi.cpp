@@ -388,16 +388,10 @@ void oracle_random_sphere(uint32_t seed, int64_t n, float * out) {
 
 // Visibility::compute for each position with Random(seed): point i draws directions [i * num_rays, (i + 1) * num_rays)
 // xf (nullable): an affine transform set on the BVH (row-major 3x4)
-void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t num_rays, uint32_t seed,
-                       float const * xf, double * out, int nthreads) {
-  MeshHandle * h = static_cast<MeshHandle *>(hv);
-  if (num_rays <= 0) num_rays = 100;
-  std::vector<V3<float>> dirs((size_t)(n * num_rays));
-  TheaRandom r(seed);
-  for (auto & u : dirs) u = theaSphere(r);
-  // getBounds(): the padded root box, or with a transform the box of its eight mapped corners (transformAndBound)
+// |extent| of getBounds(): the padded root box, or with a transform the box of its eight mapped corners
+// (transformAndBound); fills inv with the transform's inverse when xf is given
+static float boundsScale(MeshHandle const * h, float const * xf, float * inv) {
   Box<float> box = h->f.tree.nodes[0].bounds;
-  float inv[12];
   if (xf) {
     affineInverse(xf, inv);
     Box<float> w;
@@ -406,7 +400,18 @@ void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t nu
                                         (c & 4) ? box.hi.z : box.lo.z)));
     box = w;
   }
-  float scale = norm(box.extent());
+  return norm(box.extent());
+}
+
+void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t num_rays, uint32_t seed,
+                       float const * xf, double * out, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  if (num_rays <= 0) num_rays = 100;
+  std::vector<V3<float>> dirs((size_t)(n * num_rays));
+  TheaRandom r(seed);
+  for (auto & u : dirs) u = theaSphere(r);
+  float inv[12];
+  float scale = boundsScale(h, xf, inv);
   parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
     for (int64_t i = b; i < e; ++i)
       out[i] = visibilityFraction(h->f, q3<float>(positions, i), dirs.data() + i * num_rays, num_rays, scale,
@@ -415,6 +420,34 @@ void oracle_visibility(void * hv, float const * positions, int64_t n, int64_t nu
 }
 
 // Sample proximity graph with Random(seed); surface: nullable mesh handle. Outputs as thea_sample_graph.
+// ShapeDiameter per point; normals == nullptr: the closest element's normal (contract mode, no transform); scale <= 0:
+// |extent| of getBounds()
+void oracle_shape_diameter(void * hv, float const * positions, float const * normals, int64_t n, float scale,
+                           int only_interior, float const * xf, double * out, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(hv);
+  float inv[12];
+  float bs = boundsScale(h, xf, inv);
+  if (!(scale > 0.f)) scale = bs;
+  parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      V3<float> p = q3<float>(positions, i), nrm;
+      if (normals) {
+        nrm = q3<float>(normals, i);
+      } else {
+        float d2;
+        V3<float> cp;
+        int64_t k = h->f.closestContract(p, -1.0, d2, cp);
+        if (k < 0) {
+          out[i] = -1.0;
+          continue;
+        }
+        nrm = h->f.tris[(size_t)k].normal;
+      }
+      out[i] = shapeDiameter(h->f, p, nrm, scale, only_interior != 0, xf ? inv : nullptr);
+    }
+  });
+}
+
 void oracle_sample_graph(float const * P, float const * N, int64_t n, int max_degree, uint32_t seed, void * surface,
                          int32_t * out_nbr, float * out_sep, int32_t * out_deg, float * out_avg, int nthreads) {
   std::vector<V3<float>> pts((size_t)n), nrm;

@@ -876,6 +876,81 @@ inline double visibilityFraction(MeshIndex<float> const & m, V3<float> const & p
 }
 
 //============================================================================================================================
+// ShapeDiameter::compute (Algorithms/SurfaceFeatures/Local/ShapeDiameter.hpp:143-217) for a BVH-backed instance
+// (constructor at :94-101). Rays by contract-mode first hit (lowest index among equal times); the median is selected by
+// this C++ library's own std::nth_element, which permutes the values but not the weights paired with them afterwards.
+//============================================================================================================================
+
+// The reference's 30 cone directions about the local z axis (ShapeDiameter.hpp:163-193)
+static float const SDF_CONE_DIRS[30][3] = {
+    {0.407497f, 0.134086f, 0.903309f},     {0.128722f, -0.822715f, 0.553688f},   {0.359298f, 0.686129f, 0.632560f},
+    {0.813318f, -0.153956f, 0.561081f},    {-0.707169f, 0.296987f, 0.641647f},   {-0.478783f, -0.543441f, 0.689520f},
+    {0.561083f, 0.523634f, 0.641087f},     {-0.380898f, -0.655789f, 0.651811f},  {0.722588f, 0.472155f, 0.504912f},
+    {-0.535205f, 0.421235f, 0.732200f},    {0.577593f, -0.477896f, 0.661817f},   {0.393652f, -0.144484f, 0.907834f},
+    {0.141508f, -0.660777f, 0.737122f},    {-0.274967f, -0.141703f, 0.950954f},  {-0.304935f, 0.474085f, 0.825989f},
+    {0.711150f, 0.301383f, 0.635164f},     {-0.696119f, -0.112341f, 0.709082f},  {-0.248327f, 0.381035f, 0.890588f},
+    {-0.0772394f, 0.0462501f, 0.995939f},  {0.438024f, 0.656463f, 0.614159f},    {-0.483384f, -0.542477f, 0.687065f},
+    {0.498569f, -0.697466f, 0.514752f},    {-0.128902f, -0.0173429f, 0.991506f}, {0.338759f, -0.318772f, 0.885227f},
+    {-0.574364f, -0.463887f, 0.674474f},   {-0.459207f, 0.260125f, 0.849390f},   {-0.628057f, -0.528928f, 0.570771f},
+    {0.232916f, -0.328273f, 0.915416f},    {0.231667f, -0.796882f, 0.557951f},   {-0.270612f, -0.809654f, 0.520797f},
+};
+
+// Math::orthogonalDirection (MatrixUtil.hpp:225-231)
+inline V3<float> orthogonalDirection(V3<float> const & v) {
+  return maxAbsAxis(v) == 0 ? normalized(V3<float>(v.y, -v.x, 0.f)) : normalized(V3<float>(0.f, v.z, -v.y));
+}
+
+// One point with its outward normal; inv (nullable): the inverse of the BVH's transform (rays into object space, hit
+// normals back through its transpose)
+inline double shapeDiameter(MeshIndex<float> const & m, V3<float> const & position, V3<float> const & normal,
+                            float scale, bool only_interior, float const * inv) {
+  V3<float> nn = normalized(normal);
+  V3<float> in(-nn.x, -nn.y, -nn.z);
+  // Math::orthonormalBasis(in) (MatrixUtil.hpp:241-249): columns u, v, w
+  V3<float> w = normalized(in);
+  V3<float> u = orthogonalDirection(in);
+  V3<float> v = cross(w, u);
+  V3<float> offset = 0.001f * scale * in;
+  double values[30], weights[30];
+  int num_values = 0;
+  for (int i = 0; i < 30; ++i) {
+    float const * c = SDF_CONE_DIRS[i];
+    V3<float> dir(u.x * c[0] + (v.x * c[1] + w.x * c[2]), u.y * c[0] + (v.y * c[1] + w.y * c[2]),
+                  u.z * c[0] + (v.z * c[1] + w.z * c[2]));
+    V3<float> o = position + offset, d = dir;
+    if (inv) o = affinePoint(inv, o), d = affineLinear(inv, d);
+    auto hit = rayContract(m, o, d, -1.f);
+    if (hit.idx < 0) continue;
+    V3<float> hn = m.tris[(size_t)hit.idx].normal;
+    if (inv) hn = normalToWorld(inv, hn);
+    if (!only_interior || dot(hn, dir) >= 0.f) {
+      values[num_values] = hit.t;
+      weights[num_values] = c[2];
+      ++num_values;
+    }
+  }
+  if (num_values <= 0) return -1.0;
+  int mid = num_values / 2;
+  std::nth_element(values, values + mid, values + num_values);
+  double sum_values = 0, sum_squares = 0;
+  for (int i = 0; i < num_values; ++i) {
+    sum_values += values[i];
+    sum_squares += values[i] * values[i];
+  }
+  double avg = sum_values / num_values;
+  double var = sum_squares / num_values - avg * avg;
+  sum_values = 0;
+  double sum_weights = 0;
+  for (int i = 0; i < num_values; ++i)
+    if ((values[i] - values[mid]) * (values[i] - values[mid]) <= var) {
+      sum_values += weights[i] * values[i];
+      sum_weights += weights[i];
+    }
+  double r = sum_weights > 0 ? sum_values / (sum_weights * scale) : values[mid] / scale;
+  return r < 0.0 ? 0.0 : (r > 1.0 ? 1.0 : r);
+}
+
+//============================================================================================================================
 // Sample proximity graph: PointSet3::updateGraph without oversampling (Algorithms/PointSet3.hpp:324-391), with
 // findSampleNeighbors / NeighborFunctor (:586-681) and updateAverageSeparation (:688-702). The separation estimate draws
 // from the given generator in place of Random::common(). Candidates by brute force (every other sample inside the

@@ -1,0 +1,84 @@
+"""GPU parity of ShapeDiameter (Algorithms/SurfaceFeatures/Local/ShapeDiameter.hpp:143-217) against the oracle, whose
+median selection is this C++ library's own std::nth_element. The FP64 results are compared for equality: the rays, the
+kept hit times and the FP64 reduction follow the same operation sequence."""
+
+import numpy as np
+import pytest
+
+from thea_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def T():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from thea_gb300 import build as B
+    B.build()
+    import thea_gb300
+    return thea_gb300
+
+
+def _vertex_normals(V, F):
+    n = np.zeros_like(V, dtype=np.float64)
+    a, b, c = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    fn = np.cross(b - a, c - a)
+    for k in range(3):
+        np.add.at(n, F[:, k], fn)
+    return (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+
+
+@pytest.mark.parametrize("only_interior", [True, False])
+def test_shape_diameter_with_normals(T, oracle, only_interior):
+    import torch
+    V, F = W.noisy_icosphere(4, 31, sigma=0.02, scale=[1.0, 0.6, 0.35])
+    N = _vertex_normals(V, F)
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda())
+    got = bvh.shape_diameter(torch.from_numpy(V).cuda(), torch.from_numpy(N).cuda(), only_interior=only_interior)
+    want = oracle.MeshIndex(V, F).shape_diameter(V, N, only_interior=only_interior)
+    np.testing.assert_array_equal(got.cpu().numpy(), want)
+    assert np.all((want >= 0) & (want <= 1))
+    # host arrays and an explicit scale
+    got_h = bvh.shape_diameter(V, N, scale=2.5, only_interior=only_interior)
+    np.testing.assert_array_equal(got_h, oracle.MeshIndex(V, F).shape_diameter(V, N, scale=2.5,
+                                                                                only_interior=only_interior))
+    bvh.close()
+
+
+def test_shape_diameter_from_closest_elements(T, oracle):
+    import torch
+    V, F = W.noisy_icosphere(3, 32, sigma=0.03)
+    P, _, _ = oracle.sample_by_area(V, F, 3000, 77)
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda())
+    got = bvh.shape_diameter(torch.from_numpy(P).cuda())
+    want = oracle.MeshIndex(V, F).shape_diameter(P)
+    np.testing.assert_array_equal(got.cpu().numpy(), want)
+    bvh.close()
+
+
+def test_shape_diameter_open_surface_and_transform(T, oracle):
+    import torch
+    # a heightfield with upward normals: the inward rays leave through the open underside, so nothing counts (-1)
+    HV, HF = W.heightfield(32, 5)
+    up = np.tile(np.array([[0, 0, 1]], np.float32), (len(HV), 1))
+    hb = T.MeshBvh(HV, HF)
+    got = hb.shape_diameter(HV, up)
+    want = oracle.MeshIndex(HV, HF).shape_diameter(HV, up)
+    np.testing.assert_array_equal(got, want)
+    assert np.all(want == -1.0)
+    hb.close()
+    # a transformed sphere, with the points and normals in world space
+    V, F = W.noisy_icosphere(3, 33, sigma=0.02)
+    N = _vertex_normals(V, F)
+    xf = np.array([[0.0, -1.5, 0.0, 0.3], [1.5, 0.0, 0.0, -2.0], [0.0, 0.0, 0.75, 1.0]], np.float32)
+    Pw = V @ xf[:, :3].T + xf[:, 3]
+    L_inv_t = np.linalg.inv(xf[:, :3].astype(np.float64)).T
+    Nw = (N @ L_inv_t.T).astype(np.float32)
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda())
+    bvh.set_transform(xf)
+    got = bvh.shape_diameter(torch.from_numpy(Pw.astype(np.float32)).cuda(), torch.from_numpy(Nw).cuda())
+    want = oracle.MeshIndex(V, F).shape_diameter(Pw.astype(np.float32), Nw, transform=xf)
+    np.testing.assert_array_equal(got.cpu().numpy(), want)
+    bvh.close()

@@ -257,3 +257,18 @@ def test_visibility_restatement_limits(oracle):
     assert np.all(m.visibility(V[:50] * np.float32(4), 100, 7) > 0.9)
     on = m.visibility(V[:200], 100, 7)
     assert 0.4 < on.mean() < 0.6
+
+
+def test_shape_diameter_restatement(oracle):
+    """ShapeDiameter on a sphere: every value in (0, 1); a point sampled on a face with that face's normal gives what
+    the closest-element normal gives; with outward normals flipped the inward rays leave the sphere (-1)."""
+    V, F = W.noisy_icosphere(3, 6, sigma=0.0)
+    m = oracle.MeshIndex(V, F)
+    P, Nf, _ = oracle.sample_by_area(V, F, 400, 3)
+    with_normals = m.shape_diameter(P, Nf)
+    assert np.all((with_normals > 0) & (with_normals < 1))
+    from_closest = m.shape_diameter(P)
+    assert np.mean(with_normals == from_closest) > 0.99
+    assert np.all(m.shape_diameter(P * np.float32(1.01), -Nf) == -1.0)
+    # a sphere's diameter relative to the padded box diagonal, with the cone's cosine weighting: a stable band
+    assert 0.3 < with_normals.mean() < 0.45

@@ -235,6 +235,23 @@ class MeshBvh(_Bvh):
                                         _stream_of(io.device)))
         return out
 
+    def shape_diameter(self, positions, normals=None, scale=-1.0, only_interior=True):
+        """ShapeDiameter(bvh, scale)::compute for each position (normals: outward normals, or None for each point's
+        closest element's normal); float64 per point in [0, 1], -1 where no ray counts (CUDA tensor for CUDA input)."""
+        io = _Arrays(positions)
+        pp, n = io.input(positions, np.float32, 3)
+        pn, _ = io.input(normals, np.float32, 3) if normals is not None else (None, 0)
+        if io.device:
+            import torch
+            out = torch.empty(n, dtype=torch.float64, device="cuda")
+            po = ctypes.c_void_p(out.data_ptr() if n else 0)
+        else:
+            out = np.empty(n, np.float64)
+            po = ctypes.c_void_p(out.ctypes.data if n else 0)
+        N.check(N.lib().thea_shape_diameter(self._h, pp, pn, n, float(scale), 1 if only_interior else 0, po,
+                                            _stream_of(io.device)))
+        return out
+
     def closest_element_ex(self, queries, dist_bound=-1.0, precision="fp32", closest_points=True, errors=True):
         """closest_element with a precision mode ("fp32": the reference's arithmetic; "fp64": FP64 re-check band) and
         per-query |returned distance - FP64 distance of the returned element|: (index, distance, cp, error)."""

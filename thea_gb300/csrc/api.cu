@@ -11,6 +11,7 @@
 #include "visibility.hpp"
 #include "sample_graph.hpp"
 #include "mesh_io.hpp"
+#include "shape_diameter.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -1198,6 +1199,47 @@ THEA_API thea_status thea_server_reset_stats(thea_server * server) {
   return guarded([&] {
     THEA_REQUIRE(server, "server_reset_stats: null server");
     server_reset_stats(server);
+  });
+}
+
+THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float * positions, const float * normals,
+                                         int64_t num_points, float scale, int32_t only_interior, double * out_sdf,
+                                         void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh && mesh_bvh->num_segments == 1,
+                 "shape_diameter: a mesh BVH (not a forest) is required");
+    THEA_REQUIRE(mesh_bvh->ray_rec, "shape_diameter: the BVH was built without THEA_LAYOUT_RAY");
+    THEA_REQUIRE(normals || query_target(mesh_bvh)->cp_rec,
+                 "shape_diameter: without normals the BVH needs THEA_LAYOUT_CLOSEST");
+    THEA_REQUIRE(num_points >= 0, "shape_diameter: negative point count");
+    if (num_points == 0) return;
+    THEA_REQUIRE(positions && out_sdf, "shape_diameter: null positions or out_sdf");
+    THEA_REQUIRE(num_points * 30 < ((int64_t)1 << 31), "shape_diameter: too many points for one call");
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch pin, nin, pout;
+    float const * pos = positions;
+    float const * nrm = normals;
+    if (is_host_pointer(positions)) {
+      pin = Scratch((size_t)num_points * 12, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(pin.ptr, positions, (size_t)num_points * 12, cudaMemcpyHostToDevice, s));
+      pos = pin.as<float>();
+    }
+    if (normals && is_host_pointer(normals)) {
+      nin = Scratch((size_t)num_points * 12, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(nin.ptr, normals, (size_t)num_points * 12, cudaMemcpyHostToDevice, s));
+      nrm = nin.as<float>();
+    }
+    double * out = out_sdf;
+    bool host_out = is_host_pointer(out_sdf);
+    if (host_out) {
+      pout = Scratch((size_t)num_points * 8, s);
+      out = pout.as<double>();
+    }
+    run_shape_diameter(mesh_bvh, pos, nrm, num_points, scale, only_interior != 0, out, s);
+    if (host_out) {
+      THEA_CUDA_CHECK(cudaMemcpyAsync(out_sdf, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
   });
 }
 
