@@ -39,7 +39,8 @@ def test_shape_diameter_with_normals(T, oracle, only_interior):
     got = bvh.shape_diameter(torch.from_numpy(V).cuda(), torch.from_numpy(N).cuda(), only_interior=only_interior)
     want = oracle.MeshIndex(V, F).shape_diameter(V, N, only_interior=only_interior)
     np.testing.assert_array_equal(got.cpu().numpy(), want)
-    assert np.all((want >= 0) & (want <= 1))
+    # -1 where no ray counts (a few vertices of the noisy surface whose cone only meets back faces)
+    assert np.all(((want >= 0) & (want <= 1)) | (want == -1)) and np.mean(want >= 0) > 0.99
     # host arrays and an explicit scale
     got_h = bvh.shape_diameter(V, N, scale=2.5, only_interior=only_interior)
     np.testing.assert_array_equal(got_h, oracle.MeshIndex(V, F).shape_diameter(V, N, scale=2.5,
@@ -60,15 +61,17 @@ def test_shape_diameter_from_closest_elements(T, oracle):
 
 def test_shape_diameter_open_surface_and_transform(T, oracle):
     import torch
-    # a heightfield with upward normals: the inward rays leave through the open underside, so nothing counts (-1)
+    # a heightfield with upward normals: about half the points keep a ray (hits on the undersides of nearby bumps);
+    # flattened, every inward ray leaves through the open underside and nothing counts (-1)
     HV, HF = W.heightfield(32, 5)
     up = np.tile(np.array([[0, 0, 1]], np.float32), (len(HV), 1))
-    hb = T.MeshBvh(HV, HF)
-    got = hb.shape_diameter(HV, up)
-    want = oracle.MeshIndex(HV, HF).shape_diameter(HV, up)
-    np.testing.assert_array_equal(got, want)
+    for verts in (HV, np.concatenate([HV[:, :2], np.zeros((len(HV), 1), np.float32)], 1)):
+        hb = T.MeshBvh(verts, HF)
+        got = hb.shape_diameter(verts, up)
+        want = oracle.MeshIndex(verts, HF).shape_diameter(verts, up)
+        np.testing.assert_array_equal(got, want)
+        hb.close()
     assert np.all(want == -1.0)
-    hb.close()
     # a transformed sphere, with the points and normals in world space
     V, F = W.noisy_icosphere(3, 33, sigma=0.02)
     N = _vertex_normals(V, F)
