@@ -561,6 +561,17 @@ def extra_workloads(T, torch, stream, flush, args):
         "ms_per_step": statistics.mean(ms), "gram_kernel_ms": g_ms / max(1, g_cnt),
         "bounded_search_ms": k_ms / max(1, k_cnt), "tensor_flop_per_step": 2 * 16 * 512 * KNN_POINTS,
         "identical_to_traversal": bool(torch.equal(i0, i1) and torch.equal(d0, d1))}
+    # closest pair and the 32 closest pairs between these samples and a second 1,048,576-sample set of the same mesh
+    pos2, _, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), KNN_POINTS, 5)
+    pb2 = T.PointBvh(pos2)
+    ms = timed_steps(lambda: pb.closest_pair(pb2), steps, 2, flush, stream)
+    ms_k = timed_steps(lambda: pb.k_closest_pairs(pb2, 32), steps, 2, flush, stream)
+    cp_pair = pb.closest_pair(pb2)
+    out["bvh_pairs_cfg2"] = {
+        "value": KNN_POINTS / (statistics.mean(ms) / 1e3) / 1e6, "unit": "Mquery elements/s",
+        "closest_pair_ms": statistics.mean(ms), "k32_closest_pairs_ms": statistics.mean(ms_k),
+        "points_per_set": KNN_POINTS, "closest_sq_distance": cp_pair[2] if cp_pair else None}
+    pb2.close()
     pb.close()
     # Visibility of 65,536 of the surface samples, 100 rays each (directions of Random(seed).sphere())
     mesh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=2)

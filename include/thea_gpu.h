@@ -232,6 +232,25 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
                                        int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
                                        float * out_avg_separation, void * stream);
 
+/* ---- pairs between two BVHs ---------------------------------------------------------------------------------------- */
+
+/* BvhN::closestPair<MetricL2> with another BVH as the query (BvhN.hpp:1082-1114; the reference descends both trees,
+ * :1916-2033): the (query element, target element) pair at the smallest distance, at least one side holding points
+ * (mesh-mesh: THEA_ERR_NOT_SUPPORTED); single BVHs, transforms applied. Ties: lowest query index, then lowest target
+ * index. dist_bound >= 0: only pairs strictly closer. Outputs are host scalars: indices (-1 when no pair), the squared
+ * distance (the reference's monotone approximate distance; -1 when none) and, nullable, the closest points on the two
+ * elements (3 floats each). Synchronizes the stream. */
+THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_bvh * query, float dist_bound,
+                                           int32_t * out_query_index, int32_t * out_target_index,
+                                           float * out_sq_distance, float * out_query_point, float * out_target_point,
+                                           void * stream);
+/* BvhN::kClosestPairs<MetricL2> between two point BVHs (BvhN.hpp:1139-1146 with a BVH query): the k (1..32) pairs with
+ * the smallest squared distances, ascending (ties: lowest query index, then lowest target index), strictly closer than
+ * dist_bound when it is >= 0. k entries per output (host or device arrays), -1 past *out_count (nullable). */
+THEA_API thea_status thea_bvh_k_closest_pairs(const thea_bvh * target, const thea_bvh * query, int32_t k,
+                                              float dist_bound, int32_t * out_query_index, int32_t * out_target_index,
+                                              float * out_sq_distance, int32_t * out_count, void * stream);
+
 /* ---- mesh files --------------------------------------------------------------------------------------------------- */
 
 /* A mesh file read into host arrays in the reference's element order, ready for thea_mesh_bvh_build. */

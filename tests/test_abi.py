@@ -96,6 +96,15 @@ def test_invalid_arguments_are_rejected_without_a_device(lib):
     assert lib.thea_sample_graph(P.ctypes.data, None, 1, 8, 1, None, out.ctypes.data, None, None, None, None) == 1
     assert lib.thea_sample_graph(P.ctypes.data, None, 4, 0, 1, None, out.ctypes.data, None, None, None, None) == 1
     assert lib.thea_sample_graph(P.ctypes.data, None, 4, 65, 1, None, out.ctypes.data, None, None, None, None) == 1
+    # shape diameter and pairs between BVHs
+    sd = np.zeros(4, np.float64)
+    assert lib.thea_shape_diameter(None, P.ctypes.data, None, 4, -1.0, 1, sd.ctypes.data, None) == 1
+    qi, ti, d2 = ctypes.c_int32(7), ctypes.c_int32(7), ctypes.c_float(0)
+    assert lib.thea_bvh_closest_pair(None, None, -1.0, ctypes.byref(qi), ctypes.byref(ti), ctypes.byref(d2), None,
+                                     None, None) == 1
+    assert qi.value == -1 and ti.value == -1
+    assert lib.thea_bvh_k_closest_pairs(None, None, 0, -1.0, out.ctypes.data, out.ctypes.data, out.ctypes.data, None,
+                                        None) == 1
     eye = np.eye(3, 4, dtype=np.float32)
     assert lib.thea_bvh_set_transform(None, eye.ctypes.data, None) == 1
     assert lib.thea_bvh_clear_transform(None) == 1

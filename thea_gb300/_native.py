@@ -107,6 +107,11 @@ SIGNATURES = {
                                          _vp]),
     "thea_random_sphere": (ctypes.c_int, [ctypes.c_uint32, _i64, _vp, _vp]),
     "thea_shape_diameter": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, ctypes.c_int32, _vp, _vp]),
+    "thea_bvh_closest_pair": (ctypes.c_int, [_vp, _vp, ctypes.c_float, ctypes.POINTER(ctypes.c_int32),
+                                             ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), _vp, _vp,
+                                             _vp]),
+    "thea_bvh_k_closest_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int32, ctypes.c_float, _vp, _vp, _vp,
+                                                ctypes.POINTER(ctypes.c_int32), _vp]),
     "thea_mesh_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "thea_mesh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(MeshInfo)]),
     "thea_mesh_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),

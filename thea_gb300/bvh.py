@@ -139,6 +139,29 @@ class _Bvh:
     def _restored(self, inf):
         pass
 
+    def closest_pair(self, query, dist_bound=-1.0):
+        """BvhN::closestPair with another BVH (``query``) as the query: (query index, target index, squared distance,
+        query point, target point), or None when no pair qualifies. One side must hold points."""
+        qi, ti, d2 = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float()
+        qp, tp = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        N.check(N.lib().thea_bvh_closest_pair(self._h, query.handle, float(dist_bound), ctypes.byref(qi),
+                                              ctypes.byref(ti), ctypes.byref(d2), qp.ctypes.data, tp.ctypes.data,
+                                              _stream_of(_cuda_ready())))
+        if qi.value < 0:
+            return None
+        return qi.value, ti.value, d2.value, qp, tp
+
+    def k_closest_pairs(self, query, k, dist_bound=-1.0):
+        """BvhN::kClosestPairs between two point BVHs: (query indices, target indices, squared distances) of the k
+        closest pairs, ascending, -1 past the number found."""
+        qi, ti = np.empty(k, np.int32), np.empty(k, np.int32)
+        d2 = np.empty(k, np.float32)
+        cnt = ctypes.c_int32()
+        N.check(N.lib().thea_bvh_k_closest_pairs(self._h, query.handle, int(k), float(dist_bound), qi.ctypes.data,
+                                                 ti.ctypes.data, d2.ctypes.data, ctypes.byref(cnt),
+                                                 _stream_of(_cuda_ready())))
+        return qi, ti, d2
+
     def close(self):
         if self._h:
             N.check(N.lib().thea_bvh_destroy(self._h))

@@ -12,6 +12,7 @@
 #include "sample_graph.hpp"
 #include "mesh_io.hpp"
 #include "shape_diameter.hpp"
+#include "pairs.hpp"
 
 #include <initializer_list>
 #include <algorithm>
@@ -1240,6 +1241,44 @@ THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float 
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_sdf, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaStreamSynchronize(s));
     }
+  });
+}
+
+THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_bvh * query, float dist_bound,
+                                           int32_t * out_query_index, int32_t * out_target_index,
+                                           float * out_sq_distance, float * out_query_point, float * out_target_point,
+                                           void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(out_query_index && out_target_index, "closest_pair: null output");
+    *out_query_index = *out_target_index = -1;
+    if (out_sq_distance) *out_sq_distance = -1.f;
+    PairResult r;
+    if (!run_closest_pair(target, query, bound_threshold(dist_bound), r, (cudaStream_t)stream)) return;
+    *out_query_index = r.query_index;
+    *out_target_index = r.target_index;
+    if (out_sq_distance) *out_sq_distance = r.d2;
+    if (out_query_point) std::memcpy(out_query_point, r.query_point, 12);
+    if (out_target_point) std::memcpy(out_target_point, r.target_point, 12);
+  });
+}
+
+THEA_API thea_status thea_bvh_k_closest_pairs(const thea_bvh * target, const thea_bvh * query, int32_t k,
+                                              float dist_bound, int32_t * out_query_index, int32_t * out_target_index,
+                                              float * out_sq_distance, int32_t * out_count, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(out_query_index && out_target_index && out_sq_distance, "k_closest_pairs: null output");
+    THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_pairs: k must be in 1..32");
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch dev((size_t)k * 12, s);
+    int32_t * qi = (int32_t *)dev.ptr;
+    int32_t * ti = qi + k;
+    float * d2 = (float *)(ti + k);
+    int64_t c = run_k_closest_pairs(target, query, k, bound_threshold(dist_bound), qi, ti, d2, s);
+    THEA_CUDA_CHECK(cudaMemcpyAsync(out_query_index, qi, (size_t)k * 4, cudaMemcpyDefault, s));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(out_target_index, ti, (size_t)k * 4, cudaMemcpyDefault, s));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, d2, (size_t)k * 4, cudaMemcpyDefault, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (out_count) *out_count = (int32_t)c;
   });
 }
 
