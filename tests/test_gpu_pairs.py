@@ -60,6 +60,14 @@ def test_point_point_pairs(T):
     np.testing.assert_array_equal(gq[:n], bq[:n])
     np.testing.assert_array_equal(gt[:n], bt[:n])
     assert np.all(gq[n:] == -1)
+    # fewer query points than k
+    tiny = T.PointBvh(A[:10])
+    sq, st, sv = _sorted_pairs(_pair_d2(A[:10], B))
+    gq, gt, gd = tb.k_closest_pairs(tiny, 32)
+    np.testing.assert_array_equal(gq, sq[:32])
+    np.testing.assert_array_equal(gt, st[:32])
+    np.testing.assert_array_equal(gd, sv[:32])
+    tiny.close()
     far = T.PointBvh(A + np.float32(10))
     assert tb.closest_pair(far, dist_bound=1.0) is None
     for h in (ta, tb, far):

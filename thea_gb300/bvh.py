@@ -151,9 +151,9 @@ class _Bvh:
             return None
         return qi.value, ti.value, d2.value, qp, tp
 
-    def k_closest_pairs(self, query, k, dist_bound=-1.0):
+    def k_closest_pairs_bvh(self, query, k, dist_bound=-1.0):
         """BvhN::kClosestPairs between two point BVHs: (query indices, target indices, squared distances) of the k
-        closest pairs, ascending, -1 past the number found."""
+        closest pairs, ascending, -1 past the number found. PointBvh.k_closest_pairs forwards here for a BVH query."""
         qi, ti = np.empty(k, np.int32), np.empty(k, np.int32)
         d2 = np.empty(k, np.float32)
         cnt = ctypes.c_int32()
@@ -449,7 +449,10 @@ class PointBvh(_Bvh):
         self.n = inf["num_elements"]
 
     def k_closest_pairs(self, queries, k, dist_bound=-1.0, exclude=None):
-        """BvhN::kClosestPairs: (indices [n, k], squared distances [n, k]); unused slots -1."""
+        """BvhN::kClosestPairs: (indices [n, k], squared distances [n, k]); unused slots -1. With another BVH as the
+        query: the k closest pairs between the two (see k_closest_pairs_bvh)."""
+        if isinstance(queries, _Bvh):
+            return self.k_closest_pairs_bvh(queries, k, dist_bound)
         io = _Arrays(queries)
         pq, n = io.input(queries, np.float32, 3)
         pe, _ = io.input(exclude, np.int32) if exclude is not None else (None, 0)

@@ -6,8 +6,9 @@
 // answer it with one query per element, and a 64-bit atomic minimum of (squared distance bits, query index) picks the
 // pair (non-negative floats order like their bit patterns). Point-point pairs query the target's points from the
 // query's; point-mesh pairs query the mesh from the points, whichever side the mesh is on. The k closest pairs of two
-// point sets are among the k nearest target points of each query point: those n k candidates are sorted by
-// (squared distance, query index) with a stable radix sort that keeps each row's target order.
+// point sets are among the k nearest target points of each query point within the k-th smallest of the rows' nearest
+// distances: those candidates are compacted in slot order and sorted by (squared distance, query index) with a stable
+// radix sort that keeps each row's target order.
 #include "pairs.hpp"
 
 #include "device_util.cuh"
@@ -63,13 +64,34 @@ __global__ void pair_tie_kernel(int32_t const * __restrict__ idx, float const * 
   if (key == *best) atomicMin(best_target, rows_are_query ? (unsigned)idx[r] : (unsigned)r);
 }
 
-// candidate c = row * k + j of the k-NN rows: key (d2 bits, row), or all ones for an empty slot
-__global__ void pair_candidates_kernel(int32_t const * __restrict__ idx, float const * __restrict__ d2, int64_t m, int k,
+// key of each row's nearest distance for the k-th-smallest selection (all ones for a row without a neighbour)
+__global__ void row_min_keys_kernel(int32_t const * __restrict__ idx, float const * __restrict__ d2, int64_t n,
+                                    unsigned long long * __restrict__ keys, uint32_t * __restrict__ vals) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  keys[r] = idx[r] < 0 ? 0xffffffffull : (unsigned long long)__float_as_uint(d2[r]);
+  vals[r] = (uint32_t)r;
+}
+
+__global__ void slot_flag_kernel(int32_t const * __restrict__ idx, int64_t slots, uint32_t * __restrict__ flag) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c < slots) flag[c] = idx[c] >= 0 ? 1u : 0u;
+}
+
+__global__ void slot_total_kernel(uint32_t const * __restrict__ flag, uint32_t const * __restrict__ pos, int64_t slots,
+                                  uint32_t * __restrict__ total) {
+  *total = pos[slots - 1] + flag[slots - 1];
+}
+
+// filled slot c = row * k + j of the k-NN rows, written at its compacted position: key (d2 bits, row), value c
+__global__ void pair_candidates_kernel(int32_t const * __restrict__ idx, float const * __restrict__ d2,
+                                       uint32_t const * __restrict__ pos, int64_t slots, int k,
                                        unsigned long long * __restrict__ keys, uint32_t * __restrict__ vals) {
   int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= m) return;
-  keys[c] = idx[c] < 0 ? ~0ull : (((unsigned long long)__float_as_uint(d2[c]) << 32) | (uint64_t)(c / k));
-  vals[c] = (uint32_t)c;
+  if (c >= slots || idx[c] < 0) return;
+  uint32_t p = pos[c];
+  keys[p] = ((unsigned long long)__float_as_uint(d2[c]) << 32) | (uint64_t)(c / k);
+  vals[p] = (uint32_t)c;
 }
 
 __global__ void pair_take_kernel(unsigned long long const * __restrict__ keys, uint32_t const * __restrict__ vals,
@@ -168,20 +190,55 @@ int64_t run_k_closest_pairs(thea_bvh const * target, thea_bvh const * query, int
   check_single(query, "k_closest_pairs");
   THEA_REQUIRE(!target->is_mesh && !query->is_mesh, "k_closest_pairs: two point BVHs are required");
   THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_pairs: k must be in 1..32");
-  int64_t n = query->n, m = n * k;
+  int64_t n = query->n;
   Scratch count(4, s);
   THEA_CUDA_CHECK(cudaMemsetAsync(count.ptr, 0, 4, s));
-  Scratch idx((size_t)std::max<int64_t>(m, 1) * 4, s), dd((size_t)std::max<int64_t>(m, 1) * 4, s);
-  Scratch keys((size_t)std::max<int64_t>(m, 1) * 8, s), vals((size_t)std::max<int64_t>(m, 1) * 4, s);
-  if (m > 0 && target->n > 0) {
+  Scratch keys(8, s), vals(4, s), idx(4, s), dd(4, s);
+  int64_t m = 0;
+  if (n > 0 && target->n > 0) {
     Scratch pts = element_points(query, s);
     thea_bvh const * searched = query_target(target);
+    unsigned blocks = (unsigned)ceil_div(n, PAIR_THREADS);
+    // 1. every row's nearest target point; the k-th smallest of those distances bounds the k-th closest pair (the k
+    //    rows with the smallest minima already give k distinct pairs within it)
+    if (n >= k) {
+      Scratch idx1((size_t)n * 4, s), d21((size_t)n * 4, s), rk((size_t)n * 8, s), rv((size_t)n * 4, s);
+      run_knn(searched, pts.as<float>(), n, 1, thresh, nullptr, idx1.as<int32_t>(), d21.as<float>(), searched->err, s);
+      THEA_LAUNCH(row_min_keys_kernel, blocks, PAIR_THREADS, 0, s, idx1.as<int32_t>(), d21.as<float>(), n,
+                  rk.as<unsigned long long>(), rv.as<uint32_t>());
+      radix_sort_pairs(rk.as<uint64_t>(), rv.as<uint32_t>(), n, 32, s);
+      unsigned long long kth = 0;
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&kth, rk.as<unsigned long long>() + (k - 1), 8, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      if (kth != 0xffffffffull) {
+        float tau;
+        uint32_t bits = (uint32_t)kth;
+        std::memcpy(&tau, &bits, 4);
+        thresh = std::min(thresh, tau);  // both accept squared distances <= the threshold
+      }
+    }
+    // 2. each row's k nearest within the bound; the global k closest pairs are among them
+    int64_t slots = n * k;
+    idx = Scratch((size_t)slots * 4, s);
+    dd = Scratch((size_t)slots * 4, s);
     run_knn(searched, pts.as<float>(), n, k, thresh, nullptr, idx.as<int32_t>(), dd.as<float>(), searched->err, s);
-    THEA_LAUNCH(pair_candidates_kernel, (unsigned)ceil_div(m, PAIR_THREADS), PAIR_THREADS, 0, s, idx.as<int32_t>(),
-                dd.as<float>(), m, k, keys.as<unsigned long long>(), vals.as<uint32_t>());
-    radix_sort_pairs(keys.as<uint64_t>(), vals.as<uint32_t>(), m, 64, s);
-  } else {
-    m = 0;
+    // 3. compact the filled slots in slot order, then sort them by (squared distance, row), stably
+    Scratch flag((size_t)slots * 4, s), pos((size_t)slots * 4, s), total(4, s);
+    unsigned sblocks = (unsigned)ceil_div(slots, PAIR_THREADS);
+    THEA_LAUNCH(slot_flag_kernel, sblocks, PAIR_THREADS, 0, s, idx.as<int32_t>(), slots, flag.as<uint32_t>());
+    exclusive_scan(flag.as<uint32_t>(), pos.as<uint32_t>(), slots, s);
+    THEA_LAUNCH(slot_total_kernel, 1, 1, 0, s, flag.as<uint32_t>(), pos.as<uint32_t>(), slots, total.as<uint32_t>());
+    uint32_t hm = 0;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&hm, total.ptr, 4, cudaMemcpyDeviceToHost, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    m = hm;
+    if (m > 0) {
+      keys = Scratch((size_t)m * 8, s);
+      vals = Scratch((size_t)m * 4, s);
+      THEA_LAUNCH(pair_candidates_kernel, sblocks, PAIR_THREADS, 0, s, idx.as<int32_t>(), dd.as<float>(),
+                  pos.as<uint32_t>(), slots, k, keys.as<unsigned long long>(), vals.as<uint32_t>());
+      radix_sort_pairs(keys.as<uint64_t>(), vals.as<uint32_t>(), m, 64, s);
+    }
   }
   THEA_LAUNCH(pair_take_kernel, 1, 32, 0, s, keys.as<unsigned long long>(), vals.as<uint32_t>(), idx.as<int32_t>(),
               dd.as<float>(), m, k, qi, ti, d2, count.as<unsigned>());
