@@ -385,3 +385,14 @@ def test_off_bin_extension(T, tmp_path):
     path.write_bytes(_binary_off(V, [struct.pack(">iiiii", 3, 0, 1, 2, 0)]))
     m = T.read_mesh(str(path))
     assert m.triangles.tolist() == [[0, 1, 2]]
+
+
+def test_sample_model_fixture(golden_dir):
+    """The fixture of the reference's sample meshes (tests/golden/make_model_fixtures.py) is self-consistent."""
+    import os
+    z = np.load(os.path.join(golden_dir, "models.npz"))
+    for name, nv, nt in (("cube", 8, 12), ("sphere", 946, 1888), ("teapot", 3644, 6320)):
+        V, F = z[name + "_vertices"], z[name + "_triangles"]
+        assert V.shape == (nv, 3) and F.shape == (nt, 3)
+        assert F.min() >= 0 and F.max() < nv
+        assert z[name + "_submesh_triangle_offsets"][-1] == nt and len(z[name + "_sha256"]) == 32
