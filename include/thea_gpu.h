@@ -290,8 +290,9 @@ THEA_API thea_status thea_mesh_destroy(thea_mesh * mesh);
 THEA_API thea_status thea_triangulate_face(const float * positions, int32_t num_vertices, int32_t * out_triangles,
                                            int32_t * out_count);
 
-/* k nearest points of a point BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
- * index first). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
+/* k nearest elements of a BVH to each query, 1 <= k <= 32, sorted by increasing squared distance (ties: lower
+ * index first): points of a point BVH, or triangles of a mesh BVH (built with THEA_LAYOUT_CLOSEST; the squared
+ * distance to the triangle's closest point, as closestElement computes it). exclude_index (nullable) gives per query an element index to skip (the reference's FilterSelf,
  * Code/Source/Algorithms/PointSet3.hpp:576-583). dist_bound < 0: unbounded; else only squared distances strictly below
  * dist_bound^2. Unused slots: index -1, squared distance -1.
  * Replaces BvhN::kClosestPairs<MetricL2>(query, BoundedSortedArrayN<k, NeighborPair>&, dist_bound) (BvhN.hpp:1139-1146). */

@@ -151,6 +151,21 @@ class _Bvh:
             return None
         return qi.value, ti.value, d2.value, qp, tp
 
+    def k_closest_pairs(self, queries, k, dist_bound=-1.0, exclude=None):
+        """BvhN::kClosestPairs: the k nearest elements of each query point (points of a PointBvh, triangles of a
+        MeshBvh): (indices [n, k], squared distances [n, k]); unused slots -1. With another BVH as the query: the k
+        closest pairs between the two (see k_closest_pairs_bvh)."""
+        if isinstance(queries, _Bvh):
+            return self.k_closest_pairs_bvh(queries, k, dist_bound)
+        io = _Arrays(queries)
+        pq, n = io.input(queries, np.float32, 3)
+        pe, _ = io.input(exclude, np.int32) if exclude is not None else (None, 0)
+        idx, pidx = io.output((n, k), np.int32)
+        d2, pd2 = io.output((n, k), np.float32)
+        N.check(N.lib().thea_k_closest(self._h, pq, n, int(k), float(dist_bound), pe, pidx, pd2,
+                                       _stream_of(io.device)))
+        return idx, d2
+
     def k_closest_pairs_bvh(self, query, k, dist_bound=-1.0):
         """BvhN::kClosestPairs between two point BVHs: (query indices, target indices, squared distances) of the k
         closest pairs, ascending, -1 past the number found. PointBvh.k_closest_pairs forwards here for a BVH query."""
@@ -447,20 +462,6 @@ class PointBvh(_Bvh):
 
     def _restored(self, inf):
         self.n = inf["num_elements"]
-
-    def k_closest_pairs(self, queries, k, dist_bound=-1.0, exclude=None):
-        """BvhN::kClosestPairs: (indices [n, k], squared distances [n, k]); unused slots -1. With another BVH as the
-        query: the k closest pairs between the two (see k_closest_pairs_bvh)."""
-        if isinstance(queries, _Bvh):
-            return self.k_closest_pairs_bvh(queries, k, dist_bound)
-        io = _Arrays(queries)
-        pq, n = io.input(queries, np.float32, 3)
-        pe, _ = io.input(exclude, np.int32) if exclude is not None else (None, 0)
-        idx, pidx = io.output((n, k), np.int32)
-        d2, pd2 = io.output((n, k), np.float32)
-        N.check(N.lib().thea_k_closest(self._h, pq, n, int(k), float(dist_bound), pe, pidx, pd2,
-                                       _stream_of(io.device)))
-        return idx, d2
 
     def radius_neighbors(self, queries, radius, exclude=None):
         """BvhN::rangeQueryIndices with a Ball3: every point within `radius` (inclusive) of each CUDA-tensor query, as

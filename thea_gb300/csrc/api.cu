@@ -719,7 +719,10 @@ THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * qu
                                     float dist_bound, const int32_t * exclude_index, int32_t * out_index,
                                     float * out_sq_distance, void * stream) {
   return guarded([&] {
-    THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "k_closest: a point BVH is required");
+    THEA_REQUIRE(point_bvh, "k_closest: null BVH");
+    THEA_REQUIRE(point_bvh->num_segments == 1, "k_closest: forests take thea_batch_k_closest");
+    THEA_REQUIRE(!point_bvh->is_mesh || query_target(point_bvh)->cp_rec,
+                 "k_closest: the mesh BVH was built without THEA_LAYOUT_CLOSEST");
     THEA_REQUIRE(k >= 1 && k <= 32, "k_closest: k must be in 1..32");
     THEA_REQUIRE(num_queries >= 0, "k_closest: negative query count");
     if (num_queries == 0) return;

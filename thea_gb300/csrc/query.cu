@@ -507,6 +507,30 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
   }
 }
 
+// k nearest triangles of a mesh BVH to each query point (kClosestPairs on a MeshBvh)
+template <int W, int K, int STACK>
+__global__ void __launch_bounds__(QUERY_THREADS, knn_min_blocks<K>())
+knn_mesh_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                float const * __restrict__ queries, int64_t n, int k_out, float thresh,
+                int32_t const * __restrict__ exclude, int32_t * __restrict__ out_index, float * __restrict__ out_d2,
+                unsigned * __restrict__ err, uint32_t const * __restrict__ order) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (order) q = order[q];
+  V3 p = load_v3(queries + 3 * q);
+  int excl = exclude ? exclude[q] : -1;
+  float bd[K];
+  int bi[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
+  knn_mesh_query<W, K, STACK>(nodes, rec, 0, 0, p, excl, bd, bi, err);
+  for (int j = 0; j < k_out; ++j) {
+    bool v = bi[j] != INT_MAX;
+    out_index[q * k_out + j] = v ? bi[j] : -1;
+    out_d2[q * k_out + j] = v ? bd[j] : -1.f;
+  }
+}
+
 constexpr int64_t CLOSEST_TWO_PHASE_MIN = 1 << 16;
 constexpr int CLOSEST_TWO_PHASE_BUDGET = 256;
 
@@ -724,9 +748,30 @@ void launch_knn_k(thea_bvh const * b, float const * q, int64_t n, int k, float t
               (WideNode<W> const *)b->nodes, b->pt_rec, q, n, k, thresh, ex, idx, d2, err, order, ib);
 }
 
+template <int W, int K, int STACK>
+void launch_knn_mesh_k(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex,
+                       int32_t * idx, float * d2, unsigned * err, uint32_t const * order, cudaStream_t s) {
+  THEA_LAUNCH((knn_mesh_kernel<W, K, STACK>), (unsigned)ceil_div(n, QUERY_THREADS), QUERY_THREADS, 0, s,
+              (WideNode<W> const *)b->nodes, b->cp_rec, q, n, k, thresh, ex, idx, d2, err, order);
+}
+
+template <int W, int STACK>
+void launch_knn_mesh(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex,
+                     int32_t * idx, float * d2, unsigned * err, uint32_t const * order, cudaStream_t s) {
+  if (k <= 1) launch_knn_mesh_k<W, 1, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+  else if (k <= 4) launch_knn_mesh_k<W, 4, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+  else if (k <= 8) launch_knn_mesh_k<W, 8, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+  else if (k <= 16) launch_knn_mesh_k<W, 16, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+  else launch_knn_mesh_k<W, 32, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+}
+
 template <int W, int STACK>
 void launch_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
                 float * d2, unsigned * err, uint32_t const * order, float const * ib, cudaStream_t s) {
+  if (b->is_mesh) {
+    launch_knn_mesh<W, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, s);
+    return;
+  }
   if (k <= 1) launch_knn_k<W, 1, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
   else if (k <= 2) launch_knn_k<W, 2, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);
   else if (k <= 4) launch_knn_k<W, 4, STACK>(b, q, n, k, thresh, ex, idx, d2, err, order, ib, s);

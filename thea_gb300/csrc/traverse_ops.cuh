@@ -972,4 +972,42 @@ __device__ __forceinline__ void knn_query(WideNode<W> const * __restrict__ nodes
   }
 }
 
+// k nearest triangles of a mesh BVH: the same search with the closest-point record test (FP32 reference arithmetic);
+// a NaN distance (coincident vertices) is never kept
+template <int W, int K, int STACK>
+__device__ __forceinline__ void knn_mesh_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
+                                               int root, int64_t elem_base, V3 p, int excl, float (&bd)[K],
+                                               int (&bi)[K], unsigned * err) {
+  int2 stk[STACK];  // (child code, bound bits)
+  int sp = 0;
+  int next = root;
+  while (next != CHILD_EMPTY || sp > 0) {
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > bd[K - 1] * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children_next<W, STACK>(nd, lb, bd[K - 1] * PRUNE_SLACK, stk, sp, next, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        int idx = cp_record_index(rec, k);
+        if (idx == excl) continue;
+        V3 cp;
+        float d2 = cp_record_test(rec, k, p, cp);
+        if (d2 < bd[K - 1] || (d2 == bd[K - 1] && idx < bi[K - 1])) knn_insert<K>(bd, bi, d2, idx);
+      }
+    }
+  }
+}
+
 }  // namespace thea
