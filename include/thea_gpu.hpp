@@ -75,6 +75,24 @@ class BvhHandle {
     check(thea_bvh_get_transform(h_, &has, nullptr, nullptr));
     return has != 0;
   }
+  // BvhN::closestPair with another BVH as the query (one side must hold points): false when no pair qualifies.
+  // query_point / target_point (nullable): the closest points on the two elements.
+  bool closestPair(BvhHandle const & query, int32_t * query_index, int32_t * target_index, float * sq_distance,
+                   double dist_bound = -1, float * query_point = nullptr, float * target_point = nullptr,
+                   void * stream = nullptr) const {
+    check(thea_bvh_closest_pair(h_, query.h_, (float)dist_bound, query_index, target_index, sq_distance, query_point,
+                                target_point, stream));
+    return *query_index >= 0;
+  }
+  // BvhN::kClosestPairs between two point BVHs: the k closest pairs, ascending; returns how many were found.
+  int32_t kClosestPairs(BvhHandle const & query, int32_t k, int32_t * query_indices, int32_t * target_indices,
+                        float * sq_distances, double dist_bound = -1, void * stream = nullptr) const {
+    int32_t count = 0;
+    check(thea_bvh_k_closest_pairs(h_, query.h_, k, (float)dist_bound, query_indices, target_indices, sq_distances,
+                                   &count, stream));
+    return count;
+  }
+
   // Byte image of the built BVH (thea_bvh_serialize); the class's fromImage reloads it without a rebuild.
   std::vector<unsigned char> serialize(void * stream = nullptr) const {
     int64_t n = 0;
@@ -160,6 +178,32 @@ class MeshBvh : public BvhHandle {
                            float max_time = -1, void * stream = nullptr) const {
     check(thea_ray_intersection(h_, origins, directions, n, max_time, times, nullptr, nullptr, stream));
   }
+
+  // BvhN::rayIntersects, batched: hit[i] = 1 if ray i meets an element within max_time (any-hit search).
+  void rayIntersects(float const * origins, float const * directions, int64_t n, uint8_t * hit, float max_time = -1,
+                     void * stream = nullptr) const {
+    check(thea_ray_intersects(h_, origins, directions, n, max_time, hit, stream));
+  }
+
+  // BvhN::kClosestPairs with point queries on a mesh: the k nearest triangles of each query, n x k, sorted.
+  void kClosestPairs(float const * queries, int64_t n, int32_t k, int32_t * indices, float * sq_distances,
+                     double dist_bound = -1, void * stream = nullptr) const {
+    check(thea_k_closest(h_, queries, n, k, (float)dist_bound, nullptr, indices, sq_distances, stream));
+  }
+  using BvhHandle::kClosestPairs;
+
+  // Visibility::compute for n points (Random(seed) in place of Random::common()): escaped fraction per point.
+  void visibility(float const * positions, int64_t n, double * fractions, int32_t num_rays = 100, uint32_t seed = 0,
+                  void * stream = nullptr) const {
+    check(thea_visibility(h_, positions, n, num_rays, seed, fractions, stream));
+  }
+
+  // ShapeDiameter(bvh, scale)::compute for n points; normals nullable (closest element's normal), scale <= 0: the
+  // BVH bounds' diagonal. -1 where no ray counts.
+  void shapeDiameter(float const * positions, float const * normals, int64_t n, double * sdf, double scale = -1,
+                     bool only_interior = true, void * stream = nullptr) const {
+    check(thea_shape_diameter(h_, positions, normals, n, (float)scale, only_interior ? 1 : 0, sdf, stream));
+  }
 };
 
 // BvhN<Vector3, 3>: a BVH over points; element index = point index.
@@ -184,6 +228,15 @@ class PointBvh : public BvhHandle {
   void kClosestPairs(float const * queries, int64_t n, int32_t k, int32_t * indices, float * sq_distances,
                      double dist_bound = -1, int32_t const * exclude = nullptr, void * stream = nullptr) const {
     check(thea_k_closest(h_, queries, n, k, (float)dist_bound, exclude, indices, sq_distances, stream));
+  }
+  using BvhHandle::kClosestPairs;
+
+  // BvhN::rangeQueryIndices with a Ball3: points within `radius` (inclusive) of each query as CSR, in two calls
+  // (thea_radius_neighbors; device arrays): indices == nullptr writes offsets (n + 1); then the same call with those
+  // offsets fills indices and squared distances (nullable), ascending per query.
+  void rangeQuery(float const * queries, int64_t n, float radius, int64_t * offsets, int32_t * indices = nullptr,
+                  float * sq_distances = nullptr, int32_t const * exclude = nullptr, void * stream = nullptr) const {
+    check(thea_radius_neighbors(h_, queries, n, radius, exclude, offsets, indices, sq_distances, stream));
   }
 
   // k-nearest-neighbour graph of the indexed points (each point excluding itself), rows in point order.

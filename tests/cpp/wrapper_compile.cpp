@@ -75,6 +75,15 @@ int main(int argc, char ** argv) {
       if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 18;
     }
   }
+  // an unreadable mesh file is reported before any CUDA call
+  {
+    try {
+      thea_gpu::MeshFile mf2(std::string(argv[0]) + ".missing.ply");
+      return 19;
+    } catch (thea_gpu::Exception const & e) {
+      if (e.status() != THEA_ERR_INVALID_ARGUMENT) return 20;
+    }
+  }
   if (no_device) return 0;
 
   float V[] = {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -99,6 +108,18 @@ int main(int argc, char ** argv) {
   float kd[2];
   pts.kClosestPairs(q, 1, 2, ki, kd);
   if (ki[0] != 0 || ki[1] != 1) { std::printf("knn %d %d\n", ki[0], ki[1]); return 6; }
+  // the closest pair between the tetrahedron's vertices and its faces is at distance 0; the nearest triangles of q
+  int32_t pq = -1, pt = -1;
+  float pd = -1;
+  if (!mesh.closestPair(pts, &pq, &pt, &pd) || pd != 0.0f) return 21;
+  int32_t mi[2];
+  float md[2];
+  mesh.kClosestPairs(q, 1, 2, mi, md);
+  if (mi[0] != 0 || md[0] != 1.0f) { std::printf("mesh knn %d %f\n", mi[0], md[0]); return 22; }
+  double sdf[1];
+  float inside[3] = {0.1f, 0.1f, 0.0f}, up[3] = {0, 0, -1};
+  mesh.shapeDiameter(inside, up, 1, sdf);
+  if (!(sdf[0] > 0.0 && sdf[0] <= 1.0)) { std::printf("sdf %f\n", sdf[0]); return 23; }
   std::printf("wrapper ok\n");
   return 0;
 }
