@@ -209,9 +209,8 @@ ray_persistent_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __r
           q = qb + rank;
           int64_t r = order ? (int64_t)order[q] : q;
           q = r;
-          // rays are read once: streaming loads (evict-first in L2) leave the cache to the nodes and records
-          o = V3{__ldcs(origins + 3 * r), __ldcs(origins + 3 * r + 1), __ldcs(origins + 3 * r + 2)};
-          d = V3{__ldcs(dirs + 3 * r), __ldcs(dirs + 3 * r + 1), __ldcs(dirs + 3 * r + 2)};
+          o = load_v3(origins + 3 * r);
+          d = load_v3(dirs + 3 * r);
           ix = 1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x));
           iy = 1.0f / (fabsf(d.y) > 1e-30f ? d.y : copysignf(1e-30f, d.y));
           iz = 1.0f / (fabsf(d.z) > 1e-30f ? d.z : copysignf(1e-30f, d.z));
@@ -232,10 +231,10 @@ ray_persistent_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __r
     int code = next;
     if (code == CHILD_EMPTY) {
       if (sp == 0) {
-        // finished: the same outputs as ray_kernel, written with streaming stores
+        // finished: the same outputs as ray_kernel
         bool found = best_idx != INT_MAX;
-        __stcs(out_time + q, found ? best : -1.f);
-        if (out_index) __stcs(out_index + q, found ? best_idx : -1);
+        out_time[q] = found ? best : -1.f;
+        if (out_index) out_index[q] = found ? best_idx : -1;
         if (out_normal) {
           V3 nn = V3{0.f, 0.f, 0.f};
           if (found) {
