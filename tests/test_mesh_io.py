@@ -396,3 +396,14 @@ def test_sample_model_fixture(golden_dir):
         assert V.shape == (nv, 3) and F.shape == (nt, 3)
         assert F.min() >= 0 and F.max() < nv
         assert z[name + "_submesh_triangle_offsets"][-1] == nt and len(z[name + "_sha256"]) == 32
+
+
+def test_ply_binary_list_longer_than_the_file(T, tmp_path):
+    from thea_gb300 import TheaError
+    head = b"ply\nformat binary_little_endian 1.0\nelement vertex 3\nproperty float x\nproperty float y\n" \
+           b"property float z\nelement face 1\nproperty list uint int vertex_indices\nend_header\n"
+    body = struct.pack("<9f", 0, 0, 0, 1, 0, 0, 0, 1, 0) + struct.pack("<I", 4000000000) + struct.pack("<3i", 0, 1, 2)
+    path = tmp_path / "long.ply"
+    path.write_bytes(head + body)
+    with pytest.raises(TheaError, match="end of input"):
+        T.read_mesh(str(path))

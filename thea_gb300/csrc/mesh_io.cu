@@ -629,6 +629,7 @@ MeshData read_ply(Input & in) {
         PlyProperty const & p = blk.props[0];
         double n = ply_number(in, p.count_type, h.big_endian);
         if (n < 0) fail(in.path, "list has negative size");
+        if (n * ply_bytes(p.item_type) > (double)(in.data.size() - in.pos)) fail(in.path, "unexpected end of input");
         idx.resize((size_t)n);
         for (auto & v : idx) v = (long long)ply_number(in, p.item_type, h.big_endian);
         for (size_t k = 1; k < blk.props.size(); ++k) skip_ply_property(in, blk.props[k], h.big_endian);
