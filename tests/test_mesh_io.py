@@ -407,3 +407,29 @@ def test_ply_binary_list_longer_than_the_file(T, tmp_path):
     path.write_bytes(head + body)
     with pytest.raises(TheaError, match="end of input"):
         T.read_mesh(str(path))
+
+
+def test_number_syntax_follows_stream_extraction(T, tmp_path):
+    """Coordinates parse as successive std::istream >> double reads do: a leading '+', an underflow to zero and junk
+    after the last number are accepted; "inf", "nan", a lone exponent, "+-", an overflow and junk before the next
+    number are errors, as they are for the reference's reader."""
+    from thea_gb300 import TheaError
+    ok = tmp_path / "ok.obj"
+    ok.write_text("v +2.5 1e-400 -0\nv 1 2 3x\nv .5 5. 1E+2\nf 1 2 3\n")
+    m = T.read_mesh(str(ok))
+    np.testing.assert_array_equal(m.vertices, np.array([[2.5, 0, -0.0], [1, 2, 3], [0.5, 5, 100]], np.float32))
+    assert np.signbit(m.vertices[0, 2])
+    for i, bad in enumerate(("v inf 0 0", "v nan 0 0", "v 1e 0 0", "v 1e+ 0 0", "v +-1 0 0", "v 1e400 0 0",
+                             "v 1.5e3x 2 3")):
+        path = tmp_path / ("bad%d.obj" % i)
+        path.write_text(bad + "\n")
+        with pytest.raises(TheaError, match="vertex position"):
+            T.read_mesh(str(path))
+    # OFF counts and indices as std::istream >> long long: '+' accepted, overflow rejected
+    off = tmp_path / "plus.off"
+    off.write_text("OFF\n+3 +1 0\n0 0 0\n1 0 0\n0 1 0\n3 +0 1 2\n")
+    assert T.read_mesh(str(off)).triangles.tolist() == [[0, 1, 2]]
+    big = tmp_path / "big.off"
+    big.write_text("OFF\n99999999999999999999 1 0\n")
+    with pytest.raises(TheaError, match="statistics"):
+        T.read_mesh(str(big))

@@ -10,14 +10,14 @@
 #include "mesh_io.hpp"
 
 #include <algorithm>
+#include <charconv>
+#include <cstdlib>
 #include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
-#include <iterator>
-#include <map>
 #include <sstream>
 
 namespace thea {
@@ -186,12 +186,92 @@ struct Input {
   }
 };
 
+bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\n' || c == '\f' || c == '\v'; }
+
+// A line of the file as [b, e) with surrounding white space removed (no copy)
+struct Span {
+  char const * b;
+  char const * e;
+  bool empty() const { return b == e; }
+  size_t size() const { return (size_t)(e - b); }
+  char operator[](size_t i) const { return b[i]; }
+  std::string str() const { return std::string(b, e); }
+};
+
+Span next_line(Input & in) {
+  char const * base = in.data.data();
+  size_t stop = in.data.find('\n', in.pos);
+  char const * b = base + in.pos;
+  char const * e = base + (stop == std::string::npos ? in.data.size() : stop);
+  in.pos = stop == std::string::npos ? in.data.size() : stop + 1;
+  while (b < e && is_space(*b)) ++b;
+  while (e > b && is_space(e[-1])) --e;
+  return Span{b, e};
+}
+
+// Successive reads from a line with the semantics of std::istream extraction (operator>> of long long and double,
+// get, peek) for the inputs a mesh file holds: numbers skip leading white space and take the longest valid prefix;
+// a read that fails leaves the scan failed. Doubles are correctly rounded (std::from_chars, as strtod); a lone or
+// incomplete exponent, "inf" and "nan" fail as they do for a stream, and an underflow gives the rounded value.
+struct Scan {
+  char const * p;
+  char const * e;
+  bool good = true;
+  Scan(char const * b, char const * end) : p(b), e(end) {}
+  explicit Scan(Span s) : p(s.b), e(s.e) {}
+
+  void skip_ws() {
+    while (p < e && is_space(*p)) ++p;
+  }
+  int get() { return p < e ? (unsigned char)*p++ : -1; }
+  int peek() const { return p < e ? (unsigned char)*p : -1; }
+
+  bool read(long long & v) {
+    if (!good) return false;
+    skip_ws();
+    char const * b = p;
+    if (b < e && *b == '+') {
+      ++b;
+      if (b == e || *b < '0' || *b > '9') return good = false;
+    }
+    auto r = std::from_chars(b, e, v);
+    if (r.ec != std::errc()) return good = false;
+    p = r.ptr;
+    return true;
+  }
+
+  bool read(double & v) {
+    if (!good) return false;
+    skip_ws();
+    char const * b = p;
+    if (b < e && *b == '+') {
+      ++b;
+      if (b < e && (*b == '+' || *b == '-')) return good = false;
+    }
+    char const * m = b < e && *b == '-' ? b + 1 : b;
+    if (m < e && ((*m | 0x20) == 'i' || (*m | 0x20) == 'n')) return good = false;  // no inf / nan
+    auto r = std::from_chars(b, e, v);
+    if (r.ec == std::errc::invalid_argument) return good = false;
+    bool has_exp = false;
+    for (char const * c = b; c < r.ptr; ++c) has_exp |= (*c | 0x20) == 'e';
+    if (!has_exp && r.ptr < e && (*r.ptr | 0x20) == 'e') return good = false;  // "1e", "1e+": an incomplete exponent
+    if (r.ec == std::errc::result_out_of_range) {
+      std::string tok(b, r.ptr);
+      double w = std::strtod(tok.c_str(), nullptr);
+      if (w == HUGE_VAL || w == -HUGE_VAL) return good = false;  // overflow fails; underflow gives the rounded value
+      v = w;
+    }
+    p = r.ptr;
+    return true;
+  }
+};
+
 // The next line that is neither blank nor a comment (the OFF reader's loop)
-std::string off_data_line(Input & in) {
-  std::string line = trim(in.line());
+Span off_data_line(Input & in) {
+  Span line = next_line(in);
   while (line.empty() || line[0] == '#') {
     if (!in.has_more()) fail(in.path, "unexpected end of input");
-    line = trim(in.line());
+    line = next_line(in);
   }
   return line;
 }
@@ -200,6 +280,8 @@ std::string off_data_line(Input & in) {
 struct SubmeshBuilder {
   MeshData & m;
   int64_t first_vertex, first_triangle, faces_before;
+  std::vector<float> pos;      // scratch: the positions of the face being triangulated
+  std::vector<int32_t> local;  // scratch: its triangles in local indices
 
   explicit SubmeshBuilder(MeshData & m_)
       : m(m_), first_vertex((int64_t)m_.vertices.size() / 3), first_triangle((int64_t)m_.triangle_face.size()),
@@ -216,10 +298,16 @@ struct SubmeshBuilder {
   void add_face(std::vector<int32_t> const & face, int32_t src_face) {
     int n = (int)face.size();
     if (n < 3) return;
-    std::vector<float> pos((size_t)3 * n);
+    if (n == 3) {  // DisplayMesh::addTriangle
+      for (int k = 0; k < 3; ++k) m.triangles.push_back((int32_t)first_vertex + face[(size_t)k]);
+      m.triangle_face.push_back(src_face);
+      ++m.num_faces;
+      return;
+    }
+    pos.resize((size_t)3 * n);
     for (int i = 0; i < n; ++i)
       for (int c = 0; c < 3; ++c) pos[(size_t)3 * i + c] = m.vertices[(size_t)(3 * (first_vertex + face[(size_t)i]) + c)];
-    std::vector<int32_t> local;
+    local.clear();
     int nt = triangulate_face(pos.data(), n, local);
     if (nt <= 0) return;
     for (int t = 0; t < nt; ++t) {
@@ -245,28 +333,29 @@ struct SubmeshBuilder {
 
 MeshData read_off_ascii(Input & in) {
   MeshData m;
-  std::istringstream counts(off_data_line(in));
+  Scan counts(off_data_line(in));
   long long nv = 0, nf = 0, ne = 0;
-  if (!(counts >> nv >> nf >> ne)) fail(in.path, "could not read the mesh statistics");
+  if (!(counts.read(nv) && counts.read(nf) && counts.read(ne))) fail(in.path, "could not read the mesh statistics");
   if (nv <= 0) return m;
   SubmeshBuilder b(m);
+  m.vertices.reserve((size_t)std::min<long long>(nv, 1 << 26) * 3);
   for (long long v = 0; v < nv; ++v) {
-    std::istringstream vs(off_data_line(in));
+    Scan vs(off_data_line(in));
     double x, y, z;
-    if (!(vs >> x >> y >> z)) fail(in.path, "could not read a vertex");
+    if (!(vs.read(x) && vs.read(y) && vs.read(z))) fail(in.path, "could not read a vertex");
     b.add_vertex((float)x, (float)y, (float)z, (int32_t)v);
   }
   std::vector<int32_t> face;
   for (long long f = 0; f < nf; ++f) {
-    std::istringstream fs(off_data_line(in));
+    Scan fs(off_data_line(in));
     long long k = 0;
-    if (!(fs >> k)) fail(in.path, "could not read the number of vertices of a face");
+    if (!fs.read(k)) fail(in.path, "could not read the number of vertices of a face");
     if (k <= 0) continue;
     face.clear();
     bool skip = false;
     for (long long v = 0; v < k && !skip; ++v) {
       long long index;
-      if (!(fs >> index) || index < 0 || index >= nv) {
+      if (!fs.read(index) || index < 0 || index >= nv) {
         skip = true;  // unreadable or out of range: the face is skipped
         break;
       }
@@ -329,23 +418,46 @@ MeshData read_off(Input & in) {
 
 using VTN = std::array<long long, 3>;  // 1-based vertex, texcoord, normal (0: none), compared lexicographically
 
-// Adds one OBJ submesh: its vertices are the distinct VTN references of its faces in sorted order
+// Adds one OBJ submesh: its vertices are the distinct VTN references of its faces in ascending order (the reference
+// collects them in a sorted map). `mark` is scratch of one entry per file vertex, all -1 between calls.
 void construct_obj_submesh(MeshData & m, std::vector<float> const & positions, std::vector<VTN> const & refs,
-                           std::vector<size_t> const & face_starts, int64_t & num_faces) {
-  std::map<VTN, int32_t> local;
-  for (VTN const & r : refs) local.emplace(r, 0);
+                           std::vector<size_t> const & face_starts, int64_t & num_faces, std::vector<int32_t> & mark) {
   SubmeshBuilder b(m);
-  int32_t next = 0;
-  for (auto & kv : local) {
-    size_t p = (size_t)(kv.first[0] - 1);
-    b.add_vertex(positions[3 * p], positions[3 * p + 1], positions[3 * p + 2], (int32_t)p);
-    kv.second = next++;
+  std::vector<int32_t> local(refs.size());
+  bool plain = std::all_of(refs.begin(), refs.end(), [](VTN const & r) { return r[1] == 0 && r[2] == 0; });
+  if (plain) {
+    // references by vertex only: the distinct vertices in ascending order, then a lookup through `mark`
+    std::vector<int32_t> used;
+    for (VTN const & r : refs) {
+      int32_t v = (int32_t)(r[0] - 1);
+      if (mark[(size_t)v] < 0) {
+        mark[(size_t)v] = 0;
+        used.push_back(v);
+      }
+    }
+    std::sort(used.begin(), used.end());
+    for (size_t i = 0; i < used.size(); ++i) {
+      size_t q = (size_t)used[i];
+      mark[q] = (int32_t)i;
+      b.add_vertex(positions[3 * q], positions[3 * q + 1], positions[3 * q + 2], (int32_t)q);
+    }
+    for (size_t j = 0; j < refs.size(); ++j) local[j] = mark[(size_t)(refs[j][0] - 1)];
+    for (int32_t v : used) mark[(size_t)v] = -1;
+  } else {
+    std::vector<VTN> keys(refs);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    for (VTN const & k : keys) {
+      size_t q = (size_t)(k[0] - 1);
+      b.add_vertex(positions[3 * q], positions[3 * q + 1], positions[3 * q + 2], (int32_t)q);
+    }
+    for (size_t j = 0; j < refs.size(); ++j)
+      local[j] = (int32_t)(std::lower_bound(keys.begin(), keys.end(), refs[j]) - keys.begin());
   }
   std::vector<int32_t> face;
   for (size_t i = 0; i < face_starts.size(); ++i) {
     size_t e = i + 1 < face_starts.size() ? face_starts[i + 1] : refs.size();
-    face.clear();
-    for (size_t j = face_starts[i]; j < e; ++j) face.push_back(local[refs[j]]);
+    face.assign(local.begin() + (std::ptrdiff_t)face_starts[i], local.begin() + (std::ptrdiff_t)e);
     b.add_face(face, (int32_t)num_faces);
     ++num_faces;  // every face is numbered, including those the triangulation drops
   }
@@ -358,26 +470,34 @@ MeshData read_obj(Input & in) {
   long long num_tex = 0, num_nrm = 0;
   std::vector<VTN> refs;          // references of the current submesh's faces, concatenated
   std::vector<size_t> face_starts;
+  std::vector<int32_t> mark;
   int64_t num_faces = 0;
+  auto flush = [&]() {
+    if (face_starts.empty()) return;
+    mark.resize(positions.size() / 3, -1);
+    construct_obj_submesh(m, positions, refs, face_starts, num_faces, mark);
+  };
   while (in.has_more()) {
-    std::string line = trim(in.line());
+    Span line = next_line(in);
     if (line.empty()) continue;
     char c0 = line[0];
     if (c0 == 'v' && line.size() >= 2) {
       if (line[1] == 't') {
-        std::istringstream vs(line.substr(2));
+        Scan vs(line.b + 2, line.e);
         double x, y;
-        if (!(vs >> x >> y)) fail(in.path, "could not read a texture coordinate on line '" + line + "'");
+        if (!(vs.read(x) && vs.read(y)))
+          fail(in.path, "could not read a texture coordinate on line '" + line.str() + "'");
         ++num_tex;
       } else if (line[1] == 'n') {
-        std::istringstream vs(line.substr(2));
+        Scan vs(line.b + 2, line.e);
         double x, y, z;
-        if (!(vs >> x >> y >> z)) fail(in.path, "could not read a normal on line '" + line + "'");
+        if (!(vs.read(x) && vs.read(y) && vs.read(z))) fail(in.path, "could not read a normal on line '" + line.str() + "'");
         ++num_nrm;
       } else if (line[1] == ' ' || line[1] == '\t') {
-        std::istringstream vs(line.substr(1));
+        Scan vs(line.b + 1, line.e);
         double x, y, z;
-        if (!(vs >> x >> y >> z)) fail(in.path, "could not read a vertex position on line '" + line + "'");
+        if (!(vs.read(x) && vs.read(y) && vs.read(z)))
+          fail(in.path, "could not read a vertex position on line '" + line.str() + "'");
         positions.push_back((float)x);
         positions.push_back((float)y);
         positions.push_back((float)z);
@@ -385,21 +505,24 @@ MeshData read_obj(Input & in) {
     } else if ((c0 == 'f' || c0 == 'p') && line.size() >= 2 && (line[1] == ' ' || line[1] == '\t')) {
       size_t start = refs.size();
       long long nvtx = (long long)(positions.size() / 3);
-      size_t b = line.find_first_not_of("fp \t");
-      if (b == std::string::npos) fail(in.path, "malformed face '" + line + "'");
+      // fields start after the leading run of 'f', 'p', spaces and tabs, and are separated by spaces and tabs
+      char const * fb = line.b;
+      while (fb < line.e && (*fb == 'f' || *fb == 'p' || *fb == ' ' || *fb == '\t')) ++fb;
+      if (fb == line.e) fail(in.path, "malformed face '" + line.str() + "'");
       bool bad_face = false;
-      for (size_t e = 0; e != std::string::npos;) {
-        e = line.find_first_of(" \t", b);
-        std::istringstream fs(line.substr(b, e == std::string::npos ? std::string::npos : e - b));
+      while (fb < line.e) {
+        char const * fe = fb;
+        while (fe < line.e && *fe != ' ' && *fe != '\t') ++fe;
+        Scan fs(fb, fe);
         VTN r{0, 0, 0};
-        bool bad = !(fs >> r[0]);
+        bool bad = !fs.read(r[0]);
         if (!bad && fs.get() == '/') {
           if (fs.peek() == '/') {
             fs.get();
-            bad = !(fs >> r[2]);
+            bad = !fs.read(r[2]);
           } else {
-            bad = !(fs >> r[1]);
-            if (!bad && fs.get() == '/') bad = !(fs >> r[2]);
+            bad = !fs.read(r[1]);
+            if (!bad && fs.get() == '/') bad = !fs.read(r[2]);
           }
         }
         if (bad || std::llabs(r[0]) < 1 || std::llabs(r[0]) > nvtx) {
@@ -412,19 +535,20 @@ MeshData read_obj(Input & in) {
         if (r[1] < 0) r[1] = num_tex + 1 + r[1];
         if (r[2] < 0) r[2] = num_nrm + 1 + r[2];
         refs.push_back(r);
-        if (e != std::string::npos) b = line.find_first_not_of(" \t", e);
+        fb = fe;
+        while (fb < line.e && (*fb == ' ' || *fb == '\t')) ++fb;
       }
       if (bad_face)
         refs.resize(start);  // the non-strict reader drops the face
       else
         face_starts.push_back(start);
     } else if ((c0 == 'g' || c0 == 'o') && (line.size() < 2 || line[1] == ' ' || line[1] == '\t')) {
-      if (!face_starts.empty()) construct_obj_submesh(m, positions, refs, face_starts, num_faces);
+      flush();
       refs.clear();
       face_starts.clear();
     }
   }
-  if (!face_starts.empty()) construct_obj_submesh(m, positions, refs, face_starts, num_faces);
+  flush();
   return m;
 }
 
@@ -592,25 +716,26 @@ MeshData read_ply(Input & in) {
     check_ply_block(blk, in.path);
     for (long long e = 0; e < blk.count; ++e) {
       if (!h.binary) {
-        std::string line;
+        Span line;
         do {
           if (!in.has_more()) fail(in.path, "unexpected end of input");
-          line = trim(in.line());
-        } while (line.empty() || line.rfind("comment", 0) == 0);
-        std::istringstream ls(line);
+          line = next_line(in);
+        } while (line.empty() || (line.size() >= 7 && std::memcmp(line.b, "comment", 7) == 0));
+        Scan ls(line);
         if (blk.kind == PlyElement::VERTEX) {
           double x, y, z;
-          if (!(ls >> x >> y >> z)) fail(in.path, "could not read vertex on line '" + line + "'");
+          if (!(ls.read(x) && ls.read(y) && ls.read(z)))
+            fail(in.path, "could not read vertex on line '" + line.str() + "'");
           b.add_vertex((float)x, (float)y, (float)z, (int32_t)nv++);
         } else if (blk.kind == PlyElement::FACE) {
           long long k;
-          if (!(ls >> k)) fail(in.path, "could not read number of vertices in face on line '" + line + "'");
+          if (!ls.read(k)) fail(in.path, "could not read number of vertices in face on line '" + line.str() + "'");
           if (k <= 0) continue;
           idx.clear();
           long long v;
           bool readable = true;
           for (long long j = 0; j < k && readable; ++j) {
-            readable = (bool)(ls >> v);
+            readable = ls.read(v);
             idx.push_back(v);
           }
           if (readable && add_checked_face(b, idx, nv, nf)) ++nf;
@@ -681,7 +806,12 @@ MeshData read_mesh_file(std::string const & path) {
   if (!f) fail(path, "cannot open the file");
   Input in;
   in.path = path;
-  in.data.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  f.seekg(0, std::ios::end);
+  std::streamoff size = f.tellg();
+  f.seekg(0, std::ios::beg);
+  if (size < 0) fail(path, "cannot read the file");
+  in.data.resize((size_t)size);
+  if (size > 0 && !f.read(&in.data[0], size)) fail(path, "cannot read the file");
   return obj ? read_obj(in) : off ? read_off(in) : read_ply(in);
 }
 
