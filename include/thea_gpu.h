@@ -272,6 +272,9 @@ typedef struct thea_mesh_info {
  * list, and elements of other kinds, are skipped as the header describes them (the reference's binary reader cannot
  * read such files). The 3DS codec (which needs lib3ds) is not built: THEA_ERR_INVALID_ARGUMENT. */
 THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh);
+/* The same readers on a file's bytes in host memory, with the codec named ("obj", "off" or "ply"): MeshGroup::read
+ * from a BinaryInputStream with an explicit codec (Graphics/MeshGroup.hpp:324-352). */
+THEA_API thea_status thea_mesh_read_buffer(const void * data, int64_t bytes, const char * codec, thea_mesh ** out_mesh);
 THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info);
 /* Copies the arrays to host buffers (each nullable): vertices (3 x num_vertices floats), vertex_source (file vertex index
  * of each vertex, 0-based), triangles (3 x num_triangles indices into vertices), triangle_face (source face index of each

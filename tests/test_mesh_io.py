@@ -433,3 +433,19 @@ def test_number_syntax_follows_stream_extraction(T, tmp_path):
     big.write_text("OFF\n99999999999999999999 1 0\n")
     with pytest.raises(TheaError, match="statistics"):
         T.read_mesh(str(big))
+
+
+def test_read_from_memory(T, tmp_path):
+    path = tmp_path / "m.obj"
+    path.write_text(OBJ_TEXT)
+    a = T.read_mesh(str(path))
+    b = T.read_mesh(OBJ_TEXT.encode(), codec="obj")
+    np.testing.assert_array_equal(a.triangles, b.triangles)
+    np.testing.assert_array_equal(a.vertices, b.vertices)
+    c = T.read_mesh(PLY_ASCII.encode(), codec="PLY")
+    assert len(c.triangles) == 6
+    from thea_gb300 import TheaError
+    with pytest.raises(TheaError, match="unknown codec"):
+        T.read_mesh(b"x", codec="stl")
+    with pytest.raises(ValueError):
+        T.read_mesh(b"x")

@@ -113,6 +113,7 @@ SIGNATURES = {
     "thea_bvh_k_closest_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int32, ctypes.c_float, _vp, _vp, _vp,
                                                 ctypes.POINTER(ctypes.c_int32), _vp]),
     "thea_mesh_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "thea_mesh_read_buffer": (ctypes.c_int, [_vp, _i64, ctypes.c_char_p, ctypes.POINTER(_vp)]),
     "thea_mesh_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(MeshInfo)]),
     "thea_mesh_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "thea_mesh_destroy": (ctypes.c_int, [_vp]),

@@ -574,11 +574,18 @@ class MeshData:
         self.num_faces = num_faces
 
 
-def read_mesh(path):
-    """Reads an OFF, OBJ or PLY file into host arrays (MeshData)."""
+def read_mesh(path, codec=None):
+    """Reads an OFF, OBJ or PLY file into host arrays (MeshData). ``path`` may also be the file's bytes, with
+    ``codec`` ("obj", "off" or "ply") naming the format."""
     lib = N.lib()
     h = ctypes.c_void_p()
-    N.check(lib.thea_mesh_read(str(path).encode(), ctypes.byref(h)))
+    if isinstance(path, (bytes, bytearray, memoryview)):
+        if codec is None:
+            raise ValueError("read_mesh: a byte buffer needs codec='obj', 'off' or 'ply'")
+        buf = bytes(path)
+        N.check(lib.thea_mesh_read_buffer(buf, len(buf), str(codec).encode(), ctypes.byref(h)))
+    else:
+        N.check(lib.thea_mesh_read(str(path).encode(), ctypes.byref(h)))
     try:
         inf = N.MeshInfo()
         N.check(lib.thea_mesh_get_info(h, ctypes.byref(inf)))

@@ -1295,6 +1295,16 @@ THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh) {
   });
 }
 
+THEA_API thea_status thea_mesh_read_buffer(const void * data, int64_t bytes, const char * codec, thea_mesh ** out_mesh) {
+  return guarded([&] {
+    THEA_REQUIRE(out_mesh, "mesh_read_buffer: null output");
+    *out_mesh = nullptr;
+    THEA_REQUIRE(codec && bytes >= 0 && (data || bytes == 0), "mesh_read_buffer: null or negative argument");
+    thea::MeshData m = thea::read_mesh_buffer(data, bytes, codec);
+    *out_mesh = reinterpret_cast<thea_mesh *>(new thea::MeshData(std::move(m)));
+  });
+}
+
 THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info) {
   return guarded([&] {
     THEA_REQUIRE(mesh && info, "mesh_get_info: null argument");

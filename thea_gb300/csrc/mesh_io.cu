@@ -815,4 +815,14 @@ MeshData read_mesh_file(std::string const & path) {
   return obj ? read_obj(in) : off ? read_off(in) : read_ply(in);
 }
 
+MeshData read_mesh_buffer(void const * data, int64_t bytes, std::string const & codec) {
+  std::string c = codec;
+  for (char & ch : c) ch = (char)std::tolower((unsigned char)ch);
+  if (c != "obj" && c != "off" && c != "ply") fail("<buffer>", "unknown codec '" + codec + "' (obj, off or ply)");
+  Input in;
+  in.path = "<buffer>";
+  if (bytes > 0) in.data.assign(static_cast<char const *>(data), (size_t)bytes);
+  return c == "obj" ? read_obj(in) : c == "off" ? read_off(in) : read_ply(in);
+}
+
 }  // namespace thea

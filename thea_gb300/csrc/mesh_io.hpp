@@ -30,4 +30,7 @@ int triangulate_face(float const * pos, int n, std::vector<int32_t> & tris);
 // (THEA_ERR_INVALID_ARGUMENT) where the reference's non-strict readers throw; faces they skip are skipped.
 MeshData read_mesh_file(std::string const & path);
 
+// The same readers on a file's bytes in memory (MeshGroup::read with an explicit codec): codec "obj", "off" or "ply".
+MeshData read_mesh_buffer(void const * data, int64_t bytes, std::string const & codec);
+
 }  // namespace thea
