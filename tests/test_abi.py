@@ -172,3 +172,11 @@ def test_bvh_images_are_checked_before_any_device_call(lib):
     for cls in (MeshBvh, PointBvh):
         with pytest.raises(N.TheaError):
             cls.from_bytes(b"")
+
+
+def test_every_entry_point_is_documented():
+    """INTEGRATION.md's table names every function the header declares, with the reference interface it replaces."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [s for s in declared_symbols() if "`%s`" % s not in doc and s + "`" not in doc
+               and s.replace("thea_server_", "") not in doc]
+    assert not missing, missing
