@@ -4,7 +4,9 @@ Some callers cannot allocate device memory themselves or let a library do it: an
 device budget through its own pool, a plugin inside such a host, or a latency-critical loop that cannot take cudaMalloc's
 implicit synchronization. This entry point keeps its scratch in a fixed array inside the library, and these tests check
 that it returns exactly what the ordinary entry point returns, on two calls in a row (the second call must not see
-leftovers of the first), and that it refuses what it cannot do without allocating.
+leftovers of the first), that it allocates nothing (the library's allocation counter and the device's free memory),
+that it refuses out-of-range face indices without reading through them, and that it refuses what it cannot do without
+allocating.
 
 The file name makes pytest collect it last, so a run that stops at the first failure has already run every other test.
 """
@@ -79,6 +81,62 @@ def test_noalloc_matches_sample_by_area_twice_in_a_row(lib):
     refc = _sample(N, L.thea_sample_by_area, V1, F1, 5000, 13, N.RNG_COUNTER)
     newc = _sample(N, L.thea_sample_by_area_noalloc, V1, F1, 5000, 13, N.RNG_COUNTER)
     _check_same(refc, newc)
+
+
+def test_noalloc_allocates_nothing(lib):
+    """The library's allocation counter (driver and pool allocations) and the device's free memory stay unchanged across
+    the call, in a fresh process or after other tests; the ordinary entry point, as a control, does allocate."""
+    import torch
+    N = lib
+    L = N.lib()
+    V, F, _ = W.config0()
+    V, F = torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda()
+    n = 150000
+    pos = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    face = torch.empty((n,), dtype=torch.int32, device="cuda")
+    got = ctypes.c_int64(-1)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = (_ptr(V), V.shape[0], _ptr(F), F.shape[0], n, ctypes.c_uint32(5), N.RNG_THEA_MT, _ptr(pos), None,
+            _ptr(face), ctypes.byref(got), stream)
+    N.check(L.thea_sample_by_area_noalloc(*args))  # first call on the device: looks up the fixed array's address
+    torch.cuda.synchronize()
+    for _ in range(2):
+        count0 = L.thea_allocation_count()
+        free0, _ = torch.cuda.mem_get_info()
+        N.check(L.thea_sample_by_area_noalloc(*args))
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert L.thea_allocation_count() == count0
+        assert free1 == free0
+        assert got.value == n
+    count0 = L.thea_allocation_count()
+    N.check(L.thea_sample_by_area(*args))
+    torch.cuda.synchronize()
+    assert L.thea_allocation_count() > count0
+
+
+def test_noalloc_rejects_out_of_range_face_indices(lib):
+    """A face index outside [0, num_vertices) is found on the device without being dereferenced and refused; the next
+    call with a valid mesh is unaffected."""
+    import torch
+    N = lib
+    L = N.lib()
+    V, F = W.noisy_icosphere(2, 15)
+    Vd = torch.from_numpy(V).cuda()
+    out = torch.empty((100, 3), dtype=torch.float32, device="cuda")
+    got = ctypes.c_int64(-1)
+    for bad in (len(V), -1, 1 << 30):
+        Fb = F.copy()
+        Fb[len(F) // 2, 1] = bad
+        Fd = torch.from_numpy(Fb).cuda()
+        st = L.thea_sample_by_area_noalloc(_ptr(Vd), len(V), _ptr(Fd), len(F), 100, 1, N.RNG_THEA_MT, _ptr(out), None,
+                                           None, ctypes.byref(got), None)
+        assert st == N.THEA_ERR_INVALID_ARGUMENT and b"face index" in L.thea_last_error_message()
+        assert got.value == 0
+    Fd = torch.from_numpy(F).cuda()
+    N.check(L.thea_sample_by_area_noalloc(_ptr(Vd), len(V), _ptr(Fd), len(F), 100, 1, N.RNG_THEA_MT, _ptr(out), None,
+                                          None, ctypes.byref(got), None))
+    assert got.value == 100
 
 
 def test_noalloc_refuses_what_needs_an_allocation(lib):

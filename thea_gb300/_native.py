@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "THEA_OK", 1: "THEA_ERR_INVALID_ARGUMENT", 2: "THEA_ERR_OUT_O
 THEA_ERR_INVALID_ARGUMENT = 1
 THEA_ERR_ADMISSION_REFUSED = 3
 THEA_ERR_DEVICE_TIMEOUT = 4
+THEA_ERR_INTERNAL = 6
 THEA_ERR_CANCELLED = 8
 THEA_ERR_WAIT_TIMEOUT = 9
 
@@ -94,6 +95,7 @@ SIGNATURES = {
     "thea_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "thea_last_error_message": (ctypes.c_char_p, []),
     "thea_launch_count": (ctypes.c_int64, []),
+    "thea_allocation_count": (ctypes.c_int64, []),
     "thea_profiling_enable": (ctypes.c_int, [ctypes.c_int]),
     "thea_profiling_reset": (ctypes.c_int, []),
     "thea_profiling_read": (ctypes.c_int, [ctypes.c_char_p, _f64p, _i64p]),
@@ -150,6 +152,7 @@ SIGNATURES = {
     "thea_k_closest_self_ex": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "thea_radius_neighbors": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp]),
     "thea_selftest_bounded_wait": (ctypes.c_int, [_i32, _vp]),
+    "thea_selftest_set_error_bits": (ctypes.c_int, [_vp, ctypes.c_uint32, _vp]),
     "thea_point_gram_tile": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp]),
     "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "thea_server_destroy": (ctypes.c_int, [_vp]),

@@ -13,6 +13,7 @@
 #include "mesh_io.hpp"
 #include "shape_diameter.hpp"
 #include "pairs.hpp"
+#include "traverse.cuh"
 
 #include <initializer_list>
 #include <algorithm>
@@ -33,6 +34,9 @@ namespace thea {
 //============================================================================================================================
 
 static std::atomic<int64_t> g_launches{0};
+static std::atomic<int64_t> g_allocations{0};
+
+void note_allocation() { g_allocations.fetch_add(1, std::memory_order_relaxed); }
 static std::atomic<bool> g_profiling{false};
 
 struct TimedLaunch {
@@ -115,6 +119,60 @@ template <class F> static thea_status guarded(F && f) {
 }
 
 //============================================================================================================================
+// Device error bits -> status
+//
+// Query kernels raise bits in their handle's device error word (a traversal stack that would overflow, a tensor-core
+// wait that gave up). Every query call ends by copying the word into the handle's pinned host mirror on its stream. A
+// call that synchronizes (host arrays) then reads the mirror before it returns; every call first reads what earlier,
+// asynchronous calls left there. Bits are reported once: the call that reports them clears the word and the mirror.
+//============================================================================================================================
+
+static thread_local bool t_synced = false;  // set by a query call that synchronized its stream
+
+static void sync_stream(cudaStream_t s) {
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  t_synced = true;
+}
+
+// Takes the bits the mirror holds (clearing the mirror and, on the stream, the device word).
+static unsigned take_device_errors(thea_bvh const * b, cudaStream_t s) {
+  if (!b || !b->err_host) return 0;
+  unsigned bits = *(volatile unsigned *)b->err_host;
+  if (!bits) return 0;
+  *(volatile unsigned *)b->err_host = 0;
+  THEA_CUDA_CHECK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), s));
+  return bits;
+}
+
+static void raise_device_errors(unsigned bits) {
+  if (!bits) return;
+  if (bits & ERR_STACK_OVERFLOW)
+    throw Error(THEA_ERR_INTERNAL, "a traversal stack overflowed on this BVH: results of the calls since the last "
+                                   "report may miss elements");
+  throw Error(THEA_ERR_DEVICE_TIMEOUT, "a tensor-core wait gave up on this BVH; the affected queries were answered by "
+                                       "the plain search (results are exact)");
+}
+
+// Runs a query call on handle b and reports device error bits: those earlier asynchronous calls left in the mirror, and
+// those of this call when it synchronized. The call's own work runs (and writes its results) either way.
+template <class F> static thea_status guarded_query(thea_bvh const * b, void * stream, F && f) {
+  return guarded([&] {
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned bits = take_device_errors(b, s);
+    t_synced = false;
+    f();
+    if (b && b->err_host) {
+      THEA_CUDA_CHECK(cudaMemcpyAsync(b->err_host, b->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      if (t_synced) {
+        THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+        bits |= take_device_errors(b, s);
+      }
+    }
+    raise_device_errors(bits);
+  });
+}
+
+//============================================================================================================================
 // Host-pointer staging
 //============================================================================================================================
 
@@ -127,6 +185,22 @@ static bool is_host_pointer(void const * p) {
     return true;
   }
   return !(a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged);
+}
+
+// True for device memory of the current device and for managed memory; false for host memory and for device memory
+// of another GPU (a kernel on this device would fault on it unless peer access happens to be enabled).
+static bool is_device_memory_here(void const * p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  if (a.type != cudaMemoryTypeDevice) return false;
+  int dev = -1;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  return a.device == dev;
 }
 
 // Device-usable addresses of caller arrays that are all pinned host memory (null entries are skipped); false if any
@@ -192,6 +266,7 @@ template <class Fn> static void run_staged(std::vector<IoArray> arrays, int64_t 
     return;
   }
   if (n <= 0) return;
+  t_synced = true;
   int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)((64u << 20) / host_bytes)));
   // four chunks: enough to overlap copies with kernels, few enough that kernel tails stay small (measured on the
   // 4.2 M-ray heightfield: 2 / 4 / 8 / 16 chunks gave 2,549 / 2,634 / 2,254 / 1,688 M rays/s end to end)
@@ -310,6 +385,8 @@ THEA_API const char * thea_last_error_message(void) { return g_error.c_str(); }
 
 THEA_API int64_t thea_launch_count(void) { return g_launches.load(); }
 
+THEA_API int64_t thea_allocation_count(void) { return g_allocations.load(); }
+
 THEA_API thea_status thea_profiling_enable(int enable) {
   g_profiling.store(enable != 0);
   return THEA_OK;
@@ -367,7 +444,7 @@ THEA_API thea_status thea_mesh_bvh_build(const float * vertices, int64_t num_ver
     DeviceView V(vertices, (size_t)num_vertices * 3 * sizeof(float), s);
     DeviceView F(faces, (size_t)num_faces * 3 * sizeof(int32_t), s);
     *out_bvh = build_bvh(true, (float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, num_faces, cfg, s);
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
   });
 }
 
@@ -385,7 +462,7 @@ THEA_API thea_status thea_point_bvh_build(const float * points, int64_t num_poin
     cudaStream_t s = (cudaStream_t)stream;
     DeviceView P(points, (size_t)num_points * 3 * sizeof(float), s);
     *out_bvh = build_bvh(false, (float const *)P.ptr, num_points, nullptr, 0, cfg, s);
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
   });
 }
 
@@ -502,7 +579,7 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
     c2.budget = 256;  // the step budget of the device-resident two-phase path
     run_closest_stream(mesh_bvh, (float const *)dp[0], num_queries, c2, (int32_t *)dp[1], (float *)dp[2],
                        (float *)dp[3], (cudaStream_t)stream);
-    THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    sync_stream((cudaStream_t)stream);
     return;
   }
   run_staged({{(void *)queries, 12, false, false}, {out_index, 4, true, false}, {out_distance, 4, true, false},
@@ -535,7 +612,7 @@ static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const flo
       pinned_host_views({origins, directions, out_time, out_index}, dp)) {
     run_ray_stream(mesh_bvh, (float const *)dp[0], (float const *)dp[1], num_rays, rp.max_time, (float *)dp[2],
                    (int32_t *)dp[3], err, (cudaStream_t)stream);
-    THEA_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    sync_stream((cudaStream_t)stream);
     return;
   }
   run_staged({{(void *)origins, 12, false, false}, {(void *)directions, 12, false, false}, {out_time, 4, true, false},
@@ -562,7 +639,7 @@ static void ray_impl(const thea_bvh * mesh_bvh, const float * origins, const flo
 THEA_API thea_status thea_closest_element(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
                                           float dist_bound, int32_t * out_index, float * out_distance,
                                           float * out_closest_point, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     closest_impl(mesh_bvh, queries, num_queries, dist_bound, THEA_PRECISION_FP32_REFERENCE, out_index, out_distance,
                  out_closest_point, nullptr, stream);
   });
@@ -572,7 +649,7 @@ THEA_API thea_status thea_closest_element_ex(const thea_bvh * mesh_bvh, const fl
                                              float dist_bound, int32_t precision, int32_t * out_index,
                                              float * out_distance, float * out_closest_point, float * out_error,
                                              void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     closest_impl(mesh_bvh, queries, num_queries, dist_bound, precision, out_index, out_distance, out_closest_point,
                  out_error, stream);
   });
@@ -581,7 +658,7 @@ THEA_API thea_status thea_closest_element_ex(const thea_bvh * mesh_bvh, const fl
 THEA_API thea_status thea_ray_intersection(const thea_bvh * mesh_bvh, const float * origins, const float * directions,
                                            int64_t num_rays, float max_time, float * out_time, int32_t * out_index,
                                            float * out_normal, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     ray_impl(mesh_bvh, origins, directions, num_rays, max_time, THEA_PRECISION_FP32_REFERENCE, out_time, out_index,
              out_normal, nullptr, nullptr, nullptr, stream);
   });
@@ -592,7 +669,7 @@ THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const f
                                               int32_t precision, float * out_time, int32_t * out_index,
                                               float * out_normal, float * out_time_fp64, int32_t * out_index_fp64,
                                               int32_t * out_flags, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     ray_impl(mesh_bvh, origins, directions, num_rays, max_time, precision, out_time, out_index, out_normal,
              out_time_fp64, out_index_fp64, out_flags, stream);
   });
@@ -600,7 +677,7 @@ THEA_API thea_status thea_ray_intersection_ex(const thea_bvh * mesh_bvh, const f
 
 THEA_API thea_status thea_ray_intersects(const thea_bvh * mesh_bvh, const float * origins, const float * directions,
                                          int64_t num_rays, float max_time, uint8_t * out_hit, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "ray_intersects: a mesh BVH is required");
     THEA_REQUIRE(mesh_bvh->ray_rec, "ray_intersects: the BVH was built without THEA_LAYOUT_RAY");
     THEA_REQUIRE(num_rays >= 0, "ray_intersects: negative ray count");
@@ -625,7 +702,7 @@ THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * ou
       Scratch d((size_t)count * 12, s);
       run_random_sphere(seed, count, d.as<float>(), s);
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_directions, d.ptr, (size_t)count * 12, cudaMemcpyDeviceToHost, s));
-      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      sync_stream(s);
     } else {
       run_random_sphere(seed, count, out_directions, s);
     }
@@ -634,7 +711,7 @@ THEA_API thea_status thea_random_sphere(uint32_t seed, int64_t count, float * ou
 
 THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * positions, int64_t num_points,
                                      int32_t num_rays, uint32_t seed, double * out_fraction, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh, "visibility: a mesh BVH is required");
     THEA_REQUIRE(mesh_bvh->ray_rec, "visibility: the BVH was built without THEA_LAYOUT_RAY");
     THEA_REQUIRE(num_points >= 0, "visibility: negative point count");
@@ -659,7 +736,7 @@ THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * po
     run_visibility(mesh_bvh, pos, num_points, num_rays, seed, out, s);
     if (host_out) {
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_fraction, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
-      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      sync_stream(s);
     }
   });
 }
@@ -700,7 +777,7 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
       std::vector<int32_t> deg(n);
       THEA_CUDA_CHECK(cudaMemcpyAsync(sep.data(), o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaMemcpyAsync(deg.data(), o.degree, n * 4, cudaMemcpyDeviceToHost, s));
-      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      sync_stream(s);
       float avg = 0.f;
       int64_t edges = 0;
       for (size_t i = 0; i < n; ++i) {
@@ -711,14 +788,14 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
       out_avg_separation[0] = o.avg_separation_estimate;
       out_avg_separation[1] = avg;
     }
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
   });
 }
 
 THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * queries, int64_t num_queries, int32_t k,
                                     float dist_bound, const int32_t * exclude_index, int32_t * out_index,
                                     float * out_sq_distance, void * stream) {
-  return guarded([&] {
+  return guarded_query(point_bvh, stream, [&] {
     THEA_REQUIRE(point_bvh, "k_closest: null BVH");
     THEA_REQUIRE(point_bvh->num_segments == 1, "k_closest: forests take thea_batch_k_closest");
     THEA_REQUIRE(!point_bvh->is_mesh || query_target(point_bvh)->cp_rec,
@@ -768,13 +845,13 @@ static void knn_self_impl(const thea_bvh * point_bvh, int32_t k, int32_t candida
   run_knn(point_bvh, nullptr, n, k, INFINITY, nullptr, pi, pd, err, s, ib);
   if (hi) THEA_CUDA_CHECK(cudaMemcpyAsync(out_index, pi, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
   if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, pd, (size_t)n * k * 4, cudaMemcpyDeviceToHost, s));
-  if (hi || hd) THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (hi || hd) sync_stream(s);
 }
 
 THEA_API thea_status thea_radius_neighbors(const thea_bvh * point_bvh, const float * queries, int64_t num_queries,
                                            float radius, const int32_t * exclude_index, int64_t * out_offsets,
                                            int32_t * out_index, float * out_sq_distance, void * stream) {
-  return guarded([&] {
+  return guarded_query(point_bvh, stream, [&] {
     THEA_REQUIRE(point_bvh && !point_bvh->is_mesh, "radius_neighbors: a point BVH is required");
     THEA_REQUIRE(num_queries >= 0, "radius_neighbors: negative query count");
     THEA_REQUIRE(radius >= 0.f, "radius_neighbors: negative or NaN radius");
@@ -801,16 +878,29 @@ THEA_API thea_status thea_selftest_bounded_wait(int32_t spin_limit, void * strea
   return g != THEA_OK ? g : r;
 }
 
+THEA_API thea_status thea_selftest_set_error_bits(thea_bvh * bvh, uint32_t bits, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(bvh, "selftest_set_error_bits: null handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned cur = 0;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&cur, bvh->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    cur |= bits;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(bvh->err, &cur, sizeof(unsigned), cudaMemcpyHostToDevice, s));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
 THEA_API thea_status thea_k_closest_self(const thea_bvh * point_bvh, int32_t k, int32_t * out_index,
                                          float * out_sq_distance, void * stream) {
-  return guarded([&] {
+  return guarded_query(point_bvh, stream, [&] {
     knn_self_impl(point_bvh, k, THEA_KNN_CANDIDATES_TRAVERSAL, out_index, out_sq_distance, stream);
   });
 }
 
 THEA_API thea_status thea_k_closest_self_ex(const thea_bvh * point_bvh, int32_t k, int32_t candidates,
                                             int32_t * out_index, float * out_sq_distance, void * stream) {
-  return guarded([&] { knn_self_impl(point_bvh, k, candidates, out_index, out_sq_distance, stream); });
+  return guarded_query(point_bvh, stream, [&] { knn_self_impl(point_bvh, k, candidates, out_index, out_sq_distance, stream); });
 }
 
 THEA_API thea_status thea_point_gram_tile(const float * a, int32_t num_a, const float * b, int32_t num_b,
@@ -859,7 +949,7 @@ THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_ver
                                      seed, rng, (float *)o[0].ptr, (float *)o[1].ptr, (int32_t *)o[2].ptr, s);
     for (auto & x : o)
       if (x.dev.ptr && got > 0) THEA_CUDA_CHECK(cudaMemcpyAsync(x.user, x.ptr, x.bytes, cudaMemcpyDeviceToHost, s));
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
     if (out_num_written) *out_num_written = got;
   });
 }
@@ -886,7 +976,7 @@ THEA_API thea_status thea_mesh_forest_build(const float * vertices, int64_t num_
     DeviceView F(faces, (size_t)nf * 3 * sizeof(int32_t), s);
     *out_forest = build_forest(true, (float const *)V.ptr, num_vertices, (int32_t const *)F.ptr, nf, mesh_face_offsets,
                                num_meshes, cfg, s);
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
   });
 }
 
@@ -906,7 +996,7 @@ THEA_API thea_status thea_point_forest_build(const float * points, const int64_t
     cudaStream_t s = (cudaStream_t)stream;
     DeviceView P(points, (size_t)n * 3 * sizeof(float), s);
     *out_forest = build_forest(false, (float const *)P.ptr, n, nullptr, n, set_offsets, num_sets, cfg, s);
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
   });
 }
 
@@ -929,7 +1019,7 @@ THEA_API thea_status thea_batch_closest_element(const thea_bvh * mesh_forest, co
                                                 int32_t precision, int32_t queries_per_warp, int32_t hard_query_budget,
                                                 int32_t * out_index, float * out_distance, float * out_closest_point,
                                                 float * out_error, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_forest, stream, [&] {
     int chunk = check_batch_common(mesh_forest, query_offsets, num_queries, queries_per_warp,
                                    {queries, out_index, out_distance, out_closest_point, out_error},
                                    "batch_closest_element");
@@ -954,7 +1044,7 @@ THEA_API thea_status thea_batch_ray_intersection(const thea_bvh * mesh_forest, c
                                                  const float * directions, const int64_t * query_offsets,
                                                  int64_t num_rays, float max_time, int32_t queries_per_warp,
                                                  float * out_time, int32_t * out_index, void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_forest, stream, [&] {
     int chunk = check_batch_common(mesh_forest, query_offsets, num_rays, queries_per_warp,
                                    {origins, directions, out_time, out_index}, "batch_ray_intersection");
     THEA_REQUIRE(mesh_forest->is_mesh && mesh_forest->ray_rec,
@@ -970,7 +1060,7 @@ THEA_API thea_status thea_batch_k_closest(const thea_bvh * point_forest, const f
                                           const int64_t * query_offsets, int64_t num_queries, int32_t k,
                                           float dist_bound, int32_t queries_per_warp, int32_t * out_index,
                                           float * out_sq_distance, void * stream) {
-  return guarded([&] {
+  return guarded_query(point_forest, stream, [&] {
     int chunk = check_batch_common(point_forest, query_offsets, num_queries, queries_per_warp,
                                    {queries, out_index, out_sq_distance}, "batch_k_closest");
     THEA_REQUIRE(!point_forest->is_mesh, "batch_k_closest: a point forest is required");
@@ -1124,7 +1214,8 @@ THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t
     THEA_REQUIRE(out_positions, "sample_by_area_noalloc: out_positions is null");
     void const * arrays[5] = {vertices, faces, out_positions, out_normals, out_faces};
     for (void const * p : arrays)
-      THEA_REQUIRE(!p || !is_host_pointer(p), "sample_by_area_noalloc: every array must be device memory");
+      THEA_REQUIRE(!p || is_device_memory_here(p),
+                   "sample_by_area_noalloc: every array must be device memory of the current device");
     int64_t got = run_sample_by_area_noalloc(vertices, num_vertices, faces, num_faces, num_samples, seed, rng,
                                              out_positions, out_normals, out_faces, (cudaStream_t)stream);
     if (out_num_written) *out_num_written = got;
@@ -1209,7 +1300,7 @@ THEA_API thea_status thea_server_reset_stats(thea_server * server) {
 THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float * positions, const float * normals,
                                          int64_t num_points, float scale, int32_t only_interior, double * out_sdf,
                                          void * stream) {
-  return guarded([&] {
+  return guarded_query(mesh_bvh, stream, [&] {
     THEA_REQUIRE(mesh_bvh && mesh_bvh->is_mesh && mesh_bvh->num_segments == 1,
                  "shape_diameter: a mesh BVH (not a forest) is required");
     THEA_REQUIRE(mesh_bvh->ray_rec, "shape_diameter: the BVH was built without THEA_LAYOUT_RAY");
@@ -1242,7 +1333,7 @@ THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float 
     run_shape_diameter(mesh_bvh, pos, nrm, num_points, scale, only_interior != 0, out, s);
     if (host_out) {
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_sdf, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
-      THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      sync_stream(s);
     }
   });
 }
@@ -1251,7 +1342,7 @@ THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_b
                                            int32_t * out_query_index, int32_t * out_target_index,
                                            float * out_sq_distance, float * out_query_point, float * out_target_point,
                                            void * stream) {
-  return guarded([&] {
+  return guarded_query(target, stream, [&] {
     THEA_REQUIRE(out_query_index && out_target_index, "closest_pair: null output");
     *out_query_index = *out_target_index = -1;
     if (out_sq_distance) *out_sq_distance = -1.f;
@@ -1268,7 +1359,7 @@ THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_b
 THEA_API thea_status thea_bvh_k_closest_pairs(const thea_bvh * target, const thea_bvh * query, int32_t k,
                                               float dist_bound, int32_t * out_query_index, int32_t * out_target_index,
                                               float * out_sq_distance, int32_t * out_count, void * stream) {
-  return guarded([&] {
+  return guarded_query(target, stream, [&] {
     THEA_REQUIRE(out_query_index && out_target_index && out_sq_distance, "k_closest_pairs: null output");
     THEA_REQUIRE(k >= 1 && k <= 32, "k_closest_pairs: k must be in 1..32");
     cudaStream_t s = (cudaStream_t)stream;
@@ -1280,7 +1371,7 @@ THEA_API thea_status thea_bvh_k_closest_pairs(const thea_bvh * target, const the
     THEA_CUDA_CHECK(cudaMemcpyAsync(out_query_index, qi, (size_t)k * 4, cudaMemcpyDefault, s));
     THEA_CUDA_CHECK(cudaMemcpyAsync(out_target_index, ti, (size_t)k * 4, cudaMemcpyDefault, s));
     THEA_CUDA_CHECK(cudaMemcpyAsync(out_sq_distance, d2, (size_t)k * 4, cudaMemcpyDefault, s));
-    THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+    sync_stream(s);
     if (out_count) *out_count = (int32_t)c;
   });
 }

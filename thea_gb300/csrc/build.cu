@@ -137,6 +137,16 @@ __global__ void elem_box_kernel(float const * __restrict__ V, int32_t const * __
   }
 }
 
+// Sets *bad when any of the 3 * nf face indices lies outside [0, nv).
+__global__ void face_range_kernel(int32_t const * __restrict__ F, int64_t count, int64_t nv, int * __restrict__ bad) {
+  bool out = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t f = F[i];
+    out |= f < 0 || (int64_t)f >= nv;
+  }
+  if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
 __global__ void init_bounds_kernel(int * __restrict__ bounds, int M) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 12 * (int64_t)M) return;
@@ -514,8 +524,8 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
   int64_t cap = (int64_t)num_small + (int64_t)std::max<unsigned long long>(nbig, 1);
 
   WideNode<W> * nodes = nullptr;
-  THEA_CUDA_CHECK(cudaMallocAsync((void **)&nodes, (size_t)cap * sizeof(WideNode<W>), stream));
-  THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->seg_root, (size_t)M * sizeof(int32_t), stream));
+  THEA_CUDA_CHECK(thea_malloc_async((void **)&nodes, (size_t)cap * sizeof(WideNode<W>), stream));
+  THEA_CUDA_CHECK(thea_malloc_async((void **)&b->seg_root, (size_t)M * sizeof(int32_t), stream));
   Scratch fa((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream), fb((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   THEA_LAUNCH((segment_roots_kernel<W>), (unsigned)ceil_div(M, BUILD_THREADS), BUILD_THREADS, 0, stream, a, n,
               is_small.as<int>(), small_rank.as<int>(), is_big.as<int>(), big_rank.as<int>(), num_small, d_bounds,
@@ -578,6 +588,8 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     starts = {0, n};
   }
 
+  if (is_mesh) check_face_indices(F, n_elems, nv, "build", stream);
+
   thea_bvh * b = new thea_bvh;
   try {
     THEA_CUDA_CHECK(cudaGetDevice(&b->device));
@@ -590,7 +602,7 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     b->num_segments = M;
     b->seg_start_host = starts;
 
-    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->seg_start, (size_t)(M + 1) * sizeof(int64_t), stream));
+    THEA_CUDA_CHECK(thea_malloc_async((void **)&b->seg_start, (size_t)(M + 1) * sizeof(int64_t), stream));
     THEA_CUDA_CHECK(cudaMemcpyAsync(b->seg_start, starts.data(), (size_t)(M + 1) * sizeof(int64_t),
                                     cudaMemcpyHostToDevice, stream));
     int64_t const * seg = b->seg_start;
@@ -641,23 +653,25 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     if (need > (width == 4 ? 256 : 512))
       throw Error(THEA_ERR_NOT_SUPPORTED, "build: tree too deep for the traversal stack (depth " +
                                               std::to_string(b->depth) + ")");
-    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->err, sizeof(unsigned), stream));
+    THEA_CUDA_CHECK(thea_malloc_async((void **)&b->err, sizeof(unsigned), stream));
     THEA_CUDA_CHECK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), stream));
-    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->leaf_to_elem, (size_t)n * sizeof(int32_t), stream));
+    THEA_CUDA_CHECK(thea_malloc_host(&b->err_host, sizeof(unsigned)));
+    *b->err_host = 0;
+    THEA_CUDA_CHECK(thea_malloc_async((void **)&b->leaf_to_elem, (size_t)n * sizeof(int32_t), stream));
     int64_t rec_bytes = n * (int64_t)sizeof(int32_t);
     if (is_mesh) {
       if (layouts & THEA_LAYOUT_CLOSEST) {
-        THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->cp_rec, (size_t)n * CP_REC_F4 * sizeof(float4), stream));
+        THEA_CUDA_CHECK(thea_malloc_async((void **)&b->cp_rec, (size_t)n * CP_REC_F4 * sizeof(float4), stream));
         rec_bytes += n * CP_REC_F4 * (int64_t)sizeof(float4);
       }
       if (layouts & THEA_LAYOUT_RAY) {
-        THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->ray_rec, (size_t)n * RAY_REC_F4 * sizeof(float4), stream));
+        THEA_CUDA_CHECK(thea_malloc_async((void **)&b->ray_rec, (size_t)n * RAY_REC_F4 * sizeof(float4), stream));
         rec_bytes += n * RAY_REC_F4 * (int64_t)sizeof(float4);
       }
       THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, seg, M, vals.as<uint32_t>(),
                   b->cp_rec, b->ray_rec, b->leaf_to_elem);
     } else {
-      THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
+      THEA_CUDA_CHECK(thea_malloc_async((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
       rec_bytes += n * (int64_t)sizeof(float4);
       THEA_LAUNCH(point_records_kernel, grid, BUILD_THREADS, 0, stream, V, n, seg, M, vals.as<uint32_t>(), b->pt_rec,
                   b->leaf_to_elem);
@@ -689,6 +703,19 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
   }
 }
 
+void check_face_indices(int32_t const * F, int64_t nf, int64_t nv, char const * what, cudaStream_t stream) {
+  if (nf <= 0) return;
+  Scratch bad(sizeof(int), stream);
+  THEA_CUDA_CHECK(cudaMemsetAsync(bad.ptr, 0, sizeof(int), stream));
+  int64_t count = 3 * nf;
+  unsigned grid = (unsigned)std::min<int64_t>(ceil_div(count, BUILD_THREADS), 152 * 8);
+  THEA_LAUNCH(face_range_kernel, grid, BUILD_THREADS, 0, stream, F, count, nv, bad.as<int>());
+  int h = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&h, bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+  THEA_REQUIRE(h == 0, std::string(what) + ": a face index lies outside [0, num_vertices)");
+}
+
 thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t nf,
                      thea_build_config const & cfg, cudaStream_t stream) {
   return build_forest(is_mesh, V, nv, F, nf, nullptr, 1, cfg, stream);
@@ -711,6 +738,7 @@ void destroy_bvh(thea_bvh * b) {
   if (b->pt_rec) cudaFree(b->pt_rec);
   if (b->leaf_to_elem) cudaFree(b->leaf_to_elem);
   if (b->err) cudaFree(b->err);
+  if (b->err_host) cudaFreeHost(b->err_host);
   if (b->seg_start) cudaFree(b->seg_start);
   if (b->seg_root) cudaFree(b->seg_root);
   if (prev >= 0) cudaSetDevice(prev);

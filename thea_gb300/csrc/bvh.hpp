@@ -22,6 +22,7 @@ struct thea_bvh {
   float4 * pt_rec = nullptr;       // point records, 1 per element, leaf order
   int32_t * leaf_to_elem = nullptr;  // leaf-order position -> element index
   unsigned * err = nullptr;          // device word: error bits raised by query kernels
+  unsigned * err_host = nullptr;     // pinned host mirror of *err, refreshed at the end of every query call
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   int64_t device_bytes = 0;
   // forest of one BVH per segment (one segment for a single mesh / point set)
@@ -47,5 +48,9 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
 thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t n_elems,
                         int64_t const * seg_start_host, int M, thea_build_config const & cfg, cudaStream_t stream);
 void destroy_bvh(thea_bvh * b);
+
+// Throws INVALID_ARGUMENT unless every face index lies in [0, nv): checked on the device before any kernel loads a
+// vertex through the faces (one pass over F and one 4-byte read back, which synchronizes `stream`).
+void check_face_indices(int32_t const * F, int64_t nf, int64_t nv, char const * what, cudaStream_t stream);
 
 }  // namespace thea

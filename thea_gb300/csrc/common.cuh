@@ -47,6 +47,25 @@ struct Error : public std::runtime_error {
 void note_launch(char const * kernel_name, cudaStream_t stream, cudaEvent_t * begin_event);
 void note_launch_end(char const * kernel_name, cudaStream_t stream, cudaEvent_t begin_event);
 
+// Counts every device or pinned-host allocation the library makes (driver or pool); the allocators below go through it.
+void note_allocation();
+template <class T> inline cudaError_t thea_malloc(T ** p, size_t n) {
+  note_allocation();
+  return cudaMalloc((void **)p, n);
+}
+template <class T> inline cudaError_t thea_malloc_host(T ** p, size_t n) {
+  note_allocation();
+  return cudaMallocHost((void **)p, n);
+}
+template <class T> inline cudaError_t thea_malloc_async(T ** p, size_t n, cudaStream_t s) {
+  note_allocation();
+  return cudaMallocAsync((void **)p, n, s);
+}
+template <class T> inline cudaError_t thea_malloc_from_pool_async(T ** p, size_t n, cudaMemPool_t pool, cudaStream_t s) {
+  note_allocation();
+  return cudaMallocFromPoolAsync((void **)p, n, pool, s);
+}
+
 struct LaunchScope {
   char const * name;
   cudaStream_t stream;

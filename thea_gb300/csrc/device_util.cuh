@@ -38,7 +38,7 @@ struct Scratch {
   cudaStream_t stream = nullptr;
   Scratch() {}
   Scratch(size_t n, cudaStream_t s) : bytes(n), stream(s) {
-    if (n) THEA_CUDA_CHECK(cudaMallocFromPoolAsync(&ptr, n, scratch_pool(), s));
+    if (n) THEA_CUDA_CHECK(thea_malloc_from_pool_async(&ptr, n, scratch_pool(), s));
   }
   Scratch(Scratch const &) = delete;
   Scratch & operator=(Scratch const &) = delete;

@@ -11,6 +11,7 @@
 // so word N - M keeps its value), then all 624 words are tempered and written out. The counter mode draws the three
 // words of sample i from Philox-4x32-10 (Salmon et al., SC'11) keyed by the seed, which is fully parallel.
 #include "device_util.cuh"
+#include "bvh.hpp"
 #include "query.hpp"
 
 #include <climits>
@@ -321,23 +322,34 @@ struct NoAllocLayout {
   double cum[THEA_NOALLOC_MAX_FACES];
   uint32_t mt_state[MT_N];
   uint32_t words[3 * NOALLOC_CHUNK];
+  int32_t bad_face;  // written by every noalloc_cdf_kernel launch: 1 if a face index lies outside [0, nv)
 };
 
 // Per-face areas computed in place (the same tri_plane arithmetic as tri_area_kernel) and summed in index order by one
-// thread, exactly as serial_cdf_kernel does; no separate area array is needed.
-__global__ void noalloc_cdf_kernel(float const * __restrict__ V, int32_t const * __restrict__ F, int64_t nf,
-                                   double * __restrict__ cum) {
+// thread, exactly as serial_cdf_kernel does; no separate area array is needed. A face with an index outside [0, nv) is
+// not loaded: it sets *bad_face (the caller then refuses the call) and counts as zero area.
+__global__ void noalloc_cdf_kernel(float const * __restrict__ V, int64_t nv, int32_t const * __restrict__ F,
+                                   int64_t nf, double * __restrict__ cum, int32_t * __restrict__ bad_face) {
   constexpr int CH = 2048;
   __shared__ float a[CH];
   __shared__ double c[CH];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   double run = 0.0;
   for (int64_t base = 0; base < nf; base += CH) {
     int m = (nf - base) < CH ? (int)(nf - base) : CH;
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
       int64_t f = base + j;
-      V3 v0 = load_v3(V + 3 * (int64_t)F[3 * f]);
-      V3 v1 = load_v3(V + 3 * (int64_t)F[3 * f + 1]);
-      V3 v2 = load_v3(V + 3 * (int64_t)F[3 * f + 2]);
+      int32_t i0 = F[3 * f], i1 = F[3 * f + 1], i2 = F[3 * f + 2];
+      if (i0 < 0 || i1 < 0 || i2 < 0 || (int64_t)i0 >= nv || (int64_t)i1 >= nv || (int64_t)i2 >= nv) {
+        bad = 1;
+        a[j] = 0.f;
+        continue;
+      }
+      V3 v0 = load_v3(V + 3 * (int64_t)i0);
+      V3 v1 = load_v3(V + 3 * (int64_t)i1);
+      V3 v2 = load_v3(V + 3 * (int64_t)i2);
       a[j] = tri_plane(v0, v1, v2).area;
     }
     __syncthreads();
@@ -351,6 +363,7 @@ __global__ void noalloc_cdf_kernel(float const * __restrict__ V, int32_t const *
     for (int j = threadIdx.x; j < m; j += blockDim.x) cum[base + j] = c[j];
     __syncthreads();
   }
+  if (threadIdx.x == 0) *bad_face = bad;
 }
 
 // Resumable form of thea_mt_stream_kernel: seeds the state when `first` is set, otherwise continues from `state`, and
@@ -422,16 +435,18 @@ static NoAllocLayout * noalloc_scratch() {
 
 int64_t run_sample_by_area_noalloc(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n,
                                    uint32_t seed, int rng, float * pos, float * nrm, int32_t * face, cudaStream_t s) {
-  (void)nv;
   THEA_REQUIRE(nf <= THEA_NOALLOC_MAX_FACES,
                "sample_by_area_noalloc: at most " + std::to_string((long long)THEA_NOALLOC_MAX_FACES) +
                    " triangles (got " + std::to_string((long long)nf) + ")");
   NoAllocLayout * scratch = noalloc_scratch();
   if (n <= 0 || nf <= 0) return 0;
-  THEA_LAUNCH(noalloc_cdf_kernel, 1, 256, 0, s, V, F, nf, scratch->cum);
+  THEA_LAUNCH(noalloc_cdf_kernel, 1, 256, 0, s, V, nv, F, nf, scratch->cum, &scratch->bad_face);
   double total = 0.0;
+  int32_t bad = 0;
   THEA_CUDA_CHECK(cudaMemcpyAsync(&total, scratch->cum + nf - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&bad, &scratch->bad_face, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  THEA_REQUIRE(!bad, "sample_by_area_noalloc: a face index lies outside [0, num_vertices)");
   if (!(total > 0.0)) return 0;
   if (rng == THEA_RNG_COUNTER) {
     THEA_LAUNCH(sample_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, V, F, nf, (double const *)scratch->cum,
@@ -456,8 +471,8 @@ void run_thea_random_words(uint32_t seed, int64_t count, uint32_t * out, cudaStr
 
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
                            float * pos, float * nrm, int32_t * face, cudaStream_t s) {
-  (void)nv;
   if (n <= 0 || nf <= 0) return 0;
+  check_face_indices(F, nf, nv, "sample_by_area", s);
   Scratch area((size_t)nf * sizeof(float), s);
   Scratch cum((size_t)nf * sizeof(double), s);
   THEA_LAUNCH(tri_area_kernel, (unsigned)ceil_div(nf, 256), 256, 0, s, V, F, nf, area.as<float>());

@@ -135,7 +135,7 @@ thea_bvh * deserialize_bvh(void const * in, int64_t bytes, cudaStream_t s) {
     char const * p = (char const *)in + sizeof(h);
     auto h2d = [&](void ** dst, int64_t nbytes) {
       if (nbytes > 0) {
-        THEA_CUDA_CHECK(cudaMallocAsync(dst, (size_t)nbytes, s));
+        THEA_CUDA_CHECK(thea_malloc_async(dst, (size_t)nbytes, s));
         THEA_CUDA_CHECK(cudaMemcpyAsync(*dst, p, (size_t)nbytes, cudaMemcpyHostToDevice, s));
       }
       p += nbytes;
@@ -156,8 +156,10 @@ thea_bvh * deserialize_bvh(void const * in, int64_t bytes, cudaStream_t s) {
     std::memcpy(b->seg_lo.data(), p, (size_t)M * 12);
     p += (int64_t)M * 12;
     std::memcpy(b->seg_hi.data(), p, (size_t)M * 12);
-    THEA_CUDA_CHECK(cudaMallocAsync((void **)&b->err, sizeof(unsigned), s));
+    THEA_CUDA_CHECK(thea_malloc_async((void **)&b->err, sizeof(unsigned), s));
     THEA_CUDA_CHECK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), s));
+    THEA_CUDA_CHECK(thea_malloc_host(&b->err_host, sizeof(unsigned)));
+    *b->err_host = 0;
     // the host image may be reused by the caller as soon as this returns
     THEA_CUDA_CHECK(cudaStreamSynchronize(s));
     if (h.has_transform) set_transform(b, h.xf, s);

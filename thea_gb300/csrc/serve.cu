@@ -482,7 +482,7 @@ void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *>
     t.k = r.k;
     char * stg = nullptr;
     if (p.bytes) {
-      THEA_CUDA_CHECK(cudaMallocFromPoolAsync(&p.staging, (size_t)p.bytes, scratch_pool(), st));
+      THEA_CUDA_CHECK(thea_malloc_from_pool_async(&p.staging, (size_t)p.bytes, scratch_pool(), st));
       stg = (char *)p.staging;
     }
     // staging layout per piece: inputs (12 B, ray 24 B per query), then outputs
@@ -712,11 +712,11 @@ thea_server * server_create(thea_server_config const & c) {
     s->owner = sv.get();
     if (!cfg.test_executor) {
       THEA_CUDA_CHECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-      THEA_CUDA_CHECK(cudaMalloc(&s->d_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
-      THEA_CUDA_CHECK(cudaMallocHost(&s->h_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
-      THEA_CUDA_CHECK(cudaMalloc(&s->d_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
-      THEA_CUDA_CHECK(cudaMallocHost(&s->h_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
-      THEA_CUDA_CHECK(cudaMalloc(&s->d_counters, 5 * sizeof(unsigned long long)));
+      THEA_CUDA_CHECK(thea_malloc(&s->d_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
+      THEA_CUDA_CHECK(thea_malloc_host(&s->h_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
+      THEA_CUDA_CHECK(thea_malloc(&s->d_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
+      THEA_CUDA_CHECK(thea_malloc_host(&s->h_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
+      THEA_CUDA_CHECK(thea_malloc(&s->d_counters, 5 * sizeof(unsigned long long)));
     }
     sv->slots.push_back(std::move(s));
   }
@@ -786,12 +786,12 @@ int32_t server_add_mesh(thea_server * sv, float const * V, int64_t nv, int32_t c
     void * tv = nullptr, * tf = nullptr;
     try {
       if (host_memory(V)) {
-        THEA_CUDA_CHECK(cudaMalloc(&tv, (size_t)nv * 12));
+        THEA_CUDA_CHECK(thea_malloc(&tv, (size_t)nv * 12));
         THEA_CUDA_CHECK(cudaMemcpyAsync(tv, V, (size_t)nv * 12, cudaMemcpyHostToDevice, st));
         dV = (float const *)tv;
       }
       if (host_memory(F)) {
-        THEA_CUDA_CHECK(cudaMalloc(&tf, (size_t)nf * 12));
+        THEA_CUDA_CHECK(thea_malloc(&tf, (size_t)nf * 12));
         THEA_CUDA_CHECK(cudaMemcpyAsync(tf, F, (size_t)nf * 12, cudaMemcpyHostToDevice, st));
         dF = (int32_t const *)tf;
       }
