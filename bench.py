@@ -236,75 +236,123 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------------------------------------------
-# CPU baseline (oracle restatement of the reference path; test infrastructure used only as the baseline here)
+# CPU baseline: the reference's algorithm on the host cores. The oracle restates the reference's kd-tree and traversals
+# (reference tie order); the timed build is compiled with the reference's release flags (-std=c++17 -O2 -DNDEBUG
+# -fno-strict-aliasing) and nothing else. One routine times every configuration, for the reference arm and for the
+# cpu_baseline legs alike: the whole workload in its own order, all host threads with a static partition of the queries
+# (a pass before the timed ones faults the tree and the inputs in), and one thread on an evenly strided sample.
+# Test infrastructure used here only as the measured baseline; the GPU path never calls it.
 # ---------------------------------------------------------------------------------------------------------------------
 
-def cpu_ray_baseline(V, F, o, d, target_s=12.0, threads=None):
+def host_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def _oracle():
     from oracle import oracle as O
     O.build()
-    threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    m = O.MeshIndex(V, F)
-    build_s = time.perf_counter() - t0
-    n = 16384
-    t0 = time.perf_counter()
-    m.ray_ref(o[:n], d[:n], threads=threads)
-    dt = time.perf_counter() - t0
-    rate = n / max(dt, 1e-6)
-    n2 = int(min(len(o), max(n, rate * target_s)))
-    sel = np.linspace(0, len(o) - 1, n2).astype(np.int64)
-    t0 = time.perf_counter()
-    m.ray_ref(o[sel], d[sel], threads=threads)
-    dt = time.perf_counter() - t0
-    # one core as well, on a smaller strided sample (the reference itself runs single-threaded)
-    n1 = int(min(len(o), max(4096, n2 // max(1, threads) // 4)))
-    sel1 = np.linspace(0, len(o) - 1, n1).astype(np.int64)
-    t0 = time.perf_counter()
-    m.ray_ref(o[sel1], d[sel1], threads=1)
-    dt1 = time.perf_counter() - t0
-    return {"value": n2 / dt / 1e6, "unit": "Mqueries/s", "cores": threads, "kind": "port",
-            "one_core_value": n1 / dt1 / 1e6, "one_core_sample": n1,
-            "sample": "%d of the %d rays (evenly strided), reference kd-tree and traversal restated in C++ (oracle), "
-                      "%d threads (and %d rays on one thread); kd-tree build %.2f s not included"
-                      % (n2, len(o), threads, n1, build_s)}
+    return O
+
+
+def _passes(run, passes, warmup):
+    for _ in range(warmup):
+        run()
+    out = []
+    for _ in range(passes):
+        t0 = time.perf_counter()
+        run()
+        out.append(time.perf_counter() - t0)
+    return out
+
+
+def cpu_workload(name, data):
+    """(count, run(threads), one-core count, run_one_core(), description) of one configuration's reference workload.
+    data: config 1 (V, F, o, d); config 0 (V, F, Q); config 2 (P,); config 3 a list of (V, F, Q) meshes."""
+    O = _oracle()
+    if name == "cfg1":
+        V, F, o, d = data
+        m = O.MeshIndex(V, F, timed=True)
+        o1, d1 = np.ascontiguousarray(o[::16]), np.ascontiguousarray(d[::16])
+        return (len(o), lambda th: m.ray_ref(o, d, threads=th), len(o1), lambda: m.ray_ref(o1, d1, threads=1),
+                "rayStructureIntersection over the reference kd-tree (leaf size 5), all %d rays in order" % len(o))
+    if name == "cfg0":
+        V, F, Q = data
+        m = O.MeshIndex(V, F, timed=True)
+        q1 = np.ascontiguousarray(Q[::16])
+        return (len(Q), lambda th: m.closest_ref(Q, threads=th), len(q1), lambda: m.closest_ref(q1, threads=1),
+                "closestElement over the reference kd-tree (leaf size 5), all %d queries in order" % len(Q))
+    if name == "cfg2":
+        (P,) = data
+        pi = O.PointIndex(P, timed=True)
+        ex = np.arange(len(P), dtype=np.int32)
+        p1, e1 = np.ascontiguousarray(P[::16]), np.ascontiguousarray(ex[::16])
+        return (len(P), lambda th: pi.knn_ref(P, 16, exclude=ex, threads=th), len(p1),
+                lambda: pi.knn_ref(p1, 16, exclude=e1, threads=1),
+                "kClosestPairs (k = 16, FilterSelf) over the reference kd-tree of the %d samples, every sample "
+                "queried" % len(P))
+    if name == "cfg3":
+        from concurrent.futures import ThreadPoolExecutor
+        idx = [O.MeshIndex(v, f, timed=True) for v, f, _ in data]
+        qs = [q for _, _, q in data]
+        n = sum(len(q) for q in qs)
+
+        def run(th):
+            # meshes handed out to the threads one at a time (each query batch single-threaded)
+            with ThreadPoolExecutor(th) as ex:
+                list(ex.map(lambda j: idx[j].closest_ref(qs[j], threads=1), range(len(idx))))
+
+        one = list(range(0, len(idx), 16))
+        n1 = sum(len(qs[j]) for j in one)
+        return (n, run, n1, lambda: [idx[j].closest_ref(qs[j], threads=1) for j in one],
+                "per mesh: the reference kd-tree and closestElement, %d meshes (%d queries) sampled evenly from the "
+                "batch" % (len(idx), n))
+    raise ValueError(name)
+
+
+def cpu_time(name, data, passes=1, warmup=1, threads=None, one_core=True):
+    """Times one configuration's reference workload: mean seconds of `passes` all-thread passes after `warmup`."""
+    threads = threads or host_threads()
+    n, run, n1, run1, what = cpu_workload(name, data)
+    ts = _passes(lambda: run(threads), passes, warmup)
+    res = {"value": n / statistics.mean(ts) / 1e6, "unit": "Mqueries/s", "cores": threads, "kind": "port",
+           "sample": what + "; %d thread(s), static partition; mean of %d pass(es) after %d untimed" %
+                     (threads, passes, warmup),
+           "seconds_per_pass": statistics.mean(ts), "build": "oracle/_build/liboracle_timed.so, reference flags"}
+    if one_core:
+        t1 = _passes(run1, 1, 0)[0]
+        res.update({"one_core_value": n1 / t1 / 1e6, "one_core_sample": "%d queries (every 16th) on one thread" % n1})
+    return res
 
 
 def reference_arm(args, rank, world):
     if rank != 0:
         return
-    from oracle import oracle as O
-    O.build()
     V, F, o, d = W.config1()
-    threads = os.cpu_count() or 1
-    m = O.MeshIndex(V, F)
-    n = 16384
-    t0 = time.perf_counter()
-    m.ray_ref(o[:n], d[:n], threads=threads)
-    rate = n / max(time.perf_counter() - t0, 1e-6)
-    # each step: a bounded sample sized to ~8 s of host work
-    per_step = int(min(len(o), max(n, rate * 8.0 / max(1, args.steps + args.warmup) * 2)))
-    rng = np.random.default_rng(0)
-    times = []
-    for s in range(args.warmup + args.steps):
-        sel = rng.choice(len(o), per_step, replace=False)
-        t0 = time.perf_counter()
-        m.ray_ref(o[sel], d[sel], threads=threads)
-        dt = time.perf_counter() - t0
-        if s >= args.warmup:
-            times.append(dt)
-    ms = 1000.0 * statistics.mean(times)
-    value = per_step / (ms / 1000.0) / 1e6
-    line = {"impl": "reference", "metric": "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)",
+    threads = host_threads()
+    n, run, _, _, what = cpu_workload("cfg1", (V, F, o, d))
+    ts = _passes(lambda: run(threads), args.steps, args.warmup)
+    ms = 1000.0 * statistics.mean(ts)
+    value = n / (ms / 1000.0) / 1e6
+    line = {"impl": "reference", "metric": HEADLINE_METRIC,
             "value": value, "unit": "Mqueries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
-            "config": {"workload": "ray_first_hit_heightfield_1024", "triangles": 2093058, "rays_per_step": per_step,
-                       "parallelism": "host threads"},
+            "data": "synthetic (seeded fBm heightfield and cosine rays)",
+            "config": headline_config(),
             "cpu_baseline": {"value": value, "unit": "Mqueries/s", "cores": threads, "kind": "port",
-                             "sample": "%d random rays of the 4,194,304 per step; reference kd-tree and traversal "
-                                       "restated in C++ (the reference needs Eigen, absent here)" % per_step},
+                             "sample": what + "; every step the whole workload, %d threads, static partition; the "
+                                              "reference's algorithm restated in C++ (the reference needs Eigen, "
+                                              "absent here), compiled with its release flags" % threads},
             "e2e": {"value": value, "unit": "Mqueries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+HEADLINE_METRIC = "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)"
+
+
+def headline_config():
+    """The workload both arms run (identical in the two JSON lines)."""
+    return {"workload": "ray_first_hit_heightfield_1024", "triangles": 2093058, "vertices": 1048576, "rays": RAYS,
+            "l2": "GPU arm: flushed by a 256 MB write before every timed step (host arm: no flush)"}
 
 
 # ---------------------------------------------------------------------------------------------------------------------
@@ -420,6 +468,13 @@ def gpu_arm(args, rank, world, local_rank):
     e2e_s = max_over_ranks(statistics.mean(e2e_times), dist, "cuda")
     assert np.array_equal(hi.numpy(), out_i.cpu().numpy()), "host and device paths disagree"
     hits = int((hi.numpy() >= 0).sum())
+    # parity of the timed results (the end-to-end call's) with the oracle, every ray: lowest index among equal times
+    parity = None
+    if rank == 0 and not args.no_cpu:
+        ot, oi = _oracle().MeshIndex(V, F).ray_contract(o, d)
+        parity = {"checked": RAYS, "indices_equal": bool(np.array_equal(hi.numpy(), oi)),
+                  "times_equal": bool(np.array_equal(ht.numpy(), ot.astype(np.float32))),
+                  "oracle": "reference kd-tree traversal restated, ties to the lowest index, FP32 arithmetic"}
 
     extra = {}
     if not args.no_extra:
@@ -450,18 +505,18 @@ def gpu_arm(args, rank, world, local_rank):
     if rank == 0:
         cpu = None
         if not args.no_cpu and world == 1:
-            cpu = cpu_ray_baseline(V, F, o, d)
+            cpu = cpu_time("cfg1", (V, F, o, d))
         traffic = ncu_traffic("ray_persistent_kernel")
         line = {
-            "metric": "Mqueries/s ray first-hit (config 1: 1024^2 heightfield, 4,194,304 rays)",
+            "metric": HEADLINE_METRIC,
             "value": value, "unit": "Mqueries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded fBm heightfield and cosine rays)",
-            "config": {"workload": "ray_first_hit_heightfield_1024", "triangles": 2093058, "vertices": 1048576,
-                       "rays": RAYS, "bvh_width": info["width"], "leaf_size": info["max_leaf_size"],
-                       "bvh_nodes": info["num_nodes"], "bvh_depth": info["depth"], "build_ms": build_ms,
-                       "hit_fraction": hits / RAYS, "l2": "flushed by a 256 MB write before every timed step",
-                       "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+            "config": headline_config(),
+            "details": {"bvh_width": info["width"], "leaf_size": info["max_leaf_size"], "bvh_nodes": info["num_nodes"],
+                        "bvh_depth": info["depth"], "build_ms": build_ms, "hit_fraction": hits / RAYS,
+                        "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+            "parity": parity,
             "e2e": {"value": world * RAYS / e2e_s / 1e6, "unit": "Mqueries/s", "h2d_bytes_per_step": RAYS * 24,
                     "d2h_bytes_per_step": RAYS * 8},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -527,6 +582,13 @@ def extra_workloads(T, torch, stream, flush, args):
                                         "d2h_bytes": 20 * CP_QUERIES, "same_as_device":
                                         bool(torch.equal(hi, bvh.closest_element(Qd)[0].cpu()))}
     bvh.close()
+    if not args.no_cpu:
+        out["closest_point_cfg0"]["cpu_baseline"] = cpu_time("cfg0", (V, F, Q))
+        oi, od2, ocp = _oracle().MeshIndex(V, F).closest_contract(Q)
+        out["closest_point_cfg0"]["parity"] = {
+            "checked": CP_QUERIES, "indices_equal": bool(np.array_equal(hi.numpy(), oi)),
+            "distances_equal": bool(np.array_equal(hd.numpy(), np.sqrt(od2.astype(np.float32)))),
+            "closest_points_equal": bool(np.array_equal(hc.numpy(), ocp.astype(np.float32)))}
     # config 2: 1,048,576 area samples of the config-0 mesh (reference Random stream), k = 16 graph excluding self
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -561,6 +623,14 @@ def extra_workloads(T, torch, stream, flush, args):
         "ms_per_step": statistics.mean(ms), "gram_kernel_ms": g_ms / max(1, g_cnt),
         "bounded_search_ms": k_ms / max(1, k_cnt), "tensor_flop_per_step": 2 * 16 * 512 * KNN_POINTS,
         "identical_to_traversal": bool(torch.equal(i0, i1) and torch.equal(d0, d1))}
+    if not args.no_cpu:
+        P = pos.cpu().numpy()
+        out["knn_graph_cfg2"]["cpu_baseline"] = cpu_time("cfg2", (P,))
+        ri, rd = _oracle().PointIndex(P).knn_contract(P, 16, exclude=np.arange(len(P), dtype=np.int32))
+        out["knn_graph_cfg2"]["parity"] = {"checked": KNN_POINTS, "k": 16,
+                                           "indices_equal": bool(np.array_equal(i0.cpu().numpy(), ri)),
+                                           "sq_distances_equal": bool(np.array_equal(d0.cpu().numpy(),
+                                                                                     rd.astype(np.float32)))}
     # closest pair and the 32 closest pairs between these samples and a second 1,048,576-sample set of the same mesh
     pos2, _, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), KNN_POINTS, 5)
     pb2 = T.PointBvh(pos2)
@@ -750,6 +820,7 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
     forest = T.MeshForest(V, F, foff, width=tune["width"], max_leaf_size=tune["max_leaf_size"], layouts=1)
     torch.cuda.synchronize()
     res["forest_build_s"] = time.perf_counter() - t0
+    results = {}
     for prec in ("fp32", "fp64"):
         out = (torch.empty(nq, dtype=torch.int32, device="cuda"), torch.empty(nq, dtype=torch.float32, device="cuda"),
                torch.empty((nq, 3), dtype=torch.float32, device="cuda"), None)
@@ -768,7 +839,36 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
         rel = (e / torch.clamp(d, min=1e-6 * float(Q.abs().max()))).max().item()
         res["batched_" + prec] = {"value": nq / (statistics.median(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
                                   "ms": statistics.median(ms), "max_rel_error_vs_fp64": rel}
+        results[prec] = (out[0].cpu().numpy(), out[1].cpu().numpy(), out[2].cpu().numpy())
     forest.close()
+    if not args.no_cpu:
+        # the reference's per-mesh CPU path on every 64th mesh, and parity of the batched results on those meshes
+        # (FP32 bit-exact against the oracle's lowest-index mode; FP64 re-check against the FP64 oracle)
+        O = _oracle()
+        meshes = []
+        for m in range(0, num_meshes, 64):
+            Fm = F[foff[m]:foff[m + 1]]
+            lo, hi = int(Fm.min()), int(Fm.max()) + 1
+            meshes.append((V[lo:hi].cpu().numpy(), (Fm - lo).cpu().numpy(), Q[qoff_h[m]:qoff_h[m + 1]].cpu().numpy()))
+        res["cpu_baseline"] = cpu_time("cfg3", meshes)
+        eq32 = eq64 = True
+        checked = 0
+        worst = 0.0
+        for j, (v, f, q) in enumerate(meshes):
+            s = slice(qoff_h[64 * j], qoff_h[64 * j + 1])
+            ri, rd2, rcp = O.MeshIndex(v, f).closest_contract(q)
+            oi, od2, _ = O.MeshIndex(v, f, fp64=True).closest_contract(q)
+            i32, d32, c32 = (x[s] for x in results["fp32"])
+            i64, d64 = results["fp64"][0][s], results["fp64"][1][s]
+            eq32 = eq32 and np.array_equal(i32, ri) and np.array_equal(d32, np.sqrt(rd2.astype(np.float32))) \
+                and np.array_equal(c32, rcp.astype(np.float32))
+            eq64 = eq64 and np.array_equal(i64, oi)
+            od = np.sqrt(od2)
+            worst = max(worst, float(np.max(np.abs(d64 - od) / np.maximum(od, 1e-30))))
+            checked += len(q)
+        res["parity"] = {"meshes_checked": len(meshes), "queries_checked": checked,
+                         "fp32_bit_exact": bool(eq32), "fp64_indices_equal_fp64_oracle": bool(eq64),
+                         "fp64_max_rel_distance_error_vs_fp64_oracle": worst}
     # the plain drop-in loop: per mesh, build its BVH and run one closest-element call (query time only is timed)
     t_build = 0.0
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(num_meshes)]

@@ -14,7 +14,11 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+# the same sources compiled with the reference's own release flags and nothing else (multiply-adds may fuse on hosts
+# that have them): the library the CPU-baseline timings use; results are not compared bit for bit
+_TIMED_PATH = os.path.join(_HERE, "_build", "liboracle_timed.so")
 _lib = None
+_timed = None
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -29,62 +33,73 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
-def lib():
-    global _lib
+def lib(timed=False):
+    """The parity build of the oracle, or with timed=True the build with the reference's release flags."""
+    global _lib, _timed
+    if timed:
+        if _timed is None:
+            if not os.path.exists(_TIMED_PATH):
+                build()
+            _timed = _declare(ctypes.CDLL(_TIMED_PATH))
+        return _timed
     if _lib is None:
         if not os.path.exists(_LIB_PATH):
             build()
-        L = ctypes.CDLL(_LIB_PATH)
-        L.oracle_mesh_create.restype = _vp
-        L.oracle_mesh_create.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_int]
-        L.oracle_mesh_destroy.argtypes = [_vp]
-        L.oracle_mesh_num_nodes.restype = _i64
-        L.oracle_mesh_num_nodes.argtypes = [_vp]
-        L.oracle_mesh_max_depth.restype = _i64
-        L.oracle_mesh_max_depth.argtypes = [_vp]
-        L.oracle_closest_ref.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f32p, ctypes.c_int]
-        L.oracle_closest_contract.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p, ctypes.c_int]
-        L.oracle_closest_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p,
-                                           ctypes.c_int, ctypes.c_int]
-        L.oracle_ray_ref.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, _f32p, _i32p, _f32p, ctypes.c_int]
-        L.oracle_ray_contract.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p, ctypes.c_int]
-        L.oracle_ray_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p,
-                                       ctypes.c_int, ctypes.c_int]
-        L.oracle_points_create.restype = _vp
-        L.oracle_points_create.argtypes = [_f32p, _i64, _i64, ctypes.c_int]
-        L.oracle_points_destroy.argtypes = [_vp]
-        for name in ("oracle_knn_ref", "oracle_knn_contract"):
-            getattr(L, name).argtypes = [_vp, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
-                                         ctypes.c_int]
-        L.oracle_range_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_float, _i32p,
-                                         ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), _i32p, _f32p,
-                                         ctypes.c_int]
-        L.oracle_range_brute.restype = None
-        L.oracle_knn_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
-                                       ctypes.c_int, ctypes.c_int]
-        L.oracle_sample_by_area.restype = _i64
-        L.oracle_sample_by_area.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_uint32, _f32p, _f32p, _i32p]
-        L.oracle_thea_random_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
-        L.oracle_std_mt19937_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
-        L.oracle_triangle_closest_points.argtypes = [_f32p, _f32p, _i64, _f32p, _f32p]
-        L.oracle_triangle_ray_times.argtypes = [_f32p, _f32p, _f32p, _i64, ctypes.c_float, _f32p]
-        L.oracle_triangle_props.argtypes = [_f32p, _i64, _f32p, _f32p, _i32p, _f32p]
-        L.oracle_box_ray_time.restype = ctypes.c_float
-        L.oracle_box_ray_time.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_float]
-        L.oracle_tree_depth.restype = _i64
-        L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
-        L.oracle_random_sphere.argtypes = [ctypes.c_uint32, _i64, _f32p]
-        L.oracle_sample_graph.argtypes = [_f32p, _f32p, _i64, ctypes.c_int, ctypes.c_uint32, _vp, _i32p, _f32p, _i32p,
-                                          _f32p, ctypes.c_int]
-        L.oracle_visibility.argtypes = [_vp, _f32p, _i64, _i64, ctypes.c_uint32, _f32p, _f64p, ctypes.c_int]
-        L.oracle_shape_diameter.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, ctypes.c_int, _f32p, _f64p,
-                                             ctypes.c_int]
-        L.oracle_affine_inverse.restype = ctypes.c_int
-        L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
-        for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
-            getattr(L, name).argtypes = [_f32p, _f32p, _i64, _f32p]
-        _lib = L
+        _lib = _declare(ctypes.CDLL(_LIB_PATH))
     return _lib
+
+
+def _declare(L):
+    """Declares the C signatures of one build of the oracle."""
+    L.oracle_mesh_create.restype = _vp
+    L.oracle_mesh_create.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_int]
+    L.oracle_mesh_destroy.argtypes = [_vp]
+    L.oracle_mesh_num_nodes.restype = _i64
+    L.oracle_mesh_num_nodes.argtypes = [_vp]
+    L.oracle_mesh_max_depth.restype = _i64
+    L.oracle_mesh_max_depth.argtypes = [_vp]
+    L.oracle_closest_ref.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f32p, ctypes.c_int]
+    L.oracle_closest_contract.argtypes = [_vp, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p, ctypes.c_int]
+    L.oracle_closest_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _i64, ctypes.c_double, _i32p, _f64p, _f64p,
+                                       ctypes.c_int, ctypes.c_int]
+    L.oracle_ray_ref.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, _f32p, _i32p, _f32p, ctypes.c_int]
+    L.oracle_ray_contract.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p, ctypes.c_int]
+    L.oracle_ray_brute.argtypes = [_f32p, _i64, _i32p, _i64, _f32p, _f32p, _i64, ctypes.c_double, _f64p, _i32p,
+                                   ctypes.c_int, ctypes.c_int]
+    L.oracle_points_create.restype = _vp
+    L.oracle_points_create.argtypes = [_f32p, _i64, _i64, ctypes.c_int]
+    L.oracle_points_destroy.argtypes = [_vp]
+    for name in ("oracle_knn_ref", "oracle_knn_contract"):
+        getattr(L, name).argtypes = [_vp, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
+                                     ctypes.c_int]
+    L.oracle_range_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_float, _i32p,
+                                     ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), _i32p, _f32p,
+                                     ctypes.c_int]
+    L.oracle_range_brute.restype = None
+    L.oracle_knn_brute.argtypes = [_f32p, _i64, _f32p, _i64, ctypes.c_int, ctypes.c_double, _i32p, _i32p, _f64p,
+                                   ctypes.c_int, ctypes.c_int]
+    L.oracle_sample_by_area.restype = _i64
+    L.oracle_sample_by_area.argtypes = [_f32p, _i64, _i32p, _i64, _i64, ctypes.c_uint32, _f32p, _f32p, _i32p]
+    L.oracle_thea_random_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
+    L.oracle_std_mt19937_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
+    L.oracle_triangle_closest_points.argtypes = [_f32p, _f32p, _i64, _f32p, _f32p]
+    L.oracle_triangle_ray_times.argtypes = [_f32p, _f32p, _f32p, _i64, ctypes.c_float, _f32p]
+    L.oracle_triangle_props.argtypes = [_f32p, _i64, _f32p, _f32p, _i32p, _f32p]
+    L.oracle_box_ray_time.restype = ctypes.c_float
+    L.oracle_box_ray_time.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_float]
+    L.oracle_tree_depth.restype = _i64
+    L.oracle_tree_depth.argtypes = [_i64, ctypes.c_int]
+    L.oracle_random_sphere.argtypes = [ctypes.c_uint32, _i64, _f32p]
+    L.oracle_sample_graph.argtypes = [_f32p, _f32p, _i64, ctypes.c_int, ctypes.c_uint32, _vp, _i32p, _f32p, _i32p,
+                                      _f32p, ctypes.c_int]
+    L.oracle_visibility.argtypes = [_vp, _f32p, _i64, _i64, ctypes.c_uint32, _f32p, _f64p, ctypes.c_int]
+    L.oracle_shape_diameter.argtypes = [_vp, _f32p, _f32p, _i64, ctypes.c_float, ctypes.c_int, _f32p, _f64p,
+                                         ctypes.c_int]
+    L.oracle_affine_inverse.restype = ctypes.c_int
+    L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
+    for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
+        getattr(L, name).argtypes = [_f32p, _f32p, _i64, _f32p]
+    return L
 
 
 def _p(a, t):
@@ -108,25 +123,26 @@ def default_threads():
 class MeshIndex:
     """Reference kd-tree over mesh triangles (BvhN::init with Method::KDTREE, leaf size 5 by default)."""
 
-    def __init__(self, V, F, max_leaf=-1, fp64=False):
+    def __init__(self, V, F, max_leaf=-1, fp64=False, timed=False):
         self.V = _f32(V).reshape(-1, 3)
         self.F = _i32(F).reshape(-1, 3)
         self.fp64 = bool(fp64)
-        self.h = lib().oracle_mesh_create(_p(self.V, _f32p), len(self.V), _p(self.F, _i32p), len(self.F), max_leaf,
+        self._L = lib(timed)
+        self.h = self._L.oracle_mesh_create(_p(self.V, _f32p), len(self.V), _p(self.F, _i32p), len(self.F), max_leaf,
                                           int(fp64))
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.oracle_mesh_destroy(self.h)
+        if getattr(self, "h", None) and getattr(self, "_L", None) is not None:
+            self._L.oracle_mesh_destroy(self.h)
             self.h = None
 
     @property
     def num_nodes(self):
-        return lib().oracle_mesh_num_nodes(self.h)
+        return self._L.oracle_mesh_num_nodes(self.h)
 
     @property
     def max_depth(self):
-        return lib().oracle_mesh_max_depth(self.h)
+        return self._L.oracle_mesh_max_depth(self.h)
 
     def closest_ref(self, q, dist_bound=-1.0, threads=None):
         """Reference mode: returns (index, distance (double, sqrt of mad), closest point (float32))."""
@@ -135,7 +151,7 @@ class MeshIndex:
         idx = np.empty(n, np.int32)
         dist = np.empty(n, np.float64)
         cp = np.empty((n, 3), np.float32)
-        lib().oracle_closest_ref(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(dist, _f64p),
+        self._L.oracle_closest_ref(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(dist, _f64p),
                                  _p(cp, _f32p), threads or default_threads())
         return idx, dist, cp
 
@@ -146,7 +162,7 @@ class MeshIndex:
         idx = np.empty(n, np.int32)
         d2 = np.empty(n, np.float64)
         cp = np.empty((n, 3), np.float64)
-        lib().oracle_closest_contract(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(d2, _f64p),
+        self._L.oracle_closest_contract(self.h, _p(q, _f32p), n, float(dist_bound), _p(idx, _i32p), _p(d2, _f64p),
                                       _p(cp, _f64p), threads or default_threads())
         return idx, d2, cp
 
@@ -158,7 +174,7 @@ class MeshIndex:
         t = np.empty(n, np.float32)
         idx = np.empty(n, np.int32)
         nrm = np.empty((n, 3), np.float32)
-        lib().oracle_ray_ref(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f32p), _p(idx, _i32p),
+        self._L.oracle_ray_ref(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f32p), _p(idx, _i32p),
                              _p(nrm, _f32p), threads or default_threads())
         return t, idx, nrm
 
@@ -168,7 +184,7 @@ class MeshIndex:
         p = _f32(positions).reshape(-1, 3)
         out = np.empty(len(p), np.float64)
         xf = _affine(transform) if transform is not None else None
-        lib().oracle_visibility(self.h, _p(p, _f32p), len(p), int(num_rays), int(seed),
+        self._L.oracle_visibility(self.h, _p(p, _f32p), len(p), int(num_rays), int(seed),
                                 _p(xf, _f32p) if xf is not None else None, _p(out, _f64p), threads or default_threads())
         return out
 
@@ -179,7 +195,7 @@ class MeshIndex:
         nr = _f32(normals).reshape(-1, 3) if normals is not None else None
         out = np.empty(len(p), np.float64)
         xf = _affine(transform) if transform is not None else None
-        lib().oracle_shape_diameter(self.h, _p(p, _f32p), _p(nr, _f32p) if nr is not None else None, len(p),
+        self._L.oracle_shape_diameter(self.h, _p(p, _f32p), _p(nr, _f32p) if nr is not None else None, len(p),
                                     float(scale), 1 if only_interior else 0,
                                     _p(xf, _f32p) if xf is not None else None, _p(out, _f64p),
                                     threads or default_threads())
@@ -191,7 +207,7 @@ class MeshIndex:
         n = len(o)
         t = np.empty(n, np.float64)
         idx = np.empty(n, np.int32)
-        lib().oracle_ray_contract(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f64p),
+        self._L.oracle_ray_contract(self.h, _p(o, _f32p), _p(d, _f32p), n, float(max_time), _p(t, _f64p),
                                   _p(idx, _i32p), threads or default_threads())
         return t, idx
 
@@ -225,13 +241,14 @@ def ray_brute(V, F, o, d, max_time=-1.0, fp64=False, threads=None):
 class PointIndex:
     """Reference kd-tree over points (BvhN<Vector3, 3>)."""
 
-    def __init__(self, P, max_leaf=-1, fp64=False):
+    def __init__(self, P, max_leaf=-1, fp64=False, timed=False):
         self.P = _f32(P).reshape(-1, 3)
-        self.h = lib().oracle_points_create(_p(self.P, _f32p), len(self.P), max_leaf, int(fp64))
+        self._L = lib(timed)
+        self.h = self._L.oracle_points_create(_p(self.P, _f32p), len(self.P), max_leaf, int(fp64))
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.oracle_points_destroy(self.h)
+        if getattr(self, "h", None) and getattr(self, "_L", None) is not None:
+            self._L.oracle_points_destroy(self.h)
             self.h = None
 
     def _knn(self, fn, q, k, dist_bound, exclude, threads):
@@ -245,10 +262,10 @@ class PointIndex:
         return idx, d2
 
     def knn_ref(self, q, k, dist_bound=-1.0, exclude=None, threads=None):
-        return self._knn(lib().oracle_knn_ref, q, k, dist_bound, exclude, threads)
+        return self._knn(self._L.oracle_knn_ref, q, k, dist_bound, exclude, threads)
 
     def knn_contract(self, q, k, dist_bound=-1.0, exclude=None, threads=None):
-        return self._knn(lib().oracle_knn_contract, q, k, dist_bound, exclude, threads)
+        return self._knn(self._L.oracle_knn_contract, q, k, dist_bound, exclude, threads)
 
 
 def knn_brute(P, q, k, dist_bound=-1.0, exclude=None, fp64=False, threads=None):

@@ -493,8 +493,17 @@ template <class S> struct MeshIndex {
           if (best_idx < 0 || d2 < bd2 || (d2 == bd2 && idx < best_idx)) { bd2 = d2; best_idx = idx; bcp = cp; }
         }
       } else {
-        stack.push_back(n.child[1]);
-        stack.push_back(n.child[0]);
+        // nearer child on top, so the bound tightens early (the result does not depend on the order: every element
+        // whose box is not farther than the best is tested)
+        S c0 = qb.squaredDistance(tree.nodes[(size_t)n.child[0]].bounds);
+        S c1 = qb.squaredDistance(tree.nodes[(size_t)n.child[1]].bounds);
+        if (c1 < c0) {
+          stack.push_back(n.child[0]);
+          stack.push_back(n.child[1]);
+        } else {
+          stack.push_back(n.child[1]);
+          stack.push_back(n.child[0]);
+        }
       }
     }
     if (best_idx >= 0) { best_d2 = bd2; cp_out = bcp; }
@@ -686,8 +695,16 @@ template <class S> struct PointIndex {
           if ((int)out.size() > k) out.pop_back();
         }
       } else {
-        stack.push_back(n.child[1]);
-        stack.push_back(n.child[0]);
+        // nearer child on top (the result does not depend on the order)
+        S c0 = qb.squaredDistance(tree.nodes[(size_t)n.child[0]].bounds);
+        S c1 = qb.squaredDistance(tree.nodes[(size_t)n.child[1]].bounds);
+        if (c1 < c0) {
+          stack.push_back(n.child[0]);
+          stack.push_back(n.child[1]);
+        } else {
+          stack.push_back(n.child[1]);
+          stack.push_back(n.child[0]);
+        }
       }
     }
   }

@@ -6,7 +6,7 @@ per model, the triangle list the reference's MeshGroup<DisplayMesh>::load would 
 of each triangle, submesh offsets) and the SHA-256 of the source file, so GPU tests can run the queries on real meshes
 without the reference present.
 
-Run: python tests/golden/make_model_fixtures.py [path to the reference's Data/Models directory]
+Run: python tests/golden/make_model_fixtures.py <path to the reference's Data/Models directory>
 """
 
 import hashlib
@@ -25,7 +25,9 @@ MODELS = ("cube", "sphere", "teapot")
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Data/Models"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_model_fixtures.py <the reference's Data/Models directory>")
+    src = sys.argv[1]
     from thea_gb300 import build as B
     B.build()
     import thea_gb300 as T
