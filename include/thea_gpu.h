@@ -149,8 +149,11 @@ THEA_API thea_status thea_bvh_get_info(const thea_bvh * bvh, thea_bvh_info * inf
 
 /* Closest element of a mesh BVH to each query point.
  * Replaces BvhN::closestElement<MetricL2>(query, dist_bound, compat, &dist, &closest_point) (BvhN.hpp:1050-1063) and
- * closestPair (BvhN.hpp:1082-1114). dist_bound < 0: unbounded; otherwise only elements with squared distance strictly
- * below dist_bound^2 are accepted. Outputs per query: index (-1 if none), distance (sqrt of the squared distance, -1 if
+ * closestPair (BvhN.hpp:1082-1114). dist_bound < 0: unbounded; otherwise the bound is applied as closestPair applies it:
+ * a query whose squared distance to the root box (the element bounds grown by 1.05 about their centre, mapped by the
+ * transform if one is set) exceeds dist_bound^2 gets no element, and otherwise elements are accepted with squared
+ * distance strictly below (dist_bound + max(0.001 |root box extent|, 100 FLT_EPSILON))^2 (the loosening closestPair
+ * adds to a given bound). Outputs per query: index (-1 if none), distance (sqrt of the squared distance, -1 if
  * none) and, if non-NULL, the closest point on the element (3 floats; unchanged slots are written as 0 when none). */
 THEA_API thea_status thea_closest_element(const thea_bvh * mesh_bvh, const float * queries, int64_t num_queries,
                                           float dist_bound, int32_t * out_index, float * out_distance,
@@ -241,9 +244,11 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
 /* ---- pairs between two BVHs ---------------------------------------------------------------------------------------- */
 
 /* BvhN::closestPair<MetricL2> with another BVH as the query (BvhN.hpp:1082-1114; the reference descends both trees,
- * :1916-2033): the (query element, target element) pair at the smallest distance, at least one side holding points
- * (mesh-mesh: THEA_ERR_NOT_SUPPORTED); single BVHs, transforms applied. Ties: lowest query index, then lowest target
- * index. dist_bound >= 0: only pairs strictly closer. Outputs are host scalars: indices (-1 when no pair), the squared
+ * :1916-2033): the (query element, target element) pair at the smallest distance, points or meshes on either side;
+ * single BVHs, transforms applied. Between two meshes the distance is TriangleN<3>::squaredDistance
+ * (Triangle3.hpp:314-400) evaluated with the target triangle as "this" (the reference evaluates a pair with either
+ * triangle as "this", depending on which tree its descent is in, which can change the last bits); both meshes need
+ * THEA_LAYOUT_CLOSEST. Ties: lowest query index, then lowest target index. dist_bound >= 0: only pairs strictly closer. Outputs are host scalars: indices (-1 when no pair), the squared
  * distance (the reference's monotone approximate distance; -1 when none) and, nullable, the closest points on the two
  * elements (3 floats each). Synchronizes the stream. */
 THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_bvh * query, float dist_bound,

@@ -2,8 +2,8 @@
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` may import this module. It restates
 Thea's CPU spatial-query path (reference mode: the reference's kd-tree and traversal order; contract mode: lowest index
-among ties) and is never used by the product path. Parity status: UNPINNED (no golden vector exists in the reference,
-whose Eigen dependency cannot be built here).
+among ties) and is never used by the product path. Parity status: pinned to the reference's own code, compiled here with
+an Eigen subset (oracle/reference.py; tests/test_oracle_pinned.py).
 """
 
 import ctypes
@@ -99,6 +99,11 @@ def _declare(L):
     L.oracle_affine_inverse.argtypes = [_f32p, _f32p]
     for name in ("oracle_affine_points", "oracle_affine_vectors", "oracle_normals_to_world"):
         getattr(L, name).argtypes = [_f32p, _f32p, _i64, _f32p]
+    L.oracle_mesh_pair_contract.argtypes = [_vp, _f32p, _i32p, _i64, ctypes.c_double, _i32p, _i32p, _f64p, _f64p,
+                                            _f64p, ctypes.c_int]
+    L.oracle_mesh_pair_brute.argtypes = [_f32p, _i32p, _i64, _f32p, _i32p, _i64, ctypes.c_double, _i32p, _i32p, _f64p,
+                                         _f64p, _f64p, ctypes.c_int, ctypes.c_int]
+    L.oracle_triangle_pair_distances.argtypes = [_f32p, _f32p, _i64, _f32p, _f32p, _f32p]
     return L
 
 
@@ -201,6 +206,19 @@ class MeshIndex:
                                     threads or default_threads())
         return out
 
+    def closest_pair_contract(self, Vq, Fq, dist_bound=-1.0, threads=None):
+        """Closest pair between this mesh (target) and a query mesh, contract mode: (query index, target index, squared
+        distance, query point, target point); indices -1 when no pair."""
+        Vq = _f32(Vq).reshape(-1, 3)
+        Fq = _i32(Fq).reshape(-1, 3)
+        qi, ti = ctypes.c_int32(-1), ctypes.c_int32(-1)
+        d2 = ctypes.c_double(-1.0)
+        qp, tp = np.zeros(3), np.zeros(3)
+        self._L.oracle_mesh_pair_contract(self.h, _p(Vq, _f32p), _p(Fq, _i32p), len(Fq), float(dist_bound),
+                                          ctypes.byref(qi), ctypes.byref(ti), ctypes.byref(d2), _p(qp, _f64p),
+                                          _p(tp, _f64p), threads or default_threads())
+        return qi.value, ti.value, d2.value, qp, tp
+
     def ray_contract(self, o, d, max_time=-1.0, threads=None):
         o = _f32(o).reshape(-1, 3)
         d = _f32(d).reshape(-1, 3)
@@ -223,6 +241,30 @@ def closest_brute(V, F, q, dist_bound=-1.0, fp64=False, threads=None):
     lib().oracle_closest_brute(_p(V, _f32p), len(V), _p(F, _i32p), len(F), _p(q, _f32p), n, float(dist_bound),
                                _p(idx, _i32p), _p(d2, _f64p), _p(cp, _f64p), int(fp64), threads or default_threads())
     return idx, d2, cp
+
+
+def mesh_pair_brute(Vt, Ft, Vq, Fq, dist_bound=-1.0, fp64=False, threads=None):
+    """Closest pair between two meshes by testing every triangle pair (contract mode): as closest_pair_contract."""
+    Vt, Vq = _f32(Vt).reshape(-1, 3), _f32(Vq).reshape(-1, 3)
+    Ft, Fq = _i32(Ft).reshape(-1, 3), _i32(Fq).reshape(-1, 3)
+    qi, ti = ctypes.c_int32(-1), ctypes.c_int32(-1)
+    d2 = ctypes.c_double(-1.0)
+    qp, tp = np.zeros(3), np.zeros(3)
+    lib().oracle_mesh_pair_brute(_p(Vt, _f32p), _p(Ft, _i32p), len(Ft), _p(Vq, _f32p), _p(Fq, _i32p), len(Fq),
+                                 float(dist_bound), ctypes.byref(qi), ctypes.byref(ti), ctypes.byref(d2), _p(qp, _f64p),
+                                 _p(tp, _f64p), int(fp64), threads or default_threads())
+    return qi.value, ti.value, d2.value, qp, tp
+
+
+def triangle_pair_distances(a, b):
+    """Squared distance and closest points of triangle pairs (TriangleN::squaredDistance, a as "this"), FP32."""
+    a = _f32(a).reshape(-1, 9)
+    b = _f32(b).reshape(-1, 9)
+    n = len(a)
+    d2 = np.empty(n, np.float32)
+    pa, pb = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+    lib().oracle_triangle_pair_distances(_p(a, _f32p), _p(b, _f32p), n, _p(d2, _f32p), _p(pa, _f32p), _p(pb, _f32p))
+    return d2, pa, pb
 
 
 def ray_brute(V, F, o, d, max_time=-1.0, fp64=False, threads=None):

@@ -1,5 +1,5 @@
 // TEST INFRASTRUCTURE ONLY -- C entry points of the CPU oracle, loaded by the tests (ctypes) and by the CPU-baseline legs
-// of bench.py. Never linked into the product library. Parity status: UNPINNED (see thea_oracle.hpp).
+// of bench.py. Never linked into the product library. Parity status: pinned to the reference (see thea_oracle.hpp).
 
 #include "thea_oracle.hpp"
 
@@ -104,14 +104,22 @@ static void closestBruteImpl(float const * V, int64_t nv, int32_t const * F, int
   std::vector<Tri<S>> tris((size_t)nf);
   for (int64_t f = 0; f < nf; ++f)
     tris[(size_t)f] = Tri<S>(q3<S>(V, F[3 * f]), q3<S>(V, F[3 * f + 1]), q3<S>(V, F[3 * f + 2]));
-  double mb = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+  // the bound as a BVH over these triangles applies it (MeshIndex::closestBound): its root box is the element bounds
+  // grown by 1.05 about their centre
+  MeshIndex<S> root_only;
+  root_only.tree.nodes.resize(1);
+  for (auto const & t : tris) root_only.tree.nodes[0].bounds.merge(t.bounds());
+  root_only.tree.nodes[0].bounds.scaleCentered(S(1.05f));
   parallelFor(n, nthreads, [&](int64_t b, int64_t e) {
     for (int64_t i = b; i < e; ++i) {
       V3<S> p = q3<S>(q, i);
       int64_t best = -1;
       S bd = 0;
       V3<S> bc;
-      for (int64_t f = 0; f < nf; ++f) {
+      Box<S> qb;
+      qb.merge(p);
+      double mb = nf > 0 ? root_only.closestBound(qb, dist_bound) : -1;
+      for (int64_t f = 0; f < nf && mb != -2; ++f) {
         V3<S> c;
         S dd = triangleClosestPoints(tris[(size_t)f], p, c);
         if (!(dd == dd)) continue;  // a NaN distance (coincident vertices) is never selected
@@ -169,6 +177,103 @@ void oracle_ray_contract(void * hv, float const * o, float const * d, int64_t n,
   MeshHandle * h = static_cast<MeshHandle *>(hv);
   if (h->fp64) rayContractImpl(h->d, o, d, n, max_time, t, idx, nthreads);
   else rayContractImpl(h->f, o, d, n, max_time, t, idx, nthreads);
+}
+
+//---------------------------------------------------------------------------------------------------------------------------
+// Closest pair between two meshes (BvhN::closestPair with a mesh BVH as the query, BvhN.hpp:1082-1114, 1916-2089; the
+// pair distance is TriangleN::squaredDistance with the target triangle as "this", Triangle3.hpp:314-400). Contract
+// mode: smallest squared distance, ties to the lowest query index, then the lowest target index. Outputs: query index,
+// target index (-1 when no pair), squared distance, closest points on the query and target triangles (3 each).
+//---------------------------------------------------------------------------------------------------------------------------
+
+extern "C++" {
+template <class S>
+static std::vector<Tri<S>> makeTris(float const * V, int32_t const * F, int64_t nf) {
+  std::vector<Tri<S>> t((size_t)nf);
+  for (int64_t f = 0; f < nf; ++f) t[(size_t)f] = Tri<S>(q3<S>(V, F[3 * f]), q3<S>(V, F[3 * f + 1]), q3<S>(V, F[3 * f + 2]));
+  return t;
+}
+
+// rows: per query triangle its best (d2, target); returns the winning (query, target) after the tie rule
+template <class S>
+static void pairReduce(std::vector<S> const & rd2, std::vector<int64_t> const & rt, std::vector<Tri<S>> const & qt,
+                       std::vector<Tri<S>> const & tt, int32_t * qi, int32_t * ti, double * d2, double * qpt,
+                       double * tpt) {
+  int64_t bq = -1;
+  for (size_t i = 0; i < rt.size(); ++i) {
+    if (rt[i] < 0) continue;
+    if (bq < 0 || rd2[i] < rd2[(size_t)bq]) bq = (int64_t)i;  // ascending scan: ties keep the lowest query, and each
+  }                                                             // row already holds its lowest target among ties
+  *qi = (int32_t)bq;
+  *ti = bq >= 0 ? (int32_t)rt[(size_t)bq] : -1;
+  *d2 = bq >= 0 ? (double)rd2[(size_t)bq] : -1.0;
+  if (bq >= 0) {
+    V3<S> pa, pb;
+    triangleTriangleSquaredDistance(tt[(size_t)*ti], qt[(size_t)bq], pa, pb);
+    for (int k = 0; k < 3; ++k) { qpt[k] = (double)pb[k]; tpt[k] = (double)pa[k]; }
+  }
+}
+
+template <class S>
+static void meshPairContractImpl(MeshIndex<S> const & m, float const * Vq, int32_t const * Fq, int64_t nfq,
+                                 double dist_bound, int32_t * qi, int32_t * ti, double * d2, double * qpt, double * tpt,
+                                 int nthreads) {
+  std::vector<Tri<S>> qt = makeTris<S>(Vq, Fq, nfq);
+  std::vector<S> rd2((size_t)nfq);
+  std::vector<int64_t> rt((size_t)nfq);
+  parallelFor(nfq, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) rt[(size_t)i] = m.closestTriangleContract(qt[(size_t)i], dist_bound, rd2[(size_t)i]);
+  });
+  pairReduce(rd2, rt, qt, m.tris, qi, ti, d2, qpt, tpt);
+}
+
+template <class S>
+static void meshPairBruteImpl(float const * Vt, int32_t const * Ft, int64_t nft, float const * Vq, int32_t const * Fq,
+                              int64_t nfq, double dist_bound, int32_t * qi, int32_t * ti, double * d2, double * qpt,
+                              double * tpt, int nthreads) {
+  std::vector<Tri<S>> tt = makeTris<S>(Vt, Ft, nft), qt = makeTris<S>(Vq, Fq, nfq);
+  double mb = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+  std::vector<S> rd2((size_t)nfq);
+  std::vector<int64_t> rt((size_t)nfq, -1);
+  parallelFor(nfq, nthreads, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      for (int64_t j = 0; j < nft; ++j) {
+        V3<S> pa, pb;
+        S d = triangleTriangleSquaredDistance(tt[(size_t)j], qt[(size_t)i], pa, pb);
+        if (!(d == d)) continue;
+        if (mb >= 0 && !((double)d < mb)) continue;
+        if (rt[(size_t)i] < 0 || d < rd2[(size_t)i]) { rd2[(size_t)i] = d; rt[(size_t)i] = j; }
+      }
+    }
+  });
+  pairReduce(rd2, rt, qt, tt, qi, ti, d2, qpt, tpt);
+}
+}  // extern "C++"
+
+void oracle_mesh_pair_contract(void * target, float const * Vq, int32_t const * Fq, int64_t nfq, double dist_bound,
+                               int32_t * qi, int32_t * ti, double * d2, double * qpt, double * tpt, int nthreads) {
+  MeshHandle * h = static_cast<MeshHandle *>(target);
+  if (h->fp64) meshPairContractImpl(h->d, Vq, Fq, nfq, dist_bound, qi, ti, d2, qpt, tpt, nthreads);
+  else meshPairContractImpl(h->f, Vq, Fq, nfq, dist_bound, qi, ti, d2, qpt, tpt, nthreads);
+}
+
+void oracle_mesh_pair_brute(float const * Vt, int32_t const * Ft, int64_t nft, float const * Vq, int32_t const * Fq,
+                            int64_t nfq, double dist_bound, int32_t * qi, int32_t * ti, double * d2, double * qpt,
+                            double * tpt, int fp64, int nthreads) {
+  if (fp64) meshPairBruteImpl<double>(Vt, Ft, nft, Vq, Fq, nfq, dist_bound, qi, ti, d2, qpt, tpt, nthreads);
+  else meshPairBruteImpl<float>(Vt, Ft, nft, Vq, Fq, nfq, dist_bound, qi, ti, d2, qpt, tpt, nthreads);
+}
+
+// Squared distance and closest points of triangle pairs (a_i as "this", b_i as "other"), FP32: one per row of 9 floats.
+void oracle_triangle_pair_distances(float const * a, float const * b, int64_t n, float * d2, float * pa, float * pb) {
+  for (int64_t i = 0; i < n; ++i) {
+    Tri<float> ta(q3<float>(a, 3 * i), q3<float>(a, 3 * i + 1), q3<float>(a, 3 * i + 2));
+    Tri<float> tb(q3<float>(b, 3 * i), q3<float>(b, 3 * i + 1), q3<float>(b, 3 * i + 2));
+    V3<float> x, y;
+    d2[i] = triangleTriangleSquaredDistance(ta, tb, x, y);
+    pa[3 * i] = x.x; pa[3 * i + 1] = x.y; pa[3 * i + 2] = x.z;
+    pb[3 * i] = y.x; pb[3 * i + 1] = y.y; pb[3 * i + 2] = y.z;
+  }
 }
 
 extern "C++" {

@@ -4,11 +4,12 @@
 // implementation can be checked against them. Only tests, the smoke check and the CPU-baseline legs of bench.py may
 // load it; the product library never links it, and nothing here is a fallback for the GPU path.
 //
-// Parity status: UNPINNED. The reference cannot be compiled in this environment (it needs Eigen >= 3.4, which is neither
-// vendored nor installed), and its own tests (Code/Source/Test/TestBvh.cpp) print results without asserting any value, so
-// no golden vector from the reference exists. The restatement follows the cited reference lines operation by operation;
-// the only partial known-answer pin is the Mersenne-Twister seeding and tempering, checked against std::mt19937 for the
-// outputs that Thea's variant shares with the standard generator.
+// Parity status: PINNED to the reference's own code. The reference's BvhN, Triangle3, AxisAlignedBoxN, Random and Math
+// sources are compiled in this build (oracle/Makefile, target `ref`) with oracle/ref_pin/eigen_subset.hpp standing in for
+// Eigen, which is absent here; the reference mode below reproduces their outputs bit for bit (element indices,
+// distances, closest points, hit times, normals, k-NN lists, random words: tests/test_oracle_pinned.py against
+// tests/golden/reference_outputs.npz). What both share, and what remains assumed, is the order of Eigen's 3-term sums
+// (next paragraph).
 //
 // Arithmetic order. The reference computes in FP32 (Real = float, Code/Source/NumericType.hpp:40) through Eigen
 // fixed-size 3-vectors. Eigen reduces a 3-element sum (dot, squaredNorm) as e0 + (e1 + e2) when no SIMD packet fits the
@@ -314,6 +315,275 @@ S rayTriangleIntersectionTime(V3<S> const & origin, V3<S> const & dir, V3<S> con
   return S(-1);
 }
 
+//============================================================================================================================
+// Triangle-triangle distance: TriangleN<3>::squaredDistance(other, this_pt, other_pt) (Triangle3.hpp:314-400, after
+// Ericson, "Real-Time Collision Detection"), with Moller's intersection test that also returns the line of intersection
+// (Triangle3Internal::tri_tri_intersect_with_isectline, Triangle3.hpp:1117-1290, coplanar_tri_tri :730-776) and the
+// segment-segment closest points of Internal::closestPtSegmentSegment (LineSegmentN.hpp:262-340).
+//
+// Arithmetic order: the intersection test works on raw coordinate arrays with the reference's C expressions, so its
+// three-term dot products add left to right ((a0 b0 + a1 b1) + a2 b2); the segment-segment and plane-projection steps
+// use Eigen vectors (the e0 + (e1 + e2) reduction of dot() above).
+//============================================================================================================================
+
+namespace tritri {
+
+template <class S> inline S dotLR(S const * a, S const * b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <class S> inline void crossA(S * d, S const * a, S const * b) {
+  d[0] = a[1] * b[2] - a[2] * b[1];
+  d[1] = a[2] * b[0] - a[0] * b[2];
+  d[2] = a[0] * b[1] - a[1] * b[0];
+}
+template <class S> inline void subA(S * d, S const * a, S const * b) {
+  d[0] = a[0] - b[0]; d[1] = a[1] - b[1]; d[2] = a[2] - b[2];
+}
+
+// EDGE_EDGE_TEST (Triangle3.hpp:674-693): edge (v0, v0 + A) against edge (u0, u1) in the projection (i0, i1)
+template <class S>
+inline bool edgeEdge(S Ax, S Ay, S const * v0, S const * u0, S const * u1, int i0, int i1) {
+  S Bx = u0[i0] - u1[i0], By = u0[i1] - u1[i1];
+  S Cx = v0[i0] - u0[i0], Cy = v0[i1] - u0[i1];
+  S f = Ay * Bx - Ax * By;
+  S d = By * Cx - Bx * Cy;
+  if ((f > 0 && d >= 0 && d <= f) || (f < 0 && d <= 0 && d >= f)) {
+    S e = Ax * Cy - Ay * Cx;
+    if (f > 0) {
+      if (e >= 0 && e <= f) return true;
+    } else {
+      if (e <= 0 && e >= f) return true;
+    }
+  }
+  return false;
+}
+
+// EDGE_AGAINST_TRI_EDGES (Triangle3.hpp:695-707)
+template <class S>
+inline bool edgeAgainstTri(S const * v0, S const * v1, S const * u0, S const * u1, S const * u2, int i0, int i1) {
+  S Ax = v1[i0] - v0[i0], Ay = v1[i1] - v0[i1];
+  return edgeEdge(Ax, Ay, v0, u0, u1, i0, i1) || edgeEdge(Ax, Ay, v0, u1, u2, i0, i1) ||
+         edgeEdge(Ax, Ay, v0, u2, u0, i0, i1);
+}
+
+// POINT_IN_TRI (Triangle3.hpp:709-728)
+template <class S> inline bool pointInTri(S const * v0, S const * u0, S const * u1, S const * u2, int i0, int i1) {
+  S a = u1[i1] - u0[i1], b = -(u1[i0] - u0[i0]);
+  S c = -a * u0[i0] - b * u0[i1];
+  S d0 = a * v0[i0] + b * v0[i1] + c;
+  a = u2[i1] - u1[i1]; b = -(u2[i0] - u1[i0]);
+  c = -a * u1[i0] - b * u1[i1];
+  S d1 = a * v0[i0] + b * v0[i1] + c;
+  a = u0[i1] - u2[i1]; b = -(u0[i0] - u2[i0]);
+  c = -a * u2[i0] - b * u2[i1];
+  S d2 = a * v0[i0] + b * v0[i1] + c;
+  return d0 * d1 > 0 && d0 * d2 > 0;
+}
+
+// coplanar_tri_tri (Triangle3.hpp:730-776)
+template <class S>
+bool coplanar(S const * N, S const * v0, S const * v1, S const * v2, S const * u0, S const * u1, S const * u2) {
+  S A0 = std::fabs(N[0]), A1 = std::fabs(N[1]), A2 = std::fabs(N[2]);
+  int i0, i1;
+  if (A0 > A1) {
+    if (A0 > A2) { i0 = 1; i1 = 2; }
+    else { i0 = 0; i1 = 1; }
+  } else {
+    if (A2 > A1) { i0 = 0; i1 = 1; }
+    else { i0 = 0; i1 = 2; }
+  }
+  if (edgeAgainstTri(v0, v1, u0, u1, u2, i0, i1)) return true;
+  if (edgeAgainstTri(v1, v2, u0, u1, u2, i0, i1)) return true;
+  if (edgeAgainstTri(v2, v0, u0, u1, u2, i0, i1)) return true;
+  if (pointInTri(v0, u0, u1, u2, i0, i1)) return true;
+  if (pointInTri(u0, v0, v1, v2, i0, i1)) return true;
+  return false;
+}
+
+// isect2 (Triangle3.hpp:1023-1039)
+template <class S>
+inline void isect2(S const * x0, S const * x1, S const * x2, S vv0, S vv1, S vv2, S d0, S d1, S d2, S & is0, S & is1,
+                   S * p0, S * p1) {
+  S tmp = d0 / (d0 - d1);
+  S diff[3];
+  is0 = vv0 + (vv1 - vv0) * tmp;
+  subA(diff, x1, x0);
+  for (int k = 0; k < 3; ++k) diff[k] = tmp * diff[k];
+  for (int k = 0; k < 3; ++k) p0[k] = diff[k] + x0[k];
+  tmp = d0 / (d0 - d2);
+  is1 = vv0 + (vv2 - vv0) * tmp;
+  subA(diff, x2, x0);
+  for (int k = 0; k < 3; ++k) diff[k] = tmp * diff[k];
+  for (int k = 0; k < 3; ++k) p1[k] = x0[k] + diff[k];
+}
+
+// compute_intervals_isectline (Triangle3.hpp:1041-1077); true when the triangles are coplanar
+template <class S>
+inline bool intervals(S const * x0, S const * x1, S const * x2, S vv0, S vv1, S vv2, S d0, S d1, S d2, S d0d1, S d0d2,
+                      S & is0, S & is1, S * p0, S * p1) {
+  if (d0d1 > 0) isect2(x2, x0, x1, vv2, vv0, vv1, d2, d0, d1, is0, is1, p0, p1);
+  else if (d0d2 > 0) isect2(x1, x0, x2, vv1, vv0, vv2, d1, d0, d2, is0, is1, p0, p1);
+  else if (d1 * d2 > 0 || d0 != 0) isect2(x0, x1, x2, vv0, vv1, vv2, d0, d1, d2, is0, is1, p0, p1);
+  else if (d1 != 0) isect2(x1, x0, x2, vv1, vv0, vv2, d1, d0, d2, is0, is1, p0, p1);
+  else if (d2 != 0) isect2(x2, x0, x1, vv2, vv0, vv1, d2, d0, d1, is0, is1, p0, p1);
+  else return true;
+  return false;
+}
+
+// tri_tri_intersect_with_isectline (Triangle3.hpp:1117-1290): 1 if the triangles intersect; *coplanar_out tells whether
+// they are coplanar, and if not, pt1 and pt2 are the ends of the intersection segment
+template <class S>
+int intersect(S const * V0, S const * V1, S const * V2, S const * U0, S const * U1, S const * U2, int & coplanar_out,
+              S * pt1, S * pt2) {
+  S const EPS = std::numeric_limits<S>::epsilon();
+  S E1[3], E2[3], N1[3], N2[3], D[3];
+  S isA[2] = {0, 0}, isB[2] = {0, 0};
+  S pA1[3] = {0, 0, 0}, pA2[3] = {0, 0, 0}, pB1[3] = {0, 0, 0}, pB2[3] = {0, 0, 0};
+  subA(E1, V1, V0);
+  subA(E2, V2, V0);
+  crossA(N1, E1, E2);
+  S d1 = -dotLR(N1, V0);
+  S du0 = dotLR(N1, U0) + d1, du1 = dotLR(N1, U1) + d1, du2 = dotLR(N1, U2) + d1;
+  if (std::fabs(du0) < EPS) du0 = 0;
+  if (std::fabs(du1) < EPS) du1 = 0;
+  if (std::fabs(du2) < EPS) du2 = 0;
+  S du0du1 = du0 * du1, du0du2 = du0 * du2;
+  if (du0du1 > 0 && du0du2 > 0) return 0;
+  subA(E1, U1, U0);
+  subA(E2, U2, U0);
+  crossA(N2, E1, E2);
+  S d2 = -dotLR(N2, U0);
+  S dv0 = dotLR(N2, V0) + d2, dv1 = dotLR(N2, V1) + d2, dv2 = dotLR(N2, V2) + d2;
+  if (std::fabs(dv0) < EPS) dv0 = 0;
+  if (std::fabs(dv1) < EPS) dv1 = 0;
+  if (std::fabs(dv2) < EPS) dv2 = 0;
+  S dv0dv1 = dv0 * dv1, dv0dv2 = dv0 * dv2;
+  if (dv0dv1 > 0 && dv0dv2 > 0) return 0;
+  crossA(D, N1, N2);
+  S mx = std::fabs(D[0]);
+  int index = 0;
+  S b = std::fabs(D[1]), c = std::fabs(D[2]);
+  if (b > mx) { mx = b; index = 1; }
+  if (c > mx) { mx = c; index = 2; }
+  S vp0 = V0[index], vp1 = V1[index], vp2 = V2[index];
+  S up0 = U0[index], up1 = U1[index], up2 = U2[index];
+  coplanar_out = intervals(V0, V1, V2, vp0, vp1, vp2, dv0, dv1, dv2, dv0dv1, dv0dv2, isA[0], isA[1], pA1, pA2) ? 1 : 0;
+  if (coplanar_out) return coplanar(N1, V0, V1, V2, U0, U1, U2) ? 1 : 0;
+  intervals(U0, U1, U2, up0, up1, up2, du0, du1, du2, du0du1, du0du2, isB[0], isB[1], pB1, pB2);
+  int smallest1 = 0, smallest2 = 0;
+  if (isA[0] > isA[1]) { std::swap(isA[0], isA[1]); smallest1 = 1; }
+  if (isB[0] > isB[1]) { std::swap(isB[0], isB[1]); smallest2 = 1; }
+  if (isA[1] < isB[0] || isB[1] < isA[0]) return 0;
+  S const * a_lo = smallest1 == 0 ? pA1 : pA2;  // end of A's interval at isA[0]
+  S const * a_hi = smallest1 == 0 ? pA2 : pA1;
+  S const * b_lo = smallest2 == 0 ? pB1 : pB2;
+  S const * b_hi = smallest2 == 0 ? pB2 : pB1;
+  if (isB[0] < isA[0]) {
+    std::copy(a_lo, a_lo + 3, pt1);
+    if (isB[1] < isA[1]) std::copy(b_hi, b_hi + 3, pt2);
+    else std::copy(a_hi, a_hi + 3, pt2);
+  } else {
+    std::copy(b_lo, b_lo + 3, pt1);
+    if (isB[1] > isA[1]) std::copy(a_hi, a_hi + 3, pt2);
+    else std::copy(b_hi, b_hi + 3, pt2);
+  }
+  return 1;
+}
+
+// Math::fuzzyEq(a, 0) (Math.hpp:131-148)
+template <class S> inline bool fuzzyZero(S a) { return !fuzzyNeZero(a); }
+
+// Math::clamp (Math.hpp:249)
+template <class S> inline S clamp01(S x) { return x < S(0) ? S(0) : (x > S(1) ? S(1) : x); }
+
+// Internal::closestPtSegmentSegment for two segments (LineSegmentN.hpp:262-340)
+template <class S>
+S segmentSegment(V3<S> const & p1, V3<S> const & q1, V3<S> const & p2, V3<S> const & q2, V3<S> & c1, V3<S> & c2) {
+  V3<S> d1 = q1 - p1, d2 = q2 - p2, r = p1 - p2;
+  S a = squaredNorm(d1), e = squaredNorm(d2), f = dot(d2, r);
+  S s, t;
+  if (fuzzyZero(a)) {
+    if (fuzzyZero(e)) {
+      c1 = p1;
+      c2 = p2;
+      return dot(c1 - c2, c1 - c2);
+    }
+    s = 0;
+    t = clamp01(f / e);
+  } else {
+    S c = dot(d1, r);
+    if (fuzzyZero(e)) {
+      t = 0;
+      s = clamp01(-c / a);
+    } else {
+      S b = dot(d1, d2);
+      S denom = a * e - b * b;
+      s = denom != 0 ? clamp01((b * f - c * e) / denom) : S(0);
+      t = (b * s + f) / e;
+      if (t < 0) {
+        t = 0;
+        s = clamp01(-c / a);
+      } else if (t > 1) {
+        t = 1;
+        s = clamp01((b - c) / a);
+      }
+    }
+  }
+  c1 = p1 + s * d1;
+  c2 = p2 + t * d2;
+  return squaredNorm(c1 - c2);
+}
+
+}  // namespace tritri
+
+// TriangleN<3>::squaredDistance(other, this_pt, other_pt): Triangle3.hpp:314-400. `a` is the triangle whose method runs
+// ("this"); pa and pb receive the closest points on a and b.
+template <class S> S triangleTriangleSquaredDistance(Tri<S> const & a, Tri<S> const & b, V3<S> & pa, V3<S> & pb) {
+  V3<S> c1(0, 0, 0), c2(0, 0, 0);
+  S best = std::numeric_limits<S>::max();
+  S A0[3] = {a.v0.x, a.v0.y, a.v0.z}, A1[3] = {a.v1.x, a.v1.y, a.v1.z}, A2[3] = {a.v2.x, a.v2.y, a.v2.z};
+  S B0[3] = {b.v0.x, b.v0.y, b.v0.z}, B1[3] = {b.v1.x, b.v1.y, b.v1.z}, B2[3] = {b.v2.x, b.v2.y, b.v2.z};
+  int cop = 0;
+  S i1[3] = {0, 0, 0}, i2[3] = {0, 0, 0};
+  if (tritri::intersect(A0, A1, A2, B0, B1, B2, cop, i1, i2)) {
+    if (cop) {
+      // centroids: (v0 + v1 + v2) / 3 (Triangle3.hpp:149)
+      V3<S> ca = (a.v0 + a.v1 + a.v2) / S(3), cb = (b.v0 + b.v1 + b.v2) / S(3);
+      c1 = c2 = S(0.5) * (ca + cb);
+    } else {
+      // LineSegmentN(isectpt1, isectpt2) keeps (point, direction); getPoint(t) = point + t * direction
+      V3<S> pt(i1[0], i1[1], i1[2]), dir = V3<S>(i2[0], i2[1], i2[2]) - pt;
+      c1 = c2 = S(0.5) * ((pt + S(0) * dir) + (pt + S(1) * dir));
+    }
+    best = 0;
+  } else {
+    V3<S> av[3] = {a.v0, a.v1, a.v2}, bv[3] = {b.v0, b.v1, b.v2};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        V3<S> p, q;
+        S d2 = tritri::segmentSegment(av[i], av[(i + 1) % 3], bv[j], bv[(j + 1) % 3], p, q);
+        if (d2 < best) { best = d2; c1 = p; c2 = q; }
+      }
+    for (int i = 0; i < 3; ++i) {  // vertices of b projected into a
+      V3<S> q = bv[i];
+      V3<S> p = q - (dot(q, a.normal) - a.dist) * a.normal;
+      if (isPointInsideTriangle(a.v0, a.v1, a.v2, a.primary_axis, p)) {
+        S d2 = squaredNorm(p - q);
+        if (d2 < best) { best = d2; c1 = p; c2 = q; }
+      }
+    }
+    for (int i = 0; i < 3; ++i) {  // vertices of a projected into b
+      V3<S> p = av[i];
+      V3<S> q = p - (dot(p, b.normal) - b.dist) * b.normal;
+      if (isPointInsideTriangle(b.v0, b.v1, b.v2, b.primary_axis, q)) {
+        S d2 = squaredNorm(p - q);
+        if (d2 < best) { best = d2; c1 = p; c2 = q; }
+      }
+    }
+  }
+  pa = c1;
+  pb = c2;
+  return best;
+}
+
 // TriangleN<3>::rayIntersection time: Triangle3.hpp:542-552 (hit if t >= 0 and (max_time < 0 or t <= max_time))
 template <class S> S triangleRayTime(Tri<S> const & t, V3<S> const & o, V3<S> const & d, S max_time) {
   S time = rayTriangleIntersectionTime(o, d, t.v0, t.edge01, t.edge02);
@@ -418,21 +688,37 @@ template <class S> struct MeshIndex {
                                load3<S>(V + 3 * (int64_t)F[3 * f + 2]));
     std::vector<Box<S>> boxes((size_t)nf);
     std::vector<V3<S>> centers((size_t)nf);
-    for (size_t f = 0; f < (size_t)nf; ++f) { boxes[f] = tris[f].bounds(); centers[f] = boxes[f].center(); }
+    // split key: BoundedTraitsN<TriangleN>::getCenter = the cached centroid (v0 + v1 + v2) / 3 (BoundedTraitsN.hpp:219,
+    // Triangle3.hpp:149), not the box centre
+    for (size_t f = 0; f < (size_t)nf; ++f) {
+      boxes[f] = tris[f].bounds();
+      centers[f] = (tris[f].v0 + tris[f].v1 + tris[f].v2) / S(3);
+    }
     tree.build(nf, [&](int64_t i) -> Box<S> const & { return boxes[(size_t)i]; },
                [&](int64_t i) -> V3<S> const & { return centers[(size_t)i]; }, max_leaf);
   }
 
   // ---- closest point, reference mode (closestElement -> closestPair -> processNeighbors, BvhN.hpp:1050-1114,1868-1893,
   //      2038-2089). Returns the element index or -1; mad is the squared distance as stored by the reference (double).
+  // BvhN::closestPair with a distance bound (BvhN.hpp:1093-1107): a query farther from the root box than the bound
+  // (squared distances, FP32 box distance compared in double) has no element; otherwise accelerationBound returns the
+  // bound itself, which is loosened by max(0.001 |root box extent|, 100 eps) before the search. Returns the loosened
+  // squared bound, or -2 when the query is cut, -1 when unbounded.
+  double closestBound(Box<S> const & qb, double dist_bound) const {
+    if (dist_bound < 0) return -1;
+    double lb = (double)qb.squaredDistance(tree.nodes[0].bounds);
+    if (lb >= 0 && lb > dist_bound * dist_bound) return -2;
+    double fudge = std::max((double)(0.001 * (double)norm(tree.nodes[0].bounds.extent())),
+                            (double)(S(100) * std::numeric_limits<S>::epsilon()));
+    double b = dist_bound + fudge;
+    return b * b;
+  }
+
   int64_t closestRef(V3<S> const & q, double dist_bound, double & mad_out, V3<S> & cp_out) const {
     if (tree.nodes.empty()) return -1;
     Box<S> qb; qb.merge(q);
-    double mon_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
-    if (mon_bound >= 0) {
-      double lb = (double)qb.squaredDistance(tree.nodes[0].bounds);
-      if (lb >= 0 && lb > mon_bound) return -1;
-    }
+    double mon_bound = closestBound(qb, dist_bound);
+    if (mon_bound == -2) return -1;
     int64_t best_idx = -1;
     double best_mad = mon_bound >= 0 ? mon_bound : -1;
     V3<S> best_cp;
@@ -471,7 +757,8 @@ template <class S> struct MeshIndex {
   int64_t closestContract(V3<S> const & q, double dist_bound, S & best_d2, V3<S> & cp_out) const {
     if (tree.nodes.empty()) return -1;
     Box<S> qb; qb.merge(q);
-    double mon_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    double mon_bound = closestBound(qb, dist_bound);
+    if (mon_bound == -2) return -1;
     int64_t best_idx = -1;
     S bd2 = std::numeric_limits<S>::infinity();
     V3<S> bcp;
@@ -507,6 +794,49 @@ template <class S> struct MeshIndex {
       }
     }
     if (best_idx >= 0) { best_d2 = bd2; cp_out = bcp; }
+    return best_idx;
+  }
+
+  // ---- nearest element to a query triangle, contract mode: smallest squared triangle-triangle distance computed with
+  //      the element as "this" (TriangleN::squaredDistance, Triangle3.hpp:314-400), lowest index among ties; only
+  //      distances with (double)d2 < dist_bound^2 when dist_bound >= 0. Node boxes (padded by the build) prune by the
+  //      box-box distance (AxisAlignedBoxN::squaredDistance, AxisAlignedBoxN.hpp:429-442).
+  int64_t closestTriangleContract(Tri<S> const & q, double dist_bound, S & best_d2) const {
+    if (tree.nodes.empty()) return -1;
+    Box<S> qb = q.bounds();
+    double mon_bound = dist_bound >= 0 ? dist_bound * dist_bound : -1;
+    int64_t best_idx = -1;
+    S bd2 = std::numeric_limits<S>::infinity();
+    std::vector<int64_t> stack;
+    stack.push_back(0);
+    while (!stack.empty()) {
+      int64_t ni = stack.back(); stack.pop_back();
+      KdNode<S> const & n = tree.nodes[(size_t)ni];
+      S bd = qb.squaredDistance(n.bounds);
+      if (best_idx >= 0 && bd > bd2) continue;
+      if (mon_bound >= 0 && (double)bd > mon_bound) continue;
+      if (n.isLeaf()) {
+        for (int64_t k = n.first; k < n.first + n.count; ++k) {
+          int64_t idx = tree.index[(size_t)k];
+          V3<S> pa, pb;
+          S d2 = triangleTriangleSquaredDistance(tris[(size_t)idx], q, pa, pb);
+          if (!(d2 == d2)) continue;
+          if (mon_bound >= 0 && !((double)d2 < mon_bound)) continue;
+          if (best_idx < 0 || d2 < bd2 || (d2 == bd2 && idx < best_idx)) { bd2 = d2; best_idx = idx; }
+        }
+      } else {
+        S c0 = qb.squaredDistance(tree.nodes[(size_t)n.child[0]].bounds);
+        S c1 = qb.squaredDistance(tree.nodes[(size_t)n.child[1]].bounds);
+        if (c1 < c0) {
+          stack.push_back(n.child[0]);
+          stack.push_back(n.child[1]);
+        } else {
+          stack.push_back(n.child[1]);
+          stack.push_back(n.child[0]);
+        }
+      }
+    }
+    if (best_idx >= 0) best_d2 = bd2;
     return best_idx;
   }
 

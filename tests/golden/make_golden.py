@@ -2,8 +2,8 @@
 
 Inputs are small and seeded; outputs are the oracle's contract-mode results (lowest index among ties) and its
 reference-mode results (the reference kd-tree and traversal order). The fixtures pin the oracle against regressions and
-give the GPU tests exact expected values. They are not outputs of the reference itself: the reference cannot be built
-here (Eigen is absent), so parity remains unpinned against it.
+give the GPU tests exact expected values. Outputs of the reference itself are in reference_outputs.npz
+(make_ref_golden.py), which pins the oracle's reference mode to the reference's own code.
 
 The "testbvh" fixture restates the seeded scenario of the reference's own BVH test (Code/Source/Test/TestBvh.cpp:120-126,
 143-150, 318-326, 369-378, 405-407): one Random(0xFFFF) stream feeds 10,000 points, a second set of 10,000 points, 1,000

@@ -93,12 +93,82 @@ def test_point_mesh_pairs_both_ways(T, oracle):
     assert got2[:3] == (int(ri[o2]), int(o2), float(d2[o2]))
     np.testing.assert_array_equal(got2[3], rcp[o2].astype(np.float32))
     np.testing.assert_array_equal(got2[4], P[o2])
-    # mesh-mesh pairs are not supported
-    from thea_gb300 import TheaError
-    with pytest.raises(TheaError):
-        mesh.closest_pair(mesh)
     mesh.close()
     pts.close()
+
+
+def _mesh_pair_check(oracle, got, want):
+    """GPU (query, target, d2, query point, target point) against the oracle's, bit for bit."""
+    assert want[0] >= 0 and got is not None
+    assert got[:2] == (want[0], want[1])
+    assert got[2] == np.float32(want[2])
+    np.testing.assert_array_equal(got[3], want[3].astype(np.float32))
+    np.testing.assert_array_equal(got[4], want[4].astype(np.float32))
+
+
+def test_mesh_mesh_closest_pair_against_brute_force(T, oracle):
+    """Closest pair between two triangle meshes: TriangleN::squaredDistance with the target triangle as "this"
+    (Triangle3.hpp:314-400), lowest query then target index among ties, against every triangle pair on the CPU."""
+    Vt, Ft = W.noisy_icosphere(3, 51)
+    target = T.MeshBvh(Vt, Ft)
+    rng = np.random.default_rng(52)
+    for case in range(6):
+        Vq, Fq = W.noisy_icosphere(2 + case % 2, 60 + case)
+        scale = rng.uniform(0.2, 0.7)
+        shift = rng.normal(size=3)
+        shift *= (1.05 + scale + 0.3 * case / 5) / np.linalg.norm(shift)
+        if case == 5:
+            shift *= 0.5  # the spheres intersect: distance 0 at the first intersecting pair
+        Vq = (Vq * scale + shift).astype(np.float32)
+        query = T.MeshBvh(Vq, Fq)
+        want = oracle.mesh_pair_brute(Vt, Ft, Vq, Fq)
+        _mesh_pair_check(oracle, target.closest_pair(query), want)
+        assert target.closest_pair(query)[:3] == tuple(oracle.MeshIndex(Vt, Ft).closest_pair_contract(Vq, Fq)[:3])
+        # the other way round: roles of "this" and "other" swap
+        want2 = oracle.mesh_pair_brute(Vq, Fq, Vt, Ft)
+        _mesh_pair_check(oracle, query.closest_pair(target), want2)
+        # a bound below the closest distance: no pair; just above it: the same pair
+        d = float(np.sqrt(want[2]))
+        if d > 0:
+            assert target.closest_pair(query, dist_bound=d * 0.999) is None
+            assert target.closest_pair(query, dist_bound=d * 1.001)[:2] == (want[0], want[1])
+        query.close()
+    target.close()
+
+
+def test_mesh_mesh_pairs_touching_and_coplanar(T, oracle):
+    """Meshes that share vertices, edges and whole faces (coplanar triangles, Moller's coplanar test) and a mesh against
+    itself: every pair with a shared vertex is at distance 0, so the tie rule decides."""
+    V, F = W.noisy_icosphere(2, 53)
+    m = T.MeshBvh(V, F)
+    got = m.closest_pair(m)
+    want = oracle.mesh_pair_brute(V, F, V, F)
+    _mesh_pair_check(oracle, got, want)
+    assert got[:3] == (0, 0, 0.0)
+    # a flat grid and a copy lifted by a little, and one with a shared strip
+    Vg, Fg = W.heightfield(12, 54, amplitude=0.0)
+    Vh = Vg.copy()
+    Vh[:, 2] += 0.01
+    g, h = T.MeshBvh(Vg, Fg), T.MeshBvh(Vh, Fg)
+    _mesh_pair_check(oracle, g.closest_pair(h), oracle.mesh_pair_brute(Vg, Fg, Vh, Fg))
+    Vs = Vg.copy()
+    Vs[:, 0] += 0.5  # overlapping coplanar grids
+    s = T.MeshBvh(Vs, Fg)
+    _mesh_pair_check(oracle, g.closest_pair(s), oracle.mesh_pair_brute(Vg, Fg, Vs, Fg))
+    for x in (m, g, h, s):
+        x.close()
+
+
+def test_mesh_mesh_pair_larger_meshes_against_the_oracle_tree(T, oracle):
+    """Two 20,480-triangle noisy spheres, one stretched and shifted: the GPU pair against the oracle's kd-tree search."""
+    Vt, Ft = W.noisy_icosphere(5, 55)
+    Vq, Fq = W.noisy_icosphere(5, 56, scale=np.array([0.6, 1.3, 0.8]))
+    Vq = (Vq + np.array([1.9, 0.4, -0.2], np.float32)).astype(np.float32)
+    t, q = T.MeshBvh(Vt, Ft, width=8), T.MeshBvh(Vq, Fq)
+    want = oracle.MeshIndex(Vt, Ft).closest_pair_contract(Vq, Fq)
+    _mesh_pair_check(oracle, t.closest_pair(q), want)
+    t.close()
+    q.close()
 
 
 def test_pairs_with_a_transformed_target(T, oracle):

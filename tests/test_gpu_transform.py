@@ -48,6 +48,23 @@ def affine(seed, scale=(1.7, 0.6, 1.2), shear=0.3, shift=(0.4, -1.1, 2.5)):
     return m.astype(np.float32)
 
 
+def bounded_contract(oracle, V, M, Q, ri, rd2, bound):
+    """Closest elements under dist_bound on a BVH of V with transform M, from the unbounded lowest-index results."""
+    f32 = np.float32
+    lo, hi = V.min(0).astype(f32), V.max(0).astype(f32)
+    c = f32(0.5) * (hi + lo)
+    lo, hi = f32(1.05) * (lo - c) + c, f32(1.05) * (hi - c) + c
+    corners = np.array([[(hi if k & (1 << a) else lo)[a] for a in range(3)] for k in range(8)], f32)
+    w = oracle.affine_points(M, corners)
+    wlo, whi = w.min(0), w.max(0)
+    e = whi - wlo
+    fudge = max(0.001 * float(np.sqrt(f32(e[0] * e[0] + (e[1] * e[1] + e[2] * e[2])))), float(f32(100) * f32(2.0 ** -23)))
+    d = np.maximum(np.maximum(Q, wlo) - np.minimum(Q, whi), f32(0)).astype(f32)
+    lb = d[:, 0] * d[:, 0] + (d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    keep = (lb.astype(np.float64) <= bound * bound) & (rd2.astype(np.float32).astype(np.float64) < (bound + fudge) ** 2)
+    return np.where(keep, ri, -1)
+
+
 def test_closest_point_on_transformed_mesh(T, oracle):
     V, F = W.noisy_icosphere(4, 51)
     M = affine(52)
@@ -70,10 +87,11 @@ def test_closest_point_on_transformed_mesh(T, oracle):
     # FP64 re-check mode runs on the world-space copy too
     i64, _, _, err = bvh.closest_element_ex(dev(Q), precision="fp64")
     assert host(err).max() <= 1e-6 * max(1.0, float(np.abs(Vw).max()))
-    # dist_bound applies in world space
+    # dist_bound applies in world space, as the reference's closestPair applies it to a transformed BVH: the root box
+    # is the object-space element box grown by 1.05 and mapped by transformAndBound, a query farther than the bound
+    # from it gets nothing, and the bound is loosened by 0.1 % of that box's diagonal
     bi, _, _ = bvh.closest_element(dev(Q), dist_bound=0.2)
-    rbi, _, _ = oracle.MeshIndex(Vw, F).closest_contract(Q, dist_bound=0.2)
-    assert np.array_equal(host(bi), rbi)
+    assert np.array_equal(host(bi), bounded_contract(oracle, V, M, Q, ri, rd2, 0.2))
     # clearing the transform restores the object-space answers
     bvh.clear_transform()
     assert bvh.transform() is None

@@ -141,7 +141,8 @@ class _Bvh:
 
     def closest_pair(self, query, dist_bound=-1.0):
         """BvhN::closestPair with another BVH (``query``) as the query: (query index, target index, squared distance,
-        query point, target point), or None when no pair qualifies. One side must hold points."""
+        query point, target point), or None when no pair qualifies. Points and meshes on either side; between two
+        meshes the distance is TriangleN::squaredDistance with the target triangle as "this"."""
         qi, ti, d2 = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float()
         qp, tp = np.zeros(3, np.float32), np.zeros(3, np.float32)
         N.check(N.lib().thea_bvh_closest_pair(self._h, query.handle, float(dist_bound), ctypes.byref(qi),

@@ -563,10 +563,12 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
   THEA_REQUIRE(num_queries >= 0, "closest_element: negative query count");
   if (num_queries == 0) return;
   THEA_REQUIRE(queries && out_index, "closest_element: null queries or out_index");
+  // the reference's handling of dist_bound (root-box cut, loosened bound), from the handle's own (object-space) box
+  BoundCut cut = closest_bound_cut(mesh_bvh, dist_bound);
   mesh_bvh = query_target(mesh_bvh);
   ClosestParams cp;
-  cp.thresh = bound_threshold(dist_bound);
-  cp.bound2 = dist_bound >= 0.f ? (double)dist_bound * (double)dist_bound : -1.0;
+  cp.thresh = cut.thresh;
+  cp.bound2 = cut.bound2;
   cp.precision = precision;
   cp.scene_scale = scene_scale_of(mesh_bvh);
   unsigned * err = handle_error_word(mesh_bvh);
@@ -579,6 +581,8 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
     c2.budget = 256;  // the step budget of the device-resident two-phase path
     run_closest_stream(mesh_bvh, (float const *)dp[0], num_queries, c2, (int32_t *)dp[1], (float *)dp[2],
                        (float *)dp[3], (cudaStream_t)stream);
+    run_closest_cut((float const *)dp[0], num_queries, cut, nullptr, 1, nullptr, (int32_t *)dp[1], (float *)dp[2],
+                    (float *)dp[3], nullptr, (cudaStream_t)stream);
     sync_stream((cudaStream_t)stream);
     return;
   }
@@ -588,6 +592,8 @@ static void closest_impl(const thea_bvh * mesh_bvh, const float * queries, int64
              [&](int64_t, int64_t cnt, std::vector<void *> const & p, cudaStream_t s) {
                run_closest(mesh_bvh, (float const *)p[0], cnt, cp, (int32_t *)p[1], (float *)p[2], (float *)p[3],
                            (float *)p[4], err, s);
+               run_closest_cut((float const *)p[0], cnt, cut, nullptr, 1, nullptr, (int32_t *)p[1], (float *)p[2],
+                               (float *)p[3], (float *)p[4], s);
              });
 }
 
@@ -1030,13 +1036,22 @@ THEA_API thea_status thea_batch_closest_element(const thea_bvh * mesh_forest, co
     if (num_queries == 0) return;
     THEA_REQUIRE(queries && out_index, "batch_closest_element: null queries or out_index");
     ClosestParams cp;
-    cp.thresh = bound_threshold(dist_bound);
-    cp.bound2 = dist_bound >= 0.f ? (double)dist_bound * (double)dist_bound : -1.0;
     cp.precision = precision;
     cp.scene_scale = scene_scale_of(mesh_forest);
     cp.budget = hard_query_budget == 0 ? 32 : (hard_query_budget < 0 ? 0 : hard_query_budget);
+    // each mesh applies the bound as closestElement on that mesh alone would (BoundCut): per-mesh cuts on the device
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch cuts;
+    if (dist_bound >= 0.f) {
+      cuts = Scratch((size_t)mesh_forest->num_segments * sizeof(BoundCut), s);
+      run_segment_cuts(mesh_forest, dist_bound, cuts.as<BoundCut>(), s);
+      cp.seg_cut = cuts.as<BoundCut>();
+    }
     run_batch_closest(mesh_forest, queries, query_offsets, num_queries, cp, chunk, out_index, out_distance,
-                      out_closest_point, out_error, (cudaStream_t)stream);
+                      out_closest_point, out_error, s);
+    if (dist_bound >= 0.f)
+      run_closest_cut(queries, num_queries, BoundCut(), query_offsets, mesh_forest->num_segments, cuts.as<BoundCut>(),
+                      out_index, out_distance, out_closest_point, out_error, s);
   });
 }
 
@@ -1353,6 +1368,7 @@ THEA_API thea_status thea_bvh_closest_pair(const thea_bvh * target, const thea_b
     if (out_sq_distance) *out_sq_distance = r.d2;
     if (out_query_point) std::memcpy(out_query_point, r.query_point, 12);
     if (out_target_point) std::memcpy(out_target_point, r.target_point, 12);
+    sync_stream((cudaStream_t)stream);
   });
 }
 

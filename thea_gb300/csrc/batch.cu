@@ -78,7 +78,15 @@ struct ClosestArgs {
   float * out_dist;
   float * out_cp;
   float * out_err;
+  BoundCut const * seg_cut = nullptr;  // per mesh: thresh and bound2 of that mesh (nullptr: the scalars for all)
 };
+
+__device__ __forceinline__ float thresh_of(ClosestArgs const & a, int m) {
+  return a.seg_cut ? a.seg_cut[m].thresh : a.thresh;
+}
+__device__ __forceinline__ double bound2_of(ClosestArgs const & a, int m) {
+  return a.seg_cut ? a.seg_cut[m].bound2 : a.bound2;
+}
 
 // One round: lane query q when active. Called by all 32 lanes of the warp together.
 template <int W, int STACK, int PREC>
@@ -88,11 +96,15 @@ __device__ __forceinline__ void closest_round(BatchForest const & f, ClosestArgs
   int root = 0;
   int64_t ebase = 0;
   V3 p = V3{0.f, 0.f, 0.f};
+  float thresh = a.thresh;
+  double bound2 = a.bound2;
   if (active) {
     int m = mesh_of_query(a.qoff, f.M, q);
     root = __ldg(f.seg_root + m);
     ebase = __ldg(f.seg_start + m);
     p = load_v3(a.queries + 3 * q);
+    thresh = thresh_of(a, m);
+    bound2 = bound2_of(a, m);
   }
   ClosestOut r;
   r.idx = INT_MAX;
@@ -105,13 +117,13 @@ __device__ __forceinline__ void closest_round(BatchForest const & f, ClosestArgs
   if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
     float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
     F64Search s;
-    if (active) closest_search_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, a.bound2, scale, f.err, s, budget);
+    if (active) closest_search_f64<W, STACK>(nodes, f.cp_rec, root, ebase, p, bound2, scale, f.err, s, budget);
     else f64_search_init(s);
-    f64_resolve_warp(s, active && s.done, f.cp_rec, ebase, p, a.bound2, *buf);
+    f64_resolve_warp(s, active && s.done, f.cp_rec, ebase, p, bound2, *buf);
     r = f64_result(s);
     dist = (float)sqrt(r.d2_64);
   } else {
-    if (active) r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, a.thresh, f.err, budget);
+    if (active) r = closest_query<W, STACK>(nodes, f.cp_rec, root, ebase, p, thresh, f.err, budget);
     dist = sqrtf(r.d2);
   }
   if (active && !r.done) {
@@ -189,6 +201,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
   F64Search s;
   float best32 = INFINITY, abs_tol = 0.f;
   int pops = 0;  // stack entries taken by this lane's query (two-phase form: budget > 0)
+  double bound2 = a.bound2;  // this lane's mesh's FP64 bound
   if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) f64_search_init(s);
   while (true) {
     unsigned idle = __ballot_sync(FULL, q < 0);
@@ -213,13 +226,14 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
           sp = 0;
           next = __ldg(f.seg_root + m);
           pops = 0;
+          bound2 = bound2_of(a, m);
           if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
             f64_search_init(s);
             float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-            best = f64_band_start(a.bound2, scale, abs_tol);
+            best = f64_band_start(bound2, scale, abs_tol);
             best32 = INFINITY;
           } else {
-            best = a.thresh;
+            best = thresh_of(a, m);
             best_idx = INT_MAX;
             best_slot = -1;
           }
@@ -231,7 +245,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
       unsigned pend = __ballot_sync(FULL, pending);
       unsigned trav = __ballot_sync(FULL, q >= 0 && !pending);
       if (pend && (__popc(pend) >= REFILL_RESOLVE_AT || trav == 0)) {
-        f64_resolve_warp(s, pending, f.cp_rec, ebase, p, a.bound2, *buf);
+        f64_resolve_warp(s, pending, f.cp_rec, ebase, p, bound2, *buf);
         if (pending) {
           ClosestOut r = f64_result(s);
           write_closest(q, r.idx != INT_MAX, (float)sqrt(r.d2_64), r.cp, r.idx, r.d2_64, a.out_index, a.out_dist,
@@ -290,7 +304,7 @@ batch_closest_refill_kernel(BatchForest f, ClosestArgs a, int64_t nq, unsigned l
       int first, count;
       decode_leaf(code, first, count);
       if constexpr (PREC == THEA_PRECISION_FP64_RECHECK)
-        cp_leaf_f64(f.cp_rec, ebase, first, count, p, a.bound2, abs_tol, best, best32, s);
+        cp_leaf_f64(f.cp_rec, ebase, first, count, p, bound2, abs_tol, best, best32, s);
       else
         cp_leaf_fp32(f.cp_rec, ebase, first, count, p, best, best_idx, best_slot, best_cp);
     }
@@ -321,7 +335,7 @@ batch_closest_phase2_kernel(BatchForest f, ClosestArgs a, HardQueue hq, unsigned
     V3 p = load_v3(a.queries + 3 * q);
     if (PREC == THEA_PRECISION_FP64_RECHECK) {
       float scale = fmaxf(a.scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
-      WarpBest64 b = closest_warp_query_f64<W>(nodes, f.cp_rec, root, ebase, p, a.bound2, scale, hq.bound[j],
+      WarpBest64 b = closest_warp_query_f64<W>(nodes, f.cp_rec, root, ebase, p, bound2_of(a, m), scale, hq.bound[j],
                                                s_code[warp], s_lb[warp], s_cd[warp], s_ck[warp], f.err);
       if (lane == 0) {
         bool found = b.idx != INT_MAX;
@@ -337,7 +351,7 @@ batch_closest_phase2_kernel(BatchForest f, ClosestArgs a, HardQueue hq, unsigned
     } else {
       WarpBest init;
       init.idx = hq.idx[j];
-      init.d2 = init.idx != INT_MAX ? hq.bound[j] : a.thresh;
+      init.d2 = init.idx != INT_MAX ? hq.bound[j] : thresh_of(a, m);
       init.slot = hq.slot[j];
       WarpBest b = closest_warp_query<W>(nodes, f.cp_rec, root, ebase, p, init, s_code[warp], s_lb[warp], f.err);
       if (lane == 0) {
@@ -647,7 +661,7 @@ void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff
   if (nq <= 0) return;
   BatchForest f = forest_view(b);
   bool sm = small_stack_ok(b);
-  ClosestArgs a{q, qoff, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, err};
+  ClosestArgs a{q, qoff, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, err, cp.seg_cut};
   int budget = cp.budget > 0 ? cp.budget : 0;
   Scratch counters(3 * sizeof(unsigned long long), s);
   THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));

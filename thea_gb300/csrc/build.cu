@@ -15,6 +15,7 @@
 // and element records store the element's index within its segment (the face index within its mesh).
 #include "bvh.hpp"
 #include "device_util.cuh"
+#include "query.hpp"
 
 #include <algorithm>
 #include <vector>
@@ -695,12 +696,24 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
       }
     }
     b->device_bytes = node_bytes + rec_bytes;
+    init_segment_roots(b, stream);
     return b;
   } catch (...) {
     cudaStreamSynchronize(stream);
     destroy_bvh(b);
     throw;
   }
+}
+
+void init_segment_roots(thea_bvh * b, cudaStream_t stream) {
+  int M = b->num_segments;
+  std::vector<RootCut> h((size_t)M);
+  for (int s = 0; s < M; ++s) h[(size_t)s] = root_cut_of(&b->seg_lo[3 * (size_t)s], &b->seg_hi[3 * (size_t)s], nullptr);
+  if (b->seg_roots) cudaFree(b->seg_roots);
+  b->seg_roots = nullptr;
+  THEA_CUDA_CHECK(thea_malloc(&b->seg_roots, (size_t)M * sizeof(RootCut)));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(b->seg_roots, h.data(), (size_t)M * sizeof(RootCut), cudaMemcpyHostToDevice, stream));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
 }
 
 void check_face_indices(int32_t const * F, int64_t nf, int64_t nv, char const * what, cudaStream_t stream) {
@@ -741,6 +754,7 @@ void destroy_bvh(thea_bvh * b) {
   if (b->err_host) cudaFreeHost(b->err_host);
   if (b->seg_start) cudaFree(b->seg_start);
   if (b->seg_root) cudaFree(b->seg_root);
+  if (b->seg_roots) cudaFree(b->seg_roots);
   if (prev >= 0) cudaSetDevice(prev);
   delete b;
 }

@@ -5,6 +5,13 @@
 
 #include <vector>
 
+// A BVH's root box as the reference's closestPair sees it (the element bounds grown by 1.05 about their centre, mapped
+// by the transform if any) and the loosening it adds to a distance bound: max(0.001 |root box extent|, 100 eps)
+struct RootCut {
+  float lo[3], hi[3];
+  double fudge;
+};
+
 // Opaque to C callers; immutable once built.
 struct thea_bvh {
   int32_t is_mesh = 0;
@@ -31,6 +38,7 @@ struct thea_bvh {
   int32_t * seg_root = nullptr;      // device, num_segments: root wide node of each segment
   std::vector<int64_t> seg_start_host;
   std::vector<float> seg_lo, seg_hi;  // per-segment element bounds (3 floats each)
+  RootCut * seg_roots = nullptr;      // device, num_segments: per-segment root cuts (distance bounds of closest queries)
   // affine transform (BvhN::setTransform): row-major 3x4 [L | t] and its FP32 inverse; `world` is the world-space copy
   // of the element records that closest-point, k-NN and radius queries read (it shares this handle's error word)
   int32_t has_transform = 0;
@@ -48,6 +56,9 @@ thea_bvh * build_bvh(bool is_mesh, float const * V, int64_t nv, int32_t const * 
 thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const * F, int64_t n_elems,
                         int64_t const * seg_start_host, int M, thea_build_config const & cfg, cudaStream_t stream);
 void destroy_bvh(thea_bvh * b);
+
+// Fills seg_roots from seg_lo / seg_hi (allocates it; synchronizes the stream)
+void init_segment_roots(thea_bvh * b, cudaStream_t stream);
 
 // Throws INVALID_ARGUMENT unless every face index lies in [0, nv): checked on the device before any kernel loads a
 // vertex through the faces (one pass over F and one 4-byte read back, which synchronizes `stream`).

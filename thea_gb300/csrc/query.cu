@@ -3,6 +3,7 @@
 #include "bvh.hpp"
 #include "device_util.cuh"
 #include "query.hpp"
+#include "transform.hpp"
 #include "traverse_ops.cuh"
 #include "batch.hpp"
 
@@ -643,6 +644,90 @@ void launch_range(thea_bvh const * b, float const * q, int64_t n, float r2, int3
   THEA_LAUNCH(range_emit_kernel, (unsigned)ceil_div(total, 256), 256, 0, s, keys.as<uint64_t>(), perm.as<uint32_t>(),
               d2.as<float>(), total, out_idx, out_d2);
 }
+
+//============================================================================================================================
+// Distance bounds of closest-element queries (BoundCut in query.hpp)
+//============================================================================================================================
+
+}  // namespace
+
+RootCut root_cut_of(float const * elem_lo, float const * elem_hi, float const * xf) {
+  RootCut r;
+  float lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    // scaleCentered(1.05f): centre = 0.5 (hi + lo); lo = 1.05 (lo - centre) + centre, hi likewise
+    float ctr = 0.5f * (elem_hi[a] + elem_lo[a]);
+    lo[a] = 1.05f * (elem_lo[a] - ctr) + ctr;
+    hi[a] = 1.05f * (elem_hi[a] - ctr) + ctr;
+  }
+  if (xf) {
+    // transformAndBound: the box of the eight mapped corners
+    float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 8; ++k) {
+      V3 w = affine_point(xf, V3{(k & 1) ? hi[0] : lo[0], (k & 2) ? hi[1] : lo[1], (k & 4) ? hi[2] : lo[2]});
+      float wc[3] = {w.x, w.y, w.z};
+      for (int a = 0; a < 3; ++a) {
+        wlo[a] = std::min(wlo[a], wc[a]);
+        whi[a] = std::max(whi[a], wc[a]);
+      }
+    }
+    for (int a = 0; a < 3; ++a) lo[a] = wlo[a], hi[a] = whi[a];
+  }
+  for (int a = 0; a < 3; ++a) r.lo[a] = lo[a], r.hi[a] = hi[a];
+  V3 ext = V3{hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  float nrm = std::sqrt(squared_norm(ext));
+  r.fudge = std::max(0.001 * (double)nrm, (double)(100.0f * 1.1920928955078125e-07f));
+  return r;
+}
+
+namespace {
+
+__global__ void closest_cut_kernel(float const * __restrict__ q, int64_t n, int64_t const * __restrict__ qoff, int M,
+                                   BoundCut one, BoundCut const * __restrict__ cuts, int32_t * __restrict__ idx,
+                                   float * __restrict__ dist, float * __restrict__ cpt, float * __restrict__ errout) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  BoundCut c = one;
+  if (cuts) {
+    int lo = 0, hi = M - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (__ldg(qoff + mid) <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    c = cuts[lo];
+  }
+  if (!bound_cut_out(c, load_v3(q + 3 * i))) return;
+  idx[i] = -1;
+  if (dist) dist[i] = -1.f;
+  if (cpt) cpt[3 * i] = cpt[3 * i + 1] = cpt[3 * i + 2] = 0.f;
+  if (errout) errout[i] = -1.f;
+}
+
+}  // namespace
+
+namespace {
+__global__ void segment_cuts_kernel(RootCut const * __restrict__ roots, int M, float dist_bound,
+                                    BoundCut * __restrict__ out) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < M) out[m] = make_bound_cut(roots[m], dist_bound);
+}
+}  // namespace
+
+void run_segment_cuts(thea_bvh const * b, float dist_bound, BoundCut * out, cudaStream_t s) {
+  THEA_REQUIRE(b->seg_roots, "segment cuts: the forest has no per-segment root boxes");
+  THEA_LAUNCH(segment_cuts_kernel, (unsigned)ceil_div(b->num_segments, 256), 256, 0, s, b->seg_roots,
+              b->num_segments, dist_bound, out);
+}
+
+void run_closest_cut(float const * q, int64_t n, BoundCut const & one, int64_t const * qoff, int M,
+                     BoundCut const * cuts, int32_t * idx, float * dist, float * cpt, float * errout, cudaStream_t s) {
+  if (n <= 0 || (!cuts && one.b2 < 0.0)) return;
+  THEA_LAUNCH(closest_cut_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, q, n, qoff, M, one, cuts, idx, dist, cpt,
+              errout);
+}
+
+namespace {
 
 //============================================================================================================================
 // Query ordering: large batches can be traversed in the order of a Morton code of the query point (rays: of the

@@ -47,6 +47,7 @@ struct ServeTask {
   float scene_scale;
   int32_t k;
   int32_t pad;
+  BoundCut cut;        // closest: the reference's distance-bound cut of the mesh (queries it removes get no element)
 };
 
 __device__ __forceinline__ int task_of(int64_t const * __restrict__ off, int T, int64_t q) {
@@ -132,7 +133,7 @@ serve_closest_kernel(ServeTask const * __restrict__ tasks, int64_t const * __res
       active = false;
     }
     if (active) {
-      bool found = r.idx != INT_MAX;
+      bool found = r.idx != INT_MAX && !bound_cut_out(t->cut, p);
       t->out_index[i] = found ? r.idx : -1;
       if (t->out_value) t->out_value[i] = found ? dist : -1.f;
       if (t->out_point) {
@@ -195,6 +196,7 @@ serve_closest_phase2_kernel(ServeTask const * __restrict__ tasks, int64_t const 
       if (found && lane == 0 && t->out_point) cp_record_test(t->rec, b.slot, p, cp);
     }
     if (lane == 0) {
+      found = found && !bound_cut_out(t->cut, p);
       t->out_index[i] = found ? idx : -1;
       if (t->out_value) t->out_value[i] = found ? dist : -1.f;
       if (t->out_point) {
@@ -514,6 +516,10 @@ void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *>
     t.scene_scale = m->scene_scale;
     if (type == THEA_REQUEST_RAY) {
       t.thresh = r.bound >= 0.f ? r.bound : -1.f;
+    } else if (type == THEA_REQUEST_CLOSEST) {
+      t.cut = closest_bound_cut(m->mesh, r.bound);
+      t.thresh = t.cut.thresh;
+      t.bound2 = t.cut.bound2;
     } else {
       t.thresh = threshold_of(r.bound);
       t.bound2 = r.bound >= 0.f ? (double)r.bound * (double)r.bound : -1.0;
