@@ -747,12 +747,14 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     # the client is this Python loop: keep the garbage collector from pausing it in the middle of the arrival stream
     gc.collect()
     gc.disable()
+    late = np.zeros(n_req)
     with ClockSampler(torch.cuda.current_device()) as clk:
         start = time.perf_counter()
         for r in range(n_req):
             now = time.perf_counter() - start
             if arrive[r] > now:
                 time.sleep(arrive[r] - now)
+            late[r] = time.perf_counter() - start - arrive[r]
             n, m, kd = int(nq[r]), int(mesh[r]), names[kind[r]]
             k = 8 if kd == "knn" else 1
             oi, ov = outputs(n * k)
@@ -770,7 +772,26 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     st = srv.stats()
     srv.close()
     small = nq <= 65536
+    # algorithmic bytes of the queries (12 B per point or 24 B per ray in; 20 B closest, 8 B ray, 8 x 8 B k-NN out)
+    qbytes = np.where(kind == 0, 32, np.where(kind == 1, 32, 12 + 8 * 8)) * nq
+    per_kind = {}
+    for kd_i, kd in enumerate(names):
+        sel = kind == kd_i
+        sm = sel & small
+        per_kind[kd] = {"requests": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
+                        "p99_ms": float(np.percentile(lat[sel], 99)),
+                        "small_p50_ms": float(np.percentile(lat[sm], 50)) if sm.any() else None,
+                        "small_p99_ms": float(np.percentile(lat[sm], 99)) if sm.any() else None}
     res.update({
+        "per_kind": per_kind,
+        "hbm": {"query_bytes": int(qbytes.sum()), "achieved_gbs": float(qbytes.sum() / st["busy_seconds"] / 1e9),
+                "frac": float(qbytes.sum() / st["busy_seconds"] / 1e9 / peaks()[0]),
+                "basis": "query input and output bytes over the server's busy time; the resident meshes are read "
+                         "from L2/HBM by every batch and not counted"},
+        "client_lateness_ms": {"p50": float(1e3 * np.percentile(late, 50)), "p99": float(1e3 * np.percentile(late, 99)),
+                               "max": float(1e3 * late.max()),
+                               "meaning": "submit time minus scheduled arrival (the Python client); latency itself is "
+                                          "measured by the server from submit to results written"},
         "requests": n_req, "offered_rate_per_s": n_req / arrive[-1], "submit_span_s": submit_s, "drain_s": total_s,
         "queries": int(nq.sum()), "mix": {"closest": int((kind == 0).sum()), "ray": int((kind == 1).sum()),
                                            "knn": int((kind == 2).sum())},
@@ -798,6 +819,9 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
     res["generate_s"] = time.perf_counter() - t0
     nq = Q.shape[0]
     qoff_h = qoff.cpu().numpy()
+    # algorithmic bytes: 32 B per query (12 in, 20 out) + every mesh once (12 B per vertex and per face)
+    algo = 32 * nq + 12 * V.shape[0] + 12 * F.shape[0]
+    res["algorithmic_bytes"] = int(algo)
     # autotune on every 16th mesh
     samp = np.arange(0, num_meshes, 16)
     sv, sf, sq, sfo, sqo, vb = [], [], [], [0], [0], 0
@@ -838,7 +862,8 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
         _, d, _, e = forest.batch_closest_element(Q, qoff, errors=True, **kw)
         rel = (e / torch.clamp(d, min=1e-6 * float(Q.abs().max()))).max().item()
         res["batched_" + prec] = {"value": nq / (statistics.median(ms) / 1e3) / 1e6, "unit": "Mqueries/s",
-                                  "ms": statistics.median(ms), "max_rel_error_vs_fp64": rel}
+                                  "ms": statistics.median(ms), "max_rel_error_vs_fp64": rel,
+                                  "roofline_frac": algo / (statistics.median(ms) / 1e3) / 1e9 / peaks()[0]}
         results[prec] = (out[0].cpu().numpy(), out[1].cpu().numpy(), out[2].cpu().numpy())
     forest.close()
     if not args.no_cpu:
@@ -887,7 +912,8 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
     torch.cuda.synchronize()
     q_ms = sum(a.elapsed_time(b) for a, b in ev)
     res["plain_loop"] = {"value": nq / (q_ms / 1e3) / 1e6, "unit": "Mqueries/s", "query_ms": q_ms,
-                         "build_s": t_build, "meshes": num_meshes}
+                         "build_s": t_build, "meshes": num_meshes,
+                         "roofline_frac": algo / (q_ms / 1e3) / 1e9 / peaks()[0]}
     res["batched_vs_plain_fp32"] = res["batched_fp32"]["value"] / res["plain_loop"]["value"]
     res["batched_vs_plain_fp64"] = res["batched_fp64"]["value"] / res["plain_loop"]["value"]
     return res
