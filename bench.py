@@ -98,6 +98,18 @@ def case_gram_knn():
     torch.cuda.synchronize()
 
 
+def case_knn():
+    """k-NN graph (k = 16) of 1,048,576 area samples of the config-0 mesh by the traversal: three calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, _ = W.config0()
+    pos, _, _ = T.sample_evenly_by_area(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), 1 << 20, 2)
+    pb = T.PointBvh(pos)
+    for _ in range(3):
+        pb.k_closest_self(16, device=True)
+    torch.cuda.synchronize()
+
+
 def case_cfg0():
     """Config 0: closest point of 262,144 queries on the noisy icosphere, three calls."""
     import torch
@@ -155,7 +167,7 @@ def case_cfg0_host():
                                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
 
 
-CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host,
+CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host, "knn": case_knn,
          "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
 
 
