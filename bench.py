@@ -75,6 +75,41 @@ def case_ray():
     torch.cuda.synchronize()
 
 
+def _case_ray_grid(grid):
+    import torch
+    import thea_gb300 as T
+    V, F, o, d = W.config1(grid=grid)
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=2)
+    od, dd = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    for _ in range(3):
+        bvh.ray_structure_intersection(od, dd)
+    torch.cuda.synchronize()
+
+
+def case_ray_hf512():
+    """The config-1 rays on a 512 x 512-vertex heightfield (522,242 triangles; nodes + ray records about 42 MB, a
+    third of L2): three plain calls."""
+    _case_ray_grid(512)
+
+
+def case_ray_hf2048():
+    """The config-1 rays on a 2048 x 2048-vertex heightfield (8,380,418 triangles; nodes + ray records about 670 MB):
+    three plain calls."""
+    _case_ray_grid(2048)
+
+
+def case_cfg0_32k():
+    """Closest point of the first 32,768 config-0 queries (one query per thread, oriented slabs): three calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, Q = W.config0()
+    bvh = T.MeshBvh(torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda(), layouts=1, max_leaf_size=1)
+    q = torch.from_numpy(Q[:32768]).cuda()
+    for _ in range(3):
+        bvh.closest_element(q)
+    torch.cuda.synchronize()
+
+
 def case_cfg3_fp64_64():
     """Batched closest point with FP64 re-check over 64 meshes of the config-3 distribution: two calls."""
     import torch
@@ -167,7 +202,8 @@ def case_cfg0_host():
                                              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
 
 
-CASES = {"ray": case_ray, "ray_host": case_ray_host, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host, "knn": case_knn,
+CASES = {"ray": case_ray, "ray_host": case_ray_host, "ray_hf512": case_ray_hf512, "ray_hf2048": case_ray_hf2048,
+         "cfg0_32k": case_cfg0_32k, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host, "knn": case_knn,
          "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
 
 
@@ -593,6 +629,12 @@ def extra_workloads(T, torch, stream, flush, args):
                                         "ms": 1e3 * statistics.mean(e2e_t), "h2d_bytes": 12 * CP_QUERIES,
                                         "d2h_bytes": 20 * CP_QUERIES, "same_as_device":
                                         bool(torch.equal(hi, bvh.closest_element(Qd)[0].cpu()))}
+    # a batch below the two-kernel threshold: one query per thread, children pruned by box and oriented slab
+    Qs = Qd[:32768].contiguous()
+    ms_s = timed_steps(lambda: bvh.closest_element(Qs), steps, 2, flush, stream)
+    out["closest_point_cfg0"]["first_32768_queries"] = {
+        "value": 32768 / (statistics.mean(ms_s) / 1e3) / 1e6, "unit": "Mqueries/s", "ms_per_step": statistics.mean(ms_s),
+        "same_as_full_batch": bool(torch.equal(bvh.closest_element(Qs)[0], bvh.closest_element(Qd)[0][:32768]))}
     bvh.close()
     if not args.no_cpu:
         out["closest_point_cfg0"]["cpu_baseline"] = cpu_time("cfg0", (V, F, Q))

@@ -480,8 +480,9 @@ THEA_API thea_status thea_sample_by_area(const float * vertices, int64_t num_ver
  * at the same time) race on it and must be serialized by the caller. Face indices outside [0, num_vertices) are
  * detected on the device without being dereferenced and rejected with THEA_ERR_INVALID_ARGUMENT. The call synchronizes
  * `stream` once, to read back the total area. The cumulative areas are summed by one thread in index order (the
- * reference's sequence of FP64 roundings): about 7 ms for 81,920 triangles, growing linearly to about 90 ms at
- * THEA_NOALLOC_MAX_FACES, where thea_sample_by_area takes an exact parallel scan (0.05 ms for 81,920). */
+ * reference's sequence of FP64 roundings): measured on a GB300 with 100,000 samples, 7.5 ms a call for 81,920
+ * triangles, growing linearly to 91 ms at 1,048,352, where thea_sample_by_area (an exact parallel scan) takes 0.35 and
+ * 0.41 ms. */
 THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t num_vertices, const int32_t * faces,
                                                  int64_t num_faces, int64_t num_samples, uint32_t seed, int32_t rng,
                                                  float * out_positions, float * out_normals, int32_t * out_faces,

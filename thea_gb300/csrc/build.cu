@@ -16,6 +16,7 @@
 #include "bvh.hpp"
 #include "device_util.cuh"
 #include "query.hpp"
+#include "traverse_ops.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -362,7 +363,7 @@ template <int W>
 __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
                                      int const * __restrict__ chosen, int const * __restrict__ offsets,
                                      int64_t level_base, int64_t next_base, WideNode<W> * __restrict__ nodes,
-                                     int * __restrict__ next_frontier) {
+                                     int * __restrict__ next_frontier, int2 * __restrict__ ranges) {
   int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= fsize) return;
   WideNode<W> node;
@@ -385,6 +386,8 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
     node.lox[e] = lo.x; node.loy[e] = lo.y; node.loz[e] = lo.z;
     node.hix[e] = hi.x; node.hiy[e] = hi.y; node.hiz[e] = hi.z;
     int cnt = code_count(a, code);
+    // the child slot's elements, a run of sorted positions, for its oriented slab
+    if (ranges) ranges[(level_base + f) * W + e] = make_int2((int)code_first(a, code), cnt);
     if (cnt <= a.leaf_size) {
       node.child[e] = encode_leaf((int)(code_first(a, code) - seg_base), cnt);
     } else {
@@ -413,7 +416,7 @@ __global__ void segment_roots_kernel(CollapseArgs a, int64_t n, int const * __re
                                      int const * __restrict__ small_rank, int const * __restrict__ is_big,
                                      int const * __restrict__ big_rank, int num_small, int const * __restrict__ bounds,
                                      WideNode<W> * __restrict__ nodes, int * __restrict__ frontier,
-                                     int * __restrict__ seg_root) {
+                                     int * __restrict__ seg_root, int2 * __restrict__ ranges) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.M) return;
   int64_t sa = a.seg_start ? a.seg_start[s] : 0, sb = a.seg_start ? a.seg_start[s + 1] : n;
@@ -431,6 +434,7 @@ __global__ void segment_roots_kernel(CollapseArgs a, int64_t n, int const * __re
     node.hix[0] = hi.x; node.hiy[0] = hi.y; node.hiz[0] = hi.z;
     node.child[0] = encode_leaf(0, (int)(sb - sa));
     nodes[small_rank[s]] = node;
+    if (ranges) ranges[(int64_t)small_rank[s] * W] = make_int2((int)sa, (int)(sb - sa));
     seg_root[s] = small_rank[s];
   } else {
     seg_root[s] = -1;  // empty segment
@@ -496,8 +500,83 @@ __global__ void point_records_kernel(float const * __restrict__ P, int64_t n, in
   pt_rec[s] = make_float4(p.x, p.y, p.z, __int_as_float(e));
 }
 
+// Oriented slab of every child slot (slab_normal / slab_lower_bound in traverse_ops.cuh): n = the area-weighted mean of
+// the slot's triangle normals (triangles with a non-finite normal or area left out; +z if the mean vanishes), encoded
+// and decoded as the searches decode it, and the range of n . v over the slot's vertices, accumulated in double
+// (products of floats are exact in double) and rounded outwards to float. One block per slot, slots taken in a
+// grid-stride loop; slots with no elements get an empty slab.
+constexpr int SLAB_THREADS = 128;
+
+__global__ void __launch_bounds__(SLAB_THREADS)
+slab_kernel(int2 const * __restrict__ ranges, int64_t slots, float4 const * __restrict__ rec, float4 * __restrict__ out) {
+  __shared__ float s_n[3][SLAB_THREADS / 32];
+  __shared__ double s_d[2][SLAB_THREADS / 32];
+  __shared__ float4 s_enc;
+  int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int64_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
+    int2 r = ranges[slot];
+    if (r.y <= 0) {
+      if (t == 0) out[slot] = make_float4(0.f, 0.f, INFINITY, -INFINITY);
+      continue;
+    }
+    int64_t k0 = r.x, k1 = (int64_t)r.x + r.y;
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    for (int64_t k = k0 + t; k < k1; k += SLAB_THREADS) {
+      float4 nn = __ldg(rec + k * CP_REC_F4 + 3);
+      float area = __ldg(rec + k * CP_REC_F4 + 6).w;
+      if (isfinite(nn.x) && isfinite(nn.y) && isfinite(nn.z) && isfinite(area)) {
+        nx += nn.x * area;
+        ny += nn.y * area;
+        nz += nn.z * area;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      nx += __shfl_xor_sync(0xffffffffu, nx, o);
+      ny += __shfl_xor_sync(0xffffffffu, ny, o);
+      nz += __shfl_xor_sync(0xffffffffu, nz, o);
+    }
+    if (lane == 0) s_n[0][warp] = nx, s_n[1][warp] = ny, s_n[2][warp] = nz;
+    __syncthreads();
+    if (t == 0) {
+      float x = 0.f, y = 0.f, z = 0.f;
+      for (int w = 0; w < SLAB_THREADS / 32; ++w) x += s_n[0][w], y += s_n[1][w], z += s_n[2][w];
+      float l = sqrtf(x * x + y * y + z * z);
+      if (!(l > 0.f) || !isfinite(l)) x = 0.f, y = 0.f, z = 1.f, l = 1.f;
+      s_enc = slab_encode(V3{x / l, y / l, z / l});
+    }
+    __syncthreads();
+    float4 enc = s_enc;
+    V3 n = slab_normal(enc);
+    double lo = INFINITY, hi = -INFINITY;
+    for (int64_t k = k0 + t; k < k1; k += SLAB_THREADS) {
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        float4 q = __ldg(rec + k * CP_REC_F4 + v);
+        double d = (double)n.x * (double)q.x + (double)n.y * (double)q.y + (double)n.z * (double)q.z;
+        lo = fmin(lo, d);
+        hi = fmax(hi, d);
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) s_d[0][warp] = lo, s_d[1][warp] = hi;
+    __syncthreads();
+    if (t == 0) {
+      for (int w = 1; w < SLAB_THREADS / 32; ++w) lo = fmin(lo, s_d[0][w]), hi = fmax(hi, s_d[1][w]);
+      enc.z = __double2float_rd(lo);
+      enc.w = __double2float_ru(hi);
+      out[slot] = enc;
+    }
+    __syncthreads();
+  }
+}
+
+// ranges != nullptr: also records each child slot's run of sorted element positions (for the oriented slabs)
 template <int W>
-void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, cudaStream_t stream) {
+void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, Scratch * ranges,
+              cudaStream_t stream) {
   int M = a.M;
   // segment roots
   Scratch is_small((size_t)M * sizeof(int), stream), is_big((size_t)M * sizeof(int), stream);
@@ -528,9 +607,15 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
   THEA_CUDA_CHECK(thea_malloc_async((void **)&nodes, (size_t)cap * sizeof(WideNode<W>), stream));
   THEA_CUDA_CHECK(thea_malloc_async((void **)&b->seg_root, (size_t)M * sizeof(int32_t), stream));
   Scratch fa((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream), fb((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
+  int2 * rg = nullptr;
+  if (ranges) {
+    *ranges = Scratch((size_t)cap * W * sizeof(int2), stream);
+    THEA_CUDA_CHECK(cudaMemsetAsync(ranges->ptr, 0, ranges->bytes, stream));
+    rg = ranges->as<int2>();
+  }
   THEA_LAUNCH((segment_roots_kernel<W>), (unsigned)ceil_div(M, BUILD_THREADS), BUILD_THREADS, 0, stream, a, n,
               is_small.as<int>(), small_rank.as<int>(), is_big.as<int>(), big_rank.as<int>(), num_small, d_bounds,
-              nodes, fa.as<int>(), b->seg_root);
+              nodes, fa.as<int>(), b->seg_root, rg);
   Scratch chosen((size_t)std::max<int64_t>(cap, 1) * W * sizeof(int), stream);
   Scratch nint((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   Scratch offs((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
@@ -546,7 +631,7 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
                 nint.as<int>());
     exclusive_scan<int>(nint.as<int>(), offs.as<int>(), fsize, stream);
     THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
-                offs.as<int>(), base, base + fsize, nodes, nxt);
+                offs.as<int>(), base, base + fsize, nodes, nxt, rg);
     int tail[2];
     THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[0], offs.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[1], nint.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -646,8 +731,13 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     CollapseArgs a{left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), elo.as<float4>(),
                    ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(), ihi.as<float4>(),
                    M > 1 ? seg : nullptr, M, leaf};
-    if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), stream);
-    else collapse<8>(b, a, n, bounds.as<int>(), stream);
+    // Oriented slabs go with single-mesh BVHs that have the closest layout: they shorten the longest searches of the
+    // one-query-per-thread kernels (small batches, serving), whose warps wait for their slowest lane. The persistent
+    // batched kernels, which refill a lane as soon as its query ends, ran faster with boxes alone, so forests have none.
+    bool want_slabs = is_mesh && M == 1 && (layouts & THEA_LAYOUT_CLOSEST);
+    Scratch child_ranges;
+    if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), want_slabs ? &child_ranges : nullptr, stream);
+    else collapse<8>(b, a, n, bounds.as<int>(), want_slabs ? &child_ranges : nullptr, stream);
     int64_t node_bytes = b->num_nodes * (width == 4 ? (int64_t)sizeof(WideNode<4>) : (int64_t)sizeof(WideNode<8>));
 
     int need = b->depth * (width - 1) + 1;
@@ -671,6 +761,13 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
       }
       THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, seg, M, vals.as<uint32_t>(),
                   b->cp_rec, b->ray_rec, b->leaf_to_elem);
+      if (want_slabs) {
+        int64_t slots = b->num_nodes * width;
+        THEA_CUDA_CHECK(thea_malloc_async((void **)&b->slabs, (size_t)slots * sizeof(float4), stream));
+        rec_bytes += slots * (int64_t)sizeof(float4);
+        unsigned sgrid = (unsigned)std::min<int64_t>(slots, (int64_t)sm_count() * 16);
+        THEA_LAUNCH(slab_kernel, sgrid, SLAB_THREADS, 0, stream, child_ranges.as<int2>(), slots, b->cp_rec, b->slabs);
+      }
     } else {
       THEA_CUDA_CHECK(thea_malloc_async((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
       rec_bytes += n * (int64_t)sizeof(float4);
@@ -747,6 +844,7 @@ void destroy_bvh(thea_bvh * b) {
   cudaDeviceSynchronize();
   if (b->nodes) cudaFree(b->nodes);
   if (b->cp_rec) cudaFree(b->cp_rec);
+  if (b->slabs) cudaFree(b->slabs);
   if (b->ray_rec) cudaFree(b->ray_rec);
   if (b->pt_rec) cudaFree(b->pt_rec);
   if (b->leaf_to_elem) cudaFree(b->leaf_to_elem);

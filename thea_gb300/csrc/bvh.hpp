@@ -27,6 +27,8 @@ struct thea_bvh {
   float4 * cp_rec = nullptr;       // mesh closest-point records, CP_REC_F4 per element, leaf order
   float4 * ray_rec = nullptr;      // mesh ray records, RAY_REC_F4 per element, leaf order
   float4 * pt_rec = nullptr;       // point records, 1 per element, leaf order
+  float4 * slabs = nullptr;        // single mesh with the closest layout: one oriented slab per node child slot (width
+                                   // per node); not in byte images, so a deserialized handle searches by boxes alone
   int32_t * leaf_to_elem = nullptr;  // leaf-order position -> element index
   unsigned * err = nullptr;          // device word: error bits raised by query kernels
   unsigned * err_host = nullptr;     // pinned host mirror of *err, refreshed at the end of every query call

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(QUERY_THREADS)
 closest_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec, float const * __restrict__ queries,
                int64_t n, float thresh, double bound2, float scene_scale, int32_t * __restrict__ out_index,
                float * __restrict__ out_dist, float * __restrict__ out_cp, float * __restrict__ out_err,
-               unsigned * __restrict__ err, uint32_t const * __restrict__ order) {
+               unsigned * __restrict__ err, uint32_t const * __restrict__ order, float4 const * __restrict__ slabs) {
   // no early exit: the FP64 step and the error estimate run with the warp's lanes together
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool active = q < n;
@@ -40,13 +40,13 @@ closest_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict
     __shared__ F64WarpBuf buf[QUERY_THREADS / 32];
     float scale = fmaxf(scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
     F64Search s;
-    if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, bound2, scale, err, s);
+    if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, bound2, scale, err, s, 0, slabs);
     else f64_search_init(s);
     f64_resolve_warp(s, active, rec, 0, p, bound2, buf[threadIdx.x >> 5]);
     r = f64_result(s);
     dist = (float)sqrt(r.d2_64);
   } else {
-    if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, thresh, err);
+    if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, thresh, err, 0, slabs);
     dist = sqrtf(r.d2);
   }
   bool found = r.idx != INT_MAX;
@@ -501,6 +501,22 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
 #pragma unroll
   for (int j = 0; j < K; ++j) { bd[j] = start; bi[j] = INT_MAX; }
   knn_query<W, K, STACK>(nodes, pts, 0, 0, p, excl, bd, bi, err);
+  uintptr_t outs = reinterpret_cast<uintptr_t>(out_index) | reinterpret_cast<uintptr_t>(out_d2);
+  if (K % 4 == 0 && k_out == K && (outs & 15) == 0) {
+    // whole rows in 16-byte stores: rows land at scattered element indices (self mode), and full-sector writes keep
+    // the L2 from sending partial sectors to DRAM
+    int4 * oi = reinterpret_cast<int4 *>(out_index + row * K);
+    float4 * od = reinterpret_cast<float4 *>(out_d2 + row * K);
+#pragma unroll
+    for (int j = 0; j < K; j += 4) {
+      int i0 = bi[j] != INT_MAX ? bi[j] : -1, i1 = bi[j + 1] != INT_MAX ? bi[j + 1] : -1;
+      int i2 = bi[j + 2] != INT_MAX ? bi[j + 2] : -1, i3 = bi[j + 3] != INT_MAX ? bi[j + 3] : -1;
+      oi[j / 4] = make_int4(i0, i1, i2, i3);
+      od[j / 4] = make_float4(i0 >= 0 ? bd[j] : -1.f, i1 >= 0 ? bd[j + 1] : -1.f, i2 >= 0 ? bd[j + 2] : -1.f,
+                              i3 >= 0 ? bd[j + 3] : -1.f);
+    }
+    return;
+  }
   for (int j = 0; j < k_out; ++j) {
     bool v = bi[j] != INT_MAX;
     out_index[row * k_out + j] = v ? bi[j] : -1;
@@ -794,11 +810,11 @@ void launch_closest(thea_bvh const * b, float const * q, int64_t n, ClosestParam
   if (cp.precision == THEA_PRECISION_FP64_RECHECK)
     THEA_LAUNCH((closest_kernel<W, STACK, THEA_PRECISION_FP64_RECHECK>), grid, QUERY_THREADS, 0, s,
                 (WideNode<W> const *)b->nodes, b->cp_rec, q, n, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt,
-                errout, err, order);
+                errout, err, order, b->slabs);
   else
     THEA_LAUNCH((closest_kernel<W, STACK, THEA_PRECISION_FP32_REFERENCE>), grid, QUERY_THREADS, 0, s,
                 (WideNode<W> const *)b->nodes, b->cp_rec, q, n, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt,
-                errout, err, order);
+                errout, err, order, b->slabs);
 }
 
 template <int W, int STACK>

@@ -35,6 +35,7 @@ constexpr int MAX_TASKS = 4096;  // pieces per batch and query kind
 struct ServeTask {
   void const * nodes;
   float4 const * rec;  // closest: CP records; ray: ray records; k-NN: point records
+  float4 const * slabs;  // closest: oriented slabs of the mesh BVH's child slots
   float const * in0;   // query points / ray origins of the piece
   float const * in1;   // ray directions
   int32_t * out_index;
@@ -115,13 +116,13 @@ serve_closest_kernel(ServeTask const * __restrict__ tasks, int64_t const * __res
     if constexpr (PREC == THEA_PRECISION_FP64_RECHECK) {
       float scale = active ? fmaxf(t->scene_scale, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)))) : 0.f;
       F64Search s;
-      if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, t->bound2, scale, t->err, s, budget);
+      if (active) closest_search_f64<W, STACK>(nodes, rec, 0, 0, p, t->bound2, scale, t->err, s, budget, t->slabs);
       else f64_search_init(s);
       f64_resolve_warp(s, active && s.done, rec, 0, p, active ? t->bound2 : -1.0, *buf);
       r = f64_result(s);
       dist = (float)sqrt(r.d2_64);
     } else {
-      if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, t->thresh, t->err, budget);
+      if (active) r = closest_query<W, STACK>(nodes, rec, 0, 0, p, t->thresh, t->err, budget, t->slabs);
       dist = sqrtf(r.d2);
     }
     if (active && !r.done) {
@@ -512,6 +513,7 @@ void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *>
     thea_bvh const * b = type == THEA_REQUEST_KNN ? m->pts : m->mesh;
     t.nodes = b->nodes;
     t.rec = type == THEA_REQUEST_CLOSEST ? b->cp_rec : type == THEA_REQUEST_RAY ? b->ray_rec : b->pt_rec;
+    t.slabs = type == THEA_REQUEST_CLOSEST ? b->slabs : nullptr;
     t.err = b->err;
     t.scene_scale = m->scene_scale;
     if (type == THEA_REQUEST_RAY) {

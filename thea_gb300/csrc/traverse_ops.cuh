@@ -296,6 +296,114 @@ __device__ __forceinline__ void point_child_bounds(NodeRegs<W> const & nd, V3 p,
     lb[c] = point_box_d2(p.x, p.y, p.z, nd.lox[c], nd.loy[c], nd.loz[c], nd.hix[c], nd.hiy[c], nd.hiz[c]);
 }
 
+// Oriented slab of a child slot: float4 (nx, ny, dmin, dmax). The unit normal n has nz = +-sqrt(1 - nx^2 - ny^2), its
+// sign in the lowest bit of nx's encoding; every vertex v of the child's triangles satisfies dmin <= n . v <= dmax for
+// the decoded n. An empty slot has dmin = +inf, dmax = -inf.
+__host__ __device__ __forceinline__ uint32_t slab_bits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+
+__host__ __device__ __forceinline__ float slab_float(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+#endif
+}
+
+__host__ __device__ __forceinline__ V3 slab_normal(float4 s) {
+  float nz = sqrtf(fmaxf(0.f, 1.f - (s.x * s.x + s.y * s.y)));
+  return V3{s.x, s.y, (slab_bits(s.x) & 1u) ? -nz : nz};
+}
+
+__host__ __device__ __forceinline__ float4 slab_encode(V3 n) {
+  float x = slab_float((slab_bits(n.x) & ~1u) | (n.z < 0.f ? 1u : 0u));
+  return make_float4(x, n.y, 0.f, 0.f);
+}
+
+// Squared lower bound on the distance from q to a child's triangles by its slab, with d = n . q in FP32 (q1 = |q.x| +
+// |q.y| + |q.z|). A triangle lies between the slab's planes, so its distance to q is at least the distance from q to
+// the slab, |n . q - n . v| / |n| over its points v. The decoded |n| is 1 to within a few ulps; the margin subtracted
+// (2^-20 of the magnitudes involved) covers that and the FP32 rounding of n . q and of the difference.
+__device__ __forceinline__ float slab_lower_bound(float4 s, V3 q, float q1, float & d) {
+  V3 n = slab_normal(s);
+  d = n.x * q.x + (n.y * q.y + n.z * q.z);
+  float margin = (q1 + fabsf(s.z) + fabsf(s.w)) * (1.0f / 1048576.0f);
+  float g = fmaxf(d - s.w, s.z - d) - margin;
+  return g > 0.f ? g * g : 0.f;
+}
+
+// Raises the box bounds `lb` of a node's children to their slab bounds where those are larger. `order` is the visiting
+// key: the box bound, except where q lies on the inner side of every child's slab (below dmin: inside a closed
+// surface), where the slabs separate the children better than their boxes and the raised bound orders them.
+template <int W>
+__device__ __forceinline__ void slab_child_bounds(NodeRegs<W> const & nd, float4 const * __restrict__ slabs, int node,
+                                                  V3 p, float q1, float (&lb)[W], float (&order)[W]) {
+#pragma unroll
+  for (int c = 0; c < W; ++c) order[c] = lb[c];
+  float4 const * sp = slabs + (int64_t)node * W;
+  bool inner = true;
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    float4 sl = __ldg(sp + c);
+    float d;
+    lb[c] = fmaxf(lb[c], slab_lower_bound(sl, p, q1, d));
+    inner = inner && (nd.child[c] == CHILD_EMPTY || d < sl.z);
+  }
+  if (inner) {
+#pragma unroll
+    for (int c = 0; c < W; ++c) order[c] = lb[c];
+  }
+}
+
+// push_children_next with a visiting key apart from the pruning bound: the children whose bound passes `lim` are kept,
+// the one with the smallest key goes to `next`, the others are pushed with their bounds, largest key first.
+template <int W, int STACK>
+__device__ __forceinline__ void push_children_ordered(NodeRegs<W> const & nd, float const (&lb)[W],
+                                                      float const (&order)[W], float lim, int2 (&stk)[STACK], int & sp,
+                                                      int & next, unsigned * err) {
+  uint32_t key[W];
+  int slot[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    bool keep = nd.child[c] != CHILD_EMPTY && lb[c] <= lim;
+    key[c] = keep ? __float_as_uint(order[c]) : 0xffffffffu;
+    slot[c] = c;
+  }
+  sort_children<W>(key, slot);
+  // the arrays stay in registers: a slot's code and bound are picked by select loops, not by dynamic indexing
+  int code0 = CHILD_EMPTY;
+#pragma unroll
+  for (int u = 0; u < W; ++u) code0 = u == slot[0] ? nd.child[u] : code0;
+  next = key[0] != 0xffffffffu ? code0 : CHILD_EMPTY;
+#pragma unroll
+  for (int c = W - 1; c >= 1; --c) {
+    if (key[c] != 0xffffffffu) {
+      if (sp < STACK) {
+        int code = CHILD_EMPTY;
+        float bound = 0.f;
+#pragma unroll
+        for (int u = 0; u < W; ++u) {
+          code = u == slot[c] ? nd.child[u] : code;
+          bound = u == slot[c] ? lb[u] : bound;
+        }
+        stk[sp] = make_int2(code, __float_as_int(bound));
+        ++sp;
+      } else {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+      }
+    }
+  }
+}
+
 // Element tests of one leaf (segment-relative elements [first, first + count)), FP32 reference arithmetic: keeps the
 // smallest (d2, index) with d2 <= best.
 __device__ __forceinline__ void cp_leaf_fp32(float4 const * __restrict__ rec, int64_t elem_base, int first, int count,
@@ -317,11 +425,14 @@ __device__ __forceinline__ void cp_leaf_fp32(float4 const * __restrict__ rec, in
 }
 
 // FP32 reference-arithmetic search: smallest (d2, index), accepting d2 <= thresh. With budget > 0 the search stops
-// after that many stack pops (done = false), leaving the best found so far.
+// after that many stack pops (done = false), leaving the best found so far. With the BVH's oriented slabs (single
+// mesh BVHs) the children's bounds are raised to their slab bounds; the result is the same, the search shorter.
 template <int W, int STACK>
 __device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restrict__ nodes,
                                                     float4 const * __restrict__ rec, int root, int64_t elem_base, V3 p,
-                                                    float thresh, unsigned * err, int budget = 0) {
+                                                    float thresh, unsigned * err, int budget = 0,
+                                                    float4 const * __restrict__ slabs = nullptr) {
+  float q1 = fabsf(p.x) + fabsf(p.y) + fabsf(p.z);
   bool done = true;
   float best = thresh;
   int best_idx = INT_MAX;
@@ -348,7 +459,13 @@ __device__ __forceinline__ ClosestOut closest_query(WideNode<W> const * __restri
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, err);
+      if (slabs) {
+        float order[W];
+        slab_child_bounds<W>(nd, slabs, code, p, q1, lb, order);
+        push_children_ordered<W, STACK>(nd, lb, order, best * PRUNE_SLACK, stk, sp, next, err);
+      } else {
+        push_children_next<W, STACK>(nd, lb, best * PRUNE_SLACK, stk, sp, next, err);
+      }
     } else {
       int first, count;
       decode_leaf(code, first, count);
@@ -483,7 +600,8 @@ template <int W, int STACK>
 __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restrict__ nodes,
                                                    float4 const * __restrict__ rec, int root, int64_t elem_base, V3 p,
                                                    double bound2, float scale, unsigned * err, F64Search & s,
-                                                   int budget = 0) {
+                                                   int budget = 0, float4 const * __restrict__ slabs = nullptr) {
+  float q1 = fabsf(p.x) + fabsf(p.y) + fabsf(p.z);
   f64_search_init(s);
   int pops = 0;
   float abs_tol;
@@ -509,7 +627,13 @@ __device__ __forceinline__ void closest_search_f64(WideNode<W> const * __restric
       load_node(nodes, code, nd);
       float lb[W];
       point_child_bounds<W>(nd, p, lb);
-      push_children_next<W, STACK>(nd, lb, lim * PRUNE_SLACK, stk, sp, next, err);
+      if (slabs) {
+        float order[W];
+        slab_child_bounds<W>(nd, slabs, code, p, q1, lb, order);
+        push_children_ordered<W, STACK>(nd, lb, order, lim * PRUNE_SLACK, stk, sp, next, err);
+      } else {
+        push_children_next<W, STACK>(nd, lb, lim * PRUNE_SLACK, stk, sp, next, err);
+      }
     } else {
       int first, count;
       decode_leaf(code, first, count);
