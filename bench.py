@@ -932,7 +932,8 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
         res["cpu_baseline"] = cpu_time("cfg3", meshes)
         eq32 = eq64 = True
         checked = 0
-        worst = 0.0
+        worst = worst32 = 0.0
+        differ32 = 0
         for j, (v, f, q) in enumerate(meshes):
             s = slice(qoff_h[64 * j], qoff_h[64 * j + 1])
             ri, rd2, rcp = O.MeshIndex(v, f).closest_contract(q)
@@ -944,10 +945,15 @@ def batched_config3(T, torch, stream, flush, args, num_meshes=4096):
             eq64 = eq64 and np.array_equal(i64, oi)
             od = np.sqrt(od2)
             worst = max(worst, float(np.max(np.abs(d64 - od) / np.maximum(od, 1e-30))))
+            # the reference's FP32 answer against the FP64 nearest element (the FP64 oracle)
+            worst32 = max(worst32, float(np.max(np.abs(d32.astype(np.float64) - od) / np.maximum(od, 1e-30))))
+            differ32 += int(np.count_nonzero(i32 != oi))
             checked += len(q)
         res["parity"] = {"meshes_checked": len(meshes), "queries_checked": checked,
                          "fp32_bit_exact": bool(eq32), "fp64_indices_equal_fp64_oracle": bool(eq64),
-                         "fp64_max_rel_distance_error_vs_fp64_oracle": worst}
+                         "fp64_max_rel_distance_error_vs_fp64_oracle": worst,
+                         "fp32_max_rel_distance_error_vs_fp64_oracle": worst32,
+                         "fp32_elements_differing_from_fp64_oracle": differ32}
     # the plain drop-in loop: per mesh, build its BVH and run one closest-element call (query time only is timed)
     t_build = 0.0
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(num_meshes)]

@@ -225,6 +225,14 @@ THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float 
                                          int64_t num_points, float scale, int32_t only_interior, double * out_sdf,
                                          void * stream);
 
+/* BestFitSphereN<3> (Algorithms/BestFitSphereN.hpp:62-91): the smallest ball enclosing the points, which the reference
+ * computes with its miniball on the points cast to double. out_center: 3 doubles; out_radius: 1 double. No points: the
+ * zero ball at the origin; non-finite points are skipped. ShapeDiameter(mesh) (SurfaceFeatures/Local/ShapeDiameter.hpp:
+ * 60-70) takes twice this radius over the mesh's vertices, rounded to float, as its default scale; pass it as `scale`
+ * to thea_shape_diameter to reproduce that constructor. Host or device points; synchronizes the stream. */
+THEA_API thea_status thea_best_fit_sphere(const float * points, int64_t num_points, double * out_center,
+                                          double * out_radius, void * stream);
+
 /* Sample proximity graph: PointSet3::updateGraph (Algorithms/PointSet3.hpp:324-391, no oversampling) with options
  * max_degree (1..64). Random(seed) replaces the reference's Random::common() in the mean-separation estimate (100
  * samples' nearest-neighbour distances); everything else is the reference's: radius sqrt(max_degree) x estimate,
@@ -499,7 +507,8 @@ THEA_API thea_status thea_sample_by_area_noalloc(const float * vertices, int64_t
  * pending pieces (smallest remaining request first; a request pending longer than max_wait_ms goes first) into batches
  * of at most max_batch_queries queries, one persistent launch per query kind. Up to `slots` batches are in flight at
  * once, each on its own stream, so requests that arrive while others run are admitted as soon as a slot and memory
- * free up, and their copies and kernels overlap with the batches already on the device.
+ * free up, and their copies and kernels overlap with the batches already on the device. A batch made only of requests
+ * of at most small_request_queries queries runs on a stream of the device's highest priority.
  *
  * Admission: resident BVHs (mesh BVH with both layouts plus a point BVH over the mesh's vertices) and the device staging
  * buffers of in-flight pieces count against memory_budget_bytes. A mesh that does not fit is refused at
@@ -512,8 +521,8 @@ typedef struct thea_server thea_server;
 
 typedef struct thea_server_config {
   int64_t memory_budget_bytes;   /* resident BVHs + staging of in-flight pieces (0: 8 GiB) */
-  int32_t slots;                 /* batches in flight at once, one stream each (0: 4) */
-  int32_t max_batch_queries;     /* queries per batch (0: 131072) */
+  int32_t slots;                 /* batches in flight at once, one stream pair each (0: 6) */
+  int32_t max_batch_queries;     /* queries per batch (0: 65536) */
   int32_t max_piece_queries;     /* largest piece of one request (0: 65536) */
   int32_t precision;             /* closest-element requests: THEA_PRECISION_* */
   int32_t width;                 /* BVH width of resident meshes, 4 or 8 (0: 4) */

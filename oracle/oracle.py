@@ -462,3 +462,46 @@ def sample_graph(P, N=None, max_degree=8, seed=0, surface=None, threads=None):
                               surface.h if surface is not None else None, _p(nbr, _i32p), _p(sep, _f32p),
                               _p(deg, _i32p), _p(avg, _f32p), threads or default_threads())
     return nbr, sep, deg, (float(avg[0]), float(avg[1]))
+
+
+def best_fit_sphere(P):
+    """BestFitSphereN<3> (Algorithms/BestFitSphereN.hpp:62-91): the smallest ball enclosing the points, computed in
+    double from the float coordinates as the reference's miniball is. This restatement uses Welzl's move-to-front
+    recursion (Gaertner's form: the support set grows by the point found outside, the loop restarts over the points
+    before it), not the reference's pivoting code; the ball is unique, so both give it up to rounding. Non-finite
+    points are skipped; no points give the zero ball at the origin. Returns (centre float64 [3], radius float)."""
+    pts = [tuple(float(x) for x in p) for p in np.asarray(P, np.float32).reshape(-1, 3) if np.all(np.isfinite(p))]
+    if not pts:
+        return np.zeros(3), 0.0
+
+    def ball_of(sup):
+        # the ball through the support points with its centre in their affine hull
+        p0 = np.array(sup[0])
+        if len(sup) == 1:
+            return p0, 0.0
+        v = np.array(sup[1:]) - p0
+        A = 2.0 * v @ v.T
+        b = (v * v).sum(1)
+        lam = np.linalg.solve(A, b)
+        c = p0 + lam @ v
+        return c, max(float(((np.array(s) - c) ** 2).sum()) for s in sup)
+
+    def outside(p, c, r2):
+        d = (p[0] - c[0]) ** 2 + (p[1] - c[1]) ** 2 + (p[2] - c[2]) ** 2
+        return d > r2 * (1.0 + 1e-12) + 1e-300
+
+    def mtf(end, sup):
+        c, r2 = ball_of(sup) if sup else (np.zeros(3), -1.0)
+        if len(sup) == 4:
+            return c, r2
+        i = 0
+        while i < end:
+            p = pts[i]
+            if outside(p, c, r2):
+                c, r2 = mtf(i, sup + [p])
+                pts.insert(0, pts.pop(i))  # move to front
+            i += 1
+        return c, r2
+
+    c, r2 = mtf(len(pts), [])
+    return np.asarray(c, np.float64), float(np.sqrt(max(r2, 0.0)))

@@ -1,10 +1,11 @@
 // TEST INFRASTRUCTURE ONLY -- C entry points over the REFERENCE's own spatial-query code, compiled in this build from the
-// reference's sources (Code/Source/Algorithms/BvhN.hpp, Triangle3.hpp, AxisAlignedBoxN.hpp, Random.cpp, Math.cpp, ...)
-// against eigen_subset.hpp in place of Eigen (which is absent here). Built into oracle/_ref/ by the oracle's Makefile
-// when the reference sources are present; used only to pin the oracle (tests/golden/make_ref_golden.py writes its
-// outputs as fixtures, and the CPU tests compare the oracle with it). Nothing here is restated: every query below is a
+// reference's sources (Code/Source/Algorithms/BvhN.hpp, BestFitSphereN.hpp with its vendored miniball, Triangle3.hpp,
+// AxisAlignedBoxN.hpp, Random.cpp, ...) against eigen_subset.hpp in place of Eigen (which is absent here). Built into
+// oracle/_ref/ by the oracle's Makefile when the reference sources are present; used only to pin the oracle
+// (tests/golden/make_ref_golden.py writes its outputs as fixtures, and the CPU tests compare the oracle with it). Nothing here is restated: every query below is a
 // call into the reference's classes.
 
+#include "Algorithms/BestFitSphereN.hpp"
 #include "Algorithms/BvhN.hpp"
 #include "Algorithms/MetricL2.hpp"
 #include "Algorithms/RayIntersectionTester.hpp"
@@ -199,5 +200,16 @@ void ref_random_bits(uint32_t seed, int64_t n, uint32_t * out) {
 
 // Math::treeDepth (Math.cpp:23-36)
 int64_t ref_tree_depth(int64_t n, int max_leaf) { return Math::treeDepth(n, max_leaf, 0.5f); }
+
+// BestFitSphereN<3> (the reference's miniball) over n points: centre and radius as the reference returns them (Real)
+void ref_best_fit_sphere(float const * P, int64_t n, float * center, float * radius) {
+  BestFitSphereN<3> s;
+  for (int64_t i = 0; i < n; ++i) s.addPoint(v3(P, i));
+  Vector3 const & c = s.getCenter();
+  center[0] = c[0];
+  center[1] = c[1];
+  center[2] = c[2];
+  *radius = s.getRadius();
+}
 
 }  // extern "C"

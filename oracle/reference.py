@@ -55,6 +55,7 @@ def lib():
         L.ref_random_bits.argtypes = [ctypes.c_uint32, _i64, _u32p]
         L.ref_tree_depth.restype = _i64
         L.ref_tree_depth.argtypes = [_i64, ctypes.c_int]
+        L.ref_best_fit_sphere.argtypes = [_f32p, _i64, _f32p, _f32p]
         _lib = L
     return _lib
 
@@ -164,3 +165,12 @@ def random_bits(seed, n):
 
 def tree_depth(n, max_leaf=5):
     return lib().ref_tree_depth(int(n), int(max_leaf))
+
+
+def best_fit_sphere(P):
+    """BestFitSphereN<3> of the points: (centre float32 [3], radius float32), the reference's Real."""
+    P = _f32(P)
+    c = np.zeros(3, np.float32)
+    r = np.zeros(1, np.float32)
+    lib().ref_best_fit_sphere(_p(P, _f32p), len(P), _p(c, _f32p), _p(r, _f32p))
+    return c, float(r[0])

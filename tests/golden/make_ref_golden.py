@@ -12,6 +12,7 @@ regenerated by the tests from thea_gb300.workloads, so the fixture holds outputs
                 degenerate ones included
   pair_*        closestPair between two mesh BVHs (two noisy icospheres) in both roles
   random_*      Random(seed).bits() for three seeds; tree_depth: Math::treeDepth
+  sphere_*      BestFitSphereN<3> (the reference's miniball) of seven point sets: centre and radius
 
 Run (needs the reference sources): python tests/golden/make_ref_golden.py <the reference's Code/Source directory>
 """
@@ -57,6 +58,14 @@ def inputs():
     Vb, Fb = W.noisy_icosphere(2, 76)
     Vb = (Vb * np.float32(0.4) + np.array([1.5, 0.3, -0.2], np.float32)).astype(np.float32)
     d["pair"] = (Va, Fa, Vb, Fb)
+    # point sets for the best-fit sphere: a mesh's vertices, a stretched one, a box, one and two points, points all on
+    # one sphere (many equally valid supports), a planar grid (a flat support)
+    Vs, _ = W.noisy_icosphere(4, 77, scale=[2.0, 0.5, 1.0], center=[0.3, -1.0, 2.0])
+    Vc, _ = W.noisy_icosphere(3, 78, sigma=0.0)
+    g = np.linspace(-1.0, 1.0, 21, dtype=np.float32)
+    grid = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    plane = np.concatenate([grid, np.full((len(grid), 1), 0.3, np.float32)], 1).astype(np.float32)
+    d["sphere"] = [V, Vs, W.uniform_box_points(1000, [0] * 3, [1] * 3, 79), V[:1], V[:2], Vc, plane]
     return d
 
 
@@ -96,6 +105,9 @@ def main():
         out["pair_points" + tag] = np.stack([qp, tp])
     for s in (5489, 0xFFFF, 1234):
         out["random_%d" % s] = R.random_bits(s, 1248)
+    for j, P in enumerate(d["sphere"]):
+        out["sphere_center_%d" % j], r = R.best_fit_sphere(P)
+        out["sphere_radius_%d" % j] = np.float32(r)
     ns = np.array([1, 5, 6, 11, 100, 81920, 1048576, 2093058], np.int64)
     out["tree_depth_n"] = ns
     out["tree_depth"] = np.array([R.tree_depth(int(n)) for n in ns], np.int64)

@@ -190,7 +190,7 @@ thea_batch_k_closest thea_autotune_batch_closest
 thea_graph_capture_begin thea_graph_capture_end thea_graph_launch thea_graph_destroy
 thea_server_create thea_server_destroy thea_server_add_mesh thea_server_remove_mesh thea_server_submit
 thea_server_wait thea_server_cancel thea_server_get_stats thea_server_reset_stats
-thea_shape_diameter thea_bvh_closest_pair thea_bvh_k_closest_pairs
+thea_shape_diameter thea_best_fit_sphere thea_bvh_closest_pair thea_bvh_k_closest_pairs
 thea_mesh_read thea_mesh_read_buffer thea_mesh_get_info thea_mesh_copy thea_mesh_destroy thea_triangulate_face
 """.split())
 

@@ -85,3 +85,44 @@ def test_shape_diameter_open_surface_and_transform(T, oracle):
     want = oracle.MeshIndex(V, F).shape_diameter(Pw.astype(np.float32), Nw, transform=xf)
     np.testing.assert_array_equal(got.cpu().numpy(), want)
     bvh.close()
+
+
+def test_best_fit_sphere_against_the_reference(T, oracle):
+    """thea_best_fit_sphere (BestFitSphereN, the default scale of ShapeDiameter(mesh)) on the point sets whose
+    reference results are recorded in tests/golden/reference_outputs.npz: the radius rounded to float equals the
+    reference's (the ball is unique; both compute in double), the centre agrees to float rounding, and device and host
+    inputs give the same ball."""
+    import os
+    import sys
+    import torch
+    from tests.conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_ref_golden as G
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "reference_outputs.npz"))
+    for j, P in enumerate(G.inputs()["sphere"]):
+        c, r = T.best_fit_sphere(torch.from_numpy(np.ascontiguousarray(P)).cuda())
+        ch, rh = T.best_fit_sphere(P)
+        assert r == rh and np.array_equal(c, ch), j
+        rc, rr = ref["sphere_center_%d" % j], ref["sphere_radius_%d" % j]
+        assert np.float32(r) == rr, (j, r, rr)
+        scale = max(1.0, float(np.abs(P).max()))
+        assert np.abs(c - rc.astype(np.float64)).max() <= 4e-7 * scale, j
+        oc, orad = oracle.best_fit_sphere(P)
+        assert abs(r - orad) <= 1e-12 * max(orad, 1.0), j
+    # the constructor's default scale, passed explicitly
+    V, F, _ = W.config0()
+    assert T.shape_diameter_scale(V) == float(np.float32(2) * ref["sphere_radius_0"])
+
+
+def test_best_fit_sphere_edge_cases(T, oracle):
+    c, r = T.best_fit_sphere(np.zeros((0, 3), np.float32))
+    assert r == 0.0 and not c.any()
+    P = W.uniform_box_points(5000, [-2] * 3, [3] * 3, 81)
+    P[::7] = np.nan  # non-finite points are skipped
+    P[3] = [np.inf, 0, 0]
+    c, r = T.best_fit_sphere(P)
+    oc, orad = oracle.best_fit_sphere(P)
+    assert abs(r - orad) <= 1e-12 * orad and np.abs(c - oc).max() <= 1e-9
+    Q = np.repeat(P[1:2], 100, 0)  # one point, repeated
+    c, r = T.best_fit_sphere(Q)
+    assert r == 0.0 and np.array_equal(c, Q[0].astype(np.float64))

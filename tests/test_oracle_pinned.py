@@ -129,3 +129,32 @@ def test_live_reference_on_more_inputs(oracle):
         ex = np.arange(500, dtype=np.int32)
         a, c = pi.knn_ref(P[:500], k, exclude=ex), rp.knn(P[:500], k, exclude=ex)
         assert np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1]), k
+
+
+def test_best_fit_sphere_is_the_reference(oracle, ref, cases):
+    """The smallest enclosing ball (BestFitSphereN, the reference's miniball): the oracle's radius rounded to float is the
+    reference's radius, and the centres agree to float rounding."""
+    for j, P in enumerate(cases["sphere"]):
+        c, r = oracle.best_fit_sphere(P)
+        rc, rr = ref["sphere_center_%d" % j], ref["sphere_radius_%d" % j]
+        assert np.float32(r) == rr, j
+        scale = max(1.0, float(np.abs(P).max()))
+        assert np.abs(c - rc.astype(np.float64)).max() <= 4e-7 * scale, j
+        # every point inside, some on the boundary
+        d = np.sqrt(((P.astype(np.float64) - c) ** 2).sum(1))
+        assert d.max() <= r * (1 + 1e-12) + 1e-300 and (len(P) == 1 or d.max() >= r * (1 - 1e-12)), j
+
+
+def test_live_best_fit_sphere(oracle):
+    """Where the reference library was built here: more seeded point sets against the reference's miniball."""
+    from oracle import reference as R
+    if not R.available():
+        pytest.skip("the reference library is built only where the reference sources are present")
+    rng = np.random.default_rng(80)
+    for t in range(20):
+        n = int(rng.integers(1, 3000))
+        P = (rng.normal(size=(n, 3)) * rng.uniform(0.01, 10, 3) + rng.normal(size=3) * 5).astype(np.float32)
+        c, r = oracle.best_fit_sphere(P)
+        rc, rr = R.best_fit_sphere(P)
+        assert abs(np.float32(r) - np.float32(rr)) <= np.spacing(np.float32(rr)), t
+        assert np.abs(c - rc).max() <= 1e-6 * max(1.0, float(np.abs(P).max())), t

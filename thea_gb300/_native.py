@@ -109,6 +109,7 @@ SIGNATURES = {
                                          _vp]),
     "thea_random_sphere": (ctypes.c_int, [ctypes.c_uint32, _i64, _vp, _vp]),
     "thea_shape_diameter": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, ctypes.c_int32, _vp, _vp]),
+    "thea_best_fit_sphere": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp]),
     "thea_bvh_closest_pair": (ctypes.c_int, [_vp, _vp, ctypes.c_float, ctypes.POINTER(ctypes.c_int32),
                                              ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), _vp, _vp,
                                              _vp]),

@@ -545,6 +545,25 @@ def write_sample_graph(path, neighbors, separations, degrees, max_degree, write_
             f.write(" ".join(parts) + "\n")
 
 
+def best_fit_sphere(points):
+    """BestFitSphereN<3>: the smallest ball enclosing the points (float32 [n, 3], host array or CUDA tensor), as
+    (centre: float64 [3], radius: float)."""
+    io = _Arrays(points)
+    pp, n = io.input(points, np.float32, 3)
+    c = np.zeros(3, np.float64)
+    r = ctypes.c_double(0.0)
+    N.check(N.lib().thea_best_fit_sphere(pp, n, ctypes.c_void_p(c.ctypes.data), ctypes.byref(r),
+                                         _stream_of(io.device)))
+    return c, r.value
+
+
+def shape_diameter_scale(vertices):
+    """The default scale of ShapeDiameter(mesh) (ShapeDiameter.hpp:60-70): the diameter of the mesh vertices' best-fit
+    sphere, in float32 as the reference's Real. Pass it as MeshBvh.shape_diameter(..., scale=...)."""
+    _, r = best_fit_sphere(vertices)
+    return float(np.float32(2.0) * np.float32(r))
+
+
 def random_sphere(seed, count, device=False):
     """`count` directions of Random(seed).sphere() in stream order (float32 [count, 3])."""
     if device:

@@ -12,6 +12,7 @@
 #include "sample_graph.hpp"
 #include "mesh_io.hpp"
 #include "shape_diameter.hpp"
+#include "bounding_sphere.hpp"
 #include "pairs.hpp"
 #include "traverse.cuh"
 
@@ -1350,6 +1351,24 @@ THEA_API thea_status thea_shape_diameter(const thea_bvh * mesh_bvh, const float 
       THEA_CUDA_CHECK(cudaMemcpyAsync(out_sdf, out, (size_t)num_points * 8, cudaMemcpyDeviceToHost, s));
       sync_stream(s);
     }
+  });
+}
+
+THEA_API thea_status thea_best_fit_sphere(const float * points, int64_t num_points, double * out_center,
+                                          double * out_radius, void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(num_points >= 0, "best_fit_sphere: negative point count");
+    THEA_REQUIRE(out_center && out_radius, "best_fit_sphere: null output");
+    THEA_REQUIRE(num_points == 0 || points, "best_fit_sphere: null points");
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch pin;
+    float const * pts = points;
+    if (num_points > 0 && is_host_pointer(points)) {
+      pin = Scratch((size_t)num_points * 12, s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(pin.ptr, points, (size_t)num_points * 12, cudaMemcpyHostToDevice, s));
+      pts = pin.as<float>();
+    }
+    run_bounding_sphere(pts, num_points, out_center, out_radius, s);
   });
 }
 

@@ -335,7 +335,9 @@ struct ServePiece {
 
 struct ServeSlot {
   thea_server * owner = nullptr;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // batches with a large request
+  cudaStream_t express = nullptr;  // batches of small requests only: the device's highest stream priority
+  cudaStream_t active = nullptr;   // the stream the slot's current batch was enqueued on
   thea::ServeTask * d_tasks = nullptr;  // [3][MAX_TASKS]
   thea::ServeTask * h_tasks = nullptr;  // pinned mirror
   int64_t * d_off = nullptr;            // [3][MAX_TASKS + 1]
@@ -470,7 +472,12 @@ bool form_batch_locked(thea_server * sv, ServeSlot & s) {
 // Enqueues the slot's batch on its stream (called without the lock; only the dispatcher touches slots and the meshes of
 // admitted requests stay alive until those requests end).
 void launch_slot(thea_server * sv, ServeSlot & s, std::vector<ServeMesh const *> const & piece_mesh) {
-  cudaStream_t st = s.stream;
+  // A batch of small requests only goes to the high-priority stream: its blocks are scheduled ahead of the waiting
+  // blocks of batches already launched on other slots, instead of queueing behind a large request's launch
+  bool small_only = true;
+  for (ServePiece const & p : s.pieces) small_only = small_only && p.req->r.num_queries <= sv->cfg.small_request_queries;
+  cudaStream_t st = small_only ? s.express : s.stream;
+  s.active = st;
   int T[3] = {0, 0, 0};
   int64_t nq[3] = {0, 0, 0};
   int maxk = 1;
@@ -669,7 +676,7 @@ void dispatcher_main(thea_server * sv) {
         }
         if (st != THEA_OK) {
           // drain what was enqueued (the callback may or may not have been queued), then fail the batch
-          cudaStreamSynchronize(s.stream);
+          cudaStreamSynchronize(s.active);
           cudaGetLastError();
           for (ServePiece & p : s.pieces)
             if (p.staging) cudaFree(p.staging);
@@ -706,8 +713,8 @@ thea_server * server_create(thea_server_config const & c) {
   thea_server_config & cfg = sv->cfg;
   cfg = c;
   if (!cfg.memory_budget_bytes) cfg.memory_budget_bytes = int64_t(8) << 30;
-  if (!cfg.slots) cfg.slots = 4;
-  if (!cfg.max_batch_queries) cfg.max_batch_queries = 131072;
+  if (!cfg.slots) cfg.slots = 6;
+  if (!cfg.max_batch_queries) cfg.max_batch_queries = 65536;
   if (!cfg.max_piece_queries) cfg.max_piece_queries = 65536;
   cfg.max_piece_queries = std::min(cfg.max_piece_queries, cfg.max_batch_queries);
   if (!cfg.width) cfg.width = 4;
@@ -719,7 +726,11 @@ thea_server * server_create(thea_server_config const & c) {
     std::unique_ptr<ServeSlot> s(new ServeSlot);
     s->owner = sv.get();
     if (!cfg.test_executor) {
-      THEA_CUDA_CHECK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+      int least = 0, greatest = 0;
+      THEA_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      THEA_CUDA_CHECK(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, least));
+      THEA_CUDA_CHECK(cudaStreamCreateWithPriority(&s->express, cudaStreamNonBlocking, greatest));
+      s->active = s->stream;
       THEA_CUDA_CHECK(thea_malloc(&s->d_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
       THEA_CUDA_CHECK(thea_malloc_host(&s->h_tasks, sizeof(ServeTask) * 3 * MAX_TASKS));
       THEA_CUDA_CHECK(thea_malloc(&s->d_off, sizeof(int64_t) * 3 * (MAX_TASKS + 1)));
@@ -749,9 +760,10 @@ void server_destroy(thea_server * sv) {
   if (!sv->cfg.test_executor)
     for (auto & sp : sv->slots) {
       ServeSlot & s = *sp;
-      if (s.stream) {
-        cudaStreamSynchronize(s.stream);
-        cudaStreamDestroy(s.stream);
+      for (cudaStream_t t : {s.stream, s.express}) {
+        if (!t) continue;
+        cudaStreamSynchronize(t);
+        cudaStreamDestroy(t);
       }
       cudaFree(s.d_tasks);
       cudaFreeHost(s.h_tasks);
