@@ -249,6 +249,22 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
                                        int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
                                        float * out_avg_separation, void * stream);
 
+/* The sample graph with a dense oversampling of the surface: PointSet3::addOversampling + updateGraph
+ * (Algorithms/PointSet3.hpp:231-290, 324-391) and extractOriginalAdjacencies (PointSet3.cpp:157-176). The graph of
+ * thea_sample_graph is built over the samples followed by the num_dense dense samples (dense_normals are required, and
+ * used, when normals are given); then each sample's neighbours are the first max_degree other samples that Dijkstra's
+ * algorithm settles from it over that graph (edge lengths: the separations, summed in double), and their separations
+ * the path lengths rounded to float. Ties in path length settle the lowest index first. Outputs as thea_sample_graph,
+ * for the num_samples samples only; out_avg_separation[0] is the estimate over all samples and dense samples.
+ * THEA_ERR_NOT_SUPPORTED if one search needs more than 896 vertices (too dense an oversampling for max_degree). Host
+ * or device arrays; synchronizes the stream. */
+THEA_API thea_status thea_sample_graph_oversampled(const float * positions, const float * normals,
+                                                   int64_t num_samples, const float * dense_positions,
+                                                   const float * dense_normals, int64_t num_dense,
+                                                   int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                                   int32_t * out_neighbors, float * out_separations,
+                                                   int32_t * out_degree, float * out_avg_separation, void * stream);
+
 /* ---- pairs between two BVHs ---------------------------------------------------------------------------------------- */
 
 /* BvhN::closestPair<MetricL2> with another BVH as the query (BvhN.hpp:1082-1114; the reference descends both trees,

@@ -464,6 +464,59 @@ def sample_graph(P, N=None, max_degree=8, seed=0, surface=None, threads=None):
     return nbr, sep, deg, (float(avg[0]), float(avg[1]))
 
 
+def sample_graph_oversampled(P, N, D, DN, max_degree=8, seed=0, surface=None, threads=None):
+    """PointSet3::updateGraph with a dense oversampling D (normals DN, used when N is given): the graph of sample_graph
+    over P followed by D, then extractOriginalAdjacencies (PointSet3.cpp:157-176): per sample, Dijkstra over that graph
+    (edge lengths the separations, summed in double; ties settle the lowest index) until max_degree other samples of P
+    are settled; separations the path lengths as float, neighbours in (separation, index) order. Returns the outputs of
+    sample_graph for P (the estimate over P and D, the final mean over P's new neighbours)."""
+    import heapq
+    P = _f32(P).reshape(-1, 3)
+    D = _f32(D).reshape(-1, 3)
+    n, m = len(P), int(max_degree)
+    agg = np.concatenate([P, D])
+    aggn = np.concatenate([_f32(N).reshape(-1, 3), _f32(DN).reshape(-1, 3)]) if N is not None else None
+    nbr, sep, deg, (est, _) = sample_graph(agg, aggn, m, seed, surface, threads)
+    out_n = np.full((n, m), -1, np.int32)
+    out_s = np.zeros((n, m), np.float32)
+    out_d = np.zeros(n, np.int32)
+    for src in range(n):
+        dist = {src: 0.0}
+        done = set()
+        heap = [(0.0, src)]
+        found = []
+        while heap:
+            d, v = heapq.heappop(heap)
+            if v in done or d > dist[v]:
+                continue
+            done.add(v)
+            if v != src and v < n:
+                found.append((np.float32(d), v))
+                if len(found) >= m:
+                    break
+            for k in range(int(deg[v])):
+                u = int(nbr[v, k])
+                nd = d + float(sep[v, k])
+                if u not in done and nd < dist.get(u, np.inf):
+                    dist[u] = nd
+                    heapq.heappush(heap, (nd, u))
+        found.sort()
+        out_d[src] = len(found)
+        for k, (sp, v) in enumerate(found):
+            out_n[src, k] = v
+            out_s[src, k] = sp
+    # updateAverageSeparation (PointSet3.hpp:688-702): a float sum in sample order
+    avg = np.float32(0)
+    edges = 0
+    for i in range(n):
+        for k in range(int(out_d[i])):
+            avg = np.float32(avg + out_s[i, k])
+        edges += int(out_d[i])
+    if edges:
+        avg = np.float32(avg / np.float32(edges))
+    return out_n, out_s, out_d, (est, float(avg))
+
+
 def best_fit_sphere(P):
     """BestFitSphereN<3> (Algorithms/BestFitSphereN.hpp:62-91): the smallest ball enclosing the points, computed in
     double from the float coordinates as the reference's miniball is. This restatement uses Welzl's move-to-front

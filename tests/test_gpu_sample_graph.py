@@ -97,3 +97,31 @@ def test_graph_with_duplicate_samples(T, oracle):
     same(got, oracle.sample_graph(P, None, 8, 8))
     tiny = P[:6]
     same(T.sample_graph(tiny, max_degree=4, seed=1), oracle.sample_graph(tiny, None, 4, 1))
+
+
+@pytest.mark.parametrize("max_degree", [8, 4])
+def test_oversampled_graph(T, oracle, max_degree):
+    """PointSet3 with a dense oversampling: the graph over samples + dense samples, then each sample's first
+    max_degree samples along shortest paths (extractOriginalAdjacencies), bit-exact against the oracle's Dijkstra."""
+    V, F, P, _ = sphere_samples(800, 251, T)
+    D, _, _ = T.sample_evenly_by_area(V, F, 4000, 253)
+    D = np.asarray(D)
+    got = T.sample_graph(dev(P), max_degree=max_degree, seed=9, dense_positions=dev(D))
+    same(got, oracle.sample_graph_oversampled(P, None, D, None, max_degree, 9))
+    # the new separations are path lengths: never below the straight-line separation of the plain graph's metric
+    nbr, sep = got[0].cpu().numpy(), got[1].cpu().numpy()
+    i = np.repeat(np.arange(len(P)), max_degree).reshape(len(P), max_degree)
+    ok = nbr >= 0
+    straight = np.linalg.norm(P[i[ok]].astype(np.float64) - P[nbr[ok]], axis=1)
+    assert np.all(sep[ok] >= straight * (1 - 5e-3))  # Math::fastSqrt is a one-step approximation
+
+
+def test_oversampled_graph_with_normals_and_surface(T, oracle):
+    V, F, P, Nm = sphere_samples(600, 261, T)
+    D, DN, _ = T.sample_evenly_by_area(V, F, 2400, 263)
+    D, DN = np.asarray(D), np.asarray(DN)
+    surf = T.MeshBvh(dev(V), dev(F))
+    got = T.sample_graph(P, Nm, max_degree=8, seed=10, surface=surf, dense_positions=D, dense_normals=DN)  # host
+    same(got, oracle.sample_graph_oversampled(P, Nm, D, DN, 8, 10, surface=oracle.MeshIndex(V, F)))
+    with pytest.raises(T.TheaError):
+        T.sample_graph(P, Nm, max_degree=8, seed=10, dense_positions=D)  # dense normals are needed with normals

@@ -107,6 +107,8 @@ SIGNATURES = {
     "thea_ray_intersects": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, _vp, _vp]),
     "thea_sample_graph": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
+    "thea_sample_graph_oversampled": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _i64, ctypes.c_int32, ctypes.c_uint32,
+                                                     _vp, _vp, _vp, _vp, _vp, _vp]),
     "thea_random_sphere": (ctypes.c_int, [ctypes.c_uint32, _i64, _vp, _vp]),
     "thea_shape_diameter": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, ctypes.c_int32, _vp, _vp]),
     "thea_best_fit_sphere": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp]),

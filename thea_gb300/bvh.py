@@ -512,10 +512,13 @@ def point_gram_tile(a, b):
     return keys
 
 
-def sample_graph(positions, normals=None, max_degree=8, seed=0, surface=None):
-    """PointSet3::updateGraph (no oversampling) with Random(seed) for the separation estimate. Returns (neighbours
-    [n, max_degree] int32 with -1 past the degree, separations [n, max_degree], degrees [n], (estimate, final mean
-    separation)). surface: a MeshBvh for the reachability test (used with normals, as in the reference)."""
+def sample_graph(positions, normals=None, max_degree=8, seed=0, surface=None, dense_positions=None,
+                 dense_normals=None):
+    """PointSet3::updateGraph with Random(seed) for the separation estimate. Returns (neighbours [n, max_degree] int32
+    with -1 past the degree, separations [n, max_degree], degrees [n], (estimate, final mean separation)). surface: a
+    MeshBvh for the reachability test (used with normals, as in the reference). dense_positions (and dense_normals,
+    needed with normals): an oversampling (PointSet3::addOversampling); neighbours are then the nearest samples along
+    shortest paths through the graph of all points (extractOriginalAdjacencies)."""
     io = _Arrays(positions)
     pp, n = io.input(positions, np.float32, 3)
     pn, _ = io.input(normals, np.float32, 3) if normals is not None else (None, 0)
@@ -523,9 +526,15 @@ def sample_graph(positions, normals=None, max_degree=8, seed=0, surface=None):
     sep, psp = io.output((n, max_degree), np.float32)
     deg, pdg = io.output((n,), np.int32)
     avg = np.zeros(2, np.float32)
-    N.check(N.lib().thea_sample_graph(pp, pn, n, int(max_degree), int(seed) & 0xffffffff,
-                                      surface.handle if surface is not None else None, pnb, psp, pdg,
-                                      avg.ctypes.data, _stream_of(io.device)))
+    sh = surface.handle if surface is not None else None
+    if dense_positions is None:
+        N.check(N.lib().thea_sample_graph(pp, pn, n, int(max_degree), int(seed) & 0xffffffff, sh, pnb, psp, pdg,
+                                          avg.ctypes.data, _stream_of(io.device)))
+    else:
+        pd, nd = io.input(dense_positions, np.float32, 3)
+        pdn, _ = io.input(dense_normals, np.float32, 3) if dense_normals is not None else (None, 0)
+        N.check(N.lib().thea_sample_graph_oversampled(pp, pn, n, pd, pdn, nd, int(max_degree), int(seed) & 0xffffffff,
+                                                      sh, pnb, psp, pdg, avg.ctypes.data, _stream_of(io.device)))
     return nbr, sep, deg, (float(avg[0]), float(avg[1]))
 
 

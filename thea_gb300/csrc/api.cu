@@ -748,19 +748,29 @@ THEA_API thea_status thea_visibility(const thea_bvh * mesh_bvh, const float * po
   });
 }
 
-THEA_API thea_status thea_sample_graph(const float * positions, const float * normals, int64_t num_samples,
-                                       int32_t max_degree, uint32_t seed, const thea_bvh * surface,
-                                       int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
-                                       float * out_avg_separation, void * stream) {
+// thea_sample_graph with or without an oversampling
+static thea_status sample_graph_call(const float * positions, const float * normals, int64_t num_samples,
+                                     bool oversampled, const float * dense, const float * dense_normals,
+                                     int64_t num_dense,
+                                     int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                     int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
+                                     float * out_avg_separation, void * stream) {
   return guarded([&] {
     THEA_REQUIRE(positions && out_neighbors, "sample_graph: null positions or out_neighbors");
     THEA_REQUIRE(!surface || (surface->is_mesh && surface->ray_rec),
                  "sample_graph: the surface must be a mesh BVH with THEA_LAYOUT_RAY");
-    THEA_REQUIRE(num_samples >= 2, "sample_graph: at least two samples are needed");
     THEA_REQUIRE(max_degree >= 1 && max_degree <= 64, "sample_graph: max_degree must be in 1..64");
+    if (oversampled) {
+      THEA_REQUIRE(dense && num_dense >= 1, "sample_graph_oversampled: the oversampling is empty");
+      THEA_REQUIRE(num_samples >= 1, "sample_graph_oversampled: no samples");
+      THEA_REQUIRE(!normals || dense_normals, "sample_graph: samples with normals need dense normals");
+    } else {
+      THEA_REQUIRE(num_samples >= 2, "sample_graph: at least two samples are needed");
+    }
     cudaStream_t s = (cudaStream_t)stream;
     size_t n = (size_t)num_samples, m = (size_t)max_degree;
     DeviceView pos(positions, n * 12, s), nrm(normals, n * 12, s);
+    DeviceView dpos(dense, (size_t)num_dense * 12, s), dnrm(normals ? dense_normals : nullptr, (size_t)num_dense * 12, s);
     // outputs: device buffers, copied out when the caller's arrays are host memory; separations and degrees are
     // always produced when the final mean separation is asked for
     bool need_sep = out_separations || out_avg_separation, need_deg = out_degree || out_avg_separation;
@@ -774,7 +784,12 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
     if (hn) { bn = Scratch(n * m * 4, s); o.neighbors = bn.as<int32_t>(); }
     if (need_sep && (!out_separations || hs)) { bs = Scratch(n * m * 4, s); o.separations = bs.as<float>(); }
     if (need_deg && (!out_degree || hd)) { bd = Scratch(n * 4, s); o.degree = bd.as<int32_t>(); }
-    run_sample_graph((float const *)pos.ptr, (float const *)nrm.ptr, num_samples, max_degree, seed, surface, o, s);
+    if (oversampled)
+      run_sample_graph_oversampled((float const *)pos.ptr, (float const *)nrm.ptr, num_samples,
+                                   (float const *)dpos.ptr, (float const *)dnrm.ptr, num_dense, max_degree, seed,
+                                   surface, o, s);
+    else
+      run_sample_graph((float const *)pos.ptr, (float const *)nrm.ptr, num_samples, max_degree, seed, surface, o, s);
     if (hn) THEA_CUDA_CHECK(cudaMemcpyAsync(out_neighbors, o.neighbors, n * m * 4, cudaMemcpyDeviceToHost, s));
     if (hs) THEA_CUDA_CHECK(cudaMemcpyAsync(out_separations, o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
     if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_degree, o.degree, n * 4, cudaMemcpyDeviceToHost, s));
@@ -797,6 +812,24 @@ THEA_API thea_status thea_sample_graph(const float * positions, const float * no
     }
     sync_stream(s);
   });
+}
+
+THEA_API thea_status thea_sample_graph(const float * positions, const float * normals, int64_t num_samples,
+                                       int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                       int32_t * out_neighbors, float * out_separations, int32_t * out_degree,
+                                       float * out_avg_separation, void * stream) {
+  return sample_graph_call(positions, normals, num_samples, false, nullptr, nullptr, 0, max_degree, seed, surface,
+                           out_neighbors, out_separations, out_degree, out_avg_separation, stream);
+}
+
+THEA_API thea_status thea_sample_graph_oversampled(const float * positions, const float * normals,
+                                                   int64_t num_samples, const float * dense_positions,
+                                                   const float * dense_normals, int64_t num_dense,
+                                                   int32_t max_degree, uint32_t seed, const thea_bvh * surface,
+                                                   int32_t * out_neighbors, float * out_separations,
+                                                   int32_t * out_degree, float * out_avg_separation, void * stream) {
+  return sample_graph_call(positions, normals, num_samples, true, dense_positions, dense_normals, num_dense, max_degree,
+                           seed, surface, out_neighbors, out_separations, out_degree, out_avg_separation, stream);
 }
 
 THEA_API thea_status thea_k_closest(const thea_bvh * point_bvh, const float * queries, int64_t num_queries, int32_t k,

@@ -135,6 +135,124 @@ __global__ void select_kernel(int32_t const * __restrict__ active, int64_t n_act
   if (out_deg) out_deg[s] = cnt;
 }
 
+// extractOriginalAdjacencies (PointSet3.cpp:157-176, DijkstraCallback :131-148): for each original sample, Dijkstra
+// over the graph of all samples (originals first, then the oversampling), edge lengths the separations held in double,
+// until max_degree original samples other than itself are settled; their path lengths, rounded to Real, are the new
+// separations. One warp per original sample: the settled and tentative vertices live in a shared-memory hash table
+// (EXTRACT_SLOTS per warp); each step the warp finds the smallest tentative (distance, index), settles it and relaxes its
+// edges, one lane per edge. Ties settle the lowest index first (the reference's Fibonacci heap breaks them by its own
+// internal order). A search that would outgrow the table raises `flag` and stops.
+constexpr int EXTRACT_WARPS = 2;
+constexpr int EXTRACT_SLOTS = 1024;  // power of two
+constexpr int EXTRACT_FILL = EXTRACT_SLOTS - 2 * MAX_GRAPH_DEGREE;
+
+__device__ __forceinline__ int extract_slot(int v) { return (int)(((uint32_t)v * 2654435761u) >> 22); }
+
+__global__ void __launch_bounds__(EXTRACT_WARPS * 32)
+extract_kernel(int32_t const * __restrict__ nbr, float const * __restrict__ sep, int32_t const * __restrict__ deg,
+               int m, int64_t n_orig, int32_t * __restrict__ out_nbr, float * __restrict__ out_sep,
+               int32_t * __restrict__ out_deg, unsigned * __restrict__ flag) {
+  __shared__ int s_vert[EXTRACT_WARPS][EXTRACT_SLOTS];
+  __shared__ double s_dist[EXTRACT_WARPS][EXTRACT_SLOTS];
+  __shared__ unsigned char s_done[EXTRACT_WARPS][EXTRACT_SLOTS];
+  __shared__ int s_idx[EXTRACT_WARPS][MAX_GRAPH_DEGREE];
+  __shared__ float s_sep[EXTRACT_WARPS][MAX_GRAPH_DEGREE];
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t src = (int64_t)blockIdx.x * EXTRACT_WARPS + w;
+  if (src >= n_orig) return;  // the whole warp
+  int * vert = s_vert[w];
+  double * dist = s_dist[w];
+  unsigned char * done = s_done[w];
+  for (int k = lane; k < EXTRACT_SLOTS; k += 32) {
+    vert[k] = -1;
+    done[k] = 0;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    int h = extract_slot((int)src);
+    vert[h] = (int)src;
+    dist[h] = 0.0;
+  }
+  __syncwarp();
+  int found = 0, used = 1;
+  bool full = false;
+  while (true) {
+    double bd = INFINITY;
+    int bv = INT_MAX, bs = -1;
+    for (int k = lane; k < EXTRACT_SLOTS; k += 32) {
+      int v = vert[k];
+      if (v < 0 || done[k]) continue;
+      double d = dist[k];
+      if (d < bd || (d == bd && v < bv)) bd = d, bv = v, bs = k;
+    }
+    for (int o = 16; o; o >>= 1) {
+      double od = __shfl_xor_sync(0xffffffffu, bd, o);
+      int ov = __shfl_xor_sync(0xffffffffu, bv, o), os = __shfl_xor_sync(0xffffffffu, bs, o);
+      if (os >= 0 && (bs < 0 || od < bd || (od == bd && ov < bv))) bd = od, bv = ov, bs = os;
+    }
+    if (bs < 0) break;  // the component is exhausted
+    if (lane == 0) done[bs] = 1;
+    if (bv != (int)src && bv < n_orig) {
+      if (lane == 0) {
+        s_idx[w][found] = bv;
+        s_sep[w][found] = (float)bd;
+      }
+      if (++found >= m) break;
+    }
+    int dv = deg[bv];
+    if (used + dv > EXTRACT_FILL) {
+      full = true;
+      break;
+    }
+    bool inserted = false;
+    if (lane < dv) {  // dv <= max_degree <= 64: at most two edges per lane
+      for (int k = lane; k < dv; k += 32) {
+        int u = nbr[(int64_t)bv * m + k];
+        double nd = bd + (double)sep[(int64_t)bv * m + k];
+        int h = extract_slot(u);
+        for (int probe = 0; probe < EXTRACT_SLOTS; ++probe) {
+          int prev = atomicCAS(&vert[h], -1, u);
+          if (prev == -1) {
+            dist[h] = nd;
+            inserted = true;
+            break;
+          }
+          if (prev == u) {
+            if (!done[h] && nd < dist[h]) dist[h] = nd;
+            break;
+          }
+          h = (h + 1) & (EXTRACT_SLOTS - 1);
+        }
+      }
+    }
+    // each lane inserts at most two vertices: count them all
+    used += __popc(__ballot_sync(0xffffffffu, inserted)) * (dv > 32 ? 2 : 1);
+    __syncwarp();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    // the neighbour set's order: (separation, index)
+    for (int a = 1; a < found; ++a) {
+      int ia = s_idx[w][a];
+      float sa = s_sep[w][a];
+      int b = a - 1;
+      while (b >= 0 && (s_sep[w][b] > sa || (s_sep[w][b] == sa && s_idx[w][b] > ia))) {
+        s_idx[w][b + 1] = s_idx[w][b];
+        s_sep[w][b + 1] = s_sep[w][b];
+        --b;
+      }
+      s_idx[w][b + 1] = ia;
+      s_sep[w][b + 1] = sa;
+    }
+    for (int k = 0; k < m; ++k) {
+      out_nbr[src * m + k] = k < found ? s_idx[w][k] : -1;
+      if (out_sep) out_sep[src * m + k] = k < found ? s_sep[w][k] : 0.f;
+    }
+    if (out_deg) out_deg[src] = found;
+    if (full) atomicOr(flag, 1u);
+  }
+}
+
 }  // namespace
 
 void run_sample_graph(float const * positions, float const * normals, int64_t n, int max_degree, uint32_t seed,
@@ -231,6 +349,47 @@ void run_sample_graph(float const * positions, float const * normals, int64_t n,
   }
   THEA_CUDA_CHECK(cudaStreamSynchronize(s));
   destroy_bvh(pts);
+}
+
+}  // namespace thea
+
+namespace thea {
+
+void run_sample_graph_oversampled(float const * positions, float const * normals, int64_t n, float const * dense,
+                                  float const * dense_normals, int64_t n_dense, int max_degree, uint32_t seed,
+                                  thea_bvh const * surface, SampleGraphOut & out, cudaStream_t s) {
+  THEA_REQUIRE(n >= 1 && n_dense >= 1, "sample_graph: oversampling needs samples and dense samples");
+  THEA_REQUIRE(n + n_dense < ((int64_t)1 << 31), "sample_graph: too many samples");
+  THEA_REQUIRE(max_degree >= 1 && max_degree <= MAX_GRAPH_DEGREE, "sample_graph: max_degree must be in 1..64");
+  int64_t na = n + n_dense;
+  size_t m = (size_t)max_degree;
+  // the aggregate: originals first, then the oversampling (updateGraph's sample_ptrs order)
+  Scratch agg((size_t)na * 12, s), aggn(normals ? (size_t)na * 12 : 0, s);
+  THEA_CUDA_CHECK(cudaMemcpyAsync(agg.ptr, positions, (size_t)n * 12, cudaMemcpyDeviceToDevice, s));
+  THEA_CUDA_CHECK(cudaMemcpyAsync(agg.as<float>() + 3 * n, dense, (size_t)n_dense * 12, cudaMemcpyDeviceToDevice, s));
+  if (normals) {
+    THEA_CUDA_CHECK(cudaMemcpyAsync(aggn.ptr, normals, (size_t)n * 12, cudaMemcpyDeviceToDevice, s));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(aggn.as<float>() + 3 * n, dense_normals, (size_t)n_dense * 12,
+                                    cudaMemcpyDeviceToDevice, s));
+  }
+  Scratch gn((size_t)na * m * 4, s), gs((size_t)na * m * 4, s), gd((size_t)na * 4, s);
+  SampleGraphOut g;
+  g.neighbors = gn.as<int32_t>();
+  g.separations = gs.as<float>();
+  g.degree = gd.as<int32_t>();
+  run_sample_graph(agg.as<float>(), normals ? aggn.as<float>() : nullptr, na, max_degree, seed, surface, g, s);
+  out.avg_separation_estimate = g.avg_separation_estimate;
+  Scratch flag(sizeof(unsigned), s);
+  THEA_CUDA_CHECK(cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s));
+  THEA_LAUNCH(extract_kernel, (unsigned)ceil_div(n, EXTRACT_WARPS), EXTRACT_WARPS * 32, 0, s, g.neighbors,
+              g.separations, g.degree, max_degree, n, out.neighbors, out.separations, out.degree, flag.as<unsigned>());
+  unsigned h = 0;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&h, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  if (h)
+    throw Error(THEA_ERR_NOT_SUPPORTED, "sample_graph: a sample's geodesic search outgrew its " +
+                                            std::to_string(EXTRACT_FILL) + "-vertex working set (oversampling too "
+                                            "dense for max_degree; use fewer dense samples)");
 }
 
 }  // namespace thea

@@ -1,4 +1,4 @@
-// Sample proximity graph (PointSet3::updateGraph without oversampling).
+// Sample proximity graph (PointSet3::updateGraph, with or without a dense oversampling).
 #pragma once
 
 #include "bvh.hpp"
@@ -16,5 +16,14 @@ struct SampleGraphOut {
 // normals, as in the reference. Synchronizes the stream.
 void run_sample_graph(float const * positions, float const * normals, int64_t n, int max_degree, uint32_t seed,
                       thea_bvh const * surface, SampleGraphOut & out, cudaStream_t s);
+
+// The same with a dense oversampling (PointSet3::addOversampling + updateGraph, PointSet3.hpp:231-290, 324-391): the
+// graph is built over samples + dense samples, then each sample's neighbours are the first max_degree other samples
+// reached along shortest paths in it (extractOriginalAdjacencies, PointSet3.cpp:157-176), their separations the path
+// lengths. dense_normals are used when normals are. Device pointers; synchronizes the stream. Raises
+// THEA_ERR_NOT_SUPPORTED if a shortest-path search needs more than its fixed working set.
+void run_sample_graph_oversampled(float const * positions, float const * normals, int64_t n, float const * dense,
+                                  float const * dense_normals, int64_t n_dense, int max_degree, uint32_t seed,
+                                  thea_bvh const * surface, SampleGraphOut & out, cudaStream_t s);
 
 }  // namespace thea
