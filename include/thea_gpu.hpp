@@ -389,6 +389,97 @@ class MeshSampler {
   int64_t nf_;
 };
 
+// BestFitSphereN<3> (Algorithms/BestFitSphereN.hpp): points collected on the host, the smallest enclosing ball computed
+// on the GPU when first asked for. getDiameter() over a mesh's vertices is ShapeDiameter(mesh)'s default scale.
+class BestFitSphere3 {
+ public:
+  void addPoint(float x, float y, float z) {
+    pts_.push_back(x);
+    pts_.push_back(y);
+    pts_.push_back(z);
+    updated_ = false;
+  }
+  void addPoints(float const * xyz, int64_t n) {
+    pts_.insert(pts_.end(), xyz, xyz + 3 * n);
+    updated_ = false;
+  }
+  void clear() {
+    pts_.clear();
+    updated_ = false;
+  }
+  // centre and radius as the reference returns them (Real = float)
+  void getCenter(float * c) const {
+    update();
+    c[0] = (float)c_[0], c[1] = (float)c_[1], c[2] = (float)c_[2];
+  }
+  float getRadius() const { update(); return (float)r_; }
+  float getDiameter() const { return 2.0f * getRadius(); }
+
+ private:
+  void update() const {
+    if (updated_) return;
+    check(thea_best_fit_sphere(pts_.data(), (int64_t)(pts_.size() / 3), c_, &r_, nullptr));
+    updated_ = true;
+  }
+  std::vector<float> pts_;
+  mutable double c_[3] = {0, 0, 0};
+  mutable double r_ = 0;
+  mutable bool updated_ = true;
+};
+
+// PointSet3's sample graph (Algorithms/PointSet3.hpp): samples (and optional normals) set once, an optional dense
+// oversampling, then updateGraph() with Random(seed) in place of Random::common(). Host arrays.
+class PointSet3 {
+ public:
+  explicit PointSet3(int32_t max_degree = 8, uint32_t seed = 0) : max_degree_(max_degree), seed_(seed) {}
+
+  void setSamples(float const * positions, float const * normals, int64_t n) {
+    pos_.assign(positions, positions + 3 * n);
+    if (normals) nrm_.assign(normals, normals + 3 * n);
+    else nrm_.clear();
+    valid_ = false;
+  }
+  void addOversampling(float const * positions, float const * normals, int64_t n) {
+    dpos_.insert(dpos_.end(), positions, positions + 3 * n);
+    if (normals) dnrm_.insert(dnrm_.end(), normals, normals + 3 * n);
+    valid_ = false;
+  }
+  int64_t numSamples() const { return (int64_t)(pos_.size() / 3); }
+
+  // surface: a mesh BVH with the ray layout for the reachability test (used with normals), or nullptr
+  void updateGraph(MeshBvh const * surface = nullptr) const {
+    if (valid_) return;
+    int64_t n = numSamples();
+    nbr_.assign((size_t)(n * max_degree_), -1);
+    sep_.assign((size_t)(n * max_degree_), 0.f);
+    deg_.assign((size_t)n, 0);
+    float const * nrm = nrm_.empty() ? nullptr : nrm_.data();
+    thea_bvh const * surf = surface ? surface->get() : nullptr;
+    if (dpos_.empty())
+      check(thea_sample_graph(pos_.data(), nrm, n, max_degree_, seed_, surf, nbr_.data(), sep_.data(), deg_.data(),
+                              avg_, nullptr));
+    else
+      check(thea_sample_graph_oversampled(pos_.data(), nrm, n, dpos_.data(), nrm ? dnrm_.data() : nullptr,
+                                          (int64_t)(dpos_.size() / 3), max_degree_, seed_, surf, nbr_.data(),
+                                          sep_.data(), deg_.data(), avg_, nullptr));
+    valid_ = true;
+  }
+  // sample i's neighbours (ascending separation, then index) and their separations; numNeighbors(i) of them
+  int32_t numNeighbors(int64_t i) const { updateGraph(); return deg_[(size_t)i]; }
+  int32_t const * neighbors(int64_t i) const { updateGraph(); return nbr_.data() + i * max_degree_; }
+  float const * separations(int64_t i) const { updateGraph(); return sep_.data() + i * max_degree_; }
+  float getAverageSeparation() const { updateGraph(); return avg_[1]; }
+
+ private:
+  int32_t max_degree_;
+  uint32_t seed_;
+  std::vector<float> pos_, nrm_, dpos_, dnrm_;
+  mutable std::vector<int32_t> nbr_, deg_;
+  mutable std::vector<float> sep_;
+  mutable float avg_[2] = {0, 0};
+  mutable bool valid_ = false;
+};
+
 // MeshGroup<DisplayMesh>::load for OFF, OBJ and PLY files, flattened into host arrays in the reference's element order;
 // MeshBvh(file.vertices.data(), file.numVertices(), file.triangles.data(), file.numTriangles()) indexes its triangles.
 class MeshFile {

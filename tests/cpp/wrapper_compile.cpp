@@ -120,6 +120,27 @@ int main(int argc, char ** argv) {
   float inside[3] = {0.1f, 0.1f, 0.0f}, up[3] = {0, 0, -1};
   mesh.shapeDiameter(inside, up, 1, sdf);
   if (!(sdf[0] > 0.0 && sdf[0] <= 1.0)) { std::printf("sdf %f\n", sdf[0]); return 23; }
+  // the tetrahedron's smallest enclosing ball is the circle of its face x + y + z = 1 (the circumsphere's centre lies
+  // outside the tetrahedron): centre (1/3, 1/3, 1/3), radius sqrt(2/3); the origin lies inside
+  thea_gpu::BestFitSphere3 sphere;
+  sphere.addPoints(V, 4);
+  float c[3];
+  sphere.getCenter(c);
+  if (std::fabs(sphere.getRadius() - 0.81649658f) > 1e-6f || std::fabs(c[0] - 0.33333333f) > 1e-6f) {
+    std::printf("sphere %f\n", sphere.getRadius());
+    return 24;
+  }
+  // a ring of eight samples: each one's two nearest are its ring neighbours
+  float ring[24];
+  for (int i = 0; i < 8; ++i) {
+    ring[3 * i] = std::cos(0.785398163f * i);
+    ring[3 * i + 1] = std::sin(0.785398163f * i);
+    ring[3 * i + 2] = 0.f;
+  }
+  thea_gpu::PointSet3 ps(2, 1);
+  ps.setSamples(ring, nullptr, 8);
+  int32_t const * nb = ps.neighbors(0);
+  if (ps.numNeighbors(0) != 2 || nb[0] + nb[1] != 8 || (nb[0] != 1 && nb[0] != 7)) return 25;
   std::printf("wrapper ok\n");
   return 0;
 }
