@@ -15,8 +15,8 @@ are seeded synthetic data with the benchmark's shapes and distributions (no data
              on config 1, closest point (config 0), the k-NN graph (config 2), Visibility, the sample graph and
              ShapeDiameter on the config-0 mesh, the batched forest (config 3) and the serving loop (config 4).
 
---impl reference times the reference's algorithm on the host cores instead (the CPU restatement, since the reference
-itself needs Eigen, which is absent).
+--impl reference times the reference's algorithm on the host cores instead: the oracle's restatement, pinned bit for bit
+to the reference's own code (which builds only where its sources are, against an Eigen subset; Eigen itself is absent).
 
 Multi-GPU: one process per GPU (torchrun); each rank runs an independent replica on its own batch (weak scaling);
 the only exchange is the max-over-ranks of the timed region.
@@ -388,8 +388,8 @@ def reference_arm(args, rank, world):
             "config": headline_config(),
             "cpu_baseline": {"value": value, "unit": "Mqueries/s", "cores": threads, "kind": "port",
                              "sample": what + "; every step the whole workload, %d threads, static partition; the "
-                                              "reference's algorithm restated in C++ (the reference needs Eigen, "
-                                              "absent here), compiled with its release flags" % threads},
+                                              "reference's algorithm restated in C++ and pinned bit for bit to the "
+                                              "reference's own code, compiled with its release flags" % threads},
             "e2e": {"value": value, "unit": "Mqueries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
