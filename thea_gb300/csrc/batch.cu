@@ -656,12 +656,72 @@ BatchForest forest_view(thea_bvh const * b) {
   return f;
 }
 
-void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff, int64_t nq, ClosestParams const & cp,
-                       int chunk, int32_t * idx, float * dist, float * cpt, float * err, cudaStream_t s) {
-  if (nq <= 0) return;
+namespace {
+
+// FP64 re-check batches take their queries in (mesh, Morton code) order: a warp's round of 32 queries then holds
+// neighbours, whose searches take similar paths and share band candidates (256 config-3 meshes: 24.9 -> 20.8 ms). The
+// FP32 kernels refill lanes one query at a time and ran slower on sorted queries (11.2 -> 12.4 ms), so they keep the
+// caller's order. Results do not depend on the order.
+constexpr int64_t SORTED_QUERIES_MIN = 1 << 15;
+
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000ffu;
+  x = (x | (x << 8)) & 0x0300f00fu;
+  x = (x | (x << 4)) & 0x030c30c3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+__global__ void sorted_query_keys_kernel(float const * __restrict__ q, int64_t const * __restrict__ qoff, int M,
+                                         int64_t nq, float lx, float ly, float lz, float sx, float sy, float sz,
+                                         uint64_t * __restrict__ keys, uint32_t * __restrict__ vals) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  int m = mesh_of_query(qoff, M, i);
+  float c[3] = {(q[3 * i] - lx) * sx, (q[3 * i + 1] - ly) * sy, (q[3 * i + 2] - lz) * sz};
+  uint32_t g[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    float u = fminf(fmaxf(c[t], 0.f), 1.f);  // NaN-safe: fminf/fmaxf drop a NaN operand
+    g[t] = min((uint32_t)(u * 1024.f), 1023u);
+  }
+  keys[i] = ((uint64_t)m << 30) | (spread10(g[0]) << 2) | (spread10(g[1]) << 1) | spread10(g[2]);
+  vals[i] = (uint32_t)i;
+}
+
+__global__ void gather_queries_kernel(float const * __restrict__ q, uint32_t const * __restrict__ order, int64_t nq,
+                                      float * __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  int64_t j = order[i];
+  out[3 * i] = q[3 * j];
+  out[3 * i + 1] = q[3 * j + 1];
+  out[3 * i + 2] = q[3 * j + 2];
+}
+
+__global__ void scatter_closest_kernel(uint32_t const * __restrict__ order, int64_t nq, int32_t const * __restrict__ si,
+                                       float const * __restrict__ sd, float const * __restrict__ sc,
+                                       float const * __restrict__ se, int32_t * __restrict__ idx,
+                                       float * __restrict__ dist, float * __restrict__ cpt, float * __restrict__ err) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  int64_t j = order[i];
+  idx[j] = si[i];
+  if (dist) dist[j] = sd[i];
+  if (cpt) {
+    cpt[3 * j] = sc[3 * i];
+    cpt[3 * j + 1] = sc[3 * i + 1];
+    cpt[3 * j + 2] = sc[3 * i + 2];
+  }
+  if (err) err[j] = se[i];
+}
+
+// One batched closest-point search of `a` (queries, offsets, outputs) over the forest
+void batch_closest_core(thea_bvh const * b, ClosestArgs const & a, int64_t nq, ClosestParams const & cp, int chunk,
+                        cudaStream_t s) {
   BatchForest f = forest_view(b);
   bool sm = small_stack_ok(b);
-  ClosestArgs a{q, qoff, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, err, cp.seg_cut};
   int budget = cp.budget > 0 ? cp.budget : 0;
   Scratch counters(3 * sizeof(unsigned long long), s);
   THEA_CUDA_CHECK(cudaMemsetAsync(counters.ptr, 0, 3 * sizeof(unsigned long long), s));
@@ -674,6 +734,50 @@ void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff
                         : launch_batch_closest<4, 256>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
   else sm ? launch_batch_closest<8, 128>(f, a, nq, cp.precision, budget, c, chunk, hq, s)
           : launch_batch_closest<8, 512>(f, a, nq, cp.precision, budget, c, chunk, hq, s);
+}
+
+// batch_closest_core on the queries in (mesh, Morton code) order: keys, a stable radix sort, the permuted copy, the
+// search into scratch outputs, then the results scattered back to the caller's order
+void batch_closest_sorted(thea_bvh const * b, float const * q, int64_t const * qoff, int64_t nq,
+                          ClosestParams const & cp, int chunk, int32_t * idx, float * dist, float * cpt, float * err,
+                          cudaStream_t s) {
+  float sc[3];
+  for (int t = 0; t < 3; ++t) {
+    float ext = b->hi[t] - b->lo[t];
+    sc[t] = ext > 0.f ? 1.0f / ext : 0.f;
+  }
+  Scratch keys((size_t)nq * sizeof(uint64_t), s), order((size_t)nq * sizeof(uint32_t), s);
+  unsigned grid = (unsigned)ceil_div(nq, 256);
+  THEA_LAUNCH(sorted_query_keys_kernel, grid, 256, 0, s, q, qoff, b->num_segments, nq, b->lo[0], b->lo[1], b->lo[2],
+              sc[0], sc[1], sc[2], keys.as<uint64_t>(), order.as<uint32_t>());
+  int seg_bits = 0;
+  while ((1 << seg_bits) < b->num_segments) ++seg_bits;
+  radix_sort_pairs(keys.as<uint64_t>(), order.as<uint32_t>(), nq, 30 + seg_bits, s, /*probe_passes=*/false);
+  keys = Scratch();
+  Scratch qs((size_t)nq * 12, s), si((size_t)nq * 4, s), sd(dist ? (size_t)nq * 4 : 0, s);
+  Scratch scp(cpt ? (size_t)nq * 12 : 0, s), se(err ? (size_t)nq * 4 : 0, s);
+  THEA_LAUNCH(gather_queries_kernel, grid, 256, 0, s, q, order.as<uint32_t>(), nq, qs.as<float>());
+  ClosestArgs a{qs.as<float>(), qoff, cp.thresh, cp.bound2, cp.scene_scale, si.as<int32_t>(),
+                dist ? sd.as<float>() : nullptr, cpt ? scp.as<float>() : nullptr, err ? se.as<float>() : nullptr,
+                cp.seg_cut};
+  batch_closest_core(b, a, nq, cp, chunk, s);
+  THEA_LAUNCH(scatter_closest_kernel, grid, 256, 0, s, order.as<uint32_t>(), nq, si.as<int32_t>(),
+              dist ? sd.as<float>() : nullptr, cpt ? scp.as<float>() : nullptr, err ? se.as<float>() : nullptr, idx,
+              dist, cpt, err);
+}
+
+}  // namespace
+
+void run_batch_closest(thea_bvh const * b, float const * q, int64_t const * qoff, int64_t nq, ClosestParams const & cp,
+                       int chunk, int32_t * idx, float * dist, float * cpt, float * err, cudaStream_t s) {
+  if (nq <= 0) return;
+  if (cp.precision == THEA_PRECISION_FP64_RECHECK && nq >= SORTED_QUERIES_MIN && nq < ((int64_t)1 << 32) &&
+      b->num_segments <= (1 << 20)) {
+    batch_closest_sorted(b, q, qoff, nq, cp, chunk, idx, dist, cpt, err, s);
+    return;
+  }
+  ClosestArgs a{q, qoff, cp.thresh, cp.bound2, cp.scene_scale, idx, dist, cpt, err, cp.seg_cut};
+  batch_closest_core(b, a, nq, cp, chunk, s);
 }
 
 template <int W, int STACK>
