@@ -363,7 +363,7 @@ template <int W>
 __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
                                      int const * __restrict__ chosen, int const * __restrict__ offsets,
                                      int64_t level_base, int64_t next_base, WideNode<W> * __restrict__ nodes,
-                                     int * __restrict__ next_frontier, int2 * __restrict__ ranges) {
+                                     int * __restrict__ next_frontier) {
   int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= fsize) return;
   WideNode<W> node;
@@ -386,8 +386,6 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
     node.lox[e] = lo.x; node.loy[e] = lo.y; node.loz[e] = lo.z;
     node.hix[e] = hi.x; node.hiy[e] = hi.y; node.hiz[e] = hi.z;
     int cnt = code_count(a, code);
-    // the child slot's elements, a run of sorted positions, for its oriented slab
-    if (ranges) ranges[(level_base + f) * W + e] = make_int2((int)code_first(a, code), cnt);
     if (cnt <= a.leaf_size) {
       node.child[e] = encode_leaf((int)(code_first(a, code) - seg_base), cnt);
     } else {
@@ -416,7 +414,7 @@ __global__ void segment_roots_kernel(CollapseArgs a, int64_t n, int const * __re
                                      int const * __restrict__ small_rank, int const * __restrict__ is_big,
                                      int const * __restrict__ big_rank, int num_small, int const * __restrict__ bounds,
                                      WideNode<W> * __restrict__ nodes, int * __restrict__ frontier,
-                                     int * __restrict__ seg_root, int2 * __restrict__ ranges) {
+                                     int * __restrict__ seg_root) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.M) return;
   int64_t sa = a.seg_start ? a.seg_start[s] : 0, sb = a.seg_start ? a.seg_start[s + 1] : n;
@@ -434,7 +432,6 @@ __global__ void segment_roots_kernel(CollapseArgs a, int64_t n, int const * __re
     node.hix[0] = hi.x; node.hiy[0] = hi.y; node.hiz[0] = hi.z;
     node.child[0] = encode_leaf(0, (int)(sb - sa));
     nodes[small_rank[s]] = node;
-    if (ranges) ranges[(int64_t)small_rank[s] * W] = make_int2((int)sa, (int)(sb - sa));
     seg_root[s] = small_rank[s];
   } else {
     seg_root[s] = -1;  // empty segment
@@ -573,10 +570,8 @@ slab_kernel(int2 const * __restrict__ ranges, int64_t slots, float4 const * __re
   }
 }
 
-// ranges != nullptr: also records each child slot's run of sorted element positions (for the oriented slabs)
 template <int W>
-void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, Scratch * ranges,
-              cudaStream_t stream) {
+void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, cudaStream_t stream) {
   int M = a.M;
   // segment roots
   Scratch is_small((size_t)M * sizeof(int), stream), is_big((size_t)M * sizeof(int), stream);
@@ -607,15 +602,9 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
   THEA_CUDA_CHECK(thea_malloc_async((void **)&nodes, (size_t)cap * sizeof(WideNode<W>), stream));
   THEA_CUDA_CHECK(thea_malloc_async((void **)&b->seg_root, (size_t)M * sizeof(int32_t), stream));
   Scratch fa((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream), fb((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
-  int2 * rg = nullptr;
-  if (ranges) {
-    *ranges = Scratch((size_t)cap * W * sizeof(int2), stream);
-    THEA_CUDA_CHECK(cudaMemsetAsync(ranges->ptr, 0, ranges->bytes, stream));
-    rg = ranges->as<int2>();
-  }
   THEA_LAUNCH((segment_roots_kernel<W>), (unsigned)ceil_div(M, BUILD_THREADS), BUILD_THREADS, 0, stream, a, n,
               is_small.as<int>(), small_rank.as<int>(), is_big.as<int>(), big_rank.as<int>(), num_small, d_bounds,
-              nodes, fa.as<int>(), b->seg_root, rg);
+              nodes, fa.as<int>(), b->seg_root);
   Scratch chosen((size_t)std::max<int64_t>(cap, 1) * W * sizeof(int), stream);
   Scratch nint((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   Scratch offs((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
@@ -631,7 +620,7 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
                 nint.as<int>());
     exclusive_scan<int>(nint.as<int>(), offs.as<int>(), fsize, stream);
     THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
-                offs.as<int>(), base, base + fsize, nodes, nxt, rg);
+                offs.as<int>(), base, base + fsize, nodes, nxt);
     int tail[2];
     THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[0], offs.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[1], nint.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -731,13 +720,8 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     CollapseArgs a{left.as<int>(), right.as<int>(), first.as<int>(), last.as<int>(), elo.as<float4>(),
                    ehi.as<float4>(), vals.as<uint32_t>(), ilo.as<float4>(), ihi.as<float4>(),
                    M > 1 ? seg : nullptr, M, leaf};
-    // Oriented slabs go with single-mesh BVHs that have the closest layout: they shorten the longest searches of the
-    // one-query-per-thread kernels (small batches, serving), whose warps wait for their slowest lane. The persistent
-    // batched kernels, which refill a lane as soon as its query ends, ran faster with boxes alone, so forests have none.
-    bool want_slabs = is_mesh && M == 1 && (layouts & THEA_LAYOUT_CLOSEST);
-    Scratch child_ranges;
-    if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), want_slabs ? &child_ranges : nullptr, stream);
-    else collapse<8>(b, a, n, bounds.as<int>(), want_slabs ? &child_ranges : nullptr, stream);
+    if (width == 4) collapse<4>(b, a, n, bounds.as<int>(), stream);
+    else collapse<8>(b, a, n, bounds.as<int>(), stream);
     int64_t node_bytes = b->num_nodes * (width == 4 ? (int64_t)sizeof(WideNode<4>) : (int64_t)sizeof(WideNode<8>));
 
     int need = b->depth * (width - 1) + 1;
@@ -761,13 +745,6 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
       }
       THEA_LAUNCH(mesh_records_kernel, grid, BUILD_THREADS, 0, stream, V, F, n, seg, M, vals.as<uint32_t>(),
                   b->cp_rec, b->ray_rec, b->leaf_to_elem);
-      if (want_slabs) {
-        int64_t slots = b->num_nodes * width;
-        THEA_CUDA_CHECK(thea_malloc_async((void **)&b->slabs, (size_t)slots * sizeof(float4), stream));
-        rec_bytes += slots * (int64_t)sizeof(float4);
-        unsigned sgrid = (unsigned)std::min<int64_t>(slots, (int64_t)sm_count() * 16);
-        THEA_LAUNCH(slab_kernel, sgrid, SLAB_THREADS, 0, stream, child_ranges.as<int2>(), slots, b->cp_rec, b->slabs);
-      }
     } else {
       THEA_CUDA_CHECK(thea_malloc_async((void **)&b->pt_rec, (size_t)n * sizeof(float4), stream));
       rec_bytes += n * (int64_t)sizeof(float4);
@@ -794,12 +771,127 @@ thea_bvh * build_forest(bool is_mesh, float const * V, int64_t nv, int32_t const
     }
     b->device_bytes = node_bytes + rec_bytes;
     init_segment_roots(b, stream);
+    init_slabs(b, stream);
+    if (b->slabs) b->device_bytes += b->num_nodes * width * (int64_t)sizeof(float4);
     return b;
   } catch (...) {
     cudaStreamSynchronize(stream);
     destroy_bvh(b);
     throw;
   }
+}
+
+// Element range [first, end) of every node's subtree, from its children's: leaves carry their run, internal children
+// follow their parent in the node array (the collapse emits level by level). One pass settles every node whose
+// children are settled; a node array that breaks those rules (an image written by another build) sets `bad`.
+template <int W>
+__global__ void subtree_range_kernel(WideNode<W> const * __restrict__ nodes, int64_t num_nodes, int64_t n,
+                                     int2 * __restrict__ range, int * __restrict__ changed, int * __restrict__ bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += (int64_t)gridDim.x * blockDim.x) {
+    if (range[i].y >= 0) continue;
+    int lo = INT_MAX, hi = -1;
+    bool ready = true;
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      int code = nodes[i].child[c];
+      if (code == CHILD_EMPTY) continue;
+      if (code < 0) {
+        int first, count;
+        decode_leaf(code, first, count);
+        if (first < 0 || count <= 0 || (int64_t)first + count > n) {
+          atomicOr(bad, 1);
+          ready = false;
+          break;
+        }
+        lo = min(lo, first);
+        hi = max(hi, first + count);
+      } else {
+        if ((int64_t)code >= num_nodes || (int64_t)code <= i) {
+          atomicOr(bad, 1);
+          ready = false;
+          break;
+        }
+        int2 r = range[code];
+        if (r.y < 0) {
+          ready = false;
+          continue;
+        }
+        lo = min(lo, r.x);
+        hi = max(hi, r.y);
+      }
+    }
+    if (!ready) continue;
+    range[i] = hi >= 0 ? make_int2(lo, hi) : make_int2(0, 0);
+    *changed = 1;
+  }
+}
+
+// Run of sorted element positions (first, count) under each child slot
+template <int W>
+__global__ void slot_range_kernel(WideNode<W> const * __restrict__ nodes, int64_t num_nodes,
+                                  int2 const * __restrict__ range, int2 * __restrict__ slot) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < num_nodes * W;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int code = nodes[k / W].child[k % W];
+    int2 r = make_int2(0, 0);
+    if (code != CHILD_EMPTY && code < 0) {
+      int first, count;
+      decode_leaf(code, first, count);
+      r = make_int2(first, count);
+    } else if (code >= 0) {
+      int2 sub = range[code];
+      r = make_int2(sub.x, sub.y - sub.x);
+    }
+    slot[k] = r;
+  }
+}
+
+template <int W>
+bool slot_ranges(thea_bvh const * b, Scratch & slots, cudaStream_t stream) {
+  WideNode<W> const * nodes = (WideNode<W> const *)b->nodes;
+  int64_t nn = b->num_nodes;
+  Scratch range((size_t)nn * sizeof(int2), stream), flags(2 * sizeof(int), stream);
+  THEA_CUDA_CHECK(cudaMemsetAsync(range.ptr, 0xff, range.bytes, stream));
+  THEA_CUDA_CHECK(cudaMemsetAsync(flags.ptr, 0, flags.bytes, stream));
+  unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nn, BUILD_THREADS), 152 * 8));
+  // every pass settles at least the deepest unsettled level; a pass that settles nothing ends the loop, and any node
+  // still unsettled then (or after the pass limit) means the array is not a tree of this build's layout
+  bool settled = false;
+  for (int pass = 0; pass < 2 * b->depth + 4 && !settled; ++pass) {
+    THEA_CUDA_CHECK(cudaMemsetAsync(flags.ptr, 0, sizeof(int), stream));
+    THEA_LAUNCH(subtree_range_kernel<W>, grid, BUILD_THREADS, 0, stream, nodes, nn, b->n, range.as<int2>(),
+                flags.as<int>(), flags.as<int>() + 1);
+    int h[2];
+    THEA_CUDA_CHECK(cudaMemcpyAsync(h, flags.ptr, sizeof(h), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+    if (h[1]) return false;
+    settled = !h[0];
+  }
+  if (!settled) return false;
+  // the root (node 0) must cover every element once settled
+  int2 root;
+  THEA_CUDA_CHECK(cudaMemcpyAsync(&root, range.ptr, sizeof(root), cudaMemcpyDeviceToHost, stream));
+  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
+  if (root.x != 0 || (int64_t)root.y != b->n) return false;
+  slots = Scratch((size_t)nn * W * sizeof(int2), stream);
+  unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nn * W, BUILD_THREADS), 152 * 8));
+  THEA_LAUNCH(slot_range_kernel<W>, sgrid, BUILD_THREADS, 0, stream, nodes, nn, range.as<int2>(), slots.as<int2>());
+  return true;
+}
+
+// Oriented slabs go with single-mesh BVHs that have the closest layout: they shorten the longest searches of the
+// one-query-per-thread kernels (small batches, serving), whose warps wait for their slowest lane. The persistent
+// batched kernels, which refill a lane as soon as its query ends, ran faster with boxes alone, so forests have none.
+void init_slabs(thea_bvh * b, cudaStream_t stream) {
+  if (!b->is_mesh || b->num_segments != 1 || !b->cp_rec || b->slabs) return;
+  Scratch slots;
+  bool ok = b->width == 4 ? slot_ranges<4>(b, slots, stream) : slot_ranges<8>(b, slots, stream);
+  if (!ok) return;  // searches use boxes alone
+  int64_t n_slots = b->num_nodes * b->width;
+  THEA_CUDA_CHECK(thea_malloc_async((void **)&b->slabs, (size_t)n_slots * sizeof(float4), stream));
+  unsigned grid = (unsigned)std::min<int64_t>(n_slots, (int64_t)sm_count() * 16);
+  THEA_LAUNCH(slab_kernel, grid, SLAB_THREADS, 0, stream, slots.as<int2>(), n_slots, b->cp_rec, b->slabs);
+  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
 }
 
 void init_segment_roots(thea_bvh * b, cudaStream_t stream) {

@@ -28,7 +28,7 @@ struct thea_bvh {
   float4 * ray_rec = nullptr;      // mesh ray records, RAY_REC_F4 per element, leaf order
   float4 * pt_rec = nullptr;       // point records, 1 per element, leaf order
   float4 * slabs = nullptr;        // single mesh with the closest layout: one oriented slab per node child slot (width
-                                   // per node); not in byte images, so a deserialized handle searches by boxes alone
+                                   // per node); recomputed when an image is loaded (not part of it)
   int32_t * leaf_to_elem = nullptr;  // leaf-order position -> element index
   unsigned * err = nullptr;          // device word: error bits raised by query kernels
   unsigned * err_host = nullptr;     // pinned host mirror of *err, refreshed at the end of every query call
@@ -61,6 +61,9 @@ void destroy_bvh(thea_bvh * b);
 
 // Fills seg_roots from seg_lo / seg_hi (allocates it; synchronizes the stream)
 void init_segment_roots(thea_bvh * b, cudaStream_t stream);
+// The oriented slabs of a single-mesh BVH with the closest layout, from its nodes and records (after a build, and after
+// loading an image); other handles, and node arrays that do not follow the build's layout, get none.
+void init_slabs(thea_bvh * b, cudaStream_t stream);
 
 // Throws INVALID_ARGUMENT unless every face index lies in [0, nv): checked on the device before any kernel loads a
 // vertex through the faces (one pass over F and one 4-byte read back, which synchronizes `stream`).

@@ -163,6 +163,7 @@ thea_bvh * deserialize_bvh(void const * in, int64_t bytes, cudaStream_t s) {
     // the host image may be reused by the caller as soon as this returns
     THEA_CUDA_CHECK(cudaStreamSynchronize(s));
     init_segment_roots(b, s);
+    init_slabs(b, s);
     if (h.has_transform) set_transform(b, h.xf, s);
     return b;
   } catch (...) {
