@@ -468,6 +468,11 @@ THEA_API thea_status thea_selftest_set_error_bits(thea_bvh * bvh, uint32_t bits,
 
 /* ---- sampling ------------------------------------------------------------------------------------------------------ */
 
+/* Streams of the reference's Random(seed) (THEA_RNG_THEA_MT sampling, thea_random_sphere, thea_visibility) of 1,024
+ * twists (638,976 words) or more are generated in parallel chunks of 512 twists from jump-ahead start states: the first
+ * such stream on a device computes the 512-twist jump as a 19,968 x 19,968 bit matrix (about 50 MB of device memory,
+ * kept until the process exits; a few milliseconds); during a stream capture without that table, or for shorter
+ * streams, one block generates the words in order. The words are the same either way. */
 #define THEA_RNG_THEA_MT 0   /* the reference's Random(seed) stream: bit-identical samples */
 #define THEA_RNG_COUNTER 1   /* counter-based (Philox-4x32-10) stream: same distribution, fully parallel */
 

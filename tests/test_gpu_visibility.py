@@ -99,3 +99,16 @@ def test_empty_and_degenerate_inputs(T, oracle):
     hit = bvh.ray_intersects(dev(O), dev(D)).cpu().numpy()
     rt, _ = oracle.MeshIndex(V, F).ray_contract(O, D)
     assert np.array_equal(hit, rt >= 0)
+
+
+def test_long_random_streams_run_in_parallel_chunks(T, oracle):
+    """Streams of 1,024 twists or more run as parallel chunks from jump-ahead start states; they must equal the
+    sequential stream word for word, at chunk boundaries and past them."""
+    for seed in (3, 0xFFFF):
+        got = T.random_sphere(seed, 1000000)
+        assert np.array_equal(got, oracle.random_sphere(seed, 1000000)), seed
+    V, F = W.noisy_icosphere(3, 12)
+    for n in (212992, 212993, 400000):  # 3n words: exactly 1,024 twists, one word more, several chunks
+        pos, nrm, face = T.sample_evenly_by_area(V, F, n, 77)
+        rpos, rnrm, rface = oracle.sample_by_area(V, F, n, 77)
+        assert np.array_equal(np.asarray(pos), rpos) and np.array_equal(np.asarray(face), rface), n

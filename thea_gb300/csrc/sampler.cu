@@ -39,41 +39,106 @@ __device__ __forceinline__ uint32_t mt_temper(uint32_t r) {
   return r;
 }
 
+// One twist of Thea's generate() (Random.cpp:99-132) by a block of MT_THREADS threads, from X into Y (shared memory).
+// The twisted state goes to the other half of a ping-pong buffer, so each phase needs one barrier (its inputs are the
+// old state and the new words of the phase before), not two. One word per thread and phase: the twist is a chain of
+// three dependent phases, and their latency is the cost (a single warp with eight words per lane and phase measured
+// 4.6x slower).
+__device__ __forceinline__ void mt_twist_block(uint32_t const * X, uint32_t * Y) {
+  int t = threadIdx.x;
+  // phase A: i in [0, N - M) from old words i, i + 1, i + M; word N - M is left as it is by Thea's twist
+  if (t < MT_N - MT_M) Y[t] = mt_mix(X[t], X[t + 1], X[t + MT_M]);
+  if (t == 0) Y[MT_N - MT_M] = X[MT_N - MT_M];
+  __syncthreads();
+  // phase B: i in [N - M + 1, 2 (N - M)) from old words i, i + 1 and new word i - (N - M)
+  int i = MT_N - MT_M + 1 + t;
+  if (i < 2 * (MT_N - MT_M)) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
+  __syncthreads();
+  // phase C: i in [2 (N - M), N - 1), and i = N - 1 (old word N - 1 with new words 0 and M - 1)
+  i = 2 * (MT_N - MT_M) + t;
+  if (i < MT_N - 1) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
+  else if (i == MT_N - 1) Y[i] = mt_mix(X[MT_N - 1], Y[0], Y[MT_M - 1]);
+  __syncthreads();
+}
+
+__device__ __forceinline__ void mt_seed_state(uint32_t seed, uint32_t * st) {
+  st[0] = seed;
+  for (int i = 1; i < MT_N; ++i) st[i] = 1812433253u * (st[i - 1] ^ (st[i - 1] >> 30)) + (uint32_t)i;
+}
+
 // Writes `count` tempered words of Random(seed): Random::Random(seed) then bits() repeatedly.
 __global__ void __launch_bounds__(MT_THREADS) thea_mt_stream_kernel(uint32_t seed, int64_t count, uint32_t * __restrict__ out) {
-  // The twisted state is written to the other half of a ping-pong buffer, so each phase needs one barrier (its inputs
-  // are the old state and the new words of the phase before), not two. One word per thread and phase: the twist is a
-  // chain of three dependent phases, and their latency is the cost (a single warp with eight words per lane and
-  // phase measured 4.6x slower).
   __shared__ uint32_t buf[2][MT_N];
   int t = threadIdx.x;
-  if (t == 0) {
-    buf[0][0] = seed;
-    for (int i = 1; i < MT_N; ++i) buf[0][i] = 1812433253u * (buf[0][i - 1] ^ (buf[0][i - 1] >> 30)) + (uint32_t)i;
-  }
+  if (t == 0) mt_seed_state(seed, buf[0]);
   __syncthreads();
   int64_t twists = ceil_div(count, MT_N);
   int cur = 0;
   for (int64_t k = 0; k < twists; ++k) {
-    uint32_t const * X = buf[cur];
-    uint32_t * Y = buf[cur ^ 1];
-    // phase A: i in [0, N - M) from old words i, i + 1, i + M; word N - M is left as it is by Thea's twist
-    if (t < MT_N - MT_M) Y[t] = mt_mix(X[t], X[t + 1], X[t + MT_M]);
-    if (t == 0) Y[MT_N - MT_M] = X[MT_N - MT_M];
-    __syncthreads();
-    // phase B: i in [N - M + 1, 2 (N - M)) from old words i, i + 1 and new word i - (N - M)
-    int i = MT_N - MT_M + 1 + t;
-    if (i < 2 * (MT_N - MT_M)) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
-    __syncthreads();
-    // phase C: i in [2 (N - M), N - 1), and i = N - 1 (old word N - 1 with new words 0 and M - 1)
-    i = 2 * (MT_N - MT_M) + t;
-    if (i < MT_N - 1) Y[i] = mt_mix(X[i], X[i + 1], Y[i - (MT_N - MT_M)]);
-    else if (i == MT_N - 1) Y[i] = mt_mix(X[MT_N - 1], Y[0], Y[MT_M - 1]);
-    __syncthreads();
+    mt_twist_block(buf[cur], buf[cur ^ 1]);
+    uint32_t const * Y = buf[cur ^ 1];
     int64_t base = k * MT_N;
     for (int j = t; j < MT_N; j += MT_THREADS)
       if (base + j < count) out[base + j] = mt_temper(Y[j]);
     // the next twist reads Y and writes the other buffer, whose last readers finished before the barrier above
+    cur ^= 1;
+  }
+}
+
+// Jump-ahead (the twist is linear over GF(2) in the 19,968 state bits, MT_A entering only through the low bit of each
+// mixed word): P = T^L as a bit matrix, column j the state reached from the unit state e_j after L twists. Then the
+// state before twist cL is P^c applied to the seeded state; chunks of L twists run in parallel from those states.
+constexpr int MT_JUMP_TWISTS = 512;  // L
+constexpr int MT_STATE_BITS = MT_N * 32;
+constexpr int MT_VEC_THREADS = 640;  // one output word per thread (>= MT_N)
+
+__global__ void __launch_bounds__(MT_THREADS) mt_jump_columns_kernel(uint32_t * __restrict__ P) {
+  __shared__ uint32_t buf[2][MT_N];
+  int j = blockIdx.x, t = threadIdx.x;
+  for (int w = t; w < MT_N; w += MT_THREADS) buf[0][w] = w == (j >> 5) ? (1u << (j & 31)) : 0u;
+  __syncthreads();
+  int cur = 0;
+  for (int k = 0; k < MT_JUMP_TWISTS; ++k) {
+    mt_twist_block(buf[cur], buf[cur ^ 1]);
+    cur ^= 1;
+  }
+  for (int w = t; w < MT_N; w += MT_THREADS) P[(int64_t)j * MT_N + w] = buf[cur][w];
+}
+
+// out ^= P v over the columns [blockIdx.x * per, ...) of P (out zeroed beforehand; partial sums combined by atomicXor)
+__global__ void __launch_bounds__(MT_VEC_THREADS) mt_jump_apply_kernel(uint32_t const * __restrict__ P,
+                                                                       uint32_t const * __restrict__ v, int per,
+                                                                       uint32_t * __restrict__ out) {
+  int w = threadIdx.x;
+  int j0 = blockIdx.x * per, j1 = min(j0 + per, MT_STATE_BITS);
+  uint32_t acc = 0;
+  for (int j = j0; j < j1; ++j)
+    if ((__ldg(v + (j >> 5)) >> (j & 31)) & 1u)
+      if (w < MT_N) acc ^= __ldg(P + (int64_t)j * MT_N + w);
+  if (w < MT_N && acc) atomicXor(out + w, acc);
+}
+
+__global__ void mt_seed_kernel(uint32_t seed, uint32_t * __restrict__ st) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) mt_seed_state(seed, st);
+}
+
+// Chunk c: L twists (fewer for the last) from its start state, tempered words written at their stream positions
+__global__ void __launch_bounds__(MT_THREADS) mt_chunk_kernel(uint32_t const * __restrict__ starts, int64_t count,
+                                                              uint32_t * __restrict__ out) {
+  __shared__ uint32_t buf[2][MT_N];
+  int t = threadIdx.x;
+  int64_t c = blockIdx.x;
+  for (int w = t; w < MT_N; w += MT_THREADS) buf[0][w] = starts[c * MT_N + w];
+  __syncthreads();
+  int64_t twists = ceil_div(count, MT_N);
+  int64_t k0 = c * MT_JUMP_TWISTS, k1 = k0 + MT_JUMP_TWISTS < twists ? k0 + MT_JUMP_TWISTS : twists;
+  int cur = 0;
+  for (int64_t k = k0; k < k1; ++k) {
+    mt_twist_block(buf[cur], buf[cur ^ 1]);
+    uint32_t const * Y = buf[cur ^ 1];
+    int64_t base = k * MT_N;
+    for (int j = t; j < MT_N; j += MT_THREADS)
+      if (base + j < count) out[base + j] = mt_temper(Y[j]);
     cur ^= 1;
   }
 }
@@ -464,9 +529,54 @@ int64_t run_sample_by_area_noalloc(float const * V, int64_t nv, int32_t const * 
   return n;
 }
 
+namespace {
+
+// Streams of at least this many twists run as parallel chunks (below it one block is faster than the jump chain)
+constexpr int64_t MT_PARALLEL_MIN_TWISTS = 2 * MT_JUMP_TWISTS;
+constexpr int MT_APPLY_BLOCKS = 156;  // column slices of one jump (128 columns each)
+
+// P = T^L per device, computed on the first long stream of the device (about 50 MB; kept for the process)
+std::mutex g_jump_mu;
+uint32_t * g_jump[64] = {nullptr};
+
+uint32_t const * jump_matrix(cudaStream_t s) {
+  int dev = 0;
+  THEA_CUDA_CHECK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_jump_mu);
+  if (g_jump[dev]) return g_jump[dev];
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  THEA_CUDA_CHECK(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return nullptr;  // no allocation inside a capture: one block instead
+  uint32_t * P = nullptr;
+  THEA_CUDA_CHECK(thea_malloc((void **)&P, (size_t)MT_STATE_BITS * MT_N * sizeof(uint32_t)));
+  THEA_LAUNCH(mt_jump_columns_kernel, MT_STATE_BITS, MT_THREADS, 0, s, P);
+  THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  g_jump[dev] = P;
+  return P;
+}
+
+}  // namespace
+
 void run_thea_random_words(uint32_t seed, int64_t count, uint32_t * out, cudaStream_t s) {
   if (count <= 0) return;
-  THEA_LAUNCH(thea_mt_stream_kernel, 1, MT_THREADS, 0, s, seed, count, out);
+  int64_t twists = ceil_div(count, MT_N);
+  uint32_t const * P = twists >= MT_PARALLEL_MIN_TWISTS ? jump_matrix(s) : nullptr;
+  if (!P) {
+    THEA_LAUNCH(thea_mt_stream_kernel, 1, MT_THREADS, 0, s, seed, count, out);
+    return;
+  }
+  // start states of the chunks: the seeded state, then one jump (P times the previous start) per chunk
+  int64_t chunks = ceil_div(twists, MT_JUMP_TWISTS);
+  Scratch starts((size_t)chunks * MT_N * sizeof(uint32_t), s);
+  uint32_t * st = starts.as<uint32_t>();
+  THEA_CUDA_CHECK(cudaMemsetAsync(st, 0, starts.bytes, s));
+  THEA_LAUNCH(mt_seed_kernel, 1, 32, 0, s, seed, st);
+  int per = (int)ceil_div(MT_STATE_BITS, MT_APPLY_BLOCKS);
+  for (int64_t c = 1; c < chunks; ++c)
+    THEA_LAUNCH(mt_jump_apply_kernel, MT_APPLY_BLOCKS, MT_VEC_THREADS, 0, s, P, st + (c - 1) * MT_N, per,
+                st + c * MT_N);
+  THEA_LAUNCH(mt_chunk_kernel, (unsigned)chunks, MT_THREADS, 0, s, st, count, out);
 }
 
 int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64_t nf, int64_t n, uint32_t seed, int rng,
@@ -498,7 +608,7 @@ int64_t run_sample_by_area(float const * V, int64_t nv, int32_t const * F, int64
   Scratch words;
   if (rng == THEA_RNG_THEA_MT) {
     words = Scratch((size_t)n * 3 * sizeof(uint32_t), s);
-    THEA_LAUNCH(thea_mt_stream_kernel, 1, MT_THREADS, 0, s, seed, 3 * n, words.as<uint32_t>());
+    run_thea_random_words(seed, 3 * n, words.as<uint32_t>(), s);
   }
   THEA_LAUNCH(sample_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, V, F, nf, cum.as<double>(), words.as<uint32_t>(),
               seed, n, pos, nrm, face);
