@@ -353,7 +353,9 @@ batch_closest_phase2_kernel(BatchForest f, ClosestArgs a, HardQueue hq, unsigned
       init.idx = hq.idx[j];
       init.d2 = init.idx != INT_MAX ? hq.bound[j] : thresh_of(a, m);
       init.slot = hq.slot[j];
-      WarpBest b = closest_warp_query<W>(nodes, f.cp_rec, root, ebase, p, init, s_code[warp], s_lb[warp], f.err);
+      // the queries over budget are the long searches (deep inside closed surfaces), which the slabs cut most
+      WarpBest b = closest_warp_query<W>(nodes, f.cp_rec, root, ebase, p, init, s_code[warp], s_lb[warp], f.err,
+                                         f.slabs);
       if (lane == 0) {
         bool found = b.idx != INT_MAX;
         V3 cp = V3{0.f, 0.f, 0.f};
@@ -649,6 +651,7 @@ BatchForest forest_view(thea_bvh const * b) {
   f.cp_rec = b->cp_rec;
   f.ray_rec = b->ray_rec;
   f.pt_rec = b->pt_rec;
+  f.slabs = b->slabs;
   f.seg_start = b->seg_start;
   f.seg_root = b->seg_root;
   f.M = b->num_segments;

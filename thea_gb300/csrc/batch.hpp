@@ -12,6 +12,7 @@ struct BatchForest {
   float4 const * cp_rec;
   float4 const * ray_rec;
   float4 const * pt_rec;
+  float4 const * slabs;  // oriented slabs of the child slots (single-mesh BVHs; nullptr otherwise)
   int64_t const * seg_start;
   int32_t const * seg_root;
   int M;

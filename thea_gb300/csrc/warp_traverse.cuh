@@ -73,7 +73,8 @@ struct WarpBest {
 template <int W>
 __device__ WarpBest closest_warp_query(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
                                        int root, int64_t elem_base, V3 p, WarpBest best, int * s_code, float * s_lb,
-                                       unsigned * err) {
+                                       unsigned * err, float4 const * __restrict__ slabs = nullptr) {
+  float q1 = fabsf(p.x) + fabsf(p.y) + fabsf(p.z);
   constexpr int NPOP = 32 / W;
   int lane = threadIdx.x & 31;
   int e = lane / W, c = lane % W;
@@ -106,6 +107,11 @@ __device__ WarpBest closest_warp_query(WideNode<W> const * __restrict__ nodes, f
       int child;
       load_child<W>(nodes, code, c, lx, hx, ly, hy, lz, hz, child);
       float d2b = point_box_d2(p.x, p.y, p.z, lx, ly, lz, hx, hy, hz);
+      if (slabs && child != CHILD_EMPTY) {
+        // the child's oriented slab raises its bound (single-mesh BVHs)
+        float d;
+        d2b = fmaxf(d2b, slab_lower_bound(__ldg(slabs + (int64_t)code * W + c), p, q1, d));
+      }
       if (child != CHILD_EMPTY && d2b <= lim) {
         if (child >= 0) {
           key = __float_as_uint(d2b);
