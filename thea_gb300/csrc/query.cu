@@ -469,9 +469,12 @@ void launch_ray_stream(thea_bvh const * b, float const * o, float const * d, int
 // Resident blocks per SM requested from the register allocator: the K-best lists live in registers, and for K = 16
 // the allocation otherwise rounds up past five blocks of 128 threads
 template <int K> constexpr int knn_min_blocks() { return K <= 8 ? 8 : (K <= 16 ? 5 : 3); }
+// Point k-NN keeps lists of K >= 8 in shared memory (knn_query_shared): 48 registers for K = 16, eight blocks resident
+template <int K> __host__ __device__ constexpr bool knn_lists_shared() { return K >= 8; }
+template <int K> constexpr int knn_point_min_blocks() { return knn_lists_shared<K>() ? (K <= 16 ? 8 : 4) : 8; }
 
 template <int W, int K, int STACK>
-__global__ void __launch_bounds__(QUERY_THREADS, knn_min_blocks<K>())
+__global__ void __launch_bounds__(QUERY_THREADS, knn_point_min_blocks<K>())
 knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
            int64_t n, int k_out, float thresh, int32_t const * __restrict__ exclude, int32_t * __restrict__ out_index,
            float * __restrict__ out_d2, unsigned * __restrict__ err, uint32_t const * __restrict__ order,
@@ -498,9 +501,28 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
   float start = init_bound ? fminf(thresh, init_bound[q]) : thresh;
   float bd[K];
   int bi[K];
+  if constexpr (knn_lists_shared<K>()) {
+    __shared__ float s_d[K][QUERY_THREADS];
+    __shared__ int s_i[K][QUERY_THREADS];
+    int t = threadIdx.x;
 #pragma unroll
-  for (int j = 0; j < K; ++j) { bd[j] = start; bi[j] = INT_MAX; }
-  knn_query<W, K, STACK>(nodes, pts, 0, 0, p, excl, bd, bi, err);
+    for (int j = 0; j < K; ++j) {
+      s_d[j][t] = start;
+      s_i[j][t] = INT_MAX;
+    }
+    float kth = start;
+    int kth_i = INT_MAX;
+    knn_query_shared<W, K, STACK, QUERY_THREADS>(nodes, pts, 0, 0, p, excl, s_d, s_i, kth, kth_i, err);
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      bd[j] = s_d[j][t];
+      bi[j] = s_i[j][t];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < K; ++j) { bd[j] = start; bi[j] = INT_MAX; }
+    knn_query<W, K, STACK>(nodes, pts, 0, 0, p, excl, bd, bi, err);
+  }
   uintptr_t outs = reinterpret_cast<uintptr_t>(out_index) | reinterpret_cast<uintptr_t>(out_d2);
   if (K % 4 == 0 && k_out == K && (outs & 15) == 0) {
     // whole rows in 16-byte stores: rows land at scattered element indices (self mode), and full-sector writes keep

@@ -1096,6 +1096,63 @@ __device__ __forceinline__ void knn_query(WideNode<W> const * __restrict__ nodes
   }
 }
 
+// knn_query with the sorted list in shared memory instead of registers: sd / si are [K][B] arrays of the block (B
+// threads, entry j of thread t at [j][t], so a warp's accesses fall in distinct banks) and the k-th entry is mirrored in
+// kth / kth_i for the reject test. An insertion shifts the larger entries up one place (the same (distance, index)
+// order as knn_insert). Holding the lists out of registers lets twice as many warps stay resident.
+template <int W, int K, int STACK, int B>
+__device__ __forceinline__ void knn_query_shared(WideNode<W> const * __restrict__ nodes,
+                                                 float4 const * __restrict__ pts, int root, int64_t elem_base, V3 p,
+                                                 int excl, float (*sd)[B], int (*si)[B], float & kth, int & kth_i,
+                                                 unsigned * err) {
+  int t = threadIdx.x;
+  int2 stk[STACK];  // (child code, bound bits)
+  int sp = 0;
+  int next = root;
+  while (next != CHILD_EMPTY || sp > 0) {
+    int code = next;
+    if (code == CHILD_EMPTY) {
+      --sp;
+      code = stk[sp].x;
+      if (__int_as_float(stk[sp].y) > kth * PRUNE_SLACK) continue;
+    }
+    next = CHILD_EMPTY;
+    if (code >= 0) {
+      NodeRegs<W> nd;
+      load_node(nodes, code, nd);
+      float lb[W];
+      point_child_bounds<W>(nd, p, lb);
+      push_children_next<W, STACK>(nd, lb, kth * PRUNE_SLACK, stk, sp, next, err);
+    } else {
+      int first, count;
+      decode_leaf(code, first, count);
+      int64_t k0 = elem_base + first;
+      for (int64_t k = k0; k < k0 + count; ++k) {
+        float4 a = __ldg(pts + k);
+        int idx = __float_as_int(a.w);
+        if (idx == excl) continue;
+        // MetricL2Impl<point, point>::closestPoints: (element - query).squaredNorm()
+        float d2 = squared_norm(xyz(a) - p);
+        if (d2 < kth || (d2 == kth && idx < kth_i)) {
+          int j = K - 1;
+          while (j > 0) {
+            float dj = sd[j - 1][t];
+            int ij = si[j - 1][t];
+            if (dj < d2 || (dj == d2 && ij < idx)) break;
+            sd[j][t] = dj;
+            si[j][t] = ij;
+            --j;
+          }
+          sd[j][t] = d2;
+          si[j][t] = idx;
+          kth = sd[K - 1][t];
+          kth_i = si[K - 1][t];
+        }
+      }
+    }
+  }
+}
+
 // k nearest triangles of a mesh BVH: the same search with the closest-point record test (FP32 reference arithmetic);
 // a NaN distance (coincident vertices) is never kept
 template <int W, int K, int STACK>
