@@ -554,10 +554,34 @@ batch_knn_kernel(BatchForest f, float const * __restrict__ queries, int64_t cons
       int m = mesh_of_query(qoff, f.M, q);
       float bd[K];
       int bi[K];
+      if constexpr (K >= 8) {
+        // the K-best list in shared memory, as the point k-NN kernel keeps it (more warps resident)
+        __shared__ float s_d[K][BATCH_THREADS];
+        __shared__ int s_i[K][BATCH_THREADS];
+        int th = threadIdx.x;
 #pragma unroll
-      for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
-      knn_query<W, K, STACK>(nodes, f.pt_rec, __ldg(f.seg_root + m), __ldg(f.seg_start + m), load_v3(queries + 3 * q),
-                             -1, bd, bi, f.err);
+        for (int j = 0; j < K; ++j) {
+          s_d[j][th] = thresh;
+          s_i[j][th] = INT_MAX;
+        }
+        float kth = thresh;
+        int kth_i = INT_MAX;
+        knn_query_shared<W, K, STACK, BATCH_THREADS>(nodes, f.pt_rec, __ldg(f.seg_root + m), __ldg(f.seg_start + m),
+                                                     load_v3(queries + 3 * q), -1, s_d, s_i, kth, kth_i, f.err);
+        // the row from shared memory
+        for (int j = 0; j < k_out; ++j) {
+          int bij = s_i[j][th];
+          bool v = bij != INT_MAX;
+          out_index[q * k_out + j] = v ? bij : -1;
+          out_d2[q * k_out + j] = v ? s_d[j][th] : -1.f;
+        }
+        continue;
+      } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
+        knn_query<W, K, STACK>(nodes, f.pt_rec, __ldg(f.seg_root + m), __ldg(f.seg_start + m),
+                               load_v3(queries + 3 * q), -1, bd, bi, f.err);
+      }
       for (int j = 0; j < k_out; ++j) {
         bool v = bi[j] != INT_MAX;
         out_index[q * k_out + j] = v ? bi[j] : -1;

@@ -473,6 +473,37 @@ template <int K> constexpr int knn_min_blocks() { return K <= 8 ? 8 : (K <= 16 ?
 template <int K> __host__ __device__ constexpr bool knn_lists_shared() { return K >= 8; }
 template <int K> constexpr int knn_point_min_blocks() { return knn_lists_shared<K>() ? (K <= 16 ? 8 : 4) : 8; }
 
+// Row `row` of the k-NN outputs from a K-entry list read through gd(j) / gi(j) (registers or shared memory): -1 for
+// empty entries. Whole rows go out as 16-byte stores when they can: rows land at scattered element indices (self
+// mode), and full-sector writes keep the L2 from sending partial sectors to DRAM.
+template <int K, class GD, class GI>
+__device__ __forceinline__ void write_knn_row(int32_t * __restrict__ out_index, float * __restrict__ out_d2, int64_t row,
+                                              int k_out, GD gd, GI gi) {
+  uintptr_t outs = reinterpret_cast<uintptr_t>(out_index) | reinterpret_cast<uintptr_t>(out_d2);
+  if (K % 4 == 0 && k_out == K && (outs & 15) == 0) {
+    int4 * oi = reinterpret_cast<int4 *>(out_index + row * K);
+    float4 * od = reinterpret_cast<float4 *>(out_d2 + row * K);
+#pragma unroll
+    for (int j = 0; j < K; j += 4) {
+      int i0 = gi(j), i1 = gi(j + 1), i2 = gi(j + 2), i3 = gi(j + 3);
+      i0 = i0 != INT_MAX ? i0 : -1;
+      i1 = i1 != INT_MAX ? i1 : -1;
+      i2 = i2 != INT_MAX ? i2 : -1;
+      i3 = i3 != INT_MAX ? i3 : -1;
+      oi[j / 4] = make_int4(i0, i1, i2, i3);
+      od[j / 4] = make_float4(i0 >= 0 ? gd(j) : -1.f, i1 >= 0 ? gd(j + 1) : -1.f, i2 >= 0 ? gd(j + 2) : -1.f,
+                              i3 >= 0 ? gd(j + 3) : -1.f);
+    }
+    return;
+  }
+  for (int j = 0; j < k_out; ++j) {
+    int i = gi(j);
+    bool v = i != INT_MAX;
+    out_index[row * k_out + j] = v ? i : -1;
+    out_d2[row * k_out + j] = v ? gd(j) : -1.f;
+  }
+}
+
 template <int W, int K, int STACK>
 __global__ void __launch_bounds__(QUERY_THREADS, knn_point_min_blocks<K>())
 knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
@@ -499,8 +530,6 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
   // init_bound (self mode, per leaf position): an upper bound on the k-th neighbour's squared distance, inclusive, from
   // actual points; the search keeps every point within it, so the result is the same as without it
   float start = init_bound ? fminf(thresh, init_bound[q]) : thresh;
-  float bd[K];
-  int bi[K];
   if constexpr (knn_lists_shared<K>()) {
     __shared__ float s_d[K][QUERY_THREADS];
     __shared__ int s_i[K][QUERY_THREADS];
@@ -513,36 +542,15 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
     float kth = start;
     int kth_i = INT_MAX;
     knn_query_shared<W, K, STACK, QUERY_THREADS>(nodes, pts, 0, 0, p, excl, s_d, s_i, kth, kth_i, err);
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      bd[j] = s_d[j][t];
-      bi[j] = s_i[j][t];
-    }
+    // the row straight from shared memory (no register copy, which the dynamic row length would put in local memory)
+    write_knn_row<K>(out_index, out_d2, row, k_out, [&](int j) { return s_d[j][t]; }, [&](int j) { return s_i[j][t]; });
   } else {
+    float bd[K];
+    int bi[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) { bd[j] = start; bi[j] = INT_MAX; }
     knn_query<W, K, STACK>(nodes, pts, 0, 0, p, excl, bd, bi, err);
-  }
-  uintptr_t outs = reinterpret_cast<uintptr_t>(out_index) | reinterpret_cast<uintptr_t>(out_d2);
-  if (K % 4 == 0 && k_out == K && (outs & 15) == 0) {
-    // whole rows in 16-byte stores: rows land at scattered element indices (self mode), and full-sector writes keep
-    // the L2 from sending partial sectors to DRAM
-    int4 * oi = reinterpret_cast<int4 *>(out_index + row * K);
-    float4 * od = reinterpret_cast<float4 *>(out_d2 + row * K);
-#pragma unroll
-    for (int j = 0; j < K; j += 4) {
-      int i0 = bi[j] != INT_MAX ? bi[j] : -1, i1 = bi[j + 1] != INT_MAX ? bi[j + 1] : -1;
-      int i2 = bi[j + 2] != INT_MAX ? bi[j + 2] : -1, i3 = bi[j + 3] != INT_MAX ? bi[j + 3] : -1;
-      oi[j / 4] = make_int4(i0, i1, i2, i3);
-      od[j / 4] = make_float4(i0 >= 0 ? bd[j] : -1.f, i1 >= 0 ? bd[j + 1] : -1.f, i2 >= 0 ? bd[j + 2] : -1.f,
-                              i3 >= 0 ? bd[j + 3] : -1.f);
-    }
-    return;
-  }
-  for (int j = 0; j < k_out; ++j) {
-    bool v = bi[j] != INT_MAX;
-    out_index[row * k_out + j] = v ? bi[j] : -1;
-    out_d2[row * k_out + j] = v ? bd[j] : -1.f;
+    write_knn_row<K>(out_index, out_d2, row, k_out, [&](int j) { return bd[j]; }, [&](int j) { return bi[j]; });
   }
 }
 
