@@ -466,10 +466,8 @@ void launch_ray_stream(thea_bvh const * b, float const * o, float const * d, int
 // BoundedSortedArrayN.hpp:137-214)
 //============================================================================================================================
 
-// Resident blocks per SM requested from the register allocator: the K-best lists live in registers, and for K = 16
-// the allocation otherwise rounds up past five blocks of 128 threads
-template <int K> constexpr int knn_min_blocks() { return K <= 8 ? 8 : (K <= 16 ? 5 : 3); }
-// Point k-NN keeps lists of K >= 8 in shared memory (knn_query_shared): 48 registers for K = 16, eight blocks resident
+// The k-NN kernels keep lists of K >= 8 in shared memory (knn_search_shared): 48-56 registers for K = 16, and the
+// register allocator is asked for eight resident blocks of 128 threads (four for K = 32, whose lists take 32 KB)
 template <int K> __host__ __device__ constexpr bool knn_lists_shared() { return K >= 8; }
 template <int K> constexpr int knn_point_min_blocks() { return knn_lists_shared<K>() ? (K <= 16 ? 8 : 4) : 8; }
 
@@ -556,7 +554,7 @@ knn_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ p
 
 // k nearest triangles of a mesh BVH to each query point (kClosestPairs on a MeshBvh)
 template <int W, int K, int STACK>
-__global__ void __launch_bounds__(QUERY_THREADS, knn_min_blocks<K>())
+__global__ void __launch_bounds__(QUERY_THREADS, knn_point_min_blocks<K>())
 knn_mesh_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ rec,
                 float const * __restrict__ queries, int64_t n, int k_out, float thresh,
                 int32_t const * __restrict__ exclude, int32_t * __restrict__ out_index, float * __restrict__ out_d2,
@@ -566,15 +564,26 @@ knn_mesh_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restric
   if (order) q = order[q];
   V3 p = load_v3(queries + 3 * q);
   int excl = exclude ? exclude[q] : -1;
-  float bd[K];
-  int bi[K];
+  if constexpr (knn_lists_shared<K>()) {
+    __shared__ float s_d[K][QUERY_THREADS];
+    __shared__ int s_i[K][QUERY_THREADS];
+    int t = threadIdx.x;
 #pragma unroll
-  for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
-  knn_mesh_query<W, K, STACK>(nodes, rec, 0, 0, p, excl, bd, bi, err);
-  for (int j = 0; j < k_out; ++j) {
-    bool v = bi[j] != INT_MAX;
-    out_index[q * k_out + j] = v ? bi[j] : -1;
-    out_d2[q * k_out + j] = v ? bd[j] : -1.f;
+    for (int j = 0; j < K; ++j) {
+      s_d[j][t] = thresh;
+      s_i[j][t] = INT_MAX;
+    }
+    float kth = thresh;
+    int kth_i = INT_MAX;
+    knn_mesh_query_shared<W, K, STACK, QUERY_THREADS>(nodes, rec, 0, 0, p, excl, s_d, s_i, kth, kth_i, err);
+    write_knn_row<K>(out_index, out_d2, q, k_out, [&](int j) { return s_d[j][t]; }, [&](int j) { return s_i[j][t]; });
+  } else {
+    float bd[K];
+    int bi[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) { bd[j] = thresh; bi[j] = INT_MAX; }
+    knn_mesh_query<W, K, STACK>(nodes, rec, 0, 0, p, excl, bd, bi, err);
+    write_knn_row<K>(out_index, out_d2, q, k_out, [&](int j) { return bd[j]; }, [&](int j) { return bi[j]; });
   }
 }
 

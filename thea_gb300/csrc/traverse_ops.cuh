@@ -1099,12 +1099,12 @@ __device__ __forceinline__ void knn_query(WideNode<W> const * __restrict__ nodes
 // knn_query with the sorted list in shared memory instead of registers: sd / si are [K][B] arrays of the block (B
 // threads, entry j of thread t at [j][t], so a warp's accesses fall in distinct banks) and the k-th entry is mirrored in
 // kth / kth_i for the reject test. An insertion shifts the larger entries up one place (the same (distance, index)
-// order as knn_insert). Holding the lists out of registers lets twice as many warps stay resident.
-template <int W, int K, int STACK, int B>
-__device__ __forceinline__ void knn_query_shared(WideNode<W> const * __restrict__ nodes,
-                                                 float4 const * __restrict__ pts, int root, int64_t elem_base, V3 p,
-                                                 int excl, float (*sd)[B], int (*si)[B], float & kth, int & kth_i,
-                                                 unsigned * err) {
+// order as knn_insert). Holding the lists out of registers lets twice as many warps stay resident. `elem(k, idx, d2)`
+// gives element k's index and squared distance (false: skip it).
+template <int W, int K, int STACK, int B, class Elem>
+__device__ __forceinline__ void knn_search_shared(WideNode<W> const * __restrict__ nodes, int root, int64_t elem_base,
+                                                  V3 p, int excl, float (*sd)[B], int (*si)[B], float & kth,
+                                                  int & kth_i, unsigned * err, Elem elem) {
   int t = threadIdx.x;
   int2 stk[STACK];  // (child code, bound bits)
   int sp = 0;
@@ -1128,11 +1128,9 @@ __device__ __forceinline__ void knn_query_shared(WideNode<W> const * __restrict_
       decode_leaf(code, first, count);
       int64_t k0 = elem_base + first;
       for (int64_t k = k0; k < k0 + count; ++k) {
-        float4 a = __ldg(pts + k);
-        int idx = __float_as_int(a.w);
-        if (idx == excl) continue;
-        // MetricL2Impl<point, point>::closestPoints: (element - query).squaredNorm()
-        float d2 = squared_norm(xyz(a) - p);
+        int idx;
+        float d2;
+        if (!elem(k, idx, d2) || idx == excl) continue;
         if (d2 < kth || (d2 == kth && idx < kth_i)) {
           int j = K - 1;
           while (j > 0) {
@@ -1151,6 +1149,37 @@ __device__ __forceinline__ void knn_query_shared(WideNode<W> const * __restrict_
       }
     }
   }
+}
+
+// Points: MetricL2Impl<point, point>::closestPoints, (element - query).squaredNorm()
+template <int W, int K, int STACK, int B>
+__device__ __forceinline__ void knn_query_shared(WideNode<W> const * __restrict__ nodes,
+                                                 float4 const * __restrict__ pts, int root, int64_t elem_base, V3 p,
+                                                 int excl, float (*sd)[B], int (*si)[B], float & kth, int & kth_i,
+                                                 unsigned * err) {
+  knn_search_shared<W, K, STACK, B>(nodes, root, elem_base, p, excl, sd, si, kth, kth_i, err,
+                                    [&](int64_t k, int & idx, float & d2) {
+                                      float4 a = __ldg(pts + k);
+                                      idx = __float_as_int(a.w);
+                                      d2 = squared_norm(xyz(a) - p);
+                                      return true;
+                                    });
+}
+
+// Triangles: the closest-point record test (FP32 reference arithmetic); a NaN distance is never kept
+template <int W, int K, int STACK, int B>
+__device__ __forceinline__ void knn_mesh_query_shared(WideNode<W> const * __restrict__ nodes,
+                                                      float4 const * __restrict__ rec, int root, int64_t elem_base,
+                                                      V3 p, int excl, float (*sd)[B], int (*si)[B], float & kth,
+                                                      int & kth_i, unsigned * err) {
+  knn_search_shared<W, K, STACK, B>(nodes, root, elem_base, p, excl, sd, si, kth, kth_i, err,
+                                    [&](int64_t k, int & idx, float & d2) {
+                                      idx = cp_record_index(rec, k);
+                                      if (idx == excl) return false;
+                                      V3 cp;
+                                      d2 = cp_record_test(rec, k, p, cp);
+                                      return true;
+                                    });
 }
 
 // k nearest triangles of a mesh BVH: the same search with the closest-point record test (FP32 reference arithmetic);
