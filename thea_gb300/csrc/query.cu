@@ -587,7 +587,16 @@ knn_mesh_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restric
   }
 }
 
-constexpr int64_t CLOSEST_TWO_PHASE_MIN = 1 << 16;
+// FP32 calls on one BVH by size (config-0 sweep of 1,024 .. 262,144 queries, event-timed):
+//  * fewer than CLOSEST_WARP_MAX queries: two kernels with a 16-step budget, so nearly every query runs as one warp
+//    over up to 8 nodes a step (4,096 queries: 0.19 ms against 0.59 ms one per thread, whose time is the longest
+//    query's chain of dependent loads);
+//  * up to CLOSEST_TWO_PHASE_MIN: one query per thread (65,536 queries: 0.71 ms; 0.72 with a 16-step budget);
+//  * from there: two kernels with a 256-step budget (persistent lanes, then a warp per query past it; 262,144 queries:
+//    1.30 ms against 1.84 one per thread).
+constexpr int64_t CLOSEST_WARP_MAX = 57344;
+constexpr int CLOSEST_WARP_BUDGET = 16;
+constexpr int64_t CLOSEST_TWO_PHASE_MIN = 98304;
 constexpr int CLOSEST_TWO_PHASE_BUDGET = 256;
 
 __global__ void query_range_kernel(int64_t * qoff, int64_t n) {
@@ -930,13 +939,14 @@ bool small_stack_ok(thea_bvh const * b) {
 void run_closest(thea_bvh const * b, float const * q, int64_t n, ClosestParams const & cp, int32_t * idx, float * dist,
                  float * cpt, float * errout, unsigned * err, cudaStream_t s) {
   if (n <= 0) return;
-  if (cp.precision == THEA_PRECISION_FP32_REFERENCE && !errout && !b->query_order && n >= CLOSEST_TWO_PHASE_MIN) {
-    // Large FP32 batches: persistent lanes with a stack-pop budget, then one warp per query over budget (the BVH is
-    // a one-mesh forest). The same searches, so the same results; config 0 (262,144 queries): 2.43 -> 1.81 ms.
+  if (cp.precision == THEA_PRECISION_FP32_REFERENCE && !errout && !b->query_order &&
+      (n < CLOSEST_WARP_MAX || n >= CLOSEST_TWO_PHASE_MIN)) {
+    // Persistent lanes with a step budget, then one warp per query over budget (the BVH is a one-mesh forest). The
+    // same searches, so the same results.
     Scratch qoff(2 * sizeof(int64_t), s);
     THEA_LAUNCH(query_range_kernel, 1, 1, 0, s, qoff.as<int64_t>(), n);
     ClosestParams c2 = cp;
-    c2.budget = CLOSEST_TWO_PHASE_BUDGET;
+    c2.budget = n < CLOSEST_WARP_MAX ? CLOSEST_WARP_BUDGET : CLOSEST_TWO_PHASE_BUDGET;
     run_batch_closest(b, q, qoff.as<int64_t>(), n, c2, 64, idx, dist, cpt, nullptr, s);
     return;
   }
