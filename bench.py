@@ -629,7 +629,7 @@ def extra_workloads(T, torch, stream, flush, args):
                                         "ms": 1e3 * statistics.mean(e2e_t), "h2d_bytes": 12 * CP_QUERIES,
                                         "d2h_bytes": 20 * CP_QUERIES, "same_as_device":
                                         bool(torch.equal(hi, bvh.closest_element(Qd)[0].cpu()))}
-    # a batch below the two-kernel threshold: one query per thread, children pruned by box and oriented slab
+    # a small call: the two-kernel path with a short step budget, so nearly every query runs as one warp
     Qs = Qd[:32768].contiguous()
     ms_s = timed_steps(lambda: bvh.closest_element(Qs), steps, 2, flush, stream)
     out["closest_point_cfg0"]["first_32768_queries"] = {
