@@ -190,7 +190,7 @@ serve_closest_phase2_kernel(ServeTask const * __restrict__ tasks, int64_t const 
       init.idx = hq.idx[j];
       init.d2 = init.idx != INT_MAX ? hq.bound[j] : t->thresh;
       init.slot = hq.slot[j];
-      WarpBest b = closest_warp_query<W>(nodes, t->rec, 0, 0, p, init, s_code[warp], s_lb[warp], t->err);
+      WarpBest b = closest_warp_query<W>(nodes, t->rec, 0, 0, p, init, s_code[warp], s_lb[warp], t->err, t->slabs);
       found = b.idx != INT_MAX;
       idx = b.idx;
       dist = sqrtf(b.d2);
