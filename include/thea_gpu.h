@@ -305,16 +305,19 @@ typedef struct thea_mesh_info {
  * DisplayMesh::addFace does (Graphics/DisplayMesh.cpp:249-320); faces the non-strict readers skip (bad, out-of-range or,
  * in OFF and PLY, repeated indices) are skipped. Binary PLY properties beyond a vertex's coordinates and a face's index
  * list, and elements of other kinds, are skipped as the header describes them (the reference's binary reader cannot
- * read such files). The 3DS codec (which needs lib3ds) is not built: THEA_ERR_INVALID_ARGUMENT. */
+ * read such files). 3DS (.3ds, Graphics/MeshCodec3ds.hpp over lib3ds 1.x): one submesh per triangle mesh of the file
+ * in lib3ds's order (sorted by object name, file order among equal names), node transforms not applied, meshes without
+ * vertices skipped; faces with an out-of-range or repeated index are skipped but numbered, and vertex and face numbers
+ * run over the whole file. */
 THEA_API thea_status thea_mesh_read(const char * path, thea_mesh ** out_mesh);
-/* The same readers on a file's bytes in host memory, with the codec named ("obj", "off" or "ply"): MeshGroup::read
+/* The same readers on a file's bytes in host memory, with the codec named ("3ds", "obj", "off" or "ply"): MeshGroup::read
  * from a BinaryInputStream with an explicit codec (Graphics/MeshGroup.hpp:324-352). */
 THEA_API thea_status thea_mesh_read_buffer(const void * data, int64_t bytes, const char * codec, thea_mesh ** out_mesh);
 THEA_API thea_status thea_mesh_get_info(const thea_mesh * mesh, thea_mesh_info * info);
 /* Copies the arrays to host buffers (each nullable): vertices (3 x num_vertices floats), vertex_source (file vertex index
  * of each vertex, 0-based), triangles (3 x num_triangles indices into vertices), triangle_face (source face index of each
- * triangle: the OFF face number, the OBJ reader's running face count, or the PLY reader's count of faces handed to
- * the mesh), submesh_vertex_offsets and
+ * triangle: the OFF face number, the OBJ reader's running face count, the PLY reader's count of faces handed to
+ * the mesh, or the 3DS reader's face number over the file), submesh_vertex_offsets and
  * submesh_triangle_offsets (num_submeshes + 1 entries each). */
 THEA_API thea_status thea_mesh_copy(const thea_mesh * mesh, float * vertices, int32_t * vertex_source,
                                     int32_t * triangles, int32_t * triangle_face, int64_t * submesh_vertex_offsets,

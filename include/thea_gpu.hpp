@@ -480,7 +480,7 @@ class PointSet3 {
   mutable bool valid_ = false;
 };
 
-// MeshGroup<DisplayMesh>::load for OFF, OBJ and PLY files, flattened into host arrays in the reference's element order;
+// MeshGroup<DisplayMesh>::load for 3DS, OFF, OBJ and PLY files, flattened into host arrays in the reference's element order;
 // MeshBvh(file.vertices.data(), file.numVertices(), file.triangles.data(), file.numTriangles()) indexes its triangles.
 class MeshFile {
  public:

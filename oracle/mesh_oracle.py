@@ -11,6 +11,12 @@ in FP32 with one rounding per operation (numpy float32 scalars) and Eigen's 3-te
   vertices are the distinct (v, t, n) references of its faces in ascending order;
 - the PLY reader (Graphics/MeshCodecPly.hpp:229-700), ASCII and binary; binary properties and elements beyond the
   vertex coordinates and the face index list are skipped as the header describes them.
+- the 3DS reader (Graphics/MeshCodec3ds.hpp:160-395) over lib3ds 1.3.0, a third-party library that is not part of
+  the reference: lib3ds keeps the file's triangle meshes in a list sorted by object name (a new mesh goes after every
+  mesh whose name is not greater, as strcmp orders them), each mesh being the N_TRI_OBJECT chunk (0x4100) of a named
+  object (0x4000) of the editor chunk (0x3D3D), with its points in POINT_ARRAY (0x4110) and faces in FACE_ARRAY
+  (0x4120); the codec, with its default options, skips meshes without points, applies no transforms, and skips (but
+  numbers) faces with an out-of-range or repeated index, numbering vertices and faces over the whole file.
 
 Small inputs only (pure-Python loops). Parity status: unpinned (the reference's readers cannot be built here).
 """
@@ -481,6 +487,92 @@ def read_ply(data):
     return m.arrays()
 
 
+def _chunks_3ds(b, start, end):
+    """(id, payload start, chunk end) of the little-endian chunks in b[start:end]."""
+    pos = start
+    while pos < end:
+        if end - pos < 6:
+            raise ValueError("truncated 3DS chunk header")
+        cid, length = struct.unpack_from("<HI", b, pos)
+        if length < 6 or length > end - pos:
+            raise ValueError("3DS chunk runs past its parent")
+        yield cid, pos + 6, pos + length
+        pos += length
+
+
+def read_3ds(data):
+    b = bytes(data)
+    meshes = []   # (name, points, faces)
+
+    def tri_object(name, p, e):
+        pts, faces = [], []
+        for cid, q, ce in _chunks_3ds(b, p, e):
+            if cid == 0x4110:
+                (n,) = struct.unpack_from("<H", b, q)
+                if ce - q - 2 < 12 * n:
+                    raise ValueError("truncated 3DS array")
+                v = struct.unpack_from("<%df" % (3 * n), b, q + 2)
+                pts = [tuple(np.float32(x) for x in v[3 * i:3 * i + 3]) for i in range(n)]
+            elif cid == 0x4120:
+                (n,) = struct.unpack_from("<H", b, q)
+                if ce - q - 2 < 8 * n:
+                    raise ValueError("truncated 3DS array")
+                w = struct.unpack_from("<%dH" % (4 * n), b, q + 2)
+                faces = [w[4 * i:4 * i + 3] for i in range(n)]
+        meshes.append((name, pts, faces))
+
+    def named_object(p, e):
+        z = b.index(b"\0", p, e)
+        if z - p > 63:
+            raise ValueError("3DS object name longer than 63 bytes")
+        name = b[p:z]
+        for cid, q, ce in _chunks_3ds(b, z + 1, e):
+            if cid == 0x4100:
+                tri_object(name, q, ce)
+
+    def editor(p, e):
+        for cid, q, ce in _chunks_3ds(b, p, e):
+            if cid == 0x4000:
+                named_object(q, ce)
+
+    if len(b) < 6:
+        raise ValueError("truncated 3DS chunk header")
+    top, e = struct.unpack_from("<HI", b, 0)
+    if e < 6 or e > len(b):
+        raise ValueError("3DS chunk runs past its parent")
+    p = 6
+    if top in (0x4D4D, 0x3DAA, 0xC23D):
+        for cid, q, ce in _chunks_3ds(b, p, e):
+            if cid == 0x3D3D:
+                editor(q, ce)
+    elif top == 0x3D3D:
+        editor(p, e)
+    else:
+        raise ValueError("not a 3DS file")
+    ordered = []
+    for mesh in meshes:   # lib3ds's sorted insertion
+        k = len(ordered)
+        for i, other in enumerate(ordered):
+            if mesh[0] < other[0]:
+                k = i
+                break
+        ordered.insert(k, mesh)
+    m = _Mesh()
+    nv_total = nf_total = 0
+    for name, pts, faces in ordered:
+        nv = len(pts)
+        if nv <= 0:
+            continue
+        kept = []
+        for i, f in enumerate(faces):
+            if max(f) < nv and len(set(f)) == 3:
+                kept.append((list(f), nf_total + i))
+        nf_total += len(faces)
+        _add_submesh(m, pts, list(range(nv_total, nv_total + nv)), kept, keep_empty=True)
+        nv_total += nv
+    return m.arrays()
+
+
 def read_mesh(path):
     with open(path, "rb") as f:
         data = f.read()
@@ -489,4 +581,6 @@ def read_mesh(path):
         return read_obj(data)
     if p.endswith(".ply"):
         return read_ply(data)
+    if p.endswith(".3ds"):
+        return read_3ds(data)
     return read_off(data)

@@ -449,3 +449,95 @@ def test_read_from_memory(T, tmp_path):
         T.read_mesh(b"x", codec="stl")
     with pytest.raises(ValueError):
         T.read_mesh(b"x")
+
+
+# ---- 3DS -------------------------------------------------------------------------------------------------------------
+
+def _chunk(cid, payload):
+    return struct.pack("<HI", cid, 6 + len(payload)) + payload
+
+
+def _tri_object(points, faces, extra=b"", texels=None):
+    body = _chunk(0x4110, struct.pack("<H", len(points)) + b"".join(struct.pack("<3f", *p) for p in points))
+    if texels is not None:
+        body += _chunk(0x4140, struct.pack("<H", len(texels)) + b"".join(struct.pack("<2f", *t) for t in texels))
+    smoothing = _chunk(0x4150, b"\0" * 4 * len(faces))
+    body += _chunk(0x4120, struct.pack("<H", len(faces)) + b"".join(struct.pack("<4H", *f, 7) for f in faces) + smoothing)
+    body += _chunk(0x4160, struct.pack("<12f", *range(12)))   # mesh matrix: not applied
+    return _chunk(0x4100, body + extra)
+
+
+def _named(name, *subchunks):
+    return _chunk(0x4000, name + b"\0" + b"".join(subchunks))
+
+
+def _file_3ds(*objects, top=0x4D4D, keyframer=True):
+    editor = _chunk(0x3D3E, struct.pack("<I", 3)) + _chunk(0xAFFF, _chunk(0xA000, b"mat\0")) + b"".join(objects)
+    body = _chunk(0x0002, struct.pack("<I", 3)) + _chunk(0x3D3D, editor)
+    if keyframer:
+        body += _chunk(0xB000, _chunk(0xB00A, b"\0" * 10))
+    return _chunk(top, body)
+
+
+def test_3ds_meshes_sorted_by_name_and_numbered_over_the_file(T, tmp_path):
+    sq = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0)]
+    data = _file_3ds(
+        _named(b"zeta", _tri_object(sq, [(0, 1, 2), (0, 2, 3)])),
+        _named(b"Light01", _chunk(0x4600, struct.pack("<3f", 1, 2, 3))),           # a light: no mesh
+        _named(b"alpha", _tri_object(sq[:3], [(0, 1, 5), (0, 0, 1), (2, 1, 0)], texels=[(0, 0)] * 3)),
+        _named(b"empty", _tri_object([], [])),                                     # no points: skipped
+        _named(b"points", _tri_object([(5, 5, 5)], [])),                           # points only: kept
+        _named(b"alpha", _tri_object([(0, 0, 2), (1, 0, 2), (0, 1, 2)], [(0, 1, 2)])))
+    path = tmp_path / "m.3ds"
+    path.write_bytes(data)
+    m = T.read_mesh(str(path))
+    _same_mesh(m, MO.read_mesh(str(path)))
+    # lib3ds order: alpha (first in the file), alpha (second), points, zeta
+    assert m.submesh_vertex_offsets.tolist() == [0, 3, 6, 7, 11]
+    assert m.submesh_triangle_offsets.tolist() == [0, 1, 2, 2, 4]
+    # alpha's faces 0 (index 5) and 1 (repeated index) are skipped but numbered; zeta's faces are numbers 4 and 5
+    assert m.triangle_face.tolist() == [2, 3, 4, 5]
+    assert m.triangles.tolist() == [[2, 1, 0], [3, 4, 5], [7, 8, 9], [7, 9, 10]]
+    assert m.vertex_source.tolist() == list(range(11)) and m.num_faces == 4
+    np.testing.assert_array_equal(m.vertices[6], [5, 5, 5])
+    # the same bytes through the buffer entry point, and a file that is only the editor chunk
+    _same_mesh(T.read_mesh(data, codec="3ds"), MO.read_mesh(str(path)))
+    bare = data[6 + 10:]                       # skip the file header and the version chunk
+    bare = bare[:struct.unpack_from("<I", bare, 2)[0]]
+    _same_mesh(T.read_mesh(bare, codec="3DS"), MO.read_mesh(str(path)))
+
+
+def test_random_3ds_matches_the_restatement(T, tmp_path):
+    rng = np.random.default_rng(5)
+    for trial in range(6):
+        objects = []
+        for o in range(int(rng.integers(1, 7))):
+            nv = int(rng.integers(0, 40))
+            pts = [tuple(float(x) for x in rng.normal(size=3).astype(np.float32)) for _ in range(nv)]
+            faces = [tuple(int(x) for x in rng.integers(0, nv + 3, size=3)) for _ in range(int(rng.integers(0, 60)))]
+            name = bytes(rng.choice(list(b"abAB_\xe9"), size=int(rng.integers(0, 4))).tolist())
+            objects.append(_named(name, _tri_object(pts, faces)))
+        path = tmp_path / ("r%d.3ds" % trial)
+        path.write_bytes(_file_3ds(*objects, top=[0x4D4D, 0xC23D][trial % 2], keyframer=trial % 3 != 0))
+        _same_mesh(T.read_mesh(str(path)), MO.read_mesh(str(path)))
+
+
+def test_3ds_errors(T, tmp_path):
+    good = _file_3ds(_named(b"a", _tri_object([(0, 0, 0), (1, 0, 0), (0, 1, 0)], [(0, 1, 2)])))
+    cases = {
+        "unknown top chunk": _chunk(0x1234, b""),
+        "truncated": good[:-5],
+        "chunk past parent": good[:2] + struct.pack("<I", len(good) + 10) + good[6:],
+        "long name": _file_3ds(_named(b"n" * 64, _tri_object([(0, 0, 0)], []))),
+        "short point array": _file_3ds(_named(b"a", _chunk(0x4100, _chunk(0x4110, struct.pack("<H", 3) + b"\0" * 24)))),
+    }
+    for why, data in cases.items():
+        path = tmp_path / "bad.3ds"
+        path.write_bytes(data)
+        with pytest.raises(Exception):
+            T.read_mesh(str(path))
+        with pytest.raises(ValueError):
+            MO.read_mesh(str(path))
+    path = tmp_path / "ok63.3ds"
+    path.write_bytes(_file_3ds(_named(b"n" * 63, _tri_object([(0, 0, 0), (1, 0, 0), (0, 1, 0)], [(0, 1, 2)]))))
+    assert T.read_mesh(str(path)).triangles.tolist() == [[0, 1, 2]]

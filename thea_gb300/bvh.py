@@ -604,13 +604,13 @@ class MeshData:
 
 
 def read_mesh(path, codec=None):
-    """Reads an OFF, OBJ or PLY file into host arrays (MeshData). ``path`` may also be the file's bytes, with
-    ``codec`` ("obj", "off" or "ply") naming the format."""
+    """Reads a 3DS, OFF, OBJ or PLY file into host arrays (MeshData). ``path`` may also be the file's bytes, with
+    ``codec`` ("3ds", "obj", "off" or "ply") naming the format."""
     lib = N.lib()
     h = ctypes.c_void_p()
     if isinstance(path, (bytes, bytearray, memoryview)):
         if codec is None:
-            raise ValueError("read_mesh: a byte buffer needs codec='obj', 'off' or 'ply'")
+            raise ValueError("read_mesh: a byte buffer needs codec='3ds', 'obj', 'off' or 'ply'")
         buf = bytes(path)
         N.check(lib.thea_mesh_read_buffer(buf, len(buf), str(codec).encode(), ctypes.byref(h)))
     else:

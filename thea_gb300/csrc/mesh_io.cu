@@ -6,6 +6,7 @@
 // of DisplayMesh::addFace (Graphics/DisplayMesh.cpp:249-320): quads by Polygon3::triangulateQuad (Polygon3.hpp:245-285),
 // larger polygons by Polygon3::triangulate (Polygon3.cpp:109-288: ear clipping after projecting onto the plane of
 // Polygon3::computeNormal, Polygon3.hpp:180-208, in the basis of Math::orthonormalBasis, MatrixUtil.hpp:225-249).
+// The 3DS reader (Graphics/MeshCodec3ds.hpp) restates the part of lib3ds 1.x it relies on (below).
 // FP32 arithmetic in the reference's operation order; this file is compiled without floating-point contraction.
 #include "mesh_io.hpp"
 
@@ -773,6 +774,154 @@ MeshData read_ply(Input & in) {
 
 }  // namespace
 
+// ---- 3DS (Graphics/MeshCodec3ds.hpp:160-395 over lib3ds 1.3.0) ---------------------------------------------------------
+// The reference hands the file to lib3ds 1.x (the codec reads lib3ds 1.x's mesh fields points / pointL / faceL) and
+// converts its mesh list with the default options: no node transforms, one display mesh per lib3ds mesh, meshes without
+// vertices skipped, faces with an index out of range or a repeated index skipped but counted, vertex and face indices
+// running over the whole file. lib3ds keeps its mesh list sorted by name (insertion after every mesh whose name is not
+// greater), and the node tree the codec then walks attaches no further meshes. Restated here from the published chunk
+// layout: a chunk is a little-endian u16 id and u32 length (header included); the meshes are the N_TRI_OBJECT chunks
+// (0x4100) of the named objects (0x4000: a zero-terminated name of at most 63 bytes, then sub-chunks) of the editor
+// chunk (0x3D3D) under the file chunk (0x4D4D, or a material or project file's 0x3DAA / 0xC23D), with points in
+// POINT_ARRAY (0x4110: u16 count, three f32 each) and faces in FACE_ARRAY (0x4120: u16 count, three u16 indices and a
+// u16 flag word each). A later point or face array of the same mesh replaces the earlier one, as lib3ds does. Every
+// other chunk is skipped whole. A chunk that runs past its parent or a truncated array is an error.
+
+struct Mesh3ds {
+  std::string name;
+  std::vector<float> points;     // xyz
+  std::vector<uint16_t> faces;   // three vertex indices per face
+};
+
+struct Chunk3ds {
+  uint16_t id;
+  size_t end;  // one past the chunk's last byte
+};
+
+Chunk3ds chunk_3ds(Input & in, size_t limit) {
+  if (limit < in.pos || limit - in.pos < 6) fail(in.path, "truncated 3DS chunk header");
+  size_t start = in.pos;
+  uint16_t id = (uint16_t)in.word(2, false);
+  uint32_t len = (uint32_t)in.word(4, false);
+  if (len < 6 || (size_t)len > limit - start) fail(in.path, "3DS chunk runs past its parent");
+  return {id, start + (size_t)len};
+}
+
+void need_3ds(Input & in, size_t end, size_t bytes) {
+  if (end < in.pos || end - in.pos < bytes) fail(in.path, "truncated 3DS array");
+}
+
+float f32_le(Input & in) {
+  uint32_t w = (uint32_t)in.word(4, false);
+  float f;
+  std::memcpy(&f, &w, 4);
+  return f;
+}
+
+void read_tri_object_3ds(Input & in, size_t end, Mesh3ds & mesh) {
+  while (in.pos < end) {
+    Chunk3ds c = chunk_3ds(in, end);
+    if (c.id == 0x4110) {  // POINT_ARRAY
+      need_3ds(in, c.end, 2);
+      size_t n = (size_t)in.word(2, false);
+      need_3ds(in, c.end, 12 * n);
+      mesh.points.resize(3 * n);
+      for (size_t i = 0; i < 3 * n; ++i) mesh.points[i] = f32_le(in);
+    } else if (c.id == 0x4120) {  // FACE_ARRAY (its material and smoothing sub-chunks are skipped)
+      need_3ds(in, c.end, 2);
+      size_t n = (size_t)in.word(2, false);
+      need_3ds(in, c.end, 8 * n);
+      mesh.faces.resize(3 * n);
+      for (size_t f = 0; f < n; ++f) {
+        for (int k = 0; k < 3; ++k) mesh.faces[3 * f + (size_t)k] = (uint16_t)in.word(2, false);
+        in.word(2, false);  // edge visibility flags
+      }
+    }
+    in.pos = c.end;
+  }
+}
+
+void read_named_object_3ds(Input & in, size_t end, std::vector<Mesh3ds> & meshes) {
+  std::string name;
+  for (;;) {
+    if (in.pos >= end) fail(in.path, "unterminated 3DS object name");
+    char ch = in.data[in.pos++];
+    if (ch == '\0') break;
+    if (name.size() == 63) fail(in.path, "3DS object name longer than 63 bytes");
+    name.push_back(ch);
+  }
+  while (in.pos < end) {
+    Chunk3ds c = chunk_3ds(in, end);
+    if (c.id == 0x4100) {  // N_TRI_OBJECT
+      Mesh3ds mesh;
+      mesh.name = name;
+      read_tri_object_3ds(in, c.end, mesh);
+      meshes.push_back(std::move(mesh));
+    }
+    in.pos = c.end;
+  }
+}
+
+// lib3ds's name order: byte-wise, as strcmp compares (unsigned)
+bool name_less_3ds(std::string const & a, std::string const & b) {
+  size_t n = std::min(a.size(), b.size());
+  for (size_t i = 0; i < n; ++i) {
+    unsigned char x = (unsigned char)a[i], y = (unsigned char)b[i];
+    if (x != y) return x < y;
+  }
+  return a.size() < b.size();
+}
+
+MeshData read_3ds(Input & in) {
+  size_t size = in.data.size();
+  Chunk3ds top = chunk_3ds(in, size);
+  std::vector<Mesh3ds> meshes;
+  auto editor = [&](size_t end) {
+    while (in.pos < end) {
+      Chunk3ds c = chunk_3ds(in, end);
+      if (c.id == 0x4000) read_named_object_3ds(in, c.end, meshes);
+      in.pos = c.end;
+    }
+  };
+  if (top.id == 0x4D4D || top.id == 0x3DAA || top.id == 0xC23D) {
+    while (in.pos < top.end) {
+      Chunk3ds c = chunk_3ds(in, top.end);
+      if (c.id == 0x3D3D) editor(c.end);
+      in.pos = c.end;
+    }
+  } else if (top.id == 0x3D3D) {
+    editor(top.end);
+  } else {
+    fail(in.path, "not a 3DS file (unknown top-level chunk)");
+  }
+  std::stable_sort(meshes.begin(), meshes.end(),
+                   [](Mesh3ds const & a, Mesh3ds const & b) { return name_less_3ds(a.name, b.name); });
+
+  MeshData m;
+  int64_t vertex_count = 0, face_count = 0;
+  std::vector<int32_t> face(3);
+  for (Mesh3ds const & mesh : meshes) {
+    int64_t nv = (int64_t)(mesh.points.size() / 3);
+    if (nv <= 0) continue;  // skip_empty_meshes
+    SubmeshBuilder b(m);
+    for (int64_t v = 0; v < nv; ++v)
+      b.add_vertex(mesh.points[(size_t)(3 * v)], mesh.points[(size_t)(3 * v + 1)], mesh.points[(size_t)(3 * v + 2)],
+                   (int32_t)vertex_count++);
+    for (size_t f = 0; f < mesh.faces.size() / 3; ++f, ++face_count) {
+      int64_t a = mesh.faces[3 * f], c1 = mesh.faces[3 * f + 1], c2 = mesh.faces[3 * f + 2];
+      if (a >= nv || c1 >= nv || c2 >= nv) continue;      // out of range: skipped, still counted
+      if (a == c1 || c1 == c2 || c2 == a) continue;       // repeated vertex: skipped, still counted
+      face[0] = (int32_t)a;
+      face[1] = (int32_t)c1;
+      face[2] = (int32_t)c2;
+      b.add_face(face, (int32_t)face_count);
+    }
+    m.submesh_vertex_offsets.push_back((int64_t)m.vertex_source.size());  // kept even without faces
+    m.submesh_triangle_offsets.push_back((int64_t)m.triangle_face.size());
+  }
+  return m;
+}
+
 int triangulate_face(float const * pos, int n, std::vector<int32_t> & tris) {
   if (n < 3) return 0;
   auto P = [&](int i) { return V3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}; };
@@ -799,9 +948,9 @@ MeshData read_mesh_file(std::string const & path) {
     return lower.size() >= n && lower.compare(lower.size() - n, n, ext) == 0;
   };
   // codecs in the reference's order of detection: 3DS, OBJ, OFF (.off, .off.bin), PLY
-  if (ends_with(".3ds")) fail(path, "the 3DS codec (which needs lib3ds) is not built");
+  bool tds = ends_with(".3ds");
   bool obj = ends_with(".obj"), off = ends_with(".off") || ends_with(".off.bin"), ply = ends_with(".ply");
-  if (!obj && !off && !ply) fail(path, "could not detect the codec from the file extension");
+  if (!tds && !obj && !off && !ply) fail(path, "could not detect the codec from the file extension");
   std::ifstream f(path, std::ios::binary);
   if (!f) fail(path, "cannot open the file");
   Input in;
@@ -812,17 +961,18 @@ MeshData read_mesh_file(std::string const & path) {
   if (size < 0) fail(path, "cannot read the file");
   in.data.resize((size_t)size);
   if (size > 0 && !f.read(&in.data[0], size)) fail(path, "cannot read the file");
-  return obj ? read_obj(in) : off ? read_off(in) : read_ply(in);
+  return tds ? read_3ds(in) : obj ? read_obj(in) : off ? read_off(in) : read_ply(in);
 }
 
 MeshData read_mesh_buffer(void const * data, int64_t bytes, std::string const & codec) {
   std::string c = codec;
   for (char & ch : c) ch = (char)std::tolower((unsigned char)ch);
-  if (c != "obj" && c != "off" && c != "ply") fail("<buffer>", "unknown codec '" + codec + "' (obj, off or ply)");
+  if (c != "3ds" && c != "obj" && c != "off" && c != "ply")
+    fail("<buffer>", "unknown codec '" + codec + "' (3ds, obj, off or ply)");
   Input in;
   in.path = "<buffer>";
   if (bytes > 0) in.data.assign(static_cast<char const *>(data), (size_t)bytes);
-  return c == "obj" ? read_obj(in) : c == "off" ? read_off(in) : read_ply(in);
+  return c == "3ds" ? read_3ds(in) : c == "obj" ? read_obj(in) : c == "off" ? read_off(in) : read_ply(in);
 }
 
 }  // namespace thea
