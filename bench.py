@@ -823,6 +823,7 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     gc.collect()
     gc.disable()
     late = np.zeros(n_req)
+    submit_call = np.zeros(n_req)
     with ClockSampler(torch.cuda.current_device()) as clk:
         start = time.perf_counter()
         for r in range(n_req):
@@ -835,7 +836,9 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
             oi, ov = outputs(n * k)
             q = pts[m][:n]
             d = dirs[:n] if kd == "ray" else None
+            t_call = time.perf_counter()
             tickets[r] = srv.submit(kd, ids[m], q, directions=d, k=k, out=(oi, ov))
+            submit_call[r] = time.perf_counter() - t_call
         submit_s = time.perf_counter() - start
         lat = np.zeros(n_req)
         for r, t in enumerate(tickets):
@@ -847,6 +850,7 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
     st = srv.stats()
     srv.close()
     small = nq <= 65536
+    slow = small & (lat > 20.0)
     # algorithmic bytes of the queries (12 B per point or 24 B per ray in; 20 B closest, 8 B ray, 8 x 8 B k-NN out)
     qbytes = np.where(kind == 0, 32, np.where(kind == 1, 32, 12 + 8 * 8)) * nq
     per_kind = {}
@@ -867,6 +871,15 @@ def serving_config4(T, torch, args, num_meshes=256, rate=2000.0, seconds=3.0, se
                                "max": float(1e3 * late.max()),
                                "meaning": "submit time minus scheduled arrival (the Python client); latency itself is "
                                           "measured by the server from submit to results written"},
+        "submit_call_ms": {"p99": float(1e3 * np.percentile(submit_call, 99)), "max": float(1e3 * submit_call.max()),
+                           "meaning": "duration of the submit call itself (the C-ABI call, its pointer-kind queries "
+                                      "and the queue lock)"},
+        "slow_small_requests": {"over_ms": 20.0, "count": int(slow.sum()),
+                                "arrival_window_s": [float(arrive[slow].min()), float(arrive[slow].max())]
+                                if slow.any() else None,
+                                "meaning": "when the requests of <= 65,536 queries slower than 20 ms arrived, in seconds "
+                                           "from the stream's start: one window in which the client was late too is a "
+                                           "pause of the whole process or driver, not queueing"},
         "requests": n_req, "offered_rate_per_s": n_req / arrive[-1], "submit_span_s": submit_s, "drain_s": total_s,
         "queries": int(nq.sum()), "mix": {"closest": int((kind == 0).sum()), "ray": int((kind == 1).sum()),
                                            "knn": int((kind == 2).sum())},
