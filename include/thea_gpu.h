@@ -469,6 +469,14 @@ THEA_API thea_status thea_selftest_bounded_wait(int32_t spin_limit, void * strea
  * can follow a device error to the status of the next query call. No counterpart in the reference. */
 THEA_API thea_status thea_selftest_set_error_bits(thea_bvh * bvh, uint32_t bits, void * stream);
 
+/* The FP32 running sum fl(... fl(fl(start + t[0]) + t[1]) ...) over num_terms terms (host or device memory), computed
+ * as the library computes updateAverageSeparation's sum (PointSet3.hpp:688-702) for thea_sample_graph: on the device,
+ * runs of terms added as exact integer multiples of the sum's ulp, bit for bit the sequential loop. Writes the sum to
+ * the host float out_sum. No counterpart in the reference (it exposes the summation for tests). Synchronizes the
+ * stream. */
+THEA_API thea_status thea_selftest_running_sum(const float * terms, int64_t num_terms, float start, float * out_sum,
+                                               void * stream);
+
 /* ---- sampling ------------------------------------------------------------------------------------------------------ */
 
 /* Streams of the reference's Random(seed) (THEA_RNG_THEA_MT sampling, thea_random_sphere, thea_visibility) of 1,024

@@ -184,6 +184,7 @@ thea_bvh_serialize thea_bvh_deserialize thea_bvh_set_transform thea_bvh_clear_tr
 thea_closest_element thea_closest_element_ex thea_ray_intersection thea_ray_intersection_ex thea_ray_intersects
 thea_random_sphere thea_visibility thea_sample_graph thea_sample_graph_oversampled thea_k_closest thea_radius_neighbors
 thea_k_closest_self thea_k_closest_self_ex thea_point_gram_tile thea_selftest_bounded_wait thea_selftest_set_error_bits
+thea_selftest_running_sum
 thea_sample_by_area thea_sample_by_area_noalloc
 thea_mesh_forest_build thea_point_forest_build thea_batch_closest_element thea_batch_ray_intersection
 thea_batch_k_closest thea_autotune_batch_closest

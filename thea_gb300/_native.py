@@ -156,6 +156,7 @@ SIGNATURES = {
     "thea_radius_neighbors": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp]),
     "thea_selftest_bounded_wait": (ctypes.c_int, [_i32, _vp]),
     "thea_selftest_set_error_bits": (ctypes.c_int, [_vp, ctypes.c_uint32, _vp]),
+    "thea_selftest_running_sum": (ctypes.c_int, [_vp, _i64, ctypes.c_float, _vp, _vp]),
     "thea_point_gram_tile": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _vp]),
     "thea_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "thea_server_destroy": (ctypes.c_int, [_vp]),

@@ -793,24 +793,19 @@ static thea_status sample_graph_call(const float * positions, const float * norm
     if (hn) THEA_CUDA_CHECK(cudaMemcpyAsync(out_neighbors, o.neighbors, n * m * 4, cudaMemcpyDeviceToHost, s));
     if (hs) THEA_CUDA_CHECK(cudaMemcpyAsync(out_separations, o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
     if (hd) THEA_CUDA_CHECK(cudaMemcpyAsync(out_degree, o.degree, n * 4, cudaMemcpyDeviceToHost, s));
+    float avg = 0.f;
+    Scratch bavg;
     if (out_avg_separation) {
       // updateAverageSeparation (PointSet3.hpp:688-702): FP32 sum over samples and their sorted neighbours, in order
-      std::vector<float> sep(n * m);
-      std::vector<int32_t> deg(n);
-      THEA_CUDA_CHECK(cudaMemcpyAsync(sep.data(), o.separations, n * m * 4, cudaMemcpyDeviceToHost, s));
-      THEA_CUDA_CHECK(cudaMemcpyAsync(deg.data(), o.degree, n * 4, cudaMemcpyDeviceToHost, s));
-      sync_stream(s);
-      float avg = 0.f;
-      int64_t edges = 0;
-      for (size_t i = 0; i < n; ++i) {
-        for (int32_t k = 0; k < deg[i]; ++k) avg += sep[i * m + (size_t)k];
-        edges += deg[i];
-      }
-      if (edges > 0) avg /= (float)edges;
+      bavg = Scratch(sizeof(float), s);
+      run_mean_separation(o.separations, o.degree, num_samples, max_degree, bavg.as<float>(), s);
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&avg, bavg.ptr, sizeof(float), cudaMemcpyDeviceToHost, s));
+    }
+    sync_stream(s);
+    if (out_avg_separation) {
       out_avg_separation[0] = o.avg_separation_estimate;
       out_avg_separation[1] = avg;
     }
-    sync_stream(s);
   });
 }
 
@@ -928,6 +923,22 @@ THEA_API thea_status thea_selftest_set_error_bits(thea_bvh * bvh, uint32_t bits,
     cur |= bits;
     THEA_CUDA_CHECK(cudaMemcpyAsync(bvh->err, &cur, sizeof(unsigned), cudaMemcpyHostToDevice, s));
     THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+  });
+}
+
+THEA_API thea_status thea_selftest_running_sum(const float * terms, int64_t num_terms, float start, float * out_sum,
+                                               void * stream) {
+  return guarded([&] {
+    THEA_REQUIRE(out_sum && (terms || num_terms == 0) && num_terms >= 0, "selftest_running_sum: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    Scratch x((size_t)std::max<int64_t>(num_terms, 1) * sizeof(float), s), r(sizeof(float), s);
+    if (num_terms > 0)
+      THEA_CUDA_CHECK(cudaMemcpyAsync(x.ptr, terms, (size_t)num_terms * sizeof(float), cudaMemcpyDefault, s));
+    run_running_sum(x.as<float>(), nullptr, num_terms, start, r.as<float>(), s);
+    float h = 0.f;
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&h, r.ptr, sizeof(float), cudaMemcpyDeviceToHost, s));
+    sync_stream(s);
+    *out_sum = h;
   });
 }
 

@@ -16,6 +16,7 @@
 #include "any_hit.cuh"
 #include "device_util.cuh"
 #include "query.hpp"
+#include "running_sum.cuh"
 #include "traverse_ops.cuh"
 
 #include <cmath>
@@ -390,6 +391,122 @@ void run_sample_graph_oversampled(float const * positions, float const * normals
     throw Error(THEA_ERR_NOT_SUPPORTED, "sample_graph: a sample's geodesic search outgrew its " +
                                             std::to_string(EXTRACT_FILL) + "-vertex working set (oversampling too "
                                             "dense for max_degree; use fewer dense samples)");
+}
+
+}  // namespace thea
+
+namespace thea {
+namespace {
+
+constexpr int RSUM_THREADS = 512;
+constexpr int RSUM_ITEMS = 16;  // consecutive terms per thread; the cursor moves in multiples of it
+
+// One block walks the terms in windows of RSUM_THREADS x RSUM_ITEMS. Each thread sums the units of its 16 terms in the
+// binade of the sum at the window's start; a block scan over the threads finds the first group that cannot be added in
+// bulk (a term to be taken alone, or a total past RUNNING_SUM_MAX_UNITS). Every group before it is added as one integer
+// sum, that group's 16 terms one fl(s + x) at a time, and the next window starts after it.
+__global__ void __launch_bounds__(RSUM_THREADS)
+running_sum_kernel(float const * __restrict__ x, int64_t const * __restrict__ count, int64_t n_host, float s0,
+                   float * __restrict__ out) {
+  __shared__ float s_sum;
+  __shared__ int64_t s_cursor;
+  __shared__ int s_first;
+  int64_t n = count ? *count : n_host;
+  int t = threadIdx.x;
+  if (t == 0) {
+    s_sum = s0;
+    s_cursor = 0;
+  }
+  __syncthreads();
+  while (true) {
+    int64_t cur = s_cursor;
+    float s = s_sum;
+    if (cur >= n) break;
+    int e = 0;
+    bool bulk = running_sum_binade(s, e);
+    long long units = 0;
+    bool ok = bulk;
+    int64_t g0 = cur + (int64_t)t * RSUM_ITEMS;
+    if (bulk && g0 < n) {
+      if (g0 + RSUM_ITEMS <= n) {
+        float4 const * v = reinterpret_cast<float4 const *>(x + g0);
+#pragma unroll
+        for (int i = 0; i < RSUM_ITEMS / 4; ++i) {
+          float4 q = v[i];
+          long long d0 = 0, d1 = 0, d2 = 0, d3 = 0;
+          ok = ok && running_sum_step_units(e, q.x, d0) && running_sum_step_units(e, q.y, d1) &&
+               running_sum_step_units(e, q.z, d2) && running_sum_step_units(e, q.w, d3);
+          units += d0 + d1 + d2 + d3;
+        }
+      } else {
+        for (int64_t j = g0; j < n; ++j) {
+          long long d = 0;
+          ok = ok && running_sum_step_units(e, x[j], d);
+          units += d;
+        }
+      }
+    }
+    long long total = 0;
+    long long before = block_exclusive_scan<long long>(units, total);
+    long long base = bulk ? running_sum_units_of(s, e) : 0;
+    bool fits = ok && base + before + units <= RUNNING_SUM_MAX_UNITS;
+    if (t == 0) s_first = RSUM_THREADS;
+    __syncthreads();
+    if (!fits && g0 < n) atomicMin(&s_first, t);
+    __syncthreads();
+    int g = s_first;
+    if (t == (g < RSUM_THREADS ? g : RSUM_THREADS - 1)) {
+      if (g < RSUM_THREADS) {
+        if (bulk && before > 0) s = running_sum_from_units(base + before, e);
+        int64_t end = g0 + RSUM_ITEMS < n ? g0 + RSUM_ITEMS : n;
+        for (int64_t j = g0; j < end; ++j) s = __fadd_rn(s, x[j]);
+        s_cursor = end;
+      } else {
+        s = running_sum_from_units(base + before + units, e);
+        s_cursor = cur + (int64_t)RSUM_THREADS * RSUM_ITEMS;
+      }
+      s_sum = s;
+    }
+    __syncthreads();
+  }
+  if (t == 0) *out = s_sum;
+}
+
+// Offsets of each sample's separations in the compact sequence (exclusive scan of the degrees, done before) -> the
+// separations themselves, in order; the last thread writes the number of terms
+__global__ void compact_separations_kernel(float const * __restrict__ sep, int32_t const * __restrict__ deg,
+                                           int32_t const * __restrict__ off, int64_t n, int m,
+                                           float * __restrict__ out, int64_t * __restrict__ count) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int d = deg[i];
+  int64_t o = off[i];
+  for (int k = 0; k < d; ++k) out[o + k] = sep[i * m + k];
+  if (i == n - 1) *count = o + d;
+}
+
+// avg = sum / (float)edges (updateAverageSeparation's `avg_separation /= num_edges`), the sum when there are no edges
+__global__ void mean_of_sum_kernel(float * __restrict__ sum, int64_t const * __restrict__ count) {
+  int64_t c = *count;
+  if (c > 0) *sum = *sum / (float)c;
+}
+
+}  // namespace
+
+void run_running_sum(float const * x, int64_t const * count, int64_t n, float s0, float * out, cudaStream_t s) {
+  THEA_REQUIRE(((uintptr_t)x & 15) == 0, "running_sum: terms must be 16-byte aligned");
+  THEA_LAUNCH(running_sum_kernel, 1, RSUM_THREADS, 0, s, x, count, n, s0, out);
+}
+
+void run_mean_separation(float const * separations, int32_t const * degree, int64_t n, int max_degree, float * out,
+                         cudaStream_t s) {
+  THEA_REQUIRE(n >= 1 && n * (int64_t)max_degree < ((int64_t)1 << 31), "mean_separation: too many separations");
+  Scratch off((size_t)n * 4, s), vals((size_t)n * max_degree * 4, s), count(8, s);
+  exclusive_scan<int32_t>(degree, off.as<int32_t>(), n, s);
+  THEA_LAUNCH(compact_separations_kernel, (unsigned)ceil_div(n, GRAPH_THREADS), GRAPH_THREADS, 0, s, separations,
+              degree, off.as<int32_t>(), n, max_degree, vals.as<float>(), count.as<int64_t>());
+  run_running_sum(vals.as<float>(), count.as<int64_t>(), 0, 0.f, out, s);
+  THEA_LAUNCH(mean_of_sum_kernel, 1, 1, 0, s, out, count.as<int64_t>());
 }
 
 }  // namespace thea

@@ -26,4 +26,15 @@ void run_sample_graph_oversampled(float const * positions, float const * normals
                                   float const * dense_normals, int64_t n_dense, int max_degree, uint32_t seed,
                                   thea_bvh const * surface, SampleGraphOut & out, cudaStream_t s);
 
+// updateAverageSeparation (PointSet3.hpp:688-702) on the device: the FP32 sum, in sample order, of each sample's first
+// degree[i] separations (rows of max_degree), divided by their count as a float (the sum as it is when there are
+// none); one float to `out` (device memory). Asynchronous.
+void run_mean_separation(float const * separations, int32_t const * degree, int64_t n, int max_degree, float * out,
+                         cudaStream_t s);
+
+// The FP32 running sum fl(... fl(fl(s0 + x[0]) + x[1]) ...) over x[0 .. count), bit for bit the sequential loop's (one
+// block, runs of terms added as integer multiples of the sum's ulp: running_sum.cuh). count: device pointer to the
+// number of terms, or null for n. One float to `out` (device memory). Asynchronous.
+void run_running_sum(float const * x, int64_t const * count, int64_t n, float s0, float * out, cudaStream_t s);
+
 }  // namespace thea
