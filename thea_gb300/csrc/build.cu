@@ -304,11 +304,26 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 
 // For each frontier binary node, choose the W binary subtrees that become the children of its wide node: starting from
 // the two children, repeatedly open the subtree with the largest surface area among those too big to be a leaf.
+// Frontier of the level being collapsed, kept on the device so that several levels run between host synchronisations:
+// its size, the wide index of its first node, and the number of levels emitted so far.
+struct CollapseLevel {
+  int64_t fsize;
+  int64_t base;
+  int64_t levels;
+  int64_t overflow;  // set if a node would have landed past the node bound (never, by the bound's construction)
+};
+
 template <int W>
-__global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
+__global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ frontier,
+                                       CollapseLevel const * __restrict__ lv, int64_t bound,
                                        int * __restrict__ chosen, int * __restrict__ num_internal) {
   int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= fsize) return;
+  if (f >= bound) return;
+  int64_t fsize = lv->fsize;
+  if (f >= fsize) {
+    num_internal[f] = 0;  // the scan runs over the host's bound
+    return;
+  }
   int b = frontier[f];
   int codes[W];
   int ne = 2;
@@ -360,12 +375,17 @@ template <int W> __device__ __forceinline__ void clear_node(WideNode<W> & node) 
 }
 
 template <int W>
-__global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, int64_t fsize,
-                                     int const * __restrict__ chosen, int const * __restrict__ offsets,
-                                     int64_t level_base, int64_t next_base, WideNode<W> * __restrict__ nodes,
-                                     int * __restrict__ next_frontier) {
+__global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, CollapseLevel * __restrict__ lv,
+                                     int64_t bound, int const * __restrict__ chosen, int const * __restrict__ offsets,
+                                     int64_t cap, WideNode<W> * __restrict__ nodes, int * __restrict__ next_frontier) {
   int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= fsize) return;
+  int64_t fsize = lv->fsize;
+  if (f >= fsize || f >= bound) return;
+  int64_t level_base = lv->base, next_base = level_base + fsize;
+  if (level_base + f >= cap) {
+    lv->overflow = 1;
+    return;
+  }
   WideNode<W> node;
   clear_node(node);
   int k = 0;
@@ -389,12 +409,31 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
     if (cnt <= a.leaf_size) {
       node.child[e] = encode_leaf((int)(code_first(a, code) - seg_base), cnt);
     } else {
+      if (next_base + off + k >= cap) {
+        lv->overflow = 1;
+        return;
+      }
       node.child[e] = (int)(next_base + off + k);
       next_frontier[off + k] = code;
       ++k;
     }
   }
   nodes[level_base + f] = node;
+}
+
+// Moves the device state to the next level: the emitted children form the next frontier
+__global__ void collapse_advance_kernel(CollapseLevel * __restrict__ lv, int64_t bound, int const * __restrict__ offsets,
+                                        int const * __restrict__ num_internal) {
+  int64_t fsize = lv->fsize;
+  if (fsize <= 0) return;
+  if (fsize > bound) {  // the host's bound did not hold: stop, reported as an overflow
+    lv->overflow = 1;
+    lv->fsize = 0;
+    return;
+  }
+  lv->base += fsize;
+  lv->fsize = (int64_t)offsets[fsize - 1] + num_internal[fsize - 1];
+  lv->levels += 1;
 }
 
 // Segment roots: big segments (more elements than a leaf) become level-0 frontier entries; small non-empty segments get
@@ -570,6 +609,8 @@ slab_kernel(int2 const * __restrict__ ranges, int64_t slots, float4 const * __re
   }
 }
 
+constexpr int COLLAPSE_LEVELS_PER_SYNC = 6;
+
 template <int W>
 void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bounds, cudaStream_t stream) {
   int M = a.M;
@@ -610,29 +651,36 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
   Scratch offs((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   int * cur = fa.as<int>();
   int * nxt = fb.as<int>();
-  int64_t fsize = num_big, base = num_small;
   int depth = num_small > 0 ? 1 : 0;
-  int levels = 0;
-  while (fsize > 0) {
-    THEA_REQUIRE(base + fsize <= cap, "BVH collapse exceeded its node bound");
-    unsigned grid = (unsigned)ceil_div(fsize, BUILD_THREADS);
-    THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
-                nint.as<int>());
-    exclusive_scan<int>(nint.as<int>(), offs.as<int>(), fsize, stream);
-    THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, fsize, chosen.as<int>(),
-                offs.as<int>(), base, base + fsize, nodes, nxt);
-    int tail[2];
-    THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[0], offs.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    THEA_CUDA_CHECK(cudaMemcpyAsync(&tail[1], nint.as<int>() + fsize - 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  // Levels run COLLAPSE_LEVELS_PER_SYNC at a time on the device state; the host only bounds each frontier (a frontier
+  // node has at most W internal children, and no level holds more than the nbig wide internal nodes) to size the
+  // launches and the scan. Levels past the last one find an empty frontier and do nothing.
+  CollapseLevel h{num_big, num_small, 0, 0};
+  Scratch lv(sizeof(CollapseLevel), stream);
+  THEA_CUDA_CHECK(cudaMemcpyAsync(lv.ptr, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
+  int64_t limit = std::max<int64_t>((int64_t)nbig, 1);
+  int64_t bound = num_big;
+  while (h.fsize > 0) {
+    for (int l = 0; l < COLLAPSE_LEVELS_PER_SYNC && bound > 0; ++l) {
+      unsigned grid = (unsigned)ceil_div(bound, BUILD_THREADS);
+      THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, lv.as<CollapseLevel>(), bound,
+                  chosen.as<int>(), nint.as<int>());
+      exclusive_scan<int>(nint.as<int>(), offs.as<int>(), bound, stream);
+      THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, lv.as<CollapseLevel>(), bound,
+                  chosen.as<int>(), offs.as<int>(), cap, nodes, nxt);
+      THEA_LAUNCH(collapse_advance_kernel, 1, 1, 0, stream, lv.as<CollapseLevel>(), bound, offs.as<int>(),
+                  nint.as<int>());
+      std::swap(cur, nxt);
+      bound = std::min<int64_t>(bound * W, limit);
+    }
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&h, lv.ptr, sizeof(h), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
-    base += fsize;
-    fsize = (int64_t)tail[0] + tail[1];
-    std::swap(cur, nxt);
-    ++levels;
+    THEA_REQUIRE(!h.overflow, "BVH collapse exceeded its node bound");
+    bound = h.fsize;
   }
   b->nodes = nodes;
-  b->num_nodes = base;
-  b->depth = std::max(depth, levels);
+  b->num_nodes = h.base;
+  b->depth = std::max<int>(depth, (int)h.levels);
 }
 
 }  // namespace
