@@ -254,6 +254,27 @@ extract_kernel(int32_t const * __restrict__ nbr, float const * __restrict__ sep,
   }
 }
 
+// Round 0's active list: every sample
+__global__ void iota_kernel(int32_t * __restrict__ out, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int32_t)i;
+}
+
+__global__ void flags_to_int_kernel(uint8_t const * __restrict__ f, int64_t n, int32_t * __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = f[i] ? 1 : 0;
+}
+
+// The samples to retry, in their order, and their count
+__global__ void compact_active_kernel(int32_t const * __restrict__ act, uint8_t const * __restrict__ again,
+                                      int32_t const * __restrict__ pos, int64_t n, int32_t * __restrict__ next,
+                                      int64_t * __restrict__ count) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (again[i]) next[pos[i]] = act[i];
+  if (i == n - 1) *count = (int64_t)pos[i] + (again[i] ? 1 : 0);
+}
+
 }  // namespace
 
 void run_sample_graph(float const * positions, float const * normals, int64_t n, int max_degree, uint32_t seed,
@@ -301,47 +322,54 @@ void run_sample_graph(float const * positions, float const * normals, int64_t n,
     int d4 = (int)(0.25 * max_degree);
     int min_degree = d4 < 4 ? 4 : (d4 > max_degree ? max_degree : d4);  // Math::clamp(x, 4, max_degree)
     bool reach = surface && normals;
-    // round 0: every sample
-    std::vector<int32_t> act((size_t)n);
-    for (int64_t i = 0; i < n; ++i) act[(size_t)i] = (int32_t)i;
-    for (int round = 0; round < 3 && !act.empty(); ++round, radius *= 2.0f) {
-      int64_t na = (int64_t)act.size();
+    // round 0: every sample; later rounds: the samples that found fewer than min_degree neighbours, compacted on the
+    // device in order (only their count comes back to the host)
+    Scratch act_a((size_t)n * 4, s), act_b((size_t)n * 4, s), pos((size_t)n * 4, s), cnt(8, s);
+    int32_t * act = act_a.as<int32_t>();
+    int32_t * nxt = act_b.as<int32_t>();
+    THEA_LAUNCH(iota_kernel, (unsigned)ceil_div(n, GRAPH_THREADS), GRAPH_THREADS, 0, s, act, n);
+    int64_t na = n;
+    for (int round = 0; round < 3 && na > 0; ++round, radius *= 2.0f) {
       bool last = round == 2;
-      Scratch ids((size_t)na * 4, s), q((size_t)na * 12, s), off((size_t)(na + 1) * 8, s), again((size_t)na, s);
-      THEA_CUDA_CHECK(cudaMemcpyAsync(ids.ptr, act.data(), (size_t)na * 4, cudaMemcpyHostToDevice, s));
+      Scratch q((size_t)na * 12, s), off((size_t)(na + 1) * 8, s), again((size_t)na, s);
+      int32_t const * ids = act;
       THEA_LAUNCH(gather_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions,
-                  ids.as<int32_t>(), na, q.as<float>());
+                  ids, na, q.as<float>());
       // candidates: Ball3(position, radius), the sample itself excluded (the identity test)
-      run_range(pts, q.as<float>(), na, radius, ids.as<int32_t>(), off.as<int64_t>(), nullptr, nullptr, pts->err, s);
+      run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), nullptr, nullptr, pts->err, s);
       int64_t total = 0;
       THEA_CUDA_CHECK(cudaMemcpyAsync(&total, off.as<int64_t>() + na, 8, cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaStreamSynchronize(s));
       Scratch cand((size_t)std::max<int64_t>(total, 1) * 4, s), owner((size_t)std::max<int64_t>(total, 1) * 4, s);
       Scratch sep((size_t)std::max<int64_t>(total, 1) * 4, s), ok((size_t)std::max<int64_t>(total, 1), s);
       if (total > 0) {
-        run_range(pts, q.as<float>(), na, radius, ids.as<int32_t>(), off.as<int64_t>(), cand.as<int32_t>(), nullptr,
+        run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), cand.as<int32_t>(), nullptr,
                   pts->err, s);
         THEA_LAUNCH(owner_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, off.as<int64_t>(), na,
                     owner.as<int32_t>());
         THEA_LAUNCH(pair_kernel, (unsigned)ceil_div(total, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions, normals,
-                    ids.as<int32_t>(), owner.as<int32_t>(), cand.as<int32_t>(), total, sep.as<float>(),
+                    ids, owner.as<int32_t>(), cand.as<int32_t>(), total, sep.as<float>(),
                     ok.as<uint8_t>());
         if (reach)
           dispatch_any(surface,
-                       ReachRays{positions, normals, ids.as<int32_t>(), owner.as<int32_t>(), cand.as<int32_t>(),
+                       ReachRays{positions, normals, ids, owner.as<int32_t>(), cand.as<int32_t>(),
                                  sep.as<float>(), inverse_of(surface)},
                        BlockedFlags{ok.as<uint8_t>()}, total, 1.0f, s);
       }
-      THEA_LAUNCH(select_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, ids.as<int32_t>(), na,
+      THEA_LAUNCH(select_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, ids, na,
                   off.as<int64_t>(), cand.as<int32_t>(), sep.as<float>(), ok.as<uint8_t>(), max_degree, min_degree,
                   last ? 1 : 0, out.neighbors, out.separations, out.degree, again.as<uint8_t>());
-      std::vector<uint8_t> h((size_t)na);
-      THEA_CUDA_CHECK(cudaMemcpyAsync(h.data(), again.ptr, (size_t)na, cudaMemcpyDeviceToHost, s));
+      if (last) break;
+      unsigned g = (unsigned)ceil_div(na, GRAPH_THREADS);
+      THEA_LAUNCH(flags_to_int_kernel, g, GRAPH_THREADS, 0, s, again.as<uint8_t>(), na, pos.as<int32_t>());
+      exclusive_scan<int32_t>(pos.as<int32_t>(), pos.as<int32_t>(), na, s);
+      THEA_LAUNCH(compact_active_kernel, g, GRAPH_THREADS, 0, s, act, again.as<uint8_t>(), pos.as<int32_t>(), na, nxt,
+                  cnt.as<int64_t>());
+      int64_t next_count = 0;
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&next_count, cnt.ptr, 8, cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaStreamSynchronize(s));
-      std::vector<int32_t> next;
-      for (int64_t a = 0; a < na; ++a)
-        if (h[(size_t)a]) next.push_back(act[(size_t)a]);
-      act.swap(next);
+      std::swap(act, nxt);
+      na = next_count;
     }
   } catch (...) {
     cudaStreamSynchronize(s);
