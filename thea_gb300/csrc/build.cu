@@ -904,22 +904,26 @@ bool slot_ranges(thea_bvh const * b, Scratch & slots, cudaStream_t stream) {
   unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nn, BUILD_THREADS), 152 * 8));
   // every pass settles at least the deepest unsettled level; a pass that settles nothing ends the loop, and any node
   // still unsettled then (or after the pass limit) means the array is not a tree of this build's layout
+  // Passes run four at a time between reads of the flags (a pass after the one that settled the last node changes
+  // nothing, so the extra passes are no-ops); the flags are those of the group's last pass, `bad` accumulates.
   bool settled = false;
-  for (int pass = 0; pass < 2 * b->depth + 4 && !settled; ++pass) {
-    THEA_CUDA_CHECK(cudaMemsetAsync(flags.ptr, 0, sizeof(int), stream));
-    THEA_LAUNCH(subtree_range_kernel<W>, grid, BUILD_THREADS, 0, stream, nodes, nn, b->n, range.as<int2>(),
-                flags.as<int>(), flags.as<int>() + 1);
+  int limit = 2 * b->depth + 4;
+  int2 root = make_int2(-1, -1);
+  for (int pass = 0; pass < limit && !settled;) {
+    for (int k = 0; k < 4 && pass < limit; ++k, ++pass) {
+      THEA_CUDA_CHECK(cudaMemsetAsync(flags.ptr, 0, sizeof(int), stream));
+      THEA_LAUNCH(subtree_range_kernel<W>, grid, BUILD_THREADS, 0, stream, nodes, nn, b->n, range.as<int2>(),
+                  flags.as<int>(), flags.as<int>() + 1);
+    }
     int h[2];
     THEA_CUDA_CHECK(cudaMemcpyAsync(h, flags.ptr, sizeof(h), cudaMemcpyDeviceToHost, stream));
+    THEA_CUDA_CHECK(cudaMemcpyAsync(&root, range.ptr, sizeof(root), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
     if (h[1]) return false;
     settled = !h[0];
   }
   if (!settled) return false;
   // the root (node 0) must cover every element once settled
-  int2 root;
-  THEA_CUDA_CHECK(cudaMemcpyAsync(&root, range.ptr, sizeof(root), cudaMemcpyDeviceToHost, stream));
-  THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
   if (root.x != 0 || (int64_t)root.y != b->n) return false;
   slots = Scratch((size_t)nn * W * sizeof(int2), stream);
   unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nn * W, BUILD_THREADS), 152 * 8));
