@@ -426,13 +426,29 @@ void run_sample_graph_oversampled(float const * positions, float const * normals
 namespace thea {
 namespace {
 
-constexpr int RSUM_THREADS = 512;
+constexpr int RSUM_THREADS = 1024;
 constexpr int RSUM_ITEMS = 16;  // consecutive terms per thread; the cursor moves in multiples of it
+constexpr int64_t RSUM_WINDOW = (int64_t)RSUM_THREADS * RSUM_ITEMS;
+
+// Units of a thread's 16 terms in binade e; false if one of them has to be taken on its own
+__device__ __forceinline__ bool rsum_group_units(float4 const (&v)[RSUM_ITEMS / 4], int e, long long & units) {
+  bool ok = true;
+  units = 0;
+#pragma unroll
+  for (int i = 0; i < RSUM_ITEMS / 4; ++i) {
+    long long d0 = 0, d1 = 0, d2 = 0, d3 = 0;
+    ok = ok && running_sum_step_units(e, v[i].x, d0) && running_sum_step_units(e, v[i].y, d1) &&
+         running_sum_step_units(e, v[i].z, d2) && running_sum_step_units(e, v[i].w, d3);
+    units += d0 + d1 + d2 + d3;
+  }
+  return ok;
+}
 
 // One block walks the terms in windows of RSUM_THREADS x RSUM_ITEMS. Each thread sums the units of its 16 terms in the
 // binade of the sum at the window's start; a block scan over the threads finds the first group that cannot be added in
 // bulk (a term to be taken alone, or a total past RUNNING_SUM_MAX_UNITS). Every group before it is added as one integer
-// sum, that group's 16 terms one fl(s + x) at a time, and the next window starts after it.
+// sum, that group's 16 terms one fl(s + x) at a time, and the next window starts after it. Each thread loads its
+// group of the following window while the current one is scanned, and keeps it when the window was taken whole.
 __global__ void __launch_bounds__(RSUM_THREADS)
 running_sum_kernel(float const * __restrict__ x, int64_t const * __restrict__ count, int64_t n_host, float s0,
                    float * __restrict__ out) {
@@ -446,26 +462,33 @@ running_sum_kernel(float const * __restrict__ x, int64_t const * __restrict__ co
     s_cursor = 0;
   }
   __syncthreads();
+  float4 v[RSUM_ITEMS / 4], nv[RSUM_ITEMS / 4];
+  int64_t have = -1;  // window start whose group is in v
   while (true) {
     int64_t cur = s_cursor;
     float s = s_sum;
     if (cur >= n) break;
     int e = 0;
     bool bulk = running_sum_binade(s, e);
+    int64_t g0 = cur + (int64_t)t * RSUM_ITEMS;
+    bool full = g0 + RSUM_ITEMS <= n;
+    if (full && have != cur) {
+      float4 const * p = reinterpret_cast<float4 const *>(x + g0);
+#pragma unroll
+      for (int i = 0; i < RSUM_ITEMS / 4; ++i) v[i] = p[i];
+    }
+    int64_t g1 = g0 + RSUM_WINDOW;
+    bool next_full = g1 + RSUM_ITEMS <= n;
+    if (next_full) {
+      float4 const * p = reinterpret_cast<float4 const *>(x + g1);
+#pragma unroll
+      for (int i = 0; i < RSUM_ITEMS / 4; ++i) nv[i] = p[i];
+    }
     long long units = 0;
     bool ok = bulk;
-    int64_t g0 = cur + (int64_t)t * RSUM_ITEMS;
     if (bulk && g0 < n) {
-      if (g0 + RSUM_ITEMS <= n) {
-        float4 const * v = reinterpret_cast<float4 const *>(x + g0);
-#pragma unroll
-        for (int i = 0; i < RSUM_ITEMS / 4; ++i) {
-          float4 q = v[i];
-          long long d0 = 0, d1 = 0, d2 = 0, d3 = 0;
-          ok = ok && running_sum_step_units(e, q.x, d0) && running_sum_step_units(e, q.y, d1) &&
-               running_sum_step_units(e, q.z, d2) && running_sum_step_units(e, q.w, d3);
-          units += d0 + d1 + d2 + d3;
-        }
+      if (full) {
+        ok = rsum_group_units(v, e, units);
       } else {
         for (int64_t j = g0; j < n; ++j) {
           long long d = 0;
@@ -491,9 +514,16 @@ running_sum_kernel(float const * __restrict__ x, int64_t const * __restrict__ co
         s_cursor = end;
       } else {
         s = running_sum_from_units(base + before + units, e);
-        s_cursor = cur + (int64_t)RSUM_THREADS * RSUM_ITEMS;
+        s_cursor = cur + RSUM_WINDOW;
       }
       s_sum = s;
+    }
+    if (g == RSUM_THREADS && next_full) {
+#pragma unroll
+      for (int i = 0; i < RSUM_ITEMS / 4; ++i) v[i] = nv[i];
+      have = cur + RSUM_WINDOW;
+    } else {
+      have = -1;
     }
     __syncthreads();
   }
