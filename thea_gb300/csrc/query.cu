@@ -610,11 +610,16 @@ __global__ void query_range_kernel(int64_t * qoff, int64_t n) {
 // each query's slice of a CSR list; the slices are then put in ascending element order by one key sort.
 //============================================================================================================================
 
-template <int W, int STACK, bool FILL>
+// MODE 0: count each query's neighbours; 1: write (query, element) keys and squared distances at the query's offset,
+// for the sort into ascending element order; 2: write the elements (and squared distances, if asked) directly, in
+// traversal order.
+template <int W, int STACK, int MODE>
 __global__ void __launch_bounds__(QUERY_THREADS)
 range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
              int64_t n, float r2, int32_t const * __restrict__ exclude, int64_t * __restrict__ count_or_offset,
-             uint64_t * __restrict__ keys, float * __restrict__ out_d2, unsigned * __restrict__ err) {
+             uint64_t * __restrict__ keys, float * __restrict__ out_d2, unsigned * __restrict__ err,
+             int32_t * __restrict__ out_idx = nullptr) {
+  constexpr bool FILL = MODE != 0;
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   V3 p = load_v3(queries + 3 * q);
@@ -649,9 +654,12 @@ range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__
         if (idx == ex) continue;
         float d2 = squared_norm(xyz(a) - p);
         if (d2 <= r2) {
-          if (FILL) {
+          if (MODE == 1) {
             keys[w + c] = ((uint64_t)q << 32) | (uint32_t)idx;
             out_d2[w + c] = d2;
+          } else if (MODE == 2) {
+            out_idx[w + c] = idx;
+            if (out_d2) out_d2[w + c] = d2;
           }
           ++c;
         }
@@ -682,11 +690,16 @@ __global__ void range_emit_kernel(uint64_t const * __restrict__ keys, uint32_t c
 
 template <int W, int STACK>
 void launch_range(thea_bvh const * b, float const * q, int64_t n, float r2, int32_t const * ex, int64_t * offsets,
-                  int32_t * out_idx, float * out_d2, unsigned * err, cudaStream_t s) {
+                  int32_t * out_idx, float * out_d2, unsigned * err, bool sorted, cudaStream_t s) {
   unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
+  if (out_idx && !sorted) {
+    THEA_LAUNCH((range_kernel<W, STACK, 2>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec, q,
+                n, r2, ex, offsets, (uint64_t *)nullptr, out_d2, err, out_idx);
+    return;
+  }
   if (!out_idx) {
     Scratch counts((size_t)n * sizeof(int64_t), s);
-    THEA_LAUNCH((range_kernel<W, STACK, false>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec,
+    THEA_LAUNCH((range_kernel<W, STACK, 0>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec,
                 q, n, r2, ex, counts.as<int64_t>(), (uint64_t *)nullptr, (float *)nullptr, err);
     exclusive_scan<int64_t>(counts.as<int64_t>(), offsets, n, s);
     THEA_LAUNCH(range_total_kernel, 1, 1, 0, s, counts.as<int64_t>(), n, offsets);
@@ -699,7 +712,7 @@ void launch_range(thea_bvh const * b, float const * q, int64_t n, float r2, int3
   THEA_REQUIRE(total < (int64_t(1) << 32), "radius_neighbors: more than 2^32 neighbours in one call");
   Scratch keys((size_t)total * sizeof(uint64_t), s), d2((size_t)total * sizeof(float), s);
   Scratch perm((size_t)total * sizeof(uint32_t), s);
-  THEA_LAUNCH((range_kernel<W, STACK, true>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec, q,
+  THEA_LAUNCH((range_kernel<W, STACK, 1>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec, q,
               n, r2, ex, offsets, keys.as<uint64_t>(), d2.as<float>(), err);
   THEA_LAUNCH(range_iota_kernel, (unsigned)ceil_div(total, 256), 256, 0, s, total, perm.as<uint32_t>());
   int qbits = 1;
@@ -984,14 +997,14 @@ void run_ray_stream(thea_bvh const * b, float const * o, float const * d, int64_
 }
 
 void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex, int64_t * offsets,
-               int32_t * idx, float * d2, unsigned * err, cudaStream_t s) {
+               int32_t * idx, float * d2, unsigned * err, cudaStream_t s, bool sorted) {
   if (n <= 0) return;
   float r2 = radius * radius;  // BallN::contains compares with radius * radius in FP32
   bool sm = small_stack_ok(b);
-  if (b->width == 4) sm ? launch_range<4, 64>(b, q, n, r2, ex, offsets, idx, d2, err, s)
-                        : launch_range<4, 256>(b, q, n, r2, ex, offsets, idx, d2, err, s);
-  else sm ? launch_range<8, 128>(b, q, n, r2, ex, offsets, idx, d2, err, s)
-          : launch_range<8, 512>(b, q, n, r2, ex, offsets, idx, d2, err, s);
+  if (b->width == 4) sm ? launch_range<4, 64>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s)
+                        : launch_range<4, 256>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s);
+  else sm ? launch_range<8, 128>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s)
+          : launch_range<8, 512>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s);
 }
 
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,

@@ -93,8 +93,10 @@ void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, Ra
 // Points of a point BVH within `radius` of each query, as CSR. idx == nullptr: counting pass, writes offsets[0..n]
 // (n + 1 entries, device). Otherwise: filling pass with the offsets of the counting pass; each query's slice holds its
 // neighbours in ascending element index, with squared distances in d2 (nullable). Synchronizes in the filling pass.
+// sorted = false: the filling pass writes each slice in traversal order instead, without the sort and without
+// synchronizing (for callers whose use of a slice does not depend on its order).
 void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex, int64_t * offsets,
-               int32_t * idx, float * d2, unsigned * err, cudaStream_t s);
+               int32_t * idx, float * d2, unsigned * err, cudaStream_t s, bool sorted = true);
 // init_bound (self mode only): per leaf position, an inclusive upper bound on the k-th neighbour's squared distance
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
              float * d2, unsigned * err, cudaStream_t s, float const * init_bound = nullptr);

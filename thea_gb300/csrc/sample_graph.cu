@@ -343,8 +343,9 @@ void run_sample_graph(float const * positions, float const * normals, int64_t n,
       Scratch cand((size_t)std::max<int64_t>(total, 1) * 4, s), owner((size_t)std::max<int64_t>(total, 1) * 4, s);
       Scratch sep((size_t)std::max<int64_t>(total, 1) * 4, s), ok((size_t)std::max<int64_t>(total, 1), s);
       if (total > 0) {
+        // the selection keeps the smallest (separation, index) pairs whatever the order of a sample's candidates
         run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), cand.as<int32_t>(), nullptr,
-                  pts->err, s);
+                  pts->err, s, false);
         THEA_LAUNCH(owner_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, off.as<int64_t>(), na,
                     owner.as<int32_t>());
         THEA_LAUNCH(pair_kernel, (unsigned)ceil_div(total, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions, normals,
