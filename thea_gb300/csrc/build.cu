@@ -311,19 +311,13 @@ struct CollapseLevel {
   int64_t base;
   int64_t levels;
   int64_t overflow;  // set if a node would have landed past the node bound (never, by the bound's construction)
+  int64_t parity;    // which of the two frontier buffers holds the current frontier
 };
 
+// The W binary subtrees that become the children of frontier node f's wide node; returns how many are internal
 template <int W>
-__global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ frontier,
-                                       CollapseLevel const * __restrict__ lv, int64_t bound,
-                                       int * __restrict__ chosen, int * __restrict__ num_internal) {
-  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= bound) return;
-  int64_t fsize = lv->fsize;
-  if (f >= fsize) {
-    num_internal[f] = 0;  // the scan runs over the host's bound
-    return;
-  }
+__device__ __forceinline__ int collapse_decide_one(CollapseArgs const & a, int const * __restrict__ frontier, int64_t f,
+                                                   int * __restrict__ chosen) {
   int b = frontier[f];
   int codes[W];
   int ne = 2;
@@ -351,7 +345,18 @@ __global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ 
     chosen[f * W + e] = codes[e];
     if (codes[e] != CHILD_EMPTY && code_count(a, codes[e]) > a.leaf_size) ++nint;
   }
-  num_internal[f] = nint;
+  return nint;
+}
+
+template <int W>
+__global__ void collapse_decide_kernel(CollapseArgs a, int const * __restrict__ fa, int const * __restrict__ fb,
+                                       CollapseLevel const * __restrict__ lv, int64_t bound,
+                                       int * __restrict__ chosen, int * __restrict__ num_internal) {
+  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= bound) return;
+  int64_t fsize = lv->fsize;
+  num_internal[f] = f < fsize ? collapse_decide_one<W>(a, lv->parity ? fb : fa, f, chosen) : 0;  // the scan covers
+                                                                                                   // the host's bound
 }
 
 // Pad a box outwards by a relative margin of its coordinates' magnitude, so that rounding in element distances and hit
@@ -374,22 +379,17 @@ template <int W> __device__ __forceinline__ void clear_node(WideNode<W> & node) 
   for (int e = 0; e < (W == 4 ? 4 : 8); ++e) node.pad[e] = 0;
 }
 
+// Writes frontier node f's wide node (level_base + f) and appends its internal children to the next frontier at
+// offset `off` (their wide indices next_base + off + k); false if a node would land past the node bound
 template <int W>
-__global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ frontier, CollapseLevel * __restrict__ lv,
-                                     int64_t bound, int const * __restrict__ chosen, int const * __restrict__ offsets,
-                                     int64_t cap, WideNode<W> * __restrict__ nodes, int * __restrict__ next_frontier) {
-  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t fsize = lv->fsize;
-  if (f >= fsize || f >= bound) return;
-  int64_t level_base = lv->base, next_base = level_base + fsize;
-  if (level_base + f >= cap) {
-    lv->overflow = 1;
-    return;
-  }
+__device__ __forceinline__ bool collapse_emit_one(CollapseArgs const & a, int const * __restrict__ frontier, int64_t f,
+                                                  int const * __restrict__ chosen, int off, int64_t level_base,
+                                                  int64_t next_base, int64_t cap, WideNode<W> * __restrict__ nodes,
+                                                  int * __restrict__ next_frontier) {
+  if (level_base + f >= cap) return false;
   WideNode<W> node;
   clear_node(node);
   int k = 0;
-  int off = offsets[f];
   // leaves store their first element relative to the segment's first sorted position
   int64_t seg_base = 0;
   if (a.M > 1) {
@@ -409,16 +409,78 @@ __global__ void collapse_emit_kernel(CollapseArgs a, int const * __restrict__ fr
     if (cnt <= a.leaf_size) {
       node.child[e] = encode_leaf((int)(code_first(a, code) - seg_base), cnt);
     } else {
-      if (next_base + off + k >= cap) {
-        lv->overflow = 1;
-        return;
-      }
+      if (next_base + off + k >= cap) return false;
       node.child[e] = (int)(next_base + off + k);
       next_frontier[off + k] = code;
       ++k;
     }
   }
   nodes[level_base + f] = node;
+  return true;
+}
+
+template <int W>
+__global__ void collapse_emit_kernel(CollapseArgs a, int * __restrict__ fa, int * __restrict__ fb,
+                                     CollapseLevel * __restrict__ lv, int64_t bound, int const * __restrict__ chosen,
+                                     int const * __restrict__ offsets, int64_t cap, WideNode<W> * __restrict__ nodes) {
+  int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t fsize = lv->fsize;
+  if (f >= fsize || f >= bound) return;
+  int64_t level_base = lv->base;
+  bool par = lv->parity != 0;
+  if (!collapse_emit_one<W>(a, par ? fb : fa, f, chosen, offsets[f], level_base, level_base + fsize, cap, nodes,
+                            par ? fa : fb))
+    lv->overflow = 1;
+}
+
+// Levels whose frontier fits in one block, one after another in one launch (the top of the tree and its tail): thread f
+// decides and emits frontier node f, a block scan places the internal children. Returns when the frontier is empty or
+// outgrows the block.
+constexpr int COLLAPSE_BLOCK = 1024;
+
+template <int W>
+__global__ void __launch_bounds__(COLLAPSE_BLOCK)
+collapse_small_levels_kernel(CollapseArgs a, int * __restrict__ fa, int * __restrict__ fb,
+                             CollapseLevel * __restrict__ lv, int * __restrict__ chosen, int64_t cap,
+                             WideNode<W> * __restrict__ nodes) {
+  __shared__ int64_t s_fsize, s_base, s_parity;
+  __shared__ int s_bad;
+  int t = threadIdx.x;
+  if (t == 0) {
+    s_fsize = lv->fsize;
+    s_base = lv->base;
+    s_parity = lv->parity;
+    s_bad = 0;
+  }
+  __syncthreads();
+  int64_t levels = 0;
+  while (true) {
+    int64_t fsize = s_fsize;
+    if (fsize <= 0 || fsize > COLLAPSE_BLOCK || s_bad) break;
+    bool par = s_parity != 0;
+    int * cur = par ? fb : fa;
+    int * nxt = par ? fa : fb;
+    int nint = t < fsize ? collapse_decide_one<W>(a, cur, t, chosen) : 0;
+    int total = 0;
+    int off = block_exclusive_scan<int>(nint, total);
+    if (t < fsize && !collapse_emit_one<W>(a, cur, t, chosen, off, s_base, s_base + fsize, cap, nodes, nxt))
+      s_bad = 1;
+    __syncthreads();
+    if (t == 0) {
+      s_base += fsize;
+      s_fsize = total;
+      s_parity = !par;
+    }
+    ++levels;
+    __syncthreads();
+  }
+  if (t == 0) {
+    lv->fsize = s_bad ? 0 : s_fsize;
+    lv->base = s_base;
+    lv->parity = s_parity;
+    lv->levels += levels;
+    if (s_bad) lv->overflow = 1;
+  }
 }
 
 // Moves the device state to the next level: the emitted children form the next frontier
@@ -434,6 +496,7 @@ __global__ void collapse_advance_kernel(CollapseLevel * __restrict__ lv, int64_t
   lv->base += fsize;
   lv->fsize = (int64_t)offsets[fsize - 1] + num_internal[fsize - 1];
   lv->levels += 1;
+  lv->parity = !lv->parity;
 }
 
 // Segment roots: big segments (more elements than a leaf) become level-0 frontier entries; small non-empty segments get
@@ -649,34 +712,36 @@ void collapse(thea_bvh * b, CollapseArgs const & a, int64_t n, int const * d_bou
   Scratch chosen((size_t)std::max<int64_t>(cap, 1) * W * sizeof(int), stream);
   Scratch nint((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
   Scratch offs((size_t)std::max<int64_t>(cap, 1) * sizeof(int), stream);
-  int * cur = fa.as<int>();
-  int * nxt = fb.as<int>();
   int depth = num_small > 0 ? 1 : 0;
-  // Levels run COLLAPSE_LEVELS_PER_SYNC at a time on the device state; the host only bounds each frontier (a frontier
-  // node has at most W internal children, and no level holds more than the nbig wide internal nodes) to size the
-  // launches and the scan. Levels past the last one find an empty frontier and do nothing.
-  CollapseLevel h{num_big, num_small, 0, 0};
+  // Levels whose frontier fits in one block run in one launch (collapse_small_levels_kernel); larger ones run
+  // COLLAPSE_LEVELS_PER_SYNC at a time, a few launches each, on the device state, with the host bounding each frontier
+  // (a frontier node has at most W internal children, and no level holds more than the nbig wide internal nodes) to
+  // size the launches and the scan. Levels past the last one find an empty frontier and do nothing.
+  CollapseLevel h{num_big, num_small, 0, 0, 0};
   Scratch lv(sizeof(CollapseLevel), stream);
   THEA_CUDA_CHECK(cudaMemcpyAsync(lv.ptr, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
   int64_t limit = std::max<int64_t>((int64_t)nbig, 1);
-  int64_t bound = num_big;
   while (h.fsize > 0) {
+    int64_t bound = h.fsize;
+    if (bound <= COLLAPSE_BLOCK) {
+      THEA_LAUNCH(collapse_small_levels_kernel<W>, 1, COLLAPSE_BLOCK, 0, stream, a, fa.as<int>(), fb.as<int>(),
+                  lv.as<CollapseLevel>(), chosen.as<int>(), cap, nodes);
+      bound = 0;  // read the state back before choosing the next step
+    }
     for (int l = 0; l < COLLAPSE_LEVELS_PER_SYNC && bound > 0; ++l) {
       unsigned grid = (unsigned)ceil_div(bound, BUILD_THREADS);
-      THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, lv.as<CollapseLevel>(), bound,
-                  chosen.as<int>(), nint.as<int>());
+      THEA_LAUNCH(collapse_decide_kernel<W>, grid, BUILD_THREADS, 0, stream, a, fa.as<int>(), fb.as<int>(),
+                  lv.as<CollapseLevel>(), bound, chosen.as<int>(), nint.as<int>());
       exclusive_scan<int>(nint.as<int>(), offs.as<int>(), bound, stream);
-      THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, cur, lv.as<CollapseLevel>(), bound,
-                  chosen.as<int>(), offs.as<int>(), cap, nodes, nxt);
+      THEA_LAUNCH(collapse_emit_kernel<W>, grid, BUILD_THREADS, 0, stream, a, fa.as<int>(), fb.as<int>(),
+                  lv.as<CollapseLevel>(), bound, chosen.as<int>(), offs.as<int>(), cap, nodes);
       THEA_LAUNCH(collapse_advance_kernel, 1, 1, 0, stream, lv.as<CollapseLevel>(), bound, offs.as<int>(),
                   nint.as<int>());
-      std::swap(cur, nxt);
       bound = std::min<int64_t>(bound * W, limit);
     }
     THEA_CUDA_CHECK(cudaMemcpyAsync(&h, lv.ptr, sizeof(h), cudaMemcpyDeviceToHost, stream));
     THEA_CUDA_CHECK(cudaStreamSynchronize(stream));
     THEA_REQUIRE(!h.overflow, "BVH collapse exceeded its node bound");
-    bound = h.fsize;
   }
   b->nodes = nodes;
   b->num_nodes = h.base;
