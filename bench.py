@@ -110,6 +110,21 @@ def case_cfg0_32k():
     torch.cuda.synchronize()
 
 
+def case_sample_graph():
+    """Sample proximity graph of 262,144 area samples of the config-0 mesh with face normals, max degree 8,
+    reachability against the mesh (the bench's row): three calls."""
+    import torch
+    import thea_gb300 as T
+    V, F, _ = W.config0()
+    Vd, Fd = torch.from_numpy(V).cuda(), torch.from_numpy(F).cuda()
+    pos, nrm, _ = T.sample_evenly_by_area(Vd, Fd, KNN_POINTS, 2)
+    mesh = T.MeshBvh(Vd, Fd, layouts=2)
+    g_pts, g_nrm = pos[:262144].contiguous(), nrm[:262144].contiguous()
+    for _ in range(3):
+        T.sample_graph(g_pts, g_nrm, max_degree=8, seed=1, surface=mesh)
+    torch.cuda.synchronize()
+
+
 def case_cfg3_fp64_64():
     """Batched closest point with FP64 re-check over 64 meshes of the config-3 distribution: two calls."""
     import torch
@@ -204,7 +219,8 @@ def case_cfg0_host():
 
 CASES = {"ray": case_ray, "ray_host": case_ray_host, "ray_hf512": case_ray_hf512, "ray_hf2048": case_ray_hf2048,
          "cfg0_32k": case_cfg0_32k, "cfg0": case_cfg0, "cfg0_host": case_cfg0_host, "knn": case_knn,
-         "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn}
+         "cfg3_fp64_64": case_cfg3_fp64_64, "cfg3_fp32_64": case_cfg3_fp32_64, "gram_knn": case_gram_knn,
+         "sample_graph": case_sample_graph}
 
 
 def peaks():
