@@ -125,3 +125,30 @@ def test_k_up_to_32_and_pinned_host_arrays(T, meshes):
             i, d2, _ = ref("knn", 1, q.numpy(), k=k)
             assert t.wait() and t.status == N.THEA_OK
             assert np.array_equal(out[0].numpy(), i) and np.array_equal(out[1].numpy(), d2)
+
+
+@pytest.mark.timeout(300)
+def test_removing_meshes_while_other_requests_run(T, meshes):
+    """A mesh removed while its own and other meshes' requests are in flight stays usable by the requests already
+    submitted, is released when the last of them ends (its BVHs destroyed outside the server's lock, while other slots'
+    completions keep arriving), and every request's results still equal the single-BVH calls."""
+    ref = Reference(T, meshes, "fp32")
+    with T.Server(slots=3, max_batch_queries=16384, max_piece_queries=4096) as s:
+        ids = [s.add_mesh(V, F) for V, F in meshes]
+        for rep in range(3):
+            spare = s.add_mesh(*meshes[rep % 3])
+            tickets = []
+            for r in range(24):
+                kind = ("closest", "ray", "knn")[r % 3]
+                m = r % 3
+                q = queries(3000 + 500 * r, 900 + 31 * rep + r)
+                d = directions(len(q), 7 + r) if kind == "ray" else None
+                on_spare = r % 4 == 0 and r <= 12
+                mesh_id = spare if on_spare else ids[m]
+                src = rep % 3 if on_spare else m
+                tickets.append((s.submit(kind, mesh_id, q, directions=d, k=8), ref(kind, src, q, d)))
+                if r == 12:
+                    s.remove_mesh(spare)  # requests on it are in flight; later ones may not use it
+            for t, want in tickets:
+                check(t, want)
+        assert s.stats()["resident_bytes"] > 0

@@ -357,6 +357,9 @@ struct thea_server {
   std::condition_variable cv;       // dispatcher: new work, a finished slot, stop
   std::condition_variable cv_done;  // waiters
   std::map<int32_t, ServeMesh> meshes;
+  // BVHs of removed meshes whose last request has ended, destroyed once the lock is released: destroy_bvh synchronizes
+  // the device, which waits for the slots' completion callbacks, and those take the lock
+  std::vector<thea_bvh *> retired;
   int32_t next_mesh = 0;
   std::map<uint64_t, std::unique_ptr<ServeRequest>> requests;
   std::vector<ServeRequest *> pending;
@@ -391,11 +394,21 @@ void release_mesh_locked(thea_server * sv, int32_t id) {
   if (--m.refs == 0 && m.removing) {
     sv->resident_bytes -= m.bytes;
     if (!sv->cfg.test_executor) {
-      destroy_bvh(m.mesh);
-      destroy_bvh(m.pts);
+      sv->retired.push_back(m.mesh);
+      sv->retired.push_back(m.pts);
     }
     sv->meshes.erase(it);
   }
+}
+
+// Destroys the retired BVHs; the caller must not hold the lock
+void destroy_retired(thea_server * sv) {
+  std::vector<thea_bvh *> r;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    r.swap(sv->retired);
+  }
+  for (thea_bvh * b : r) destroy_bvh(b);
 }
 
 void end_request_locked(thea_server * sv, ServeRequest * q, thea_status st) {
@@ -646,6 +659,11 @@ void dispatcher_main(thea_server * sv) {
       if (s.busy && s.complete) finish_slot_locked(sv, s);
       any_busy = any_busy || s.busy;
     }
+    if (!sv->retired.empty()) {
+      lk.unlock();
+      destroy_retired(sv);
+      lk.lock();
+    }
     if (sv->stopping && !any_busy) break;
     bool launched = false;
     if (!sv->stopping) {
@@ -771,11 +789,13 @@ void server_destroy(thea_server * sv) {
       cudaFreeHost(s.h_off);
       cudaFree(s.d_counters);
     }
-  if (!sv->cfg.test_executor)
+  if (!sv->cfg.test_executor) {
+    destroy_retired(sv);
     for (auto & kv : sv->meshes) {
       destroy_bvh(kv.second.mesh);
       destroy_bvh(kv.second.pts);
     }
+  }
   delete sv;
 }
 
@@ -849,11 +869,14 @@ int32_t server_add_mesh(thea_server * sv, float const * V, int64_t nv, int32_t c
 }
 
 void server_remove_mesh(thea_server * sv, int32_t id) {
-  std::lock_guard<std::mutex> lk(sv->mu);
-  auto it = sv->meshes.find(id);
-  THEA_REQUIRE(it != sv->meshes.end() && !it->second.removing, "server_remove_mesh: no such mesh");
-  it->second.removing = true;
-  release_mesh_locked(sv, id);
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->meshes.find(id);
+    THEA_REQUIRE(it != sv->meshes.end() && !it->second.removing, "server_remove_mesh: no such mesh");
+    it->second.removing = true;
+    release_mesh_locked(sv, id);
+  }
+  destroy_retired(sv);
 }
 
 uint64_t server_submit(thea_server * sv, thea_request const & r) {
@@ -924,16 +947,19 @@ thea_status server_wait(thea_server * sv, uint64_t ticket, int64_t timeout_us, t
 }
 
 void server_cancel(thea_server * sv, uint64_t ticket) {
-  std::lock_guard<std::mutex> lk(sv->mu);
-  auto it = sv->requests.find(ticket);
-  THEA_REQUIRE(it != sv->requests.end(), "server_cancel: unknown or retired ticket");
-  ServeRequest * q = it->second.get();
-  if (q->done) return;
-  q->cancelled = true;
-  auto pit = std::find(sv->pending.begin(), sv->pending.end(), q);
-  if (pit != sv->pending.end()) sv->pending.erase(pit);
-  q->scheduled = q->r.num_queries;  // no further pieces
-  if (q->pieces_done == q->pieces) end_request_locked(sv, q, THEA_ERR_CANCELLED);
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->requests.find(ticket);
+    THEA_REQUIRE(it != sv->requests.end(), "server_cancel: unknown or retired ticket");
+    ServeRequest * q = it->second.get();
+    if (q->done) return;
+    q->cancelled = true;
+    auto pit = std::find(sv->pending.begin(), sv->pending.end(), q);
+    if (pit != sv->pending.end()) sv->pending.erase(pit);
+    q->scheduled = q->r.num_queries;  // no further pieces
+    if (q->pieces_done == q->pieces) end_request_locked(sv, q, THEA_ERR_CANCELLED);
+  }
+  destroy_retired(sv);
 }
 
 void server_stats(thea_server * sv, thea_server_stats * o) {
