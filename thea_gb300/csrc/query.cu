@@ -618,8 +618,8 @@ __global__ void __launch_bounds__(QUERY_THREADS)
 range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__ pts, float const * __restrict__ queries,
              int64_t n, float r2, int32_t const * __restrict__ exclude, int64_t * __restrict__ count_or_offset,
              uint64_t * __restrict__ keys, float * __restrict__ out_d2, unsigned * __restrict__ err,
-             int32_t * __restrict__ out_idx = nullptr) {
-  constexpr bool FILL = MODE != 0;
+             int32_t * __restrict__ out_idx = nullptr, int row_cap = 0, unsigned * __restrict__ overflow = nullptr) {
+  constexpr bool FILL = MODE == 1 || MODE == 2;  // MODE 3: count, and write the first row_cap into row q of out_idx
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   V3 p = load_v3(queries + 3 * q);
@@ -660,6 +660,8 @@ range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__
           } else if (MODE == 2) {
             out_idx[w + c] = idx;
             if (out_d2) out_d2[w + c] = d2;
+          } else if (MODE == 3) {
+            if (c < row_cap) out_idx[q * row_cap + c] = idx;
           }
           ++c;
         }
@@ -667,6 +669,7 @@ range_kernel(WideNode<W> const * __restrict__ nodes, float4 const * __restrict__
     }
   }
   if (!FILL) count_or_offset[q] = c;
+  if (MODE == 3 && c > row_cap) atomicOr(overflow, 1u);
 }
 
 __global__ void range_total_kernel(int64_t const * __restrict__ counts, int64_t n, int64_t * __restrict__ offsets) {
@@ -720,6 +723,17 @@ void launch_range(thea_bvh const * b, float const * q, int64_t n, float r2, int3
   radix_sort_pairs(keys.as<uint64_t>(), perm.as<uint32_t>(), total, 32 + qbits, s);
   THEA_LAUNCH(range_emit_kernel, (unsigned)ceil_div(total, 256), 256, 0, s, keys.as<uint64_t>(), perm.as<uint32_t>(),
               d2.as<float>(), total, out_idx, out_d2);
+}
+
+template <int W, int STACK>
+void launch_range_rows(thea_bvh const * b, float const * q, int64_t n, float r2, int32_t const * ex, int64_t * offsets,
+                       int32_t * rows, int row_cap, unsigned * overflow, unsigned * err, cudaStream_t s) {
+  unsigned grid = (unsigned)ceil_div(n, QUERY_THREADS);
+  Scratch counts((size_t)n * sizeof(int64_t), s);
+  THEA_LAUNCH((range_kernel<W, STACK, 3>), grid, QUERY_THREADS, 0, s, (WideNode<W> const *)b->nodes, b->pt_rec, q, n,
+              r2, ex, counts.as<int64_t>(), (uint64_t *)nullptr, (float *)nullptr, err, rows, row_cap, overflow);
+  exclusive_scan<int64_t>(counts.as<int64_t>(), offsets, n, s);
+  THEA_LAUNCH(range_total_kernel, 1, 1, 0, s, counts.as<int64_t>(), n, offsets);
 }
 
 //============================================================================================================================
@@ -1005,6 +1019,17 @@ void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int
                         : launch_range<4, 256>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s);
   else sm ? launch_range<8, 128>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s)
           : launch_range<8, 512>(b, q, n, r2, ex, offsets, idx, d2, err, sorted, s);
+}
+
+void run_range_rows(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex,
+                    int64_t * offsets, int32_t * rows, int row_cap, unsigned * overflow, unsigned * err, cudaStream_t s) {
+  if (n <= 0) return;
+  float r2 = radius * radius;
+  bool sm = small_stack_ok(b);
+  if (b->width == 4) sm ? launch_range_rows<4, 64>(b, q, n, r2, ex, offsets, rows, row_cap, overflow, err, s)
+                        : launch_range_rows<4, 256>(b, q, n, r2, ex, offsets, rows, row_cap, overflow, err, s);
+  else sm ? launch_range_rows<8, 128>(b, q, n, r2, ex, offsets, rows, row_cap, overflow, err, s)
+          : launch_range_rows<8, 512>(b, q, n, r2, ex, offsets, rows, row_cap, overflow, err, s);
 }
 
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,

@@ -97,6 +97,10 @@ void run_ray(thea_bvh const * b, float const * o, float const * d, int64_t n, Ra
 // synchronizing (for callers whose use of a slice does not depend on its order).
 void run_range(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex, int64_t * offsets,
                int32_t * idx, float * d2, unsigned * err, cudaStream_t s, bool sorted = true);
+// The counting pass that also writes each query's first row_cap neighbours (traversal order) into row q of `rows`
+// (n x row_cap) and sets *overflow (device) if a query has more; offsets as the counting pass writes them.
+void run_range_rows(thea_bvh const * b, float const * q, int64_t n, float radius, int32_t const * ex,
+                    int64_t * offsets, int32_t * rows, int row_cap, unsigned * overflow, unsigned * err, cudaStream_t s);
 // init_bound (self mode only): per leaf position, an inclusive upper bound on the k-th neighbour's squared distance
 void run_knn(thea_bvh const * b, float const * q, int64_t n, int k, float thresh, int32_t const * ex, int32_t * idx,
              float * d2, unsigned * err, cudaStream_t s, float const * init_bound = nullptr);

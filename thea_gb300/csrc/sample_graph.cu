@@ -254,6 +254,17 @@ extract_kernel(int32_t const * __restrict__ nbr, float const * __restrict__ sep,
   }
 }
 
+// Candidate rows (CAND_ROW per sample, the first off[a + 1] - off[a] used) -> CSR
+constexpr int CAND_ROW = 64;
+
+__global__ void rows_to_csr_kernel(int32_t const * __restrict__ rows, int64_t const * __restrict__ off, int64_t n,
+                                   int32_t * __restrict__ cand) {
+  int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  int64_t o = off[a], c = off[a + 1] - o;
+  for (int64_t k = 0; k < c; ++k) cand[o + k] = rows[a * CAND_ROW + k];
+}
+
 // Round 0's active list: every sample
 __global__ void iota_kernel(int32_t * __restrict__ out, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -335,17 +346,30 @@ void run_sample_graph(float const * positions, float const * normals, int64_t n,
       int32_t const * ids = act;
       THEA_LAUNCH(gather_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions,
                   ids, na, q.as<float>());
-      // candidates: Ball3(position, radius), the sample itself excluded (the identity test)
-      run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), nullptr, nullptr, pts->err, s);
-      int64_t total = 0;
-      THEA_CUDA_CHECK(cudaMemcpyAsync(&total, off.as<int64_t>() + na, 8, cudaMemcpyDeviceToHost, s));
+      // candidates: Ball3(position, radius), the sample itself excluded (the identity test); one traversal counts them
+      // and keeps up to CAND_ROW per sample, a second one runs only if a sample has more
+      Scratch rows((size_t)na * CAND_ROW * 4, s), over(sizeof(unsigned), s);
+      THEA_CUDA_CHECK(cudaMemsetAsync(over.ptr, 0, sizeof(unsigned), s));
+      run_range_rows(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), rows.as<int32_t>(), CAND_ROW,
+                     over.as<unsigned>(), pts->err, s);
+      struct {
+        int64_t total;
+        unsigned over;
+      } h{0, 0};
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&h.total, off.as<int64_t>() + na, 8, cudaMemcpyDeviceToHost, s));
+      THEA_CUDA_CHECK(cudaMemcpyAsync(&h.over, over.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
       THEA_CUDA_CHECK(cudaStreamSynchronize(s));
+      int64_t total = h.total;
       Scratch cand((size_t)std::max<int64_t>(total, 1) * 4, s), owner((size_t)std::max<int64_t>(total, 1) * 4, s);
       Scratch sep((size_t)std::max<int64_t>(total, 1) * 4, s), ok((size_t)std::max<int64_t>(total, 1), s);
       if (total > 0) {
         // the selection keeps the smallest (separation, index) pairs whatever the order of a sample's candidates
-        run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), cand.as<int32_t>(), nullptr,
-                  pts->err, s, false);
+        if (h.over)
+          run_range(pts, q.as<float>(), na, radius, ids, off.as<int64_t>(), cand.as<int32_t>(), nullptr,
+                    pts->err, s, false);
+        else
+          THEA_LAUNCH(rows_to_csr_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s,
+                      rows.as<int32_t>(), off.as<int64_t>(), na, cand.as<int32_t>());
         THEA_LAUNCH(owner_kernel, (unsigned)ceil_div(na, GRAPH_THREADS), GRAPH_THREADS, 0, s, off.as<int64_t>(), na,
                     owner.as<int32_t>());
         THEA_LAUNCH(pair_kernel, (unsigned)ceil_div(total, GRAPH_THREADS), GRAPH_THREADS, 0, s, positions, normals,
